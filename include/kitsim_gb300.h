@@ -1,0 +1,192 @@
+/*
+ * kitsim_gb300.h - C ABI of the GB300 (sm_103a) ray-cast-and-accumulate engine.
+ *
+ * This is the drop-in boundary for kit-sim_daylight's GPU contract: every function below replaces one `gpu_*`
+ * function of the reference's `src/internal.h:125-220` (implemented there by `src/gpu.cu` over OptiX and the
+ * programs of `src/trace_dev.cu`). The C++ shim `kit-sim_daylight_gb300/shim/daylight_gpu.cpp` implements the
+ * reference's `daylight::gpu_*` signatures over these entry points, so the reference's `run.cpp` / `views.cpp`,
+ * its C ABI (`daylight_c.h`: DL_DAYLIGHT / DL_VIEWS) and its bindings run unchanged on top of this library.
+ *
+ * Conventions (the reference's, restated for C):
+ *  - Every `int` returning function returns 1 on success and 0 on failure; the message is in kgb_last_error()
+ *    (per thread, until the next failing call on that thread). No C++ exception crosses the ABI.
+ *  - Host arrays are plain host pointers; the engine owns every device buffer and grows it on demand.
+ *  - Layouts on the device follow the reference: visibility bits word-major bits[w*nc + i], transmittance bytes and
+ *    view classes / distances direction-major [d*nc + i], reflected-light rows [b*nc + i].
+ *  - One engine is used by one thread at a time (the reference's run() is one-at-a-time per process).
+ *  - Chunks and launch boundaries change no bit of any result (seeds come from global sensor indices).
+ */
+#ifndef KITSIM_GB300_H
+#define KITSIM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(_WIN32)
+#define KGB_API __declspec(dllexport)
+#else
+#define KGB_API __attribute__((visibility("default")))
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KGB_ABI_VERSION 1
+
+/* Ray flags: the bit values of OptiX's OPTIX_RAY_FLAG_* that the reference passes around (gpu_ray_flags /
+ * gpu_bounce_flags, src/gpu.cu:739-746; pinned by tests/check_gpu.cpp:98-101 as 5 / 21 / 4 / 20 and 1 / 17). */
+#define KGB_RAY_DISABLE_ANYHIT 1u          /* every triangle opaque: visibility bits, no transmittance */
+#define KGB_RAY_TERMINATE_ON_FIRST_HIT 4u  /* any-hit occlusion (the visibility pass) */
+#define KGB_RAY_CULL_BACK_FACING 16u       /* one-sided occluders: back-facing hits are ignored */
+
+/* Slot flags (src/params.h:13-19). */
+#define KGB_SLOT_GLASS 1u   /* transmittance by angle (Radiance glass); else tau at every angle */
+#define KGB_SLOT_THIN 2u    /* closed thin solid: its exit face passes everything */
+#define KGB_SLOT_INWARD 4u  /* ... wound inward: entry is the back face */
+#define KGB_SLOT_TWIN 8u    /* ... of no volume, faces in coincident pairs */
+
+/* Views: label of a triangle rays pass, most panes passed, class bit of a ray that passed glass (src/params.h:22-24). */
+#define KGB_LABEL_PASS 255u
+#define KGB_MAX_PANES 16u
+#define KGB_VIEW_GLAZED 0x80u
+#define KGB_VIEW_CLASSES 19u /* sky, ground, obstruction, 16 target groups (src/gpu.cu:48) */
+
+/* Optics of one global slot: the reference's Slot (src/params.h:7-12), same layout. */
+typedef struct kgb_slot {
+  float rho;      /* diffuse reflectance (bounce pass) */
+  float tau;      /* transmittance at normal incidence; > 0 = translucent */
+  float tn;       /* glass transmissivity (tn_from_Tn(tau)), used with KGB_SLOT_GLASS */
+  uint32_t flags; /* KGB_SLOT_* */
+} kgb_slot;
+
+typedef struct kgb_engine kgb_engine;
+
+/* A built scene (BVH, triangles, per-triangle slots) moved out of an engine: the reference's GasSlot
+ * (src/internal.h:141). */
+typedef struct kgb_scene {
+  void* handle;
+  uint64_t bytes;
+} kgb_scene;
+
+/* The reference's GpuStats (src/internal.h:211-216). */
+typedef struct kgb_stats {
+  double buildMs, traceMs, bounceMs;
+  uint64_t rays, gasBytes, launches, paths, bounceLaunches;
+  uint64_t buildTempBytes, buildOutputBytes;
+} kgb_stats;
+
+/* Cancel hook: returns non-zero once the run should stop (the reference's const std::atomic<bool>*). */
+typedef int (*kgb_cancel_fn)(void* ctx);
+
+/* Inputs of kgb_series: the reference's SeriesIn (src/internal.h:155-168), host arrays. */
+typedef struct kgb_series_in {
+  uint32_t nSky;          /* sky directions are 0..nSky-1 */
+  const int32_t* row;     /* [nSky] patch index per sky direction */
+  const float* wsky;      /* [nSky] weight per sky direction */
+  const float* S;         /* [P x T] patch radiance per step, row-major */
+  int32_t P, T;
+  const float* g;         /* [T] ground term per step */
+  const float* G;         /* [nc] ground visibility per sensor */
+  uint32_t sun0, nSun;    /* sun direction range in the direction table */
+  const int32_t* sunStep; /* [nSun] step (column) index per sun direction */
+  const float* sunVec;    /* [nSun x 3] */
+  const float* sunW;      /* [nSun] DNI (W/m2) or direct illuminance (lux) per sun direction */
+  const float* Sdc;       /* [(P+1) x T] radiance per bounce bin and step; NULL = no reflected light */
+} kgb_series_in;
+
+/* Inputs of kgb_bounce: the reference's Bounce (src/internal.h:178). */
+typedef struct kgb_bounce_in {
+  uint32_t N;      /* diffuse reflections per path */
+  uint32_t M;      /* paths per sensor */
+  int32_t mf;      /* sky density of the bins (1, 2, 4) */
+  double north;    /* degrees */
+  kgb_cancel_fn cancel;
+  void* cancelCtx;
+} kgb_bounce_in;
+
+/* Inputs of kgb_view: the reference's ViewLaunch (src/internal.h:186-195). */
+typedef struct kgb_view_in {
+  uint32_t nAz, nEl;
+  float az0, dAz;        /* degrees */
+  const float* rowSin;   /* [2 nEl] host: sin of each row's bottom and top elevation */
+  int32_t world, cull, jitter, back, vground;
+  uint32_t nS;           /* sides per element */
+  float groundZ;         /* the virtual ground plane (recentred) */
+  double north;          /* degrees */
+  kgb_cancel_fn cancel;
+  void* cancelCtx;
+} kgb_view_in;
+
+/* --- lifetime -------------------------------------------------------------------------------------------------- */
+KGB_API int32_t kgb_version(void);
+KGB_API const char* kgb_last_error(void);
+/* replaces gpu_init (src/internal.h:127): the engine on the current CUDA device; NULL + kgb_last_error on failure */
+KGB_API kgb_engine* kgb_init(void);
+/* replaces gpu_destroy (src/internal.h:128) */
+KGB_API void kgb_destroy(kgb_engine* e);
+
+/* --- scene --------------------------------------------------------------------------------------------------------- */
+/* replaces gpu_build (src/internal.h:133): v [nv x 3] floats, tri [nt x 3] vertex indices, slot [nt] global slot per
+ * triangle (NULL when not needed), the slot table. Builds the 8-wide BVH; every slot index must be < nSlots when the
+ * build is slotted (a slot transmits or perSlot). nt == 0: an empty scene, every ray misses. */
+KGB_API int kgb_build(kgb_engine* e, const float* v, size_t nv, const uint32_t* tri, size_t nt, const uint32_t* slot,
+                      const kgb_slot* slots, size_t nSlots, int perSlot);
+/* replaces gpu_build_bytes (src/internal.h:136): device bytes a build peaks at; UINT64_MAX on error */
+KGB_API uint64_t kgb_build_bytes(kgb_engine* e, size_t nv, size_t nt, int slotted);
+/* replaces gpu_trim (src/internal.h:138) */
+KGB_API void kgb_trim(kgb_engine* e, int sensors);
+/* replaces gpu_set_slots (src/internal.h:139): the slot records read at hits (tau, tn, rho, flags) */
+KGB_API int kgb_set_slots(kgb_engine* e, const kgb_slot* slots, size_t n);
+/* replace gpu_detach / gpu_attach / gpu_free / gpu_free_bytes (src/internal.h:142-145) */
+KGB_API kgb_scene kgb_detach(kgb_engine* e);
+KGB_API void kgb_attach(kgb_engine* e, kgb_scene s);
+KGB_API void kgb_free_scene(kgb_scene* s);
+KGB_API uint64_t kgb_free_bytes(void);
+/* replaces gpu_set_scene (src/internal.h:146): resident sensors (recentred, offset applied) and directions */
+KGB_API int kgb_set_scene(kgb_engine* e, const float* P, const float* N, size_t nSensors, const float* D, size_t nDir);
+/* replaces gpu_set_labels (src/internal.h:197): class per triangle in build order; n == 0: none */
+KGB_API int kgb_set_labels(kgb_engine* e, const uint8_t* label, size_t n);
+
+/* --- daylight -------------------------------------------------------------------------------------------------------- */
+/* replaces gpu_trace (src/internal.h:151): sensors [i0, i0+nc) against every direction. Without
+ * KGB_RAY_DISABLE_ANYHIT: transmittance bytes instead of bits. */
+KGB_API int kgb_trace(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags);
+/* replaces gpu_reduce (src/internal.h:154): out[i] = sum_d T(i,d) * (useCos ? max(0, N_i.D_d) : 1) * W[d] (double) */
+KGB_API int kgb_reduce(kgb_engine* e, size_t nc, const float* W, int useCos, double* out);
+/* replaces gpu_series (src/internal.h:171): E[i*T + t] (host, nc x T floats) */
+KGB_API int kgb_series(kgb_engine* e, size_t nc, const kgb_series_in* in, float* E);
+/* replaces gpu_bounce (src/internal.h:179) */
+KGB_API int kgb_bounce(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, const kgb_bounce_in* b);
+/* replaces gpu_reduce_dc (src/internal.h:180): out[i] = sum_b dc(b, i) * W[b] (double) */
+KGB_API int kgb_reduce_dc(kgb_engine* e, size_t nc, const float* W, double* out);
+/* replace gpu_download_dc / bits / bytes (src/internal.h:181-183): count must be the buffer's element count */
+KGB_API int kgb_download_dc(kgb_engine* e, size_t nc, float* out, size_t count);
+KGB_API int kgb_download_bits(kgb_engine* e, size_t nc, uint32_t* out, size_t count);
+KGB_API int kgb_download_bytes(kgb_engine* e, size_t nc, uint8_t* out, size_t count);
+
+/* --- views ----------------------------------------------------------------------------------------------------------- */
+/* replaces gpu_view (src/internal.h:201): launch carries the sub-launch size from chunk to chunk (0 = start over) */
+KGB_API int kgb_view(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, const kgb_view_in* v, size_t* launch);
+/* replaces gpu_reduce_view (src/internal.h:208): out [nc x NA] doubles,
+ * NA = 3 nClass + 1 + nReach + (glazing ? 1 : 0) + (isoDim ? 1 : 0) */
+KGB_API int kgb_reduce_view(kgb_engine* e, size_t nc, const double* wRow, size_t nRow, uint32_t nClass, double farDist,
+                            const float* reach, size_t nReach, int glazing, uint32_t isoDim, double* out);
+/* replaces gpu_download_view (src/internal.h:210): [nc x K] each (transposed from the device's [K x nc]) */
+KGB_API int kgb_download_view(kgb_engine* e, size_t nc, uint8_t* cls, float* dist, size_t count);
+
+/* --- misc ------------------------------------------------------------------------------------------------------------ */
+/* replaces gpu_stats (src/internal.h:216) */
+KGB_API kgb_stats kgb_get_stats(const kgb_engine* e);
+/* replace gpu_ray_flags / gpu_bounce_flags (src/internal.h:218-220) */
+KGB_API uint32_t kgb_ray_flags(int cullBackfaces, int translucent);
+KGB_API uint32_t kgb_bounce_flags(int cullBackfaces);
+/* Sizes of the engine's current buffers (no reference counterpart; what a C caller needs to size downloads):
+ * out[0] = nSensors, out[1] = nDir, out[2] = nWords, out[3] = nBins (last bounce), out[4] = K (last view),
+ * out[5] = 1 when the last trace wrote bytes. */
+KGB_API void kgb_dims(const kgb_engine* e, uint64_t out[6]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KITSIM_GB300_H */
