@@ -1,0 +1,294 @@
+#!/usr/bin/env python3
+"""Benchmark of the ray-cast-and-accumulate hot path on GB300: the urban block (config 2 of the measured set).
+
+Workload (one step): the seeded 20 x 20 urban block (199,976 sensor faces, 403,152 triangles, resident BVH) traced
+against 5610 directions (577 Reinhart sky patches, their ground mirror, 4456 sun-up hours of the synthetic urban
+weather year) - 1.12 G any-hit rays - then the four cumulative quantities reduced per sensor (radiation, irradiance,
+illuminance, sun hours), as the reference's chunk loop does (src/run.cpp:642-657: gpu_trace + gpu_reduce per quantity).
+The direction table and weights are the reference's own (tests/golden/urban_sky: recorded from its host code).
+
+Metric: Mrays/s (sensor x direction slots per second, the reference's GRays/s counting, x1000), higher is better.
+ value: inputs resident in HBM, CUDA events on the engine's stream around trace + reduces; L2 flushed between steps.
+ e2e:   the same through the C ABI with host buffers: set_scene (sensors, directions) from pinned memory, trace, the
+        four reduces with their weights up and sums down, every step.
+--impl reference: the oracle (the CPU restatement of the reference's path) on the host's cores, bounded samples.
+"""
+import argparse
+import importlib.util
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(REPO, "tests", "golden")
+
+
+def package():
+    if "kitsim_gb300" in sys.modules:
+        return sys.modules["kitsim_gb300"]
+    d = os.path.join(REPO, "kit-sim_daylight_gb300")
+    spec = importlib.util.spec_from_file_location("kitsim_gb300", os.path.join(d, "__init__.py"), submodule_search_locations=[d])
+    m = importlib.util.module_from_spec(spec)
+    sys.modules["kitsim_gb300"] = m
+    spec.loader.exec_module(m)
+    return m
+
+
+def urban_sky():
+    """Direction table and per-quantity weights of the urban block (the reference's host code, recorded)."""
+    calls = [json.loads(l) for l in open(os.path.join(GOLDEN, "urban_sky", "calls.jsonl"))]
+    last = max(i for i, c in enumerate(calls) if c["call"] == "gpu_set_scene")
+    c = calls[last]
+    D = np.fromfile(os.path.join(GOLDEN, "urban_sky", c["D"][2]), np.float32).reshape(-1, 3)
+    Ws = []
+    for c in calls[last:]:
+        if c["call"] == "gpu_reduce":
+            Ws.append((np.fromfile(os.path.join(GOLDEN, "urban_sky", c["W"][2]), np.float32), bool(c["useCos"])))
+    manifest = json.load(open(os.path.join(GOLDEN, "urban_sky", "manifest.json")))
+    return D, Ws, manifest
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    Q = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown," \
+        "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index=0):
+        self.rows, self.proc, self.index = [], None, index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            p = [x.strip() for x in line.split(",")]
+            if len(p) >= 8:
+                self.rows.append(p)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[4 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        m = json.load(open(p))
+        return m["hbm_gbs"], "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """Per-launch DRAM bytes of k_bits from the committed ncu summary (profiles/k_bits_urban.md), if there is one."""
+    p = os.path.join(REPO, "profiles", "k_bits_urban.md")
+    if os.path.exists(p):
+        for line in open(p):
+            if line.startswith("traffic_per_full_trace_bytes:"):
+                return float(line.split(":")[1])
+    return None
+
+
+def cpu_baseline(pkg, scene, D, Ws, sample, seed=0):
+    """The oracle (the CPU restatement) on the host's cores: trace + the four reduces of a seeded sensor sample."""
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle"), "all"])
+    lib = pkg.kgb.Lib(os.path.join(REPO, "oracle", "_build", "liboracle.so"))
+    o = pkg.kgb.Engine(lib)
+    o.build(scene["v"], scene["tri"])
+    pick = np.sort(np.random.default_rng(seed).choice(len(scene["P"]), sample, replace=False))
+    o.set_scene(scene["P"][pick], scene["N"][pick], D)
+    t0 = time.perf_counter()
+    o.trace(0, sample, lib.ray_flags(False, False))
+    for W, use_cos in Ws:
+        o.reduce(sample, W, use_cos)
+    dt = time.perf_counter() - t0
+    o.close()
+    return sample * len(D) / dt / 1e6, dt
+
+
+def run_reference(args, pkg):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    scene = pkg.workloads.urban_block()
+    D, Ws, _ = urban_sky()
+    cores = os.cpu_count()
+    sample = args.ref_sample
+    for _ in range(args.warmup):
+        cpu_baseline(pkg, scene, D, Ws, max(64, sample // 8), seed=1)
+    vals, secs = [], []
+    for k in range(args.steps):
+        v, dt = cpu_baseline(pkg, scene, D, Ws, sample, seed=100 + k)
+        vals.append(v)
+        secs.append(dt)
+    value = float(np.median(vals))
+    line = {"metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000 * float(np.median(secs)), "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded urban block; the reference's direction table and weights)", "impl": "reference",
+            "config": {"workload": "urban block: 20x20 boxes, %d sensors, %d triangles, %d directions (577 sky + ground + sun), "
+                                   "4 quantities" % (len(scene["P"]), len(scene["tri"]), len(D)), "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": cores, "kind": "port",
+                             "sample": "%d seeded sensors of the block x %d directions per step (+ the 4 reduces)" % (sample, len(D))},
+            "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, pkg):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    pkg.load()
+    scene = pkg.workloads.urban_block(seed=42 + rank)   # weak scaling: every rank its own block of the same shape
+    D, Ws, manifest = urban_sky()
+    nc, nDir = len(scene["P"]), len(D)
+    stream = torch.cuda.Stream()
+    e = pkg.engine()
+    e.set_stream(stream.cuda_stream)
+    e.build(scene["v"], scene["tri"])
+    flags = e.lib.ray_flags(False, False)
+    # pinned host copies of the step's inputs (e2e) and outputs
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    P, N, Dp = pin(scene["P"]), pin(scene["N"]), pin(D)
+    Wp = [(pin(W), c) for W, c in Ws]
+    flush = torch.empty(int(512e6) // 4, dtype=torch.float32, device="cuda")   # > the 129 MB L2
+    e.set_scene(P, N, Dp)
+
+    def step_device():
+        e.trace(0, nc, flags)
+        for W, c in Wp:
+            e.reduce(nc, W, c)
+
+    def step_e2e():
+        e.set_scene(P, N, Dp)
+        step_device()
+
+    # roofline accounting: the instrumented traversal on the same inputs (untimed)
+    cnt = e.trace_counters(0, nc, flags)
+    for _ in range(args.warmup):
+        step_device()
+        step_e2e()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    st0 = e.stats()
+    times, ttrace = [], []
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            ev[0].record(stream)
+            e.trace(0, nc, flags)
+            ev[1].record(stream)
+            for W, c in Wp:
+                e.reduce(nc, W, c)
+            ev[2].record(stream)
+            ev[2].synchronize()
+            times.append(ev[0].elapsed_time(ev[2]))
+            ttrace.append(ev[0].elapsed_time(ev[1]))
+        e2e_t = []
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            step_e2e()
+            e2e_t.append((time.perf_counter() - t0) * 1000)
+    st1 = e.stats()
+    if world > 1:
+        torch.distributed.barrier()
+    ms = float(sum(times) / len(times))
+    ms_e2e = float(sum(e2e_t) / len(e2e_t))
+    if world > 1:
+        t = torch.tensor([ms, ms_e2e], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms, ms_e2e = t.tolist()
+    rays = nc * nDir
+    launches = (st1["launches"] - st0["launches"]) // args.steps + len(Wp)
+    # roofline of k_bits: algorithmic bytes = nodes x 80 + triangles tested x 48 + bits out + sensor reads per task
+    tasks = (nc + 31) // 32 * ((nDir + 31) // 32)
+    alg = cnt["nodes"] * 80 + cnt["tris"] * 48 + nc * ((nDir + 31) // 32) * 4 + tasks * 32 * 24
+    ms_trace = float(np.median(ttrace))
+    peak, kind = peaks()
+    achieved = alg / (ms_trace / 1000) / 1e9
+    traffic = profiled_traffic()
+    if rank == 0:
+        line = {"metric": "Mrays/s", "value": world * rays / (ms / 1000) / 1e6, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded urban block; the reference's direction table and weights, tests/golden/urban_sky)",
+                "config": {"workload": "urban block: 20x20 boxes, %d sensors, %d triangles, %d directions (%d sky + %d ground + %d sun), "
+                                       "trace + 4 reduces (radiation, irradiance, illuminance, sunhours)" %
+                                       (nc, len(scene["tri"]), nDir, manifest["dirs"]["sky"], manifest["dirs"]["ground"], manifest["dirs"]["sun"]),
+                           "rays_per_step": rays, "l2": "flushed between steps (512 MB write)", "parallelism": "replicas (weak)" if world > 1 else "1 GPU"},
+                "e2e": {"value": world * rays / (ms_e2e / 1000) / 1e6, "unit": "Mrays/s",
+                        "h2d_bytes_per_step": int(P.nbytes + N.nbytes + Dp.nbytes + sum(W.nbytes for W, _ in Wp)),
+                        "d2h_bytes_per_step": int(8 * nc * len(Wp))},
+                "gpu_launches": int(launches),
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                             "traffic": traffic, "peak_kind": kind, "kernel": "k_bits",
+                             "algorithmic_bytes_per_trace": alg, "nodes_visited": cnt["nodes"], "tris_tested": cnt["tris"],
+                             "rays_traced": cnt["rays"], "trace_ms": ms_trace, "bvh_bytes": cnt["bvh_bytes"]},
+                "clocks": clk.summary()}
+        if not args.no_cpu_baseline:
+            v, dt = cpu_baseline(pkg, scene, D, Ws, args.cpu_sample)
+            line["cpu_baseline"] = {"value": v, "unit": "Mrays/s", "cores": os.cpu_count(), "kind": "port",
+                                    "sample": "%d seeded sensors of the block x %d directions + the 4 reduces (%.1f s)" % (args.cpu_sample, nDir, dt)}
+        print(json.dumps(line), flush=True)
+    e.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-sample", type=int, default=3000)
+    ap.add_argument("--ref-sample", type=int, default=2000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    pkg = package()
+    if args.impl == "reference":
+        run_reference(args, pkg)
+    else:
+        run_ours(args, pkg)
+
+
+if __name__ == "__main__":
+    main()

@@ -186,6 +186,15 @@ KGB_API uint32_t kgb_bounce_flags(int cullBackfaces);
  * out[5] = 1 when the last trace wrote bytes. */
 KGB_API void kgb_dims(const kgb_engine* e, uint64_t out[6]);
 
+/* --- no reference counterpart ---------------------------------------------------------------------------------- */
+/* The CUDA stream (a cudaStream_t) the engine's work runs on from now on; NULL: the engine's own stream. Calls still
+ * return after their work is done; a caller times them with events on this stream. */
+KGB_API int kgb_set_stream(kgb_engine* e, void* stream);
+/* Instrumentation for the traversal roofline: traces sensors [i0, i0+nc) exactly as kgb_trace does (same bits / bytes
+ * left on the device) with counting kernels, out[0] = BVH nodes visited, out[1] = triangles tested, out[2] = rays
+ * traced past the hemisphere cull, out[3] = BVH bytes (nodes + triangle records). */
+KGB_API int kgb_trace_counters(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, uint64_t out[4]);
+
 #ifdef __cplusplus
 }
 #endif

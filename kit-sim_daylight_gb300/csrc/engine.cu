@@ -1,0 +1,541 @@
+// The engine's C ABI (include/kitsim_gb300.h): device state, buffers, launch policy and the calls that replace the
+// reference's gpu_* contract (src/internal.h:125-220, implemented there by src/gpu.cu over OptiX).
+//
+// Device state per engine: one CUDA stream; the scene (8-wide BVH nodes + triangle records, a movable object so that
+// scenes can be parked and re-attached); the slot table; resident sensors (P, N) and directions (D); the chunk buffers
+// (visibility bits / bytes, reflected-light rows, view classes + distances), grown on demand and kept between calls;
+// a control block (task counter + status word) for the persistent kernels.
+// Every call returns after its work is done (as the reference's synchronous calls do), so host arrays may be reused.
+#include "engine.h"
+#include "rt.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+
+namespace kgb {
+namespace {
+
+thread_local std::string g_err;
+int fail(const std::string& m) { g_err = m; return 0; }
+
+#define CU(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) return fail(std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+struct Buf {   // device buffer, grown as needed (contents not kept)
+  void* p = nullptr;
+  size_t cap = 0;
+  void free() { if (p) cudaFree(p); p = nullptr; cap = 0; }
+};
+int grow(Buf& b, size_t bytes) {
+  if (bytes <= b.cap) return 1;
+  b.free();
+  CU(cudaMalloc(&b.p, std::max<size_t>(bytes, 256)));
+  b.cap = std::max<size_t>(bytes, 256);
+  return 1;
+}
+int upload(Buf& b, const void* h, size_t bytes, cudaStream_t st) {
+  if (!grow(b, bytes)) return 0;
+  if (bytes) CU(cudaMemcpyAsync(b.p, h, bytes, cudaMemcpyHostToDevice, st));
+  return 1;
+}
+
+struct SceneObj {
+  Buf nodes, tris;
+  uint32_t nNodes = 0, nTris = 0;
+  uint64_t bytes = 0;
+  ~SceneObj() { nodes.free(); tris.free(); }
+};
+
+}  // namespace
+
+struct Engine {
+  int device = 0, numSMs = 0;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev[2] = {};
+  SceneObj* sc = nullptr;
+  Buf slots;
+  uint32_t nSlots = 0;
+  Buf P, N, D;
+  size_t nSensors = 0, nDir = 0, nWords = 0;
+  Buf vis;
+  bool bytes = false;
+  size_t i0 = 0, visN = 0;
+  Buf dc;
+  size_t nBins = 0, dcN = 0, dcI0 = 0;
+  Buf viewCls, viewDist, rowSin;
+  size_t viewN = 0, viewK = 0, viewI0 = 0;
+  kgb_view_in view{};
+  Buf label;
+  size_t nLabel = 0;
+  Buf scratch, out;
+  Buf ctl;   // [0] task counter, [1] status, [2..7] three u64 counters of the instrumented kernels
+  bool ownStream = true;
+  kgb_stats stats{};
+  int gridBits = 0, gridView = 0;
+};
+
+namespace {
+
+Engine* E(kgb_engine* e) { return reinterpret_cast<Engine*>(e); }
+const Engine* E(const kgb_engine* e) { return reinterpret_cast<const Engine*>(e); }
+
+int sync_status(Engine& g) {   // wait for the stream, then read the kernels' status word
+  uint32_t status = 0;
+  CU(cudaMemcpyAsync(&status, static_cast<uint32_t*>(g.ctl.p) + 1, 4, cudaMemcpyDeviceToHost, g.st));
+  CU(cudaStreamSynchronize(g.st));
+  CU(cudaGetLastError());
+  if (status & kStatusStackOverflow) return fail("traversal stack overflow (BVH deeper than the kernel's stack)");
+  return 1;
+}
+int reset_ctl(Engine& g) {
+  CU(cudaMemsetAsync(g.ctl.p, 0, 32, g.st));
+  return 1;
+}
+float elapsed(Engine& g) {
+  float ms = 0;
+  cudaEventElapsedTime(&ms, g.ev[0], g.ev[1]);
+  return ms;
+}
+
+}  // namespace
+}  // namespace kgb
+
+using namespace kgb;
+
+extern "C" {
+
+KGB_API int32_t kgb_version(void) { return KGB_ABI_VERSION; }
+KGB_API const char* kgb_last_error(void) { return g_err.c_str(); }
+
+KGB_API kgb_engine* kgb_init(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) { fail("no CUDA device"); return nullptr; }
+  Engine* g = new Engine;
+  const auto bad = [&](const std::string& m) { fail(m); kgb_destroy(reinterpret_cast<kgb_engine*>(g)); return nullptr; };
+  if (cudaGetDevice(&g->device) != cudaSuccess) return bad("cudaGetDevice failed");
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, g->device) != cudaSuccess) return bad("cudaGetDeviceProperties failed");
+  if (prop.major < 10) return bad(std::string("the engine is built for sm_103a; device is ") + prop.name);
+  g->numSMs = prop.multiProcessorCount;
+  if (cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking) != cudaSuccess) return bad("cudaStreamCreate failed");
+  if (cudaEventCreate(&g->ev[0]) != cudaSuccess || cudaEventCreate(&g->ev[1]) != cudaSuccess) return bad("cudaEventCreate failed");
+  if (!grow(g->ctl, 64)) return bad(g_err);
+  g->sc = new SceneObj;
+  const kgb_slot one{0.2f, 0.f, 0.f, 0u};
+  if (!kgb_set_slots(reinterpret_cast<kgb_engine*>(g), &one, 1)) return bad(g_err);
+  return reinterpret_cast<kgb_engine*>(g);
+}
+
+KGB_API void kgb_destroy(kgb_engine* e) {
+  if (!e) return;
+  Engine* g = E(e);
+  if (g->st) cudaStreamSynchronize(g->st);
+  delete g->sc;
+  for (Buf* b : {&g->slots, &g->P, &g->N, &g->D, &g->vis, &g->dc, &g->viewCls, &g->viewDist, &g->rowSin, &g->label, &g->scratch, &g->out, &g->ctl}) b->free();
+  for (cudaEvent_t ev : g->ev) if (ev) cudaEventDestroy(ev);
+  if (g->st && g->ownStream) cudaStreamDestroy(g->st);
+  delete g;
+}
+
+// Device bytes a build of nt triangles over nv vertices peaks at: inputs stay on the host (the builder runs there),
+// the device holds the triangle records (48 B each) and at most nt/2 + 2 nodes of 80 B; counted twice (the new scene
+// and a parked one may coexist during a swap).
+KGB_API uint64_t kgb_build_bytes(kgb_engine*, size_t nv, size_t nt, int slotted) {
+  if (!nt) return 0;
+  const uint64_t inputs = uint64_t(nv) * 12 + uint64_t(nt) * (12 + (slotted ? 4 : 0));
+  const uint64_t out = uint64_t(nt) * 64 + (uint64_t(nt) / 2 + 2) * 80 + 4096;
+  return inputs + 2 * out;
+}
+
+KGB_API int kgb_build(kgb_engine* e, const float* v, size_t nv, const uint32_t* tri, size_t nt, const uint32_t* slot,
+                      const kgb_slot* slots, size_t nSlots, int perSlot) {
+  Engine& g = *E(e);
+  delete g.sc;
+  g.sc = new SceneObj;
+  g.stats.gasBytes = 0;
+  if (!nt) return 1;   // empty scene: every ray misses
+  if (slot) for (size_t k = 0; k < nt; ++k) if (slot[k] >= nSlots) return fail("gpu_build: a triangle's slot has no Slot");
+  bool anyTau = false;
+  for (size_t s = 0; s < nSlots; ++s) anyTau = anyTau || slots[s].tau > 0;
+  const bool slotted = perSlot || anyTau;
+  if (slotted && !slot) return fail("gpu_build: per-slot records need a slot per triangle");
+  if (nt > (size_t(1) << 31)) return fail("gpu_build: more than 2^31 triangles");
+  for (size_t k = 0; k < 3 * nt; ++k) if (tri[k] >= nv) return fail("gpu_build: a triangle's vertex index exceeds the vertices");
+  CU(cudaEventRecord(g.ev[0], g.st));
+  std::vector<uint8_t> translucent;
+  if (slotted) {
+    translucent.resize(nt);
+    for (size_t k = 0; k < nt; ++k) translucent[k] = slots[slot[k]].tau > 0 ? 1 : 0;
+  }
+  BvhOut b;
+  build_bvh8(v, nv, tri, nt, slotted ? slot : nullptr, slotted ? translucent.data() : nullptr, b);
+  SceneObj& s = *g.sc;
+  if (!upload(s.nodes, b.nodes.data(), b.nodes.size() * 4, g.st) || !upload(s.tris, b.tris.data(), b.tris.size() * 4, g.st)) return 0;
+  s.nNodes = b.nNodes;
+  s.nTris = uint32_t(nt);
+  s.bytes = b.nodes.size() * 4 + b.tris.size() * 4;
+  CU(cudaEventRecord(g.ev[1], g.st));
+  CU(cudaStreamSynchronize(g.st));
+  g.stats.buildMs += elapsed(g);
+  g.stats.gasBytes = s.bytes;
+  g.stats.buildTempBytes = uint64_t(nt) * 64;
+  g.stats.buildOutputBytes = s.bytes;
+  return 1;
+}
+
+KGB_API void kgb_trim(kgb_engine* e, int sensors) {
+  Engine& g = *E(e);
+  cudaStreamSynchronize(g.st);
+  g.vis.free(); g.dc.free(); g.scratch.free(); g.out.free(); g.viewCls.free(); g.viewDist.free();
+  g.viewN = 0;
+  if (sensors) { g.P.free(); g.N.free(); g.label.free(); g.nLabel = 0; g.nSensors = 0; }
+}
+
+KGB_API int kgb_set_slots(kgb_engine* e, const kgb_slot* slots, size_t n) {
+  Engine& g = *E(e);
+  const kgb_slot one{0.2f, 0.f, 0.f, 0u};
+  if (!n) { slots = &one; n = 1; }
+  if (!upload(g.slots, slots, n * sizeof(kgb_slot), g.st)) return 0;
+  g.nSlots = uint32_t(n);
+  CU(cudaStreamSynchronize(g.st));
+  return 1;
+}
+
+KGB_API kgb_scene kgb_detach(kgb_engine* e) {
+  Engine& g = *E(e);
+  kgb_scene s{g.sc, g.sc->bytes};
+  g.sc = new SceneObj;
+  g.stats.gasBytes = 0;
+  return s;
+}
+KGB_API void kgb_attach(kgb_engine* e, kgb_scene s) {
+  Engine& g = *E(e);
+  cudaStreamSynchronize(g.st);
+  delete g.sc;
+  g.sc = s.handle ? static_cast<SceneObj*>(s.handle) : new SceneObj;
+  g.stats.gasBytes = g.sc->bytes;
+}
+KGB_API void kgb_free_scene(kgb_scene* s) {
+  if (!s) return;
+  delete static_cast<SceneObj*>(s->handle);
+  s->handle = nullptr;
+  s->bytes = 0;
+}
+KGB_API uint64_t kgb_free_bytes(void) {
+  size_t f = 0, t = 0;
+  return cudaMemGetInfo(&f, &t) == cudaSuccess ? f : 0;
+}
+
+KGB_API int kgb_set_scene(kgb_engine* e, const float* P, const float* N, size_t nSensors, const float* D, size_t nDir) {
+  Engine& g = *E(e);
+  g.nSensors = nSensors; g.nDir = nDir; g.nWords = (nDir + 31) / 32;
+  if (!upload(g.P, P, nSensors * 12, g.st) || !upload(g.N, N, nSensors * 12, g.st) || !upload(g.D, D, nDir * 12, g.st)) return 0;
+  CU(cudaStreamSynchronize(g.st));
+  return 1;
+}
+
+KGB_API int kgb_set_labels(kgb_engine* e, const uint8_t* label, size_t n) {
+  Engine& g = *E(e);
+  if (!upload(g.label, label, n, g.st)) return 0;
+  g.nLabel = n;
+  CU(cudaStreamSynchronize(g.st));
+  return 1;
+}
+
+// gpu.cu:499-531: sensors [i0, i0 + nc) in sub-launches sized from the previous one's time (first 4096 sensors, then
+// ~150 ms; byte mode 2^13 threads first and at least, then ~30 ms, at most doubling): the reference's stats and
+// cancel points. Each sub-launch is one persistent grid over its (32 sensors x word) tasks.
+static int trace_impl(Engine& g, size_t i0, size_t nc, uint32_t rayFlags, uint64_t* counters) {
+  if (i0 + nc > g.nSensors) return fail("gpu_trace: sensor range exceeds the scene");
+  g.bytes = !(rayFlags & KGB_RAY_DISABLE_ANYHIT);
+  if (!grow(g.vis, g.bytes ? g.nDir * nc : g.nWords * nc * 4)) return 0;
+  g.i0 = i0; g.visN = nc;
+  if (nc == 0 || g.nWords == 0) return 1;
+  if (!g.gridBits) g.gridBits = g.numSMs * 4;
+  const bool any = g.bytes;
+  const double targetMs = any ? 30 : 150;
+  const size_t nMin = any ? std::max<size_t>(1, (size_t(1) << 13) / g.nWords) : 1024;
+  size_t done = 0, n = counters ? nc : std::min(any ? nMin : size_t(4096), nc);
+  TraceArgs a{};
+  a.nodes = static_cast<const Node8*>(g.sc->nodes.p); a.tris = static_cast<const TriRec*>(g.sc->tris.p); a.nNodes = g.sc->nNodes;
+  a.P = static_cast<const float*>(g.P.p); a.N = static_cast<const float*>(g.N.p); a.D = static_cast<const float*>(g.D.p);
+  a.stride = uint32_t(nc); a.nDir = uint32_t(g.nDir); a.nWords = uint32_t(g.nWords); a.rayFlags = rayFlags;
+  a.bits = any ? nullptr : static_cast<uint32_t*>(g.vis.p);
+  a.bytes = any ? static_cast<uint8_t*>(g.vis.p) : nullptr;
+  a.slots = static_cast<const kgb_slot*>(g.slots.p); a.nSlots = g.nSlots;
+  a.counter = static_cast<uint32_t*>(g.ctl.p); a.status = static_cast<uint32_t*>(g.ctl.p) + 1;
+  while (done < nc) {
+    a.first = uint32_t(i0 + done); a.n = uint32_t(n); a.out0 = uint32_t(done);
+    if (!reset_ctl(g)) return 0;
+    const size_t tasks = (n + 31) / 32 * g.nWords;
+    const int grid = int(std::min<size_t>(size_t(g.gridBits), (tasks + 7) / 8));
+    CU(cudaEventRecord(g.ev[0], g.st));
+    if (any) launch_bytes(a, grid, g.st); else launch_bits(a, grid, g.st, counters != nullptr);
+    CU(cudaEventRecord(g.ev[1], g.st));
+    if (!sync_status(g)) return 0;
+    if (counters) {
+      uint64_t c[3];
+      CU(cudaMemcpy(c, static_cast<uint32_t*>(g.ctl.p) + 2, sizeof c, cudaMemcpyDeviceToHost));
+      for (int k = 0; k < 3; ++k) counters[k] += c[k];
+    }
+    const double ms = elapsed(g);
+    g.stats.traceMs += ms; g.stats.rays += n * g.nDir; g.stats.launches++;
+    done += n;
+    const double want = double(n) * targetMs / std::max(ms, 1e-3);
+    n = std::min({std::max<size_t>(want > 1e12 ? size_t(1) << 40 : size_t(want), nMin), any ? 2 * n : nc, nc - done});
+  }
+  return 1;
+}
+
+KGB_API int kgb_trace(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags) { return trace_impl(*E(e), i0, nc, rayFlags, nullptr); }
+
+KGB_API int kgb_trace_counters(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, uint64_t out[4]) {
+  Engine& g = *E(e);
+  if (!(rayFlags & KGB_RAY_DISABLE_ANYHIT)) return fail("kgb_trace_counters: visibility bits only (KGB_RAY_DISABLE_ANYHIT)");
+  out[0] = out[1] = out[2] = 0;
+  out[3] = g.sc->bytes;
+  return trace_impl(g, i0, nc, rayFlags, out);
+}
+
+KGB_API int kgb_set_stream(kgb_engine* e, void* stream) {
+  Engine& g = *E(e);
+  CU(cudaStreamSynchronize(g.st));
+  if (g.ownStream) CU(cudaStreamDestroy(g.st));
+  g.ownStream = stream == nullptr;
+  if (stream) g.st = static_cast<cudaStream_t>(stream);
+  else CU(cudaStreamCreateWithFlags(&g.st, cudaStreamNonBlocking));
+  return 1;
+}
+
+KGB_API int kgb_reduce(kgb_engine* e, size_t nc, const float* W, int useCos, double* out) {
+  Engine& g = *E(e);
+  if (nc == 0) return 1;
+  if (nc != g.visN) return fail("gpu_reduce: no trace of this chunk");
+  if (!upload(g.scratch, W, g.nDir * 4, g.st) || !grow(g.out, nc * 8)) return 0;
+  const float* N = static_cast<const float*>(g.N.p) + 3 * g.i0;
+  if (g.bytes) launch_reduce_bytes(static_cast<const uint8_t*>(g.vis.p), uint32_t(nc), uint32_t(g.nDir), N, static_cast<const float*>(g.D.p),
+                                   static_cast<const float*>(g.scratch.p), useCos, static_cast<double*>(g.out.p), g.st);
+  else launch_reduce_bits(static_cast<const uint32_t*>(g.vis.p), uint32_t(nc), uint32_t(g.nWords), N, static_cast<const float*>(g.D.p),
+                          static_cast<const float*>(g.scratch.p), useCos, static_cast<double*>(g.out.p), g.st);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(out, g.out.p, nc * 8, cudaMemcpyDeviceToHost, g.st));
+  CU(cudaStreamSynchronize(g.st));
+  return 1;
+}
+
+KGB_API int kgb_series(kgb_engine* e, size_t nc, const kgb_series_in* in, float* Eh) {
+  Engine& g = *E(e);
+  if (nc == 0 || in->T <= 0) return 1;
+  if (in->Sdc && nc != g.dcN) return fail("gpu_series: no gpu_bounce rows for this chunk");
+  if (nc != g.visN) return fail("gpu_series: no trace of this chunk");
+  const size_t T = size_t(in->T);
+  for (uint32_t d = 0; d < in->nSky; ++d) if (in->row[d] < 0 || in->row[d] >= in->P) return fail("gpu_series: a sky direction's row is not a patch");
+  for (uint32_t j = 0; j < in->nSun; ++j) if (in->sunStep[j] < 0 || size_t(in->sunStep[j]) >= T) return fail("gpu_series: a sun step is not a column");
+  if (in->nSky > g.nDir || size_t(in->sun0) + in->nSun > g.nDir) return fail("gpu_series: directions beyond the direction table");
+  // one packed upload: row | wsky | S | g | G | sunStep | sunVec | sunW | Sdc, each 256-byte aligned
+  const void* src[9] = {in->row, in->wsky, in->S, in->g, in->G, in->sunStep, in->sunVec, in->sunW, in->Sdc};
+  const size_t len[9] = {size_t(in->nSky) * 4, size_t(in->nSky) * 4, size_t(in->P) * T * 4, T * 4, nc * 4, size_t(in->nSun) * 4,
+                         size_t(in->nSun) * 12, size_t(in->nSun) * 4, in->Sdc ? g.nBins * T * 4 : 0};
+  size_t off[9], total = 0;
+  for (int k = 0; k < 9; ++k) { off[k] = total; total += (len[k] + 255) & ~size_t(255); }
+  if (!grow(g.scratch, total) || !grow(g.out, nc * T * 4)) return 0;
+  char* b = static_cast<char*>(g.scratch.p);
+  for (int k = 0; k < 9; ++k) if (len[k]) CU(cudaMemcpyAsync(b + off[k], src[k], len[k], cudaMemcpyHostToDevice, g.st));
+  SeriesArgs a{};
+  a.bits = g.bytes ? nullptr : static_cast<const uint32_t*>(g.vis.p);
+  a.bytes = g.bytes ? static_cast<const uint8_t*>(g.vis.p) : nullptr;
+  a.nc = uint32_t(nc); a.nDir = uint32_t(g.nDir); a.nSky = in->nSky; a.T = uint32_t(T); a.nSun = in->nSun; a.sun0 = in->sun0;
+  a.nBins = uint32_t(g.nBins);
+  a.N = static_cast<const float*>(g.N.p) + 3 * g.i0; a.D = static_cast<const float*>(g.D.p);
+  a.row = reinterpret_cast<const int32_t*>(b + off[0]); a.wsky = reinterpret_cast<const float*>(b + off[1]);
+  a.S = reinterpret_cast<const float*>(b + off[2]); a.g = reinterpret_cast<const float*>(b + off[3]); a.G = reinterpret_cast<const float*>(b + off[4]);
+  a.sunStep = reinterpret_cast<const int32_t*>(b + off[5]); a.sunVec = reinterpret_cast<const float*>(b + off[6]);
+  a.sunW = reinterpret_cast<const float*>(b + off[7]);
+  a.dc = in->Sdc ? static_cast<const float*>(g.dc.p) : nullptr;
+  a.Sdc = in->Sdc ? reinterpret_cast<const float*>(b + off[8]) : nullptr;
+  a.E = static_cast<float*>(g.out.p);
+  launch_series_fp32(a, g.st);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(Eh, g.out.p, nc * T * 4, cudaMemcpyDeviceToHost, g.st));
+  CU(cudaStreamSynchronize(g.st));
+  return 1;
+}
+
+// gpu.cu:533-568: the whole chunk over sample ranges [done, done + n): n from 2^13 / nc (1..64), then ~100 ms, at most
+// doubling; cancel between launches. Each thread adds to its sensor's rows in sample order: deterministic.
+KGB_API int kgb_bounce(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, const kgb_bounce_in* b) {
+  Engine& g = *E(e);
+  if (i0 + nc > g.nSensors) return fail("gpu_bounce: sensor range exceeds the scene");
+  const uint32_t mf = uint32_t(b->mf);
+  g.nBins = size_t(144 * mf * mf + 1) + 1; g.dcN = nc; g.dcI0 = i0;
+  if (!grow(g.dc, g.nBins * nc * 4)) return 0;
+  if (nc == 0) return 1;
+  CU(cudaMemsetAsync(g.dc.p, 0, g.nBins * nc * 4, g.st));
+  const double rad = b->north * KGB_PI_D / 180;
+  BounceArgs a{};
+  a.nodes = static_cast<const Node8*>(g.sc->nodes.p); a.tris = static_cast<const TriRec*>(g.sc->tris.p); a.nNodes = g.sc->nNodes;
+  a.P = static_cast<const float*>(g.P.p); a.N = static_cast<const float*>(g.N.p);
+  a.i0 = uint32_t(i0); a.n = uint32_t(nc); a.nc = uint32_t(nc);
+  a.M = b->M; a.nBounce = b->N; a.mf = mf; a.nBins = uint32_t(g.nBins);
+  a.alpha = float((KGB_PI_D / 2.) / (7 * mf + .5)); a.cosN = float(std::cos(rad)); a.sinN = float(std::sin(rad));
+  a.rayFlags = rayFlags; a.slots = static_cast<const kgb_slot*>(g.slots.p); a.nSlots = g.nSlots;
+  a.dc = static_cast<float*>(g.dc.p); a.status = static_cast<uint32_t*>(g.ctl.p) + 1;
+  for (size_t done = 0, n = std::clamp<size_t>((size_t(1) << 13) / nc, 1, 64); done < b->M;) {
+    if (b->cancel && b->cancel(b->cancelCtx)) return fail("cancelled");
+    n = std::min<size_t>(n, b->M - done);
+    a.s0 = uint32_t(done); a.s1 = uint32_t(done + n);
+    if (!reset_ctl(g)) return 0;
+    CU(cudaEventRecord(g.ev[0], g.st));
+    launch_bounce(a, g.st);
+    CU(cudaEventRecord(g.ev[1], g.st));
+    if (!sync_status(g)) return 0;
+    const double ms = elapsed(g);
+    g.stats.bounceMs += ms; g.stats.paths += n * nc; g.stats.bounceLaunches++;
+    done += n;
+    const double want = double(n) * 100 / std::max(ms, 1e-3);
+    n = std::max<size_t>(1, std::min<size_t>(2 * n, want > 1e9 ? size_t(1e9) : size_t(want)));
+  }
+  return 1;
+}
+
+KGB_API int kgb_reduce_dc(kgb_engine* e, size_t nc, const float* W, double* out) {
+  Engine& g = *E(e);
+  if (nc == 0) return 1;
+  if (nc != g.dcN) return fail("gpu_reduce_dc: no gpu_bounce rows for this chunk");
+  if (!upload(g.scratch, W, g.nBins * 4, g.st) || !grow(g.out, nc * 8)) return 0;
+  launch_reduce_dc(static_cast<const float*>(g.dc.p), uint32_t(nc), uint32_t(g.nBins), static_cast<const float*>(g.scratch.p), static_cast<double*>(g.out.p), g.st);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(out, g.out.p, nc * 8, cudaMemcpyDeviceToHost, g.st));
+  CU(cudaStreamSynchronize(g.st));
+  return 1;
+}
+
+KGB_API int kgb_download_dc(kgb_engine* e, size_t nc, float* out, size_t count) {
+  Engine& g = *E(e);
+  if (nc != g.dcN) return fail("gpu_download_dc: no gpu_bounce rows for this chunk");
+  if (count != g.nBins * nc) return fail("gpu_download_dc: wrong element count");
+  if (count) CU(cudaMemcpyAsync(out, g.dc.p, count * 4, cudaMemcpyDeviceToHost, g.st));
+  CU(cudaStreamSynchronize(g.st));
+  return 1;
+}
+KGB_API int kgb_download_bits(kgb_engine* e, size_t nc, uint32_t* out, size_t count) {
+  Engine& g = *E(e);
+  if (g.bytes) return fail("gpu_download_bits: the last trace wrote bytes");
+  if (count != g.nWords * nc || nc != g.visN) return fail("gpu_download_bits: wrong element count");
+  if (count) CU(cudaMemcpyAsync(out, g.vis.p, count * 4, cudaMemcpyDeviceToHost, g.st));
+  CU(cudaStreamSynchronize(g.st));
+  return 1;
+}
+KGB_API int kgb_download_bytes(kgb_engine* e, size_t nc, uint8_t* out, size_t count) {
+  Engine& g = *E(e);
+  if (!g.bytes) return fail("gpu_download_bytes: the last trace wrote bits");
+  if (count != g.nDir * nc || nc != g.visN) return fail("gpu_download_bytes: wrong element count");
+  if (count) CU(cudaMemcpyAsync(out, g.vis.p, count, cudaMemcpyDeviceToHost, g.st));
+  CU(cudaStreamSynchronize(g.st));
+  return 1;
+}
+
+// gpu.cu:572-610: sub-launches of 2^13 threads first and at least, then ~40 ms, at most doubling, the size carried
+// from chunk to chunk in *launch; cancel between them.
+KGB_API int kgb_view(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, const kgb_view_in* v, size_t* launch) {
+  Engine& g = *E(e);
+  if (i0 + nc > g.nSensors) return fail("gpu_view: sensor range exceeds the scene");
+  const size_t K = size_t(v->nAz) * v->nEl, nWords = (K + 31) / 32;
+  if (g.nLabel && g.nLabel < g.sc->nTris) return fail("gpu_view: fewer labels than the scene's triangles");
+  if (!grow(g.viewCls, K * nc) || !grow(g.viewDist, K * nc * 4) || !upload(g.rowSin, v->rowSin, size_t(v->nEl) * 8, g.st)) return 0;
+  g.viewN = nc; g.viewK = K; g.viewI0 = i0; g.view = *v; g.view.rowSin = nullptr;
+  if (nc == 0 || K == 0) { CU(cudaStreamSynchronize(g.st)); return 1; }
+  if (!g.gridView) g.gridView = g.numSMs * 4;
+  const double rad = v->north * KGB_PI_D / 180;
+  ViewArgs a{};
+  a.nodes = static_cast<const Node8*>(g.sc->nodes.p); a.tris = static_cast<const TriRec*>(g.sc->tris.p); a.nNodes = g.sc->nNodes;
+  a.P = static_cast<const float*>(g.P.p); a.N = static_cast<const float*>(g.N.p);
+  a.stride = uint32_t(nc); a.i0 = uint32_t(i0); a.K = uint32_t(K); a.nWords = uint32_t(nWords); a.nAz = v->nAz; a.nEl = v->nEl;
+  a.rayFlags = rayFlags; a.rowSin = static_cast<const float*>(g.rowSin.p); a.az0 = v->az0; a.dAz = v->dAz; a.groundZ = v->groundZ;
+  a.cosN = float(std::cos(rad)); a.sinN = float(std::sin(rad));
+  a.world = v->world ? 1 : 0; a.cull = v->cull ? 1 : 0; a.jitter = v->jitter ? 1 : 0; a.nS = v->nS; a.back = v->back ? 1 : 0;
+  a.vground = v->vground ? 1 : 0;
+  a.label = g.nLabel ? static_cast<const uint8_t*>(g.label.p) : nullptr;
+  a.cls = static_cast<uint8_t*>(g.viewCls.p); a.dist = static_cast<float*>(g.viewDist.p);
+  a.counter = static_cast<uint32_t*>(g.ctl.p); a.status = static_cast<uint32_t*>(g.ctl.p) + 1;
+  const size_t nMin = std::max<size_t>(1, (size_t(1) << 13) / nWords);
+  size_t n = std::max(*launch, nMin);
+  for (size_t done = 0; done < nc;) {
+    if (v->cancel && v->cancel(v->cancelCtx)) return fail("cancelled");
+    const size_t m = std::min(n, nc - done);
+    a.first = uint32_t(i0 + done); a.n = uint32_t(m); a.out0 = uint32_t(done);
+    if (!reset_ctl(g)) return 0;
+    const size_t tasks = (m + 31) / 32 * nWords;
+    const int grid = int(std::min<size_t>(size_t(g.gridView), (tasks + 7) / 8));
+    CU(cudaEventRecord(g.ev[0], g.st));
+    launch_view(a, grid, g.st);
+    CU(cudaEventRecord(g.ev[1], g.st));
+    if (!sync_status(g)) return 0;
+    const double ms = elapsed(g);
+    g.stats.traceMs += ms; g.stats.rays += m * K; g.stats.launches++;
+    done += m;
+    const double want = double(m) * 40 / std::max(ms, 1e-3);
+    n = std::max(nMin, std::min(2 * n, want > 1e12 ? size_t(1) << 40 : size_t(want)));
+  }
+  *launch = n;
+  return 1;
+}
+
+KGB_API int kgb_reduce_view(kgb_engine* e, size_t nc, const double* wRow, size_t nRow, uint32_t nClass, double farDist,
+                            const float* reach, size_t nReach, int glazing, uint32_t isoDim, double* out) {
+  Engine& g = *E(e);
+  if (nc == 0) return 1;
+  if (nc != g.viewN) return fail("gpu_reduce_view: no gpu_view for this chunk");
+  if (nClass > KGB_VIEW_CLASSES || nReach > 8) return fail("gpu_reduce_view: at most 16 groups and 8 reach distances");
+  const size_t NA = 3 * size_t(nClass) + 1 + nReach + (glazing ? 1 : 0) + (isoDim ? 1 : 0);
+  if (nRow < g.view.nEl) return fail("gpu_reduce_view: fewer row weights than rows");
+  if (!upload(g.scratch, wRow, nRow * 8, g.st) || !grow(g.out, nc * NA * 8)) return 0;
+  ViewReduceArgs a{};
+  a.cls = static_cast<const uint8_t*>(g.viewCls.p); a.dist = static_cast<const float*>(g.viewDist.p);
+  a.nc = uint32_t(nc); a.K = uint32_t(g.viewK); a.nAz = g.view.nAz; a.nEl = g.view.nEl; a.nClass = nClass; a.nReach = uint32_t(nReach);
+  a.glazing = glazing ? 1 : 0; a.iso = isoDim ? 1 : 0; a.NA = uint32_t(NA);
+  a.wRow = static_cast<const double*>(g.scratch.p); a.farDist = float(farDist); a.lnFar = std::log(farDist);
+  for (size_t r = 0; r < nReach; ++r) a.reach[r] = reach[r];
+  a.isoDim = isoDim; a.world = g.view.world ? 1 : 0; a.jitter = g.view.jitter ? 1 : 0; a.i0 = uint32_t(g.viewI0); a.nS = g.view.nS;
+  a.back = g.view.back ? 1 : 0; a.az0 = g.view.az0; a.dAz = g.view.dAz; a.rowSin = static_cast<const float*>(g.rowSin.p);
+  a.out = static_cast<double*>(g.out.p);
+  launch_reduce_view(a, g.st);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(out, g.out.p, nc * NA * 8, cudaMemcpyDeviceToHost, g.st));
+  CU(cudaStreamSynchronize(g.st));
+  return 1;
+}
+
+KGB_API int kgb_download_view(kgb_engine* e, size_t nc, uint8_t* cls, float* dist, size_t count) {
+  Engine& g = *E(e);
+  if (nc != g.viewN) return fail("gpu_download_view: no gpu_view for this chunk");
+  const size_t K = g.viewK;
+  if (count != nc * K) return fail("gpu_download_view: wrong element count");
+  std::vector<uint8_t> c(count);
+  std::vector<float> t(count);
+  if (count) {
+    CU(cudaMemcpyAsync(c.data(), g.viewCls.p, count, cudaMemcpyDeviceToHost, g.st));
+    CU(cudaMemcpyAsync(t.data(), g.viewDist.p, count * 4, cudaMemcpyDeviceToHost, g.st));
+  }
+  CU(cudaStreamSynchronize(g.st));
+  for (size_t d = 0; d < K; ++d)
+    for (size_t i = 0; i < nc; ++i) { cls[i * K + d] = c[d * nc + i]; dist[i * K + d] = t[d * nc + i]; }
+  return 1;
+}
+
+KGB_API kgb_stats kgb_get_stats(const kgb_engine* e) { return E(e)->stats; }
+KGB_API uint32_t kgb_ray_flags(int cullBackfaces, int translucent) {
+  return KGB_RAY_TERMINATE_ON_FIRST_HIT | (translucent ? 0u : KGB_RAY_DISABLE_ANYHIT) | (cullBackfaces ? KGB_RAY_CULL_BACK_FACING : 0u);
+}
+KGB_API uint32_t kgb_bounce_flags(int cullBackfaces) { return KGB_RAY_DISABLE_ANYHIT | (cullBackfaces ? KGB_RAY_CULL_BACK_FACING : 0u); }
+KGB_API void kgb_dims(const kgb_engine* e, uint64_t out[6]) {
+  const Engine& g = *E(e);
+  out[0] = g.nSensors; out[1] = g.nDir; out[2] = g.nWords; out[3] = g.nBins; out[4] = g.viewK; out[5] = g.bytes ? 1 : 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,126 @@
+// Internal interface between the engine's translation units: launch argument blocks of the kernels and the host
+// BVH builder. Not part of the public ABI (include/kitsim_gb300.h is).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+#include <vector>
+#include "kitsim_gb300.h"
+
+namespace kgb {
+
+struct Node8;
+struct TriRec;
+
+enum : uint32_t { kStatusStackOverflow = 1u };
+
+// k_bits / k_bytes: sensors [first, first + n) of the engine's arrays, written to columns [out0, out0 + n) of a chunk
+// whose row stride is `stride` sensors.
+struct TraceArgs {
+  const Node8* nodes;
+  const TriRec* tris;
+  uint32_t nNodes;
+  const float* P;
+  const float* N;
+  const float* D;
+  uint32_t first, n, out0, stride;
+  uint32_t nDir, nWords, rayFlags;
+  uint32_t* bits;
+  uint8_t* bytes;
+  const kgb_slot* slots;
+  uint32_t nSlots;
+  uint32_t* counter;
+  uint32_t* status;
+};
+
+struct ViewArgs {
+  const Node8* nodes;
+  const TriRec* tris;
+  uint32_t nNodes;
+  const float* P;
+  const float* N;
+  uint32_t first, n, out0, stride, i0;
+  uint32_t K, nWords, nAz, nEl, rayFlags;
+  const float* rowSin;   // device [2 nEl]
+  float az0, dAz, groundZ, cosN, sinN;
+  uint32_t world, cull, jitter, nS, back, vground;
+  const uint8_t* label;  // device, null: every hit an obstruction
+  uint8_t* cls;
+  float* dist;
+  uint32_t* counter;
+  uint32_t* status;
+};
+
+struct BounceArgs {
+  const Node8* nodes;
+  const TriRec* tris;
+  uint32_t nNodes;
+  const float* P;
+  const float* N;
+  uint32_t i0, n, nc;
+  uint32_t s0, s1, M, nBounce, mf, nBins;
+  float alpha, cosN, sinN;
+  uint32_t rayFlags;
+  const kgb_slot* slots;
+  uint32_t nSlots;
+  float* dc;
+  uint32_t* status;
+};
+
+void launch_bits(const TraceArgs& a, int grid, cudaStream_t st, bool count = false);
+void launch_bytes(const TraceArgs& a, int grid, cudaStream_t st);
+void launch_view(const ViewArgs& a, int grid, cudaStream_t st);
+void launch_bounce(const BounceArgs& a, cudaStream_t st);
+
+// reductions (reduce.cu)
+void launch_reduce_bits(const uint32_t* bits, uint32_t nc, uint32_t nWords, const float* N, const float* D, const float* W, int useCos,
+                        double* out, cudaStream_t st);
+void launch_reduce_bytes(const uint8_t* bytes, uint32_t nc, uint32_t nDir, const float* N, const float* D, const float* W, int useCos,
+                         double* out, cudaStream_t st);
+void launch_reduce_dc(const float* dc, uint32_t nc, uint32_t nBins, const float* W, double* out, cudaStream_t st);
+struct ViewReduceArgs {
+  const uint8_t* cls;
+  const float* dist;
+  uint32_t nc, K, nAz, nEl, nClass, nReach, glazing, iso, NA;
+  const double* wRow;
+  float farDist;
+  double lnFar;
+  float reach[8];
+  // isovist
+  uint32_t isoDim, world, jitter, i0, nS, back;
+  float az0, dAz;
+  const float* rowSin;
+  double* out;
+};
+void launch_reduce_view(const ViewReduceArgs& a, cudaStream_t st);
+
+// time series (series.cu): the plain FP32 form, visibility bits or bytes
+struct SeriesArgs {
+  const uint32_t* bits;
+  const uint8_t* bytes;
+  uint32_t nc, nDir, nSky, T, nSun, sun0, nBins;
+  const float* N;
+  const float* D;
+  const int32_t* row;
+  const float* wsky;
+  const float* S;
+  const float* g;
+  const float* G;
+  const int32_t* sunStep;
+  const float* sunVec;
+  const float* sunW;
+  const float* dc;     // null: no reflected light
+  const float* Sdc;
+  float* E;
+};
+void launch_series_fp32(const SeriesArgs& a, cudaStream_t st);
+
+// host BVH builder (bvh_build.cpp): binned-SAH binary BVH, collapsed to the 8-wide quantised layout of rt.cuh
+struct BvhOut {
+  std::vector<uint32_t> nodes;   // 20 words per node
+  std::vector<float> tris;       // 12 words per triangle record
+  uint32_t nNodes = 0;
+};
+void build_bvh8(const float* v, size_t nv, const uint32_t* tri, size_t nt, const uint32_t* slot, const uint8_t* translucent, BvhOut& out);
+
+}  // namespace kgb

@@ -1,0 +1,170 @@
+// Accumulation kernels over the visibility the ray-casting kernels leave on the device (compiled with -fmad=false):
+//  k_reduce_bits / k_reduce_bytes / k_reduce_dc  out[i] = sum over d (or bins) in order of
+//      double(float(max(0, N_i . D_d) x T) ) x W[d]   (replaces the reference's k_reduce, gpu.cu:99-114)
+//  k_view_reduce  per sensor and class: weight, weight x ln d, min d; own weight; reach; glazing (replaces k_view,
+//      gpu.cu:238-274), one warp per sensor, lane l summing d = l, l + 32, ..., then a fixed shuffle tree
+//  k_iso          the isovist area / volume through the rays' end points (replaces k_iso + iso_lane, gpu.cu:187-236)
+// The summation orders are fixed (direction order per thread; lane order + shuffle tree per warp), so a sensor's
+// doubles do not depend on the chunk it is in, and equal the oracle's restatement bit for bit.
+#include "engine.h"
+#include "rt.cuh"
+
+namespace kgb {
+
+__device__ __forceinline__ float dotf(F3 a, F3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }   // per-op rounding (gpu.cu:69-72)
+
+__global__ void __launch_bounds__(256) k_reduce_bits(const uint32_t* __restrict__ bits, uint32_t nc, uint32_t nWords, const float* __restrict__ N,
+                                                     const float* __restrict__ D, const float* __restrict__ W, int useCos, double* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  const F3 n = ld3(N + 3 * size_t(i));
+  double acc = 0;
+  for (uint32_t w = 0; w < nWords; ++w) {
+    uint32_t m = bits[size_t(w) * nc + i];
+    while (m) {
+      const uint32_t d = w * 32 + (__ffs(m) - 1);
+      m &= m - 1;
+      const float c = useCos ? fmaxf(dotf(n, ld3(D + 3 * d)), 0.f) : 1.f;
+      acc += (double)(c * 1.f) * (double)__ldg(W + d);
+    }
+  }
+  out[i] = acc;
+}
+
+__global__ void __launch_bounds__(256) k_reduce_bytes(const uint8_t* __restrict__ bytes, uint32_t nc, uint32_t nDir, const float* __restrict__ N,
+                                                      const float* __restrict__ D, const float* __restrict__ W, int useCos, double* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  const F3 n = ld3(N + 3 * size_t(i));
+  double acc = 0;
+  for (uint32_t d = 0; d < nDir; ++d) {
+    const uint32_t b = bytes[size_t(d) * nc + i];
+    if (!b) continue;
+    const float at = float(b) / 255.f;
+    const float c = useCos ? fmaxf(dotf(n, ld3(D + 3 * d)), 0.f) : 1.f;
+    acc += (double)(c * at) * (double)__ldg(W + d);
+  }
+  out[i] = acc;
+}
+
+__global__ void __launch_bounds__(256) k_reduce_dc(const float* __restrict__ dc, uint32_t nc, uint32_t nBins, const float* __restrict__ W, double* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  double acc = 0;
+  for (uint32_t b = 0; b < nBins; ++b) acc += (double)(1.f * dc[size_t(b) * nc + i]) * (double)__ldg(W + b);
+  out[i] = acc;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (uint32_t s = 16; s; s >>= 1) v += __shfl_down_sync(~0u, v, s);
+  return v;
+}
+
+__global__ void __launch_bounds__(256) k_view_reduce(ViewReduceArgs a) {
+  const uint32_t i = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x & 31;
+  if (i >= a.nc) return;   // whole warps
+  double w[KGB_VIEW_CLASSES], wl[KGB_VIEW_CLASSES], rc[8], own = 0, gz = 0;
+  float mn[KGB_VIEW_CLASSES];
+#pragma unroll
+  for (uint32_t c = 0; c < KGB_VIEW_CLASSES; ++c) { w[c] = 0; wl[c] = 0; mn[c] = __int_as_float(0x7f800000); }
+#pragma unroll
+  for (uint32_t r = 0; r < 8; ++r) rc[r] = 0;
+  for (uint32_t d = lane; d < a.K; d += 32) {
+    uint32_t c = a.cls[size_t(d) * a.nc + i];
+    const float t = a.dist[size_t(d) * a.nc + i];
+    const double wd = a.wRow[d / a.nAz];
+    if (c == 254) { own += wd; continue; }
+    if (c & KGB_VIEW_GLAZED) { gz += wd; c &= ~uint32_t(KGB_VIEW_GLAZED); }
+    const float dd = fminf(fmaxf(t, 0.1f), a.farDist);
+    const double ln = dd == a.farDist ? a.lnFar : dd == 0.1f ? -2.302585092994045684 : (double)kgb_logf(dd);
+    // class-indexed accumulators stay in registers: a select per class instead of an indexed store
+#pragma unroll
+    for (uint32_t q = 0; q < KGB_VIEW_CLASSES; ++q)
+      if (q == c) { w[q] += wd; wl[q] += wd * ln; mn[q] = fminf(mn[q], dd); }
+#pragma unroll
+    for (uint32_t r = 0; r < 8; ++r) if (r < a.nReach && t >= a.reach[r]) rc[r] += wd;
+  }
+  double* o = a.out + size_t(i) * a.NA;
+  for (uint32_t c = 0; c < a.nClass; ++c) {
+    float m = mn[c];
+    for (uint32_t s = 16; s; s >>= 1) m = fminf(m, __shfl_down_sync(~0u, m, s));
+    const double x = warp_sum(w[c]), y = warp_sum(wl[c]);
+    if (!lane) { o[3 * c] = x; o[3 * c + 1] = y; o[3 * c + 2] = m; }
+  }
+  const double ow = warp_sum(own);
+  if (!lane) o[3 * a.nClass] = ow;
+  for (uint32_t r = 0; r < a.nReach; ++r) {
+    const double x = warp_sum(rc[r]);
+    if (!lane) o[3 * a.nClass + 1 + r] = x;
+  }
+  if (a.glazing) {
+    const double x = warp_sum(gz);
+    if (!lane) o[3 * a.nClass + 1 + a.nReach] = x;
+  }
+}
+
+// view cell of direction d (the reference's view_cell, params.h:77-89), sincospif as kgb_sincospi
+__device__ __forceinline__ F3 iso_cell(uint32_t d, uint32_t col, float rsx, float rsy, float az0, float dAz, bool jitter, uint32_t element, uint32_t side) {
+  float a = 0.5f, s = 0.5f * (rsx + rsy);
+  if (jitter) { const U3 h = pcg3d(element, d, side); a = u01(h.x); s = rsx + u01(h.y) * (rsy - rsx); }
+  float sa, ca;
+  kgb_sincospi((az0 + (float(col) + a) * dAz) * (1.f / 180.f), &sa, &ca);
+  const float c = sqrtf(fmaxf(0.f, 1.f - s * s));
+  return f3(c * sa, c * ca, s);
+}
+__device__ __forceinline__ float det3(F3 a, F3 b, F3 c) {
+  const F3 u = sub(b, a), w = sub(c, a);
+  return a.x * (u.y * w.z - u.z * w.y) + a.y * (u.z * w.x - u.x * w.z) + a.z * (u.x * w.y - u.y * w.x);
+}
+
+__global__ void __launch_bounds__(256) k_iso(ViewReduceArgs a) {
+  const uint32_t i = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x & 31;
+  if (i >= a.nc) return;
+  const uint32_t gi = a.i0 + i, element = gi / a.nS, side = a.nS == 2 ? gi % 2 : a.back;
+  const auto len = [&](uint32_t k) {
+    const size_t at = size_t(k) * a.nc + i;
+    return a.cls[at] == 254 ? 0.f : fminf(a.dist[at], a.farDist);
+  };
+  double sum = 0;
+  for (uint32_t base = 0; base < a.nAz; base += 32) {   // every lane runs every round: the shuffles need them all
+    const uint32_t col = min(base + lane, a.nAz - 1), c1 = col + 1 == a.nAz ? 0 : col + 1;
+    const bool on = base + lane < a.nAz && (a.world || col + 1 < a.nAz);
+    const bool alone = lane == 31 || c1 == 0;
+    const auto pair = [&](uint32_t row) {
+      const float l = len(row * a.nAz + col), nb = __shfl_down_sync(~0u, l, 1);
+      return make_float2(l, alone ? len(row * a.nAz + c1) : nb);
+    };
+    F3 p = iso_cell(col, col, a.rowSin[0], a.rowSin[1], a.az0, a.dAz, a.jitter != 0, element, side);
+    F3 q = iso_cell(c1, c1, a.rowSin[0], a.rowSin[1], a.az0, a.dAz, a.jitter != 0, element, side);
+    float2 l0 = pair(0);
+    if (a.isoDim == 2) { if (on) sum += double(0.5f * l0.x * l0.y * (p.y * q.x - p.x * q.y)); continue; }
+    for (uint32_t r = 1; r < a.nEl; ++r) {
+      const uint32_t d = r * a.nAz + col;
+      const float2 l1 = pair(r);
+      const F3 c = iso_cell(d, col, a.rowSin[2 * r], a.rowSin[2 * r + 1], a.az0, a.dAz, a.jitter != 0, element, side);
+      const F3 e = iso_cell(d - col + c1, c1, a.rowSin[2 * r], a.rowSin[2 * r + 1], a.az0, a.dAz, a.jitter != 0, element, side);
+      if (on) sum += double(l0.x * l0.y * l1.x * det3(p, q, c) + l0.y * l1.y * l1.x * det3(q, e, c));
+      p = c; q = e; l0 = l1;
+    }
+  }
+  const double v = warp_sum(a.isoDim == 2 ? sum : sum / 6);
+  if (!lane) a.out[size_t(i) * a.NA + a.NA - 1] = v;
+}
+
+void launch_reduce_bits(const uint32_t* bits, uint32_t nc, uint32_t nWords, const float* N, const float* D, const float* W, int useCos,
+                        double* out, cudaStream_t st) {
+  k_reduce_bits<<<(nc + 255) / 256, 256, 0, st>>>(bits, nc, nWords, N, D, W, useCos, out);
+}
+void launch_reduce_bytes(const uint8_t* bytes, uint32_t nc, uint32_t nDir, const float* N, const float* D, const float* W, int useCos,
+                         double* out, cudaStream_t st) {
+  k_reduce_bytes<<<(nc + 255) / 256, 256, 0, st>>>(bytes, nc, nDir, N, D, W, useCos, out);
+}
+void launch_reduce_dc(const float* dc, uint32_t nc, uint32_t nBins, const float* W, double* out, cudaStream_t st) {
+  k_reduce_dc<<<(nc + 255) / 256, 256, 0, st>>>(dc, nc, nBins, W, out);
+}
+void launch_reduce_view(const ViewReduceArgs& a, cudaStream_t st) {
+  k_view_reduce<<<(a.nc + 7) / 8, 256, 0, st>>>(a);
+  if (a.isoDim) k_iso<<<(a.nc + 7) / 8, 256, 0, st>>>(a);
+}
+
+}  // namespace kgb

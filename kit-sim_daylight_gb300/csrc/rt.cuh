@@ -1,0 +1,335 @@
+// Device-side ray casting of the engine: the watertight ray/triangle test, the compressed 8-wide BVH traversal
+// (any-hit and closest-hit), and the reference's per-hit rules (own planes, glass, offsets, hashes).
+//
+// Numerics contract: the code deciding a result (hit or miss, t, own plane, transmittance byte, direction cell, sky
+// bin) is a fixed sequence of IEEE-754 float operations: this header is compiled with -fmad=false and divisions /
+// square roots are the correctly rounded ones, so the results equal a host restatement compiled without contraction
+// bit for bit. Box tests only filter: they are conservative (boxes expanded at build, see bvh_build.cpp) and may use
+// fused operations.
+#pragma once
+#include <cfloat>
+#include <cstdint>
+#include "kgb_detmath.h"
+#include "kitsim_gb300.h"
+
+namespace kgb {
+
+// ------------------------------------------------------------------------------------------------ data layout (HBM)
+// BVH8 node, 80 bytes = 5 x 16 B, read with five 128-bit loads:
+//   n0: p.x p.y p.z (float, the node box origin), e.x e.y e.z (biased float exponents of the child quantisation
+//       steps, byte 12..14), imask (byte 15: bit k = child k is an inner node)
+//   n1: childBase (index of the node's first inner child; its inner children are consecutive in slot order),
+//       triBase (index of the node's first triangle record), meta[8] (leaf child k: count << 5 | offset of its
+//       triangles from triBase; 0: empty slot)
+//   n2..n4: qlo.x[8] qlo.y[8] | qlo.z[8] qhi.x[8] | qhi.y[8] qhi.z[8] (child boxes: p + 2^(e-127) q)
+// Triangle record, 48 bytes = 3 x 16 B: v0.xyz + primitive index | v1.xyz + flags | v2.xyz + slot.
+struct __align__(16) Node8 { uint4 n[5]; };
+struct __align__(16) TriRec { float4 a, b, c; };
+enum : uint32_t { kTriTranslucent = 1u };   // TriRec.b.w flag bits: the slot transmitted at build (any-hit)
+
+struct F3 { float x, y, z; };
+__device__ __forceinline__ F3 f3(float x, float y, float z) { return F3{x, y, z}; }
+__device__ __forceinline__ F3 add(F3 a, F3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ F3 sub(F3 a, F3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ F3 mul(float s, F3 a) { return f3(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ float dot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float comp(F3 a, int k) { return k == 0 ? a.x : k == 1 ? a.y : a.z; }
+__device__ __forceinline__ F3 ld3(const float* p) { return f3(p[0], p[1], p[2]); }
+__device__ __forceinline__ float next_up(float t) { return __uint_as_float(__float_as_uint(t) + 1u); }
+
+// Waechter & Binder 2019 (Ray Tracing Gems, ch. 6), as the reference's offset_ray (trace_dev.cu:16-25).
+__device__ __forceinline__ F3 offset_ray(F3 p, F3 n) {
+  const float origin = 1.f / 32.f, floatScale = 1.f / 65536.f, intScale = 256.f;
+  const int ox = int(intScale * n.x), oy = int(intScale * n.y), oz = int(intScale * n.z);
+  const float px = __int_as_float(__float_as_int(p.x) + (p.x < 0.f ? -ox : ox));
+  const float py = __int_as_float(__float_as_int(p.y) + (p.y < 0.f ? -oy : oy));
+  const float pz = __int_as_float(__float_as_int(p.z) + (p.z < 0.f ? -oz : oz));
+  return f3(fabsf(p.x) < origin ? p.x + floatScale * n.x : px, fabsf(p.y) < origin ? p.y + floatScale * n.y : py,
+            fabsf(p.z) < origin ? p.z + floatScale * n.z : pz);
+}
+
+// Jarzynski & Olano 2020 (JCGT 9(3)): the reference's pcg3d / u01 (params.h:64-71).
+struct U3 { uint32_t x, y, z; };
+__device__ __forceinline__ U3 pcg3d(uint32_t x, uint32_t y, uint32_t z) {
+  x = x * 1664525u + 1013904223u; y = y * 1664525u + 1013904223u; z = z * 1664525u + 1013904223u;
+  x += y * z; y += z * x; z += x * y;
+  x ^= x >> 16; y ^= y >> 16; z ^= z >> 16;
+  x += y * z; y += z * x; z += x * y;
+  return U3{x, y, z};
+}
+__device__ __forceinline__ float u01(uint32_t v) { return float(v >> 8) * (1.f / 16777216.f); }
+
+// Radiance glass (the reference's glass_TR, glass.h:17-25; rad5R4 m_glass.c), powf as kgb_powf.
+__device__ __forceinline__ void glass_TR(float c, float tn, float& T, float& R) {
+  const float n = 1.52f;
+  const float c2 = sqrtf((1.f - 1.f / (n * n)) + c * c / (n * n));
+  const float d = kgb_powf(tn, 1.f / c2), d2 = d * d;
+  float rs = (c - n * c2) / (c + n * c2), rp = (c2 - n * c) / (c2 + n * c);
+  rs *= rs; rp *= rp;
+  T = .5f * (1.f - rs) * (1.f - rs) * d / (1.f - rs * rs * d2) + .5f * (1.f - rp) * (1.f - rp) * d / (1.f - rp * rp * d2);
+  R = .5f * rs * (1.f + (1.f - 2.f * rs) * d2) / (1.f - rs * rs * d2) + .5f * rp * (1.f + (1.f - 2.f * rp) * d2) / (1.f - rp * rp * d2);
+}
+
+// ------------------------------------------------------------------------------------------------ the ray
+struct Ray {
+  F3 o, d;
+  int kx, ky, kz;
+  float Sx, Sy, Sz;
+  F3 inv;     // box test: 1 / d with zero components replaced by +-2^-80
+  F3 oinv;    // o * inv
+  uint32_t oct;   // sign bits of d (closest-hit child order)
+};
+__device__ __forceinline__ Ray make_ray(F3 o, F3 d) {
+  Ray r;
+  r.o = o; r.d = d;
+  const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+  r.kz = ax >= ay ? (ax >= az ? 0 : 2) : (ay >= az ? 1 : 2);
+  r.kx = r.kz == 2 ? 0 : r.kz + 1;
+  r.ky = r.kx == 2 ? 0 : r.kx + 1;
+  if (comp(d, r.kz) < 0.f) { const int t = r.kx; r.kx = r.ky; r.ky = t; }
+  const float dz = comp(d, r.kz);
+  r.Sx = comp(d, r.kx) / dz;
+  r.Sy = comp(d, r.ky) / dz;
+  r.Sz = 1.f / dz;
+  const float tiny = 8.27180613e-25f;   // 2^-80
+  const float dx = ax > tiny ? d.x : copysignf(tiny, d.x), dy = ay > tiny ? d.y : copysignf(tiny, d.y), dzz = az > tiny ? d.z : copysignf(tiny, d.z);
+  r.inv = f3(1.f / dx, 1.f / dy, 1.f / dzz);
+  r.oinv = f3(o.x * r.inv.x, o.y * r.inv.y, o.z * r.inv.z);
+  r.oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
+  return r;
+}
+
+struct Hit { float t, u, v; uint32_t prim; bool front; };
+
+// Woop, Benthin, Wald 2013 (JCGT 2(1)) with a tie rule on edges: the same operation sequence as the oracle's hit_tri.
+__device__ __forceinline__ bool hit_tri(const Ray& r, F3 v0, F3 v1, F3 v2, float tmin, float tmax, bool cullBack, Hit& h) {
+  const F3 A = sub(v0, r.o), B = sub(v1, r.o), C = sub(v2, r.o);
+  const float Akz = comp(A, r.kz), Bkz = comp(B, r.kz), Ckz = comp(C, r.kz);
+  const float Ax = comp(A, r.kx) - r.Sx * Akz, Ay = comp(A, r.ky) - r.Sy * Akz;
+  const float Bx = comp(B, r.kx) - r.Sx * Bkz, By = comp(B, r.ky) - r.Sy * Bkz;
+  const float Cx = comp(C, r.kx) - r.Sx * Ckz, Cy = comp(C, r.ky) - r.Sy * Ckz;
+  float U = Cx * By - Cy * Bx, V = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
+  if (U == 0.f || V == 0.f || W == 0.f) {
+    U = float(double(Cx) * double(By) - double(Cy) * double(Bx));
+    V = float(double(Ax) * double(Cy) - double(Ay) * double(Cx));
+    W = float(double(Bx) * double(Ay) - double(By) * double(Ax));
+  }
+  if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f)) return false;
+  const float det = U + V + W;
+  if (det == 0.f) return false;
+  if (cullBack && det < 0.f) return false;
+  if (U == 0.f || V == 0.f || W == 0.f) {   // the ray meets an edge's line: one of the two triangles sharing it takes it
+    const float s = det > 0.f ? 1.f : -1.f;
+    if (U == 0.f) { const float ex = s * (Cx - Bx), ey = s * (Cy - By); if (!(ey > 0.f || (ey == 0.f && ex > 0.f))) return false; }
+    if (V == 0.f) { const float ex = s * (Ax - Cx), ey = s * (Ay - Cy); if (!(ey > 0.f || (ey == 0.f && ex > 0.f))) return false; }
+    if (W == 0.f) { const float ex = s * (Bx - Ax), ey = s * (By - Ay); if (!(ey > 0.f || (ey == 0.f && ex > 0.f))) return false; }
+  }
+  const float Az = r.Sz * Akz, Bz = r.Sz * Bkz, Cz = r.Sz * Ckz;
+  const float T = U * Az + V * Bz + W * Cz;
+  const float t = T / det;
+  if (!(t >= tmin && t <= tmax)) return false;
+  h.t = t; h.u = V / det; h.v = W / det; h.front = det > 0.f;
+  return true;
+}
+
+// The reference's hit_triangle (trace_dev.cu:37-52): point, unit normal on the ray's side (1/sqrt), ext, lift.
+struct TriHit { F3 p, n, lift; float ext; bool front; };
+__device__ __forceinline__ bool tri_geom(F3 v0, F3 v1, F3 v2, const Hit& hh, TriHit& h) {
+  const F3 e1 = sub(v1, v0), e2 = sub(v2, v0);
+  const F3 ng = f3(e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x);
+  const float l2 = dot(ng, ng);
+  if (!(l2 > 0.f)) return false;
+  const float inv = 1.f / sqrtf(l2);
+  h.front = hh.front;
+  h.n = mul(h.front ? inv : -inv, ng);
+  h.p = add(add(v0, mul(hh.u, e1)), mul(hh.v, e2));
+  h.ext = fmaxf(fmaxf(fmaxf(fabsf(e1.x), fabsf(e1.y)), fmaxf(fabsf(e1.z), fabsf(e2.x))), fmaxf(fabsf(e2.y), fabsf(e2.z)));
+  h.lift = mul(h.ext * 9.5367432e-7f, h.n);
+  return true;
+}
+// own_plane / own_hit / through (trace_dev.cu:60-72, 63)
+__device__ __forceinline__ bool own_plane(const TriHit& h, float t, F3 d, F3 n) {
+  return t * fabsf(dot(d, h.n)) < h.ext * 2.3841858e-7f && dot(n, h.n) <= 0.f;
+}
+__device__ __forceinline__ bool own_hit(F3 v0, F3 v1, F3 v2, const Hit& hh, F3 d, F3 n) {
+  if (!(hh.t * dot(n, d) < 1.f / 32.f)) return false;
+  TriHit h;
+  return tri_geom(v0, v1, v2, hh, h) && own_plane(h, hh.t, d, n);
+}
+__device__ __forceinline__ F3 through(const TriHit& h) { return sub(offset_ray(h.p, mul(-1.f, h.n)), h.lift); }
+
+// ------------------------------------------------------------------------------------------------ BVH8 traversal
+__device__ __forceinline__ float ubyte(uint32_t w, int k) { return float((w >> (8 * k)) & 0xffu); }
+__device__ __forceinline__ uint32_t byte_of(uint32_t w, int k) { return (w >> (8 * k)) & 0xffu; }
+
+// Child boxes of a node against the ray in [tmin, tmax]: returns the mask of hit children (bit k), their entry
+// distances in tn[8]. Conservative: the boxes were expanded at build; the exit distance is widened by 2^-20.
+__device__ __forceinline__ uint32_t node_hits(const uint4* n, const Ray& r, float tmin, float tmax, float* tn) {
+  const float px = __uint_as_float(n[0].x), py = __uint_as_float(n[0].y), pz = __uint_as_float(n[0].z);
+  const uint32_t ew = n[0].w;
+  const float sx = __uint_as_float((ew & 0xffu) << 23), sy = __uint_as_float(((ew >> 8) & 0xffu) << 23), sz = __uint_as_float(((ew >> 16) & 0xffu) << 23);
+  const float adjx = sx * r.inv.x, adjy = sy * r.inv.y, adjz = sz * r.inv.z;
+  const float ox = __fmaf_rn(px, r.inv.x, -r.oinv.x), oy = __fmaf_rn(py, r.inv.y, -r.oinv.y), oz = __fmaf_rn(pz, r.inv.z, -r.oinv.z);
+  // quantised bounds: qlo.x = n2.x,n2.y  qlo.y = n2.z,n2.w  qlo.z = n3.x,n3.y  qhi.x = n3.z,n3.w  qhi.y = n4.x,n4.y  qhi.z = n4.z,n4.w
+  uint32_t mask = 0;
+  const uint32_t meta0 = n[1].z, meta1 = n[1].w, imask = ew >> 24;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int h = k >> 2, b = k & 3;
+    const uint32_t qlx = byte_of(h ? n[2].y : n[2].x, b), qly = byte_of(h ? n[2].w : n[2].z, b), qlz = byte_of(h ? n[3].y : n[3].x, b);
+    const uint32_t qhx = byte_of(h ? n[3].w : n[3].z, b), qhy = byte_of(h ? n[4].y : n[4].x, b), qhz = byte_of(h ? n[4].w : n[4].z, b);
+    const float t0x = __fmaf_rn(float(qlx), adjx, ox), t1x = __fmaf_rn(float(qhx), adjx, ox);
+    const float t0y = __fmaf_rn(float(qly), adjy, oy), t1y = __fmaf_rn(float(qhy), adjy, oy);
+    const float t0z = __fmaf_rn(float(qlz), adjz, oz), t1z = __fmaf_rn(float(qhz), adjz, oz);
+    const float tnear = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+    float tfar = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+    tfar = fminf(__fmaf_rn(fabsf(tfar), 9.5367431640625e-7f, tfar), tmax);
+    const uint32_t meta = byte_of(k < 4 ? meta0 : meta1, k & 3);
+    const bool live = ((imask >> k) & 1u) || meta != 0u;
+    if (live && tnear <= tfar) { mask |= 1u << k; tn[k] = tnear; }
+  }
+  return mask;
+}
+
+__device__ __forceinline__ void load_node(const Node8* nodes, uint32_t idx, uint4* n) {
+  const uint4* p = reinterpret_cast<const uint4*>(nodes + idx);
+#pragma unroll
+  for (int q = 0; q < 5; ++q) n[q] = __ldg(p + q);
+}
+__device__ __forceinline__ void load_tri(const TriRec* tris, uint32_t j, F3& v0, F3& v1, F3& v2, uint32_t& prim, uint32_t& flags, uint32_t& slot) {
+  const float4* p = reinterpret_cast<const float4*>(tris + j);
+  const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+  v0 = f3(a.x, a.y, a.z); v1 = f3(b.x, b.y, b.z); v2 = f3(c.x, c.y, c.z);
+  prim = __float_as_uint(a.w); flags = __float_as_uint(b.w); slot = __float_as_uint(c.w);
+}
+
+struct Scene {
+  const Node8* nodes;
+  const TriRec* tris;
+  uint32_t nNodes;    // 0: empty scene, every ray misses
+};
+
+constexpr int kStack = 48;   // node-group stack entries (one per level at most)
+
+// Traversal counters of the instrumented kernels (nodes visited, triangles tested); compiled out otherwise.
+struct Count {
+  uint32_t nodes = 0, tris = 0;
+};
+
+// Visit every triangle hit in [tmin, tmax] (any order); f(hit, v0, v1, v2, flags, slot) returns true to stop.
+template <bool COUNT = false, class Fn>
+__device__ __forceinline__ void for_hits(const Scene& s, const Ray& r, float tmin, float tmax, bool cull, Fn&& f, uint32_t& overflow,
+                                         Count* ctr = nullptr) {
+  if (!s.nNodes) return;
+  uint2 stack[kStack];   // node group: x = childBase, y = imask << 8 | remaining inner children
+  int sp = 0;
+  uint32_t cur = 0;      // node to visit
+  for (;;) {
+    uint4 n[5];
+    load_node(s.nodes, cur, n);
+    if (COUNT) ctr->nodes++;
+    float tn[8];
+    const uint32_t hit = node_hits(n, r, tmin, tmax, tn);
+    const uint32_t imask = n[0].w >> 24;
+    uint32_t leaves = hit & ~imask;
+    while (leaves) {
+      const int k = __ffs(leaves) - 1;
+      leaves &= leaves - 1;
+      const uint32_t meta = byte_of(k < 4 ? n[1].z : n[1].w, k & 3);
+      const uint32_t first = n[1].y + (meta & 31u), cnt = meta >> 5;
+      for (uint32_t j = first; j < first + cnt; ++j) {
+        F3 v0, v1, v2;
+        uint32_t prim, flags, slot;
+        load_tri(s.tris, j, v0, v1, v2, prim, flags, slot);
+        if (COUNT) ctr->tris++;
+        Hit h;
+        if (hit_tri(r, v0, v1, v2, tmin, tmax, cull, h)) {
+          h.prim = prim;
+          if (f(h, v0, v1, v2, flags, slot)) return;
+        }
+      }
+    }
+    const uint32_t inner = hit & imask;
+    if (inner) {
+      const int k = __ffs(inner) - 1;
+      const uint32_t rest = inner & (inner - 1);
+      if (rest) {
+        if (sp < kStack) stack[sp++] = make_uint2(n[1].x, (imask << 8) | rest);
+        else overflow = 1;
+      }
+      cur = n[1].x + __popc(imask & ((1u << k) - 1u));
+      continue;
+    }
+    if (!sp) return;
+    uint2& g = stack[sp - 1];
+    const uint32_t rem = g.y & 0xffu, im = g.y >> 8;
+    const int k = __ffs(rem) - 1;
+    cur = g.x + __popc(im & ((1u << k) - 1u));
+    const uint32_t left = rem & (rem - 1);
+    if (left) g.y = (im << 8) | left; else --sp;
+  }
+}
+
+// The closest hit in [tmin, tmax], ties broken by the smaller primitive index. Children are visited near to far; a
+// node whose entry lies beyond the best hit so far is skipped.
+struct ClosestOut { Hit h; F3 v0, v1, v2; uint32_t flags, slot; };
+__device__ __forceinline__ bool closest(const Scene& s, const Ray& r, float tmin, float tmax, bool cull, ClosestOut& out, uint32_t& overflow) {
+  if (!s.nNodes) return false;
+  struct Entry { uint32_t node; float t; };
+  Entry stack[kStack * 4];
+  int sp = 0;
+  bool any = false;
+  float best = tmax;
+  stack[sp++] = Entry{0u, tmin};
+  while (sp) {
+    const Entry e = stack[--sp];
+    if (e.t > best) continue;
+    uint4 n[5];
+    load_node(s.nodes, e.node, n);
+    float tn[8];
+    const uint32_t hit = node_hits(n, r, tmin, best, tn);
+    const uint32_t imask = n[0].w >> 24;
+    uint32_t leaves = hit & ~imask;
+    while (leaves) {
+      const int k = __ffs(leaves) - 1;
+      leaves &= leaves - 1;
+      const uint32_t meta = byte_of(k < 4 ? n[1].z : n[1].w, k & 3);
+      const uint32_t first = n[1].y + (meta & 31u), cnt = meta >> 5;
+      for (uint32_t j = first; j < first + cnt; ++j) {
+        F3 v0, v1, v2;
+        uint32_t prim, flags, slot;
+        load_tri(s.tris, j, v0, v1, v2, prim, flags, slot);
+        Hit h;
+        if (hit_tri(r, v0, v1, v2, tmin, best, cull, h)) {
+          h.prim = prim;
+          if (!any || h.t < out.h.t || (h.t == out.h.t && prim < out.h.prim)) {
+            out.h = h; out.v0 = v0; out.v1 = v1; out.v2 = v2; out.flags = flags; out.slot = slot;
+            any = true;
+            best = h.t;
+          }
+        }
+      }
+    }
+    // inner children, pushed far to near so the nearest is popped first
+    uint32_t inner = hit & imask;
+    const int cnt = __popc(inner);
+    if (sp + cnt > kStack * 4) { overflow = 1; continue; }
+    Entry ch[8];
+    int m = 0;
+    while (inner) {
+      const int k = __ffs(inner) - 1;
+      inner &= inner - 1;
+      ch[m++] = Entry{n[1].x + __popc(imask & ((1u << k) - 1u)), tn[k]};
+    }
+    for (int a = 1; a < m; ++a) {   // insertion sort, descending t
+      const Entry x = ch[a];
+      int b = a - 1;
+      while (b >= 0 && ch[b].t < x.t) { ch[b + 1] = ch[b]; --b; }
+      ch[b + 1] = x;
+    }
+    for (int a = 0; a < m; ++a) stack[sp++] = ch[a];
+  }
+  return any;
+}
+
+}  // namespace kgb

@@ -1,0 +1,316 @@
+// Ray-casting kernels of the engine (compiled with -fmad=false: see rt.cuh):
+//  k_bits   visibility bits, any-hit (replaces the reference's __raygen__bits, trace_dev.cu:91-108)
+//  k_bytes  transmittance bytes (replaces __raygen__bytes + __anyhit__tr, trace_dev.cu:115-165)
+//  k_view   class + distance of the closest hit per view cell (replaces __raygen__view, trace_dev.cu:177-232)
+//  k_bounce reflected-light paths binned by sky patch (replaces __raygen__bounce, trace_dev.cu:260-311)
+// The visibility kernels are persistent: each warp takes tasks of 32 consecutive sensors x one 32-direction word
+// from a global counter, so a warp traces one direction for 32 neighbouring sensors at a time (coherent rays).
+#include "engine.h"
+#include "rt.cuh"
+
+namespace kgb {
+
+__device__ __forceinline__ uint32_t next_task(uint32_t* counter) {
+  uint32_t t = 0;
+  if ((threadIdx.x & 31) == 0) t = atomicAdd(counter, 1u);
+  return __shfl_sync(~0u, t, 0);
+}
+
+// ---------------------------------------------------------------------------------------------------- bits
+// Direction d of a sensor is visible when n.d > 0 and every hit from tmin 1e-5 on is an own-plane hit, at most 3.
+// COUNT: the instrumented variant (same results) that adds up nodes visited, triangles tested and rays traced.
+template <bool COUNT>
+__global__ void __launch_bounds__(256) k_bits(TraceArgs a) {
+  const Scene s{a.nodes, a.tris, a.nNodes};
+  const bool cull = (a.rayFlags & KGB_RAY_CULL_BACK_FACING) != 0;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t blocks = (a.n + 31) / 32, nTasks = blocks * a.nWords;
+  uint32_t overflow = 0;
+  Count ctr;
+  uint32_t rays = 0;
+  for (uint32_t task = next_task(a.counter); task < nTasks; task = next_task(a.counter)) {
+    const uint32_t b = task / a.nWords, w = task % a.nWords, i = b * 32 + lane;
+    if (i >= a.n) continue;
+    const uint32_t gi = a.first + i;
+    const F3 n = ld3(a.N + 3 * gi), o = offset_ray(ld3(a.P + 3 * gi), n);
+    uint32_t word = 0;
+    for (uint32_t k = 0; k < 32; ++k) {
+      const uint32_t d = w * 32 + k;
+      if (d >= a.nDir) break;
+      const F3 dir = ld3(a.D + 3 * d);
+      if (!(n.x * dir.x + n.y * dir.y + n.z * dir.z > 0.f)) continue;
+      const Ray r = make_ray(o, dir);
+      bool blocked = false;
+      int own = 0;
+      if (COUNT) ++rays;
+      for_hits<COUNT>(s, r, 1e-5f, INFINITY, cull, [&](const Hit& h, F3 v0, F3 v1, F3 v2, uint32_t, uint32_t) {
+        if (own_hit(v0, v1, v2, h, dir, n) && ++own <= 3) return false;
+        blocked = true;
+        return true;
+      }, overflow, &ctr);
+      if (!blocked) word |= 1u << k;
+    }
+    a.bits[size_t(w) * a.stride + a.out0 + i] = word;
+  }
+  if (overflow) atomicOr(a.status, kStatusStackOverflow);
+  if (COUNT) {
+    unsigned long long* c = reinterpret_cast<unsigned long long*>(a.status + 1);   // ctl words 2..7: three u64 counters
+    atomicAdd(c, (unsigned long long)ctr.nodes);
+    atomicAdd(c + 1, (unsigned long long)ctr.tris);
+    atomicAdd(c + 2, (unsigned long long)rays);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------------- bytes
+// A translucent slot's crossing: tau, 1 on a thin solid's exit face, Radiance glass T(cos) (trace_dev.cu:147-165).
+__device__ __forceinline__ float crossing(const kgb_slot* slots, uint32_t nSlots, uint32_t slot, bool front, F3 v0, F3 v1, F3 v2, F3 d) {
+  const kgb_slot sl = slot < nSlots ? slots[slot] : kgb_slot{0.2f, 0.f, 0.f, 0u};
+  float T = sl.tau;
+  if ((sl.flags & KGB_SLOT_THIN) && front == ((sl.flags & KGB_SLOT_INWARD) != 0)) T = 1.f;
+  else if (sl.flags & KGB_SLOT_GLASS) {
+    const float ax = v1.x - v0.x, ay = v1.y - v0.y, az = v1.z - v0.z;
+    const float bx = v2.x - v0.x, by = v2.y - v0.y, bz = v2.z - v0.z;
+    const float nx = ay * bz - az * by, ny = az * bx - ax * bz, nz = ax * by - ay * bx;
+    float R;
+    glass_TR(fabsf(nx * d.x + ny * d.y + nz * d.z) * (1.f / sqrtf(nx * nx + ny * ny + nz * nz)), sl.tn, T, R);
+  }
+  return T;
+}
+
+constexpr int kMaxCross = 16;   // translucent crossings a ray keeps in registers before it walks them in order instead
+
+// Own-plane hits pass (at most 3), an opaque hit blocks, translucent crossings multiply in (t, primitive) order.
+__device__ uint8_t trace_byte(const Scene& s, const TraceArgs& a, F3 o, F3 n, F3 dir, bool cull, uint32_t& overflow) {
+  if (!(n.x * dir.x + n.y * dir.y + n.z * dir.z > 0.f)) return 0;
+  const Ray r = make_ray(o, dir);
+  bool blocked = false, spill = false;
+  int own = 0, nx = 0;
+  float ct[kMaxCross], cf[kMaxCross];
+  uint32_t cp[kMaxCross];
+  for_hits(s, r, 1e-5f, INFINITY, cull, [&](const Hit& h, F3 v0, F3 v1, F3 v2, uint32_t flags, uint32_t slot) {
+    if (own_hit(v0, v1, v2, h, dir, n)) { if (++own <= 3) return false; blocked = true; return true; }
+    if (!(flags & kTriTranslucent)) { blocked = true; return true; }
+    if (nx < kMaxCross) { ct[nx] = h.t; cp[nx] = h.prim; cf[nx] = crossing(a.slots, a.nSlots, slot, h.front, v0, v1, v2, dir); ++nx; }
+    else spill = true;
+    return false;
+  }, overflow);
+  if (blocked) return 0;
+  float T = 1.f;
+  if (!spill) {
+    for (int x = 1; x < nx; ++x) {   // insertion sort by (t, primitive)
+      const float tx = ct[x], fx = cf[x];
+      const uint32_t px = cp[x];
+      int y = x - 1;
+      while (y >= 0 && (ct[y] > tx || (ct[y] == tx && cp[y] > px))) { ct[y + 1] = ct[y]; cp[y + 1] = cp[y]; cf[y + 1] = cf[y]; --y; }
+      ct[y + 1] = tx; cp[y + 1] = px; cf[y + 1] = fx;
+    }
+    for (int x = 0; x < nx; ++x) {
+      T *= cf[x];
+      if (!(T >= 1.f / 510.f)) return 0;
+    }
+    return (uint8_t)__float2uint_rn(T * 255.f);
+  }
+  // more than kMaxCross crossings: walk them one at a time in (t, primitive) order
+  float lastT = -INFINITY;
+  uint32_t lastP = 0;
+  for (;;) {
+    bool found = false;
+    float bt = 0.f, bf = 0.f;
+    uint32_t bp = 0;
+    for_hits(s, r, 1e-5f, INFINITY, cull, [&](const Hit& h, F3 v0, F3 v1, F3 v2, uint32_t flags, uint32_t slot) {
+      if (!(flags & kTriTranslucent) || own_hit(v0, v1, v2, h, dir, n)) return false;
+      if (h.t < lastT || (h.t == lastT && h.prim <= lastP)) return false;
+      if (!found || h.t < bt || (h.t == bt && h.prim < bp)) {
+        found = true; bt = h.t; bp = h.prim;
+        bf = crossing(a.slots, a.nSlots, slot, h.front, v0, v1, v2, dir);
+      }
+      return false;
+    }, overflow);
+    if (!found) break;
+    T *= bf;
+    if (!(T >= 1.f / 510.f)) return 0;
+    lastT = bt; lastP = bp;
+  }
+  return (uint8_t)__float2uint_rn(T * 255.f);
+}
+
+__global__ void __launch_bounds__(256) k_bytes(TraceArgs a) {
+  const Scene s{a.nodes, a.tris, a.nNodes};
+  const bool cull = (a.rayFlags & KGB_RAY_CULL_BACK_FACING) != 0;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t blocks = (a.n + 31) / 32, nTasks = blocks * a.nWords;
+  uint32_t overflow = 0;
+  for (uint32_t task = next_task(a.counter); task < nTasks; task = next_task(a.counter)) {
+    const uint32_t b = task / a.nWords, w = task % a.nWords, i = b * 32 + lane;
+    if (i >= a.n) continue;
+    const uint32_t gi = a.first + i;
+    const F3 n = ld3(a.N + 3 * gi), o = offset_ray(ld3(a.P + 3 * gi), n);
+    for (uint32_t k = 0; k < 32; ++k) {
+      const uint32_t d = w * 32 + k;
+      if (d >= a.nDir) break;
+      a.bytes[size_t(d) * a.stride + a.out0 + i] = trace_byte(s, a, o, n, ld3(a.D + 3 * d), cull, overflow);
+    }
+  }
+  if (overflow) atomicOr(a.status, kStatusStackOverflow);
+}
+
+// ---------------------------------------------------------------------------------------------------- views
+// params.h:77-89 (view_cell), sincospif as kgb_sincospi
+__device__ __forceinline__ F3 view_cell(uint32_t d, uint32_t col, float rsx, float rsy, float az0, float dAz, bool jitter, uint32_t element, uint32_t side) {
+  float a = 0.5f, s = 0.5f * (rsx + rsy);
+  if (jitter) { const U3 h = pcg3d(element, d, side); a = u01(h.x); s = rsx + u01(h.y) * (rsy - rsx); }
+  float sa, ca;
+  kgb_sincospi((az0 + (float(col) + a) * dAz) * (1.f / 180.f), &sa, &ca);
+  const float c = sqrtf(fmaxf(0.f, 1.f - s * s));
+  return f3(c * sa, c * ca, s);
+}
+
+__global__ void __launch_bounds__(256) k_view(ViewArgs a) {
+  const Scene s{a.nodes, a.tris, a.nNodes};
+  const bool cull = (a.rayFlags & KGB_RAY_CULL_BACK_FACING) != 0;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t blocks = (a.n + 31) / 32, nTasks = blocks * a.nWords;
+  const float inf = __int_as_float(0x7f800000);
+  uint32_t overflow = 0;
+  for (uint32_t task = next_task(a.counter); task < nTasks; task = next_task(a.counter)) {
+    const uint32_t b = task / a.nWords, w = task % a.nWords, i = b * 32 + lane;
+    if (i >= a.n) continue;
+    const uint32_t gl = a.first + i;           // sensor within the engine's arrays
+    const uint32_t gi = a.i0 + a.out0 + i;     // global sensor index (seeds)
+    const uint32_t element = gi / a.nS, side = a.nS == 2 ? gi % 2 : a.back;
+    const F3 n = ld3(a.N + 3 * gl), o = offset_ray(ld3(a.P + 3 * gl), n);
+    const bool none = !(dot(n, n) > 0.f);
+    F3 f, r, u;
+    if (a.world) { f = f3(-a.sinN, a.cosN, 0.f); r = f3(a.cosN, a.sinN, 0.f); u = f3(0.f, 0.f, 1.f); }
+    else {
+      const float l = sqrtf(n.x * n.x + n.y * n.y);
+      f = n;
+      if (l > 1e-3f) r = f3(n.y / l, -n.x / l, 0.f);
+      else {
+        r = f3(a.cosN, a.sinN, 0.f);
+        if (l > 0.f) { r = sub(r, mul(dot(r, n), n)); r = mul(1.f / sqrtf(dot(r, r)), r); }
+      }
+      u = f3(r.y * f.z - r.z * f.y, r.z * f.x - r.x * f.z, r.x * f.y - r.y * f.x);
+    }
+    for (uint32_t k = 0; k < 32; ++k) {
+      const uint32_t d = w * 32 + k;
+      if (d >= a.K) break;
+      const uint32_t col = d % a.nAz, row = d / a.nAz;
+      const F3 l = view_cell(d, col, a.rowSin[2 * row], a.rowSin[2 * row + 1], a.az0, a.dAz, a.jitter != 0, element, side);
+      const F3 dir = add(add(mul(l.x, r), mul(l.y, f)), mul(l.z, u));
+      uint32_t cl = 2;
+      float t = inf;
+      if (none || (a.cull && dot(n, dir) <= 0.f)) cl = 254;
+      else if (a.vground && dir.z < 0.f && !(o.z > a.groundZ)) { cl = 1; t = 0.1f; }
+      else {
+        const bool plane = a.vground && dir.z < 0.f;
+        const float tg = plane ? (o.z - a.groundZ) / -dir.z : inf;
+        const float tmax = plane ? (o.z - a.groundZ + 0.01f) / -dir.z : FLT_MAX;
+        float tmin = 1e-5f;
+        uint32_t own = 0, panes = 0;
+        const Ray ray = make_ray(o, dir);
+        for (;;) {
+          ClosestOut c;
+          if (!closest(s, ray, tmin, tmax, cull, c, overflow)) { cl = dir.z >= 0.f ? 0 : 1; t = tg; break; }
+          t = c.h.t;
+          if (own_hit(c.v0, c.v1, c.v2, c.h, dir, n)) { if (++own == 4) break; }
+          else {
+            const uint32_t lb = a.label ? a.label[c.h.prim] : 2u;
+            if (lb != KGB_LABEL_PASS) { cl = lb; break; }
+            if (++panes > KGB_MAX_PANES) break;
+          }
+          tmin = next_up(t);
+        }
+        if (panes) cl |= KGB_VIEW_GLAZED;
+      }
+      const size_t at = size_t(d) * a.stride + a.out0 + i;
+      a.cls[at] = uint8_t(cl);
+      a.dist[at] = t;
+    }
+  }
+  if (overflow) atomicOr(a.status, kStatusStackOverflow);
+}
+
+// ---------------------------------------------------------------------------------------------------- bounce
+__device__ __forceinline__ F3 cosine_dir(F3 n, float u, float v) {   // trace_dev.cu:235-242 (Duff et al. 2017 basis)
+  const float sg = copysignf(1.f, n.z), a = -1.f / (sg + n.z), b = n.x * n.y * a;
+  const F3 t = f3(1.f + sg * n.x * n.x * a, sg * b, -sg * n.x), w = f3(b, sg + n.y * n.y * a, -n.y);
+  float s, c;
+  kgb_sincospi(2.f * v, &s, &c);
+  const float r = sqrtf(u);
+  return add(add(mul(r * c, t), mul(r * s, w)), mul(sqrtf(fmaxf(0.f, 1.f - u)), n));
+}
+__constant__ uint32_t kTnaz[7] = {30, 30, 24, 24, 18, 12, 6};
+__device__ __forceinline__ uint32_t sky_bin(F3 d, uint32_t mf, uint32_t nBins, float alpha, float cosN, float sinN) {   // trace_dev.cu:248-258
+  if (!(d.z >= 0.f)) return 0;
+  const uint32_t r = min(uint32_t(kgb_asin(fminf(d.z, 1.f)) / alpha), 7 * mf);
+  if (r == 7 * mf) return nBins - 1;
+  const uint32_t n = kTnaz[r / mf] * mf;
+  uint32_t b = 1 + (r % mf) * n;
+  for (uint32_t q = 0; q < r / mf; ++q) b += kTnaz[q] * mf * mf;
+  float az = kgb_atan2(d.x * cosN + d.y * sinN, d.y * cosN - d.x * sinN);
+  if (az < 0.f) az += 6.28318531f;
+  return b + uint32_t(az * (float(n) / 6.28318531f) + .5f) % n;
+}
+
+__global__ void __launch_bounds__(128) k_bounce(BounceArgs a) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const Scene s{a.nodes, a.tris, a.nNodes};
+  const bool cull = (a.rayFlags & KGB_RAY_CULL_BACK_FACING) != 0;
+  const uint32_t gi = a.i0 + i;
+  const F3 nn = ld3(a.N + 3 * gi), o0 = offset_ray(ld3(a.P + 3 * gi), nn);
+  const U3 rot = pcg3d(gi, ~0u, ~0u);
+  const float r0 = u01(rot.x), r1 = u01(rot.y), weight = 3.14159265f / float(a.M);
+  float* row = a.dc + i;
+  uint32_t overflow = 0;
+  for (uint32_t smp = a.s0; smp < a.s1; ++smp) {
+    const float u = float(smp) / float(a.M) + r0, v = u01(__brev(smp)) + r1;
+    F3 o = o0, d = cosine_dir(nn, u - floorf(u), v - floorf(v));
+    float w = 1.f;
+    uint32_t diffuse = 0, k = 0;
+    bool reflected = false;
+    for (uint32_t seg = 0; seg < a.nBounce + 16; ++seg) {
+      ClosestOut c;
+      if (!closest(s, make_ray(o, d), 1e-5f, FLT_MAX, cull, c, overflow)) {
+        if (reflected) { float* p = row + size_t(sky_bin(d, a.mf, a.nBins, a.alpha, a.cosN, a.sinN)) * a.nc; *p = *p + w * weight; }
+        break;
+      }
+      const kgb_slot sl = c.slot < a.nSlots ? a.slots[c.slot] : kgb_slot{0.2f, 0.f, 0.f, 0u};
+      TriHit h;
+      if (!tri_geom(c.v0, c.v1, c.v2, c.h, h)) break;
+      if (seg == 0 && own_plane(h, c.h.t, d, nn)) { o = through(h); continue; }
+      if ((sl.flags & (KGB_SLOT_THIN | KGB_SLOT_TWIN)) == KGB_SLOT_THIN && h.front == ((sl.flags & KGB_SLOT_INWARD) != 0)) { o = through(h); continue; }
+      const bool mirror = (sl.flags & KGB_SLOT_GLASS) != 0;
+      float T = sl.tau, R = sl.rho;
+      if (mirror) { glass_TR(fabsf(dot(d, h.n)), sl.tn, T, R); if (!(sl.tau > 0.f)) T = 0.f; }
+      else if (diffuse == a.nBounce) R = 0.f;
+      if (!(T + R > 0.f)) break;
+      const U3 rr = pcg3d(gi, smp, k++);
+      w *= T + R;
+      if (u01(rr.x) * (T + R) < T) { o = through(h); continue; }
+      reflected = true;
+      if (mirror) d = sub(d, mul(2.f * dot(d, h.n), h.n));
+      else {
+        d = cosine_dir(h.n, u01(rr.y), u01(rr.z));
+        if (++diffuse >= 2) {
+          if (u01(pcg3d(gi, smp, k++).x) >= w) break;
+          w = 1.f;
+        }
+      }
+      o = add(offset_ray(h.p, h.n), h.lift);
+    }
+  }
+  if (overflow) atomicOr(a.status, kStatusStackOverflow);
+}
+
+// ---------------------------------------------------------------------------------------------------- launches
+void launch_bits(const TraceArgs& a, int grid, cudaStream_t st, bool count) {
+  if (count) k_bits<true><<<grid, 256, 0, st>>>(a);
+  else k_bits<false><<<grid, 256, 0, st>>>(a);
+}
+void launch_bytes(const TraceArgs& a, int grid, cudaStream_t st) { k_bytes<<<grid, 256, 0, st>>>(a); }
+void launch_view(const ViewArgs& a, int grid, cudaStream_t st) { k_view<<<grid, 256, 0, st>>>(a); }
+void launch_bounce(const BounceArgs& a, cudaStream_t st) { k_bounce<<<(a.n + 127) / 128, 128, 0, st>>>(a); }
+
+}  // namespace kgb

@@ -1,0 +1,301 @@
+"""ctypes binding of the engine's C ABI (include/kitsim_gb300.h), with numpy arrays in and out.
+
+`Engine` mirrors the reference's GPU contract (kit-sim_daylight src/internal.h:125-220: gpu_build, gpu_set_scene,
+gpu_trace, gpu_reduce, gpu_series, gpu_bounce, gpu_view, gpu_reduce_view, ...) call for call: the same arguments, the
+same device layouts (bits word-major [nWords x nc], bytes / classes / distances direction-major [nDir x nc]), the same
+errors (a failing call raises KgbError with the engine's message, e.g. "cancelled").
+"""
+import ctypes
+from ctypes import POINTER, c_char_p, c_double, c_float, c_int, c_int32, c_size_t, c_uint32, c_uint64, c_void_p
+
+import numpy as np
+
+
+class KgbError(RuntimeError):
+    pass
+
+
+class Slot(ctypes.Structure):
+    _fields_ = [("rho", c_float), ("tau", c_float), ("tn", c_float), ("flags", c_uint32)]
+
+
+class SceneHandle(ctypes.Structure):
+    _fields_ = [("handle", c_void_p), ("bytes", c_uint64)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("buildMs", c_double), ("traceMs", c_double), ("bounceMs", c_double), ("rays", c_uint64), ("gasBytes", c_uint64),
+                ("launches", c_uint64), ("paths", c_uint64), ("bounceLaunches", c_uint64), ("buildTempBytes", c_uint64),
+                ("buildOutputBytes", c_uint64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+CANCEL_FN = ctypes.CFUNCTYPE(c_int, c_void_p)
+
+
+class SeriesIn(ctypes.Structure):
+    _fields_ = [("nSky", c_uint32), ("row", POINTER(c_int32)), ("wsky", POINTER(c_float)), ("S", POINTER(c_float)), ("P", c_int32),
+                ("T", c_int32), ("g", POINTER(c_float)), ("G", POINTER(c_float)), ("sun0", c_uint32), ("nSun", c_uint32),
+                ("sunStep", POINTER(c_int32)), ("sunVec", POINTER(c_float)), ("sunW", POINTER(c_float)), ("Sdc", POINTER(c_float))]
+
+
+class BounceIn(ctypes.Structure):
+    _fields_ = [("N", c_uint32), ("M", c_uint32), ("mf", c_int32), ("north", c_double), ("cancel", CANCEL_FN), ("cancelCtx", c_void_p)]
+
+
+class ViewIn(ctypes.Structure):
+    _fields_ = [("nAz", c_uint32), ("nEl", c_uint32), ("az0", c_float), ("dAz", c_float), ("rowSin", POINTER(c_float)),
+                ("world", c_int32), ("cull", c_int32), ("jitter", c_int32), ("back", c_int32), ("vground", c_int32), ("nS", c_uint32),
+                ("groundZ", c_float), ("north", c_double), ("cancel", CANCEL_FN), ("cancelCtx", c_void_p)]
+
+
+RAY_DISABLE_ANYHIT, RAY_TERMINATE_ON_FIRST_HIT, RAY_CULL_BACK_FACING = 1, 4, 16
+SLOT_GLASS, SLOT_THIN, SLOT_INWARD, SLOT_TWIN = 1, 2, 4, 8
+LABEL_PASS, MAX_PANES, VIEW_GLAZED = 255, 16, 0x80
+
+# every exported symbol of include/kitsim_gb300.h: (name, restype, argtypes)
+_E = c_void_p
+SIGNATURES = [
+    ("kgb_version", c_int32, []),
+    ("kgb_last_error", c_char_p, []),
+    ("kgb_init", _E, []),
+    ("kgb_destroy", None, [_E]),
+    ("kgb_build", c_int, [_E, c_void_p, c_size_t, c_void_p, c_size_t, c_void_p, c_void_p, c_size_t, c_int]),
+    ("kgb_build_bytes", c_uint64, [_E, c_size_t, c_size_t, c_int]),
+    ("kgb_trim", None, [_E, c_int]),
+    ("kgb_set_slots", c_int, [_E, c_void_p, c_size_t]),
+    ("kgb_detach", SceneHandle, [_E]),
+    ("kgb_attach", None, [_E, SceneHandle]),
+    ("kgb_free_scene", None, [POINTER(SceneHandle)]),
+    ("kgb_free_bytes", c_uint64, []),
+    ("kgb_set_scene", c_int, [_E, c_void_p, c_void_p, c_size_t, c_void_p, c_size_t]),
+    ("kgb_set_labels", c_int, [_E, c_void_p, c_size_t]),
+    ("kgb_trace", c_int, [_E, c_size_t, c_size_t, c_uint32]),
+    ("kgb_reduce", c_int, [_E, c_size_t, c_void_p, c_int, c_void_p]),
+    ("kgb_series", c_int, [_E, c_size_t, POINTER(SeriesIn), c_void_p]),
+    ("kgb_bounce", c_int, [_E, c_size_t, c_size_t, c_uint32, POINTER(BounceIn)]),
+    ("kgb_reduce_dc", c_int, [_E, c_size_t, c_void_p, c_void_p]),
+    ("kgb_download_dc", c_int, [_E, c_size_t, c_void_p, c_size_t]),
+    ("kgb_download_bits", c_int, [_E, c_size_t, c_void_p, c_size_t]),
+    ("kgb_download_bytes", c_int, [_E, c_size_t, c_void_p, c_size_t]),
+    ("kgb_view", c_int, [_E, c_size_t, c_size_t, c_uint32, POINTER(ViewIn), POINTER(c_size_t)]),
+    ("kgb_reduce_view", c_int, [_E, c_size_t, c_void_p, c_size_t, c_uint32, c_double, c_void_p, c_size_t, c_int, c_uint32, c_void_p]),
+    ("kgb_download_view", c_int, [_E, c_size_t, c_void_p, c_void_p, c_size_t]),
+    ("kgb_get_stats", Stats, [_E]),
+    ("kgb_ray_flags", c_uint32, [c_int, c_int]),
+    ("kgb_bounce_flags", c_uint32, [c_int]),
+    ("kgb_dims", None, [_E, POINTER(c_uint64)]),
+    ("kgb_set_stream", c_int, [_E, c_void_p]),
+    ("kgb_trace_counters", c_int, [_E, c_size_t, c_size_t, c_uint32, POINTER(c_uint64)]),
+]
+
+
+class Lib:
+    """A library that exports the engine's C ABI (the engine itself, or a restatement with the same symbols)."""
+
+    def __init__(self, path):
+        self.path = path
+        self.dll = ctypes.CDLL(path)
+        for name, res, args in SIGNATURES:
+            f = getattr(self.dll, name)
+            f.restype = res
+            f.argtypes = args
+
+    def err(self):
+        return (self.dll.kgb_last_error() or b"").decode()
+
+    def ray_flags(self, cull=False, translucent=False):
+        return self.dll.kgb_ray_flags(int(cull), int(translucent))
+
+    def bounce_flags(self, cull=False):
+        return self.dll.kgb_bounce_flags(int(cull))
+
+
+def _p(a):
+    return a.ctypes.data_as(c_void_p) if a is not None and a.size else None
+
+
+def _f32(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a if shape is None else a.reshape(shape)
+
+
+def _typed(a, ctype):
+    return a.ctypes.data_as(POINTER(ctype)) if a is not None else None
+
+
+class Engine:
+    """One engine (one device state) behind a Lib: the reference's Gpu."""
+
+    def __init__(self, lib):
+        self.lib = lib
+        self.d = lib.dll
+        self.h = self.d.kgb_init()
+        if not self.h:
+            raise KgbError(lib.err())
+        self._keep = []
+
+    def close(self):
+        if self.h:
+            self.d.kgb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ok(self, r):
+        if not r:
+            raise KgbError(self.lib.err())
+
+    # --- scene
+    def build(self, v, tri, slot=None, slots=None, per_slot=False):
+        v = _f32(v, (-1, 3))
+        tri = np.ascontiguousarray(tri, dtype=np.uint32).reshape(-1, 3)
+        slot = None if slot is None else np.ascontiguousarray(slot, dtype=np.uint32)
+        sl = slots_array(slots if slots is not None else [Slot(0.2, 0, 0, 0)])
+        self._ok(self.d.kgb_build(self.h, _p(v), len(v), _p(tri), len(tri), _p(slot), ctypes.cast(sl, c_void_p), len(sl), int(per_slot)))
+
+    def build_bytes(self, nv, nt, slotted=False):
+        return self.d.kgb_build_bytes(self.h, nv, nt, int(slotted))
+
+    def set_slots(self, slots):
+        sl = slots_array(slots)
+        self._ok(self.d.kgb_set_slots(self.h, ctypes.cast(sl, c_void_p), len(sl)))
+
+    def trim(self, sensors=False):
+        self.d.kgb_trim(self.h, int(sensors))
+
+    def detach(self):
+        return self.d.kgb_detach(self.h)
+
+    def attach(self, s):
+        self.d.kgb_attach(self.h, s)
+
+    def free_scene(self, s):
+        self.d.kgb_free_scene(ctypes.byref(s))
+
+    def set_scene(self, P, N, D):
+        P, N, D = _f32(P, (-1, 3)), _f32(N, (-1, 3)), _f32(D, (-1, 3))
+        self._ok(self.d.kgb_set_scene(self.h, _p(P), _p(N), len(P), _p(D), len(D)))
+
+    def set_labels(self, label):
+        label = np.ascontiguousarray(label, dtype=np.uint8)
+        self._ok(self.d.kgb_set_labels(self.h, _p(label), label.size))
+
+    def dims(self):
+        out = (c_uint64 * 6)()
+        self.d.kgb_dims(self.h, out)
+        return dict(nSensors=out[0], nDir=out[1], nWords=out[2], nBins=out[3], K=out[4], bytes=bool(out[5]))
+
+    def stats(self):
+        return self.d.kgb_get_stats(self.h).as_dict()
+
+    def set_stream(self, stream_handle):
+        """Run on this cudaStream_t (an int handle, e.g. torch.cuda.Stream().cuda_stream); None: the engine's own."""
+        self._ok(self.d.kgb_set_stream(self.h, c_void_p(stream_handle) if stream_handle else None))
+
+    def trace_counters(self, i0, nc, flags):
+        """The instrumented trace: dict(nodes, tris, rays, bvh_bytes) for the roofline (results as trace())."""
+        out = (c_uint64 * 4)()
+        self._ok(self.d.kgb_trace_counters(self.h, i0, nc, flags, out))
+        return dict(nodes=out[0], tris=out[1], rays=out[2], bvh_bytes=out[3])
+
+    # --- daylight
+    def trace(self, i0, nc, flags):
+        self._ok(self.d.kgb_trace(self.h, i0, nc, flags))
+
+    def reduce(self, nc, W, use_cos=True):
+        W = _f32(W)
+        out = np.zeros(nc, np.float64)
+        self._ok(self.d.kgb_reduce(self.h, nc, _p(W), int(use_cos), _p(out)))
+        return out
+
+    def download_bits(self, nc):
+        n = self.dims()["nWords"] * nc
+        out = np.zeros(n, np.uint32)
+        self._ok(self.d.kgb_download_bits(self.h, nc, _p(out), n))
+        return out.reshape(-1, nc) if nc else out
+
+    def download_bytes(self, nc):
+        n = self.dims()["nDir"] * nc
+        out = np.zeros(n, np.uint8)
+        self._ok(self.d.kgb_download_bytes(self.h, nc, _p(out), n))
+        return out.reshape(-1, nc) if nc else out
+
+    def series(self, nc, nSky, row, wsky, S, g, G, sun0, sunStep, sunVec, sunW, Sdc=None):
+        row = np.ascontiguousarray(row, dtype=np.int32)
+        wsky, S, g, G = _f32(wsky), _f32(S), _f32(g), _f32(G)
+        P, T = S.shape
+        sunStep = np.ascontiguousarray(sunStep, dtype=np.int32)
+        sunVec, sunW = _f32(sunVec, (-1, 3)), _f32(sunW)
+        Sdc = None if Sdc is None else _f32(Sdc)
+        s = SeriesIn(nSky, _typed(row, c_int32), _typed(wsky, c_float), _typed(S, c_float), P, T, _typed(g, c_float), _typed(G, c_float),
+                     sun0, len(sunStep), _typed(sunStep, c_int32), _typed(sunVec, c_float), _typed(sunW, c_float),
+                     _typed(Sdc, c_float) if Sdc is not None else None)
+        E = np.zeros((nc, T), np.float32)
+        self._ok(self.d.kgb_series(self.h, nc, ctypes.byref(s), _p(E)))
+        return E
+
+    def bounce(self, i0, nc, flags, N=1, M=1024, mf=1, north=0.0, cancel=None):
+        cb = CANCEL_FN(lambda _ctx: int(bool(cancel()))) if cancel else CANCEL_FN()
+        b = BounceIn(N, M, mf, north, cb, None)
+        self._ok(self.d.kgb_bounce(self.h, i0, nc, flags, ctypes.byref(b)))
+
+    def reduce_dc(self, nc, W):
+        W = _f32(W)
+        out = np.zeros(nc, np.float64)
+        self._ok(self.d.kgb_reduce_dc(self.h, nc, _p(W), _p(out)))
+        return out
+
+    def download_dc(self, nc):
+        n = self.dims()["nBins"] * nc
+        out = np.zeros(n, np.float32)
+        self._ok(self.d.kgb_download_dc(self.h, nc, _p(out), n))
+        return out.reshape(-1, nc) if nc else out
+
+    # --- views
+    def view(self, i0, nc, flags, nAz, nEl, az0, dAz, rowSin, world=False, cull=False, jitter=True, back=False, vground=True, nS=1,
+             groundZ=0.0, north=0.0, launch=0, cancel=None):
+        rowSin = _f32(rowSin)
+        cb = CANCEL_FN(lambda _ctx: int(bool(cancel()))) if cancel else CANCEL_FN()
+        v = ViewIn(nAz, nEl, az0, dAz, _typed(rowSin, c_float), int(world), int(cull), int(jitter), int(back), int(vground), nS, groundZ,
+                   north, cb, None)
+        ln = c_size_t(launch)
+        self._ok(self.d.kgb_view(self.h, i0, nc, flags, ctypes.byref(v), ctypes.byref(ln)))
+        return ln.value
+
+    def reduce_view(self, nc, wRow, nClass, farDist, reach=(), glazing=False, isoDim=0):
+        wRow = np.ascontiguousarray(wRow, dtype=np.float64)
+        reach = np.ascontiguousarray(reach, dtype=np.float32)
+        NA = 3 * nClass + 1 + len(reach) + int(bool(glazing)) + int(bool(isoDim))
+        out = np.zeros((nc, NA), np.float64)
+        self._ok(self.d.kgb_reduce_view(self.h, nc, _p(wRow), wRow.size, nClass, farDist, _p(reach), reach.size, int(glazing), isoDim, _p(out)))
+        return out
+
+    def download_view(self, nc):
+        K = self.dims()["K"]
+        cls = np.zeros(nc * K, np.uint8)
+        dist = np.zeros(nc * K, np.float32)
+        self._ok(self.d.kgb_download_view(self.h, nc, _p(cls), _p(dist), nc * K))
+        return cls.reshape(nc, K), dist.reshape(nc, K)
+
+
+def slots_array(slots):
+    """A ctypes array of Slot from Slot objects or (rho, tau, tn, flags) tuples."""
+    arr = (Slot * max(1, len(slots)))()
+    for k, s in enumerate(slots):
+        arr[k] = s if isinstance(s, Slot) else Slot(*s)
+    if not len(slots):
+        arr[0] = Slot(0.2, 0.0, 0.0, 0)
+    return arr
+
+
+def tn_from_Tn(Tn):
+    """Glass transmissivity from the transmittance at normal incidence (the reference's glass.h:11-13)."""
+    import math
+    return max(0.0, (math.sqrt(0.8402528435 + 0.0072522239 * Tn * Tn) - 0.9166530661) / 0.0036261119 / Tn)

@@ -1,0 +1,175 @@
+"""Seeded synthetic scenes for the engine's measured configurations and tests (host side, numpy).
+
+Each scene is returned as the engine takes it at its boundary, after the reference's host prep: recentred float32
+vertices and uint32 triangles (quads split 0-1-2 / 0-2-3, src/mesh.cpp:137-168), a global slot per triangle, and the
+sensors (face centre + unit normal per sensor face, recentred: src/mesh.cpp:45-71, 315-349) in mesh order.
+
+ - box_scene(): four 2 m ground quads at z 0 facing up on a 2 x 2 grid and a 1 m cube 0.5 m above the fourth, both
+   sensor meshes that block (the reference's tests/box.obj, as its measured config describes it).
+ - urban_block(): 20 x 20 extruded boxes, footprints U(10, 30) m, heights U(6, 60) m, street gaps U(5, 15) m (mt19937-
+   style seeded numpy Generator, seed 42), roofs + facades remeshed into quads as receivers, a ground as context. The
+   quad size is chosen, as the reference's own bench generator does (src/main.cpp:105: q = sqrt(area / nSens)), so that
+   the block has ~200k sensor faces and ~400k triangles (1 m quads would give ~1.2M faces).
+ - random_city(): small random box piles with optional porous / glass / thin-solid slots and labels, for parity tests.
+"""
+import numpy as np
+
+
+class Mesh:
+    """Accumulates quads (counter-clockwise seen from the side they face) into shared arrays."""
+
+    def __init__(self, triangles=False):
+        self.pts = []
+        self.quads = []
+        self.slot = []
+        self.triangles = triangles   # faces are the quads' two triangles (0-1-2, 0-2-3): a sensor per triangle
+
+    def grid(self, o, u, v, nu, nv, slot=0):
+        o, u, v = (np.asarray(x, np.float64) for x in (o, u, v))
+        b = sum(len(p) for p in self.pts)
+        i = np.arange(nu + 1)[None, :, None] / nu
+        j = np.arange(nv + 1)[:, None, None] / nv
+        P = o + u * i + v * j
+        self.pts.append(P.reshape(-1, 3))
+        jj, ii = np.meshgrid(np.arange(nv), np.arange(nu), indexing="ij")
+        a = (b + jj * (nu + 1) + ii).ravel()
+        self.quads.append(np.stack([a, a + 1, a + nu + 2, a + nu + 1], axis=1))
+        self.slot.append(np.full(nu * nv, slot, np.uint32))
+
+    def arrays(self):
+        pts = np.concatenate(self.pts) if self.pts else np.zeros((0, 3))
+        q = np.concatenate(self.quads) if self.quads else np.zeros((0, 4), np.int64)
+        s = np.concatenate(self.slot) if self.slot else np.zeros(0, np.uint32)
+        return pts, q, s
+
+
+def _faces_geom(pts, quads):
+    """Centre (area-weighted over the two triangles) and unit normal of each quad, in double."""
+    a, b, c, d = (pts[quads[:, k]] for k in range(4))
+    n1 = np.cross(b - a, c - a)
+    n2 = np.cross(c - a, d - a)
+    A1 = 0.5 * np.linalg.norm(n1, axis=1)
+    A2 = 0.5 * np.linalg.norm(n2, axis=1)
+    c1 = (a + b + c) / 3
+    c2 = (a + c + d) / 3
+    cen = (c1 * A1[:, None] + c2 * A2[:, None]) / np.maximum(A1 + A2, 1e-300)[:, None]
+    n = n1 + n2
+    n /= np.maximum(np.linalg.norm(n, axis=1), 1e-300)[:, None]
+    return cen, n
+
+
+def assemble(meshes):
+    """meshes: list of (Mesh, is_sensor, blocks). Returns the scene dict at the engine boundary."""
+    arrs = [(m.arrays(), sensor, blocks) for m, sensor, blocks in meshes]
+    m_of = {id(a[0][1]): m for a, (m, _, _) in zip(arrs, meshes)}
+    allp = np.concatenate([a[0][0] for a in arrs if len(a[0][0])])
+    centre = 0.5 * (allp.min(axis=0) + allp.max(axis=0))   # bbox centre of every mesh (src/mesh.cpp:107-118)
+    V, T, S, P, N = [], [], [], [], []
+    base = 0
+    slot_base = 0
+    for (pts, q, s), sensor, blocks in arrs:
+        if blocks:
+            V.append((pts - centre).astype(np.float32))
+            T.append(np.concatenate([q[:, [0, 1, 2]], q[:, [0, 2, 3]]], axis=1).reshape(-1, 3) + base)
+            S.append(np.repeat(s + slot_base, 2))
+            base += len(pts)
+        if sensor:
+            if m_of[id(q)].triangles:   # each triangle a face: (a, b, c, c) is that triangle as a degenerate quad
+                t = np.concatenate([q[:, [0, 1, 2, 2]], q[:, [0, 2, 3, 3]]], axis=1).reshape(-1, 4)
+                c, n = _faces_geom(pts - centre, t)
+            else:
+                c, n = _faces_geom(pts - centre, q)
+            P.append(c.astype(np.float32))
+            N.append(n.astype(np.float32))
+        slot_base += int(s.max()) + 1 if len(s) else 1
+    return dict(v=np.concatenate(V), tri=np.concatenate(T).astype(np.uint32), slot=np.concatenate(S).astype(np.uint32),
+                P=np.concatenate(P), N=np.concatenate(N), centre=centre)
+
+
+def box_scene():
+    ground, box = Mesh(), Mesh(triangles=True)
+    for x0, y0 in [(-2, -2), (0, -2), (-2, 0), (0, 0)]:
+        ground.grid((x0, y0, 0), (2, 0, 0), (0, 2, 0), 1, 1)
+    lo, hi = 0.5, 1.5
+    e = hi - lo
+    for o, u, v in [((lo, lo, lo), (0, e, 0), (e, 0, 0)), ((lo, lo, hi), (e, 0, 0), (0, e, 0)),      # bottom (-z), top
+                    ((lo, lo, lo), (e, 0, 0), (0, 0, e)), ((hi, lo, lo), (0, e, 0), (0, 0, e)),      # -y, +x
+                    ((hi, hi, lo), (-e, 0, 0), (0, 0, e)), ((lo, hi, lo), (0, -e, 0), (0, 0, e))]:  # +y, -x
+        box.grid(o, u, v, 1, 1)
+    return assemble([(ground, True, True), (box, True, True)])
+
+
+def _box_faces(m, x0, y0, w, d, h, q, slot=0, roof=True):
+    """Facades (outward) and roof of an extruded box, remeshed into ~q-sized quads."""
+    c = [(x0, y0), (x0 + w, y0), (x0 + w, y0 + d), (x0, y0 + d), (x0, y0)]   # counter-clockwise: outward walls
+    for k in range(4):
+        ux, uy = c[k + 1][0] - c[k][0], c[k + 1][1] - c[k][1]
+        L = np.hypot(ux, uy)
+        m.grid((c[k][0], c[k][1], 0), (ux, uy, 0), (0, 0, h), max(1, int(round(L / q))), max(1, int(round(h / q))), slot)
+    if roof:
+        m.grid((x0, y0, h), (w, 0, 0), (0, d, 0), max(1, int(round(w / q))), max(1, int(round(d / q))), slot)
+
+
+def urban_block(seed=42, n=20, target_sensors=200_000, glass_share=0.0, glass_seed=7):
+    """The 20 x 20 urban block. glass_share > 0 puts a share of the facade quads into slot 1 (glass windows)."""
+    rng = np.random.default_rng(seed)
+    w = rng.uniform(10, 30, (n, n))
+    d = rng.uniform(10, 30, (n, n))
+    h = rng.uniform(6, 60, (n, n))
+    gx = rng.uniform(5, 15, (n, n))
+    gy = rng.uniform(5, 15, n)
+    area = float(np.sum(2 * (w + d) * h + w * d))
+    q = np.sqrt(area / target_sensors)
+    rows_y = np.concatenate([[0.0], np.cumsum(d.max(axis=1) + gy)[:-1]])
+    build = Mesh()
+    for r in range(n):
+        x = 0.0
+        for k in range(n):
+            _box_faces(build, x, rows_y[r], w[r, k], d[r, k], h[r, k], q)
+            x += w[r, k] + gx[r, k]
+    if glass_share > 0:
+        g = np.random.default_rng(glass_seed)
+        build.slot = [np.where(g.random(len(s)) < glass_share, 1, 0).astype(np.uint32) for s in build.slot]
+    pts = np.concatenate(build.pts)
+    lo, hi = pts.min(axis=0), pts.max(axis=0)
+    ground = Mesh()
+    ground.grid((lo[0] - 50, lo[1] - 50, 0), (hi[0] - lo[0] + 100, 0, 0), (0, hi[1] - lo[1] + 100, 0), 40, 40)
+    s = assemble([(build, True, True), (ground, False, True)])
+    s["quad"] = q
+    return s
+
+
+def random_city(seed, n_boxes=40, extent=60.0, q=2.0, porous=False, glass=False, thin=False):
+    """A small random box pile on a ground, every face a sensor; slots: 0 opaque, 1 porous, 2 glass, 3 thin pane box."""
+    rng = np.random.default_rng(seed)
+    build, ground, panes = Mesh(), Mesh(), Mesh()
+    ground.grid((-extent, -extent, 0), (2 * extent, 0, 0), (0, 2 * extent, 0), 8, 8)
+    for _ in range(n_boxes):
+        x0, y0 = rng.uniform(-extent * 0.8, extent * 0.6, 2)
+        w, d = rng.uniform(3, 15, 2)
+        h = rng.uniform(3, 25)
+        choices = [0, 0] + ([1] if porous else []) + ([2] if glass else [])
+        _box_faces(build, x0, y0, w, d, h, q, int(rng.choice(choices)))
+    if thin:   # 10 cm pane boxes (thin solids), slot 3
+        for _ in range(6):
+            x0, y0 = rng.uniform(-extent * 0.7, extent * 0.7, 2)
+            _box_faces(panes, x0, y0, 8.0, 0.05, rng.uniform(4, 12), 4.0, 3)
+    meshes = [(build, True, True), (ground, True, True)]
+    if thin:
+        meshes.append((panes, False, True))
+    return assemble(meshes)
+
+
+def hemisphere_dirs(n_sky, n_sun, seed=0):
+    """A direction table shaped as the reference's: [sky n_sky | ground = -sky | sun n_sun], unit float32."""
+    rng = np.random.default_rng(seed)
+    z = rng.uniform(0.02, 1.0, n_sky)
+    a = rng.uniform(0, 2 * np.pi, n_sky)
+    r = np.sqrt(1 - z * z)
+    sky = np.stack([r * np.sin(a), r * np.cos(a), z], axis=1)
+    z2 = rng.uniform(0.01, 0.95, n_sun)
+    a2 = rng.uniform(0, 2 * np.pi, n_sun)
+    r2 = np.sqrt(1 - z2 * z2)
+    sun = np.stack([r2 * np.sin(a2), r2 * np.cos(a2), z2], axis=1)
+    D = np.concatenate([sky, -sky, sun]).astype(np.float32)
+    return D

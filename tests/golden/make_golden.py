@@ -1,0 +1,197 @@
+"""Generates the golden fixtures under tests/golden/ (run here, where the reference tree is present; the GPU machine only
+reads the committed fixtures).
+
+Each case runs the reference's own host code - its C ABI dl_run (kit-sim_daylight src/c_api.cpp) with the CLI's flags,
+compiled from the reference tree by `make -C oracle ref` - on the oracle behind the engine's C++ shim, with the shim's
+recorder on (KGB_RECORD): every call at the engine boundary (gpu_build, gpu_set_scene, gpu_trace, gpu_reduce, ...) is
+written with its inputs and results to tests/golden/<case>/. The tests replay them on the engine and on the oracle.
+
+It also extracts the reference's published outputs for tests/box.obj from its docs (docs/daylight.md, docs/views.md:
+the example blocks) into published.json, and checks the recorded runs against them.
+
+usage: python tests/golden/make_golden.py [--ref /root/reference]
+"""
+import argparse
+import ctypes
+import json
+import os
+import shutil
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+DL_DAYLIGHT, DL_VIEWS = 0, 1
+
+CASES = {
+    # config 1: box.obj, a clear-sky year in Berlin, Tregenza sky (docs/daylight.md:133-149 publishes radiation + sunhours)
+    "box_clearsky": (DL_DAYLIGHT, ["--clear-sky", "--lat", "52.52", "--lon", "13.41", "--quantity", "radiation,direct,diffuse,sunhours"]),
+    # sun hours of 21 June in 10-minute steps (docs/daylight.md:163-179)
+    "box_sunhours_day": (DL_DAYLIGHT, ["--quantity", "sunhours", "--lat", "52.52", "--lon", "13.41", "--tz", "1", "--from", "06-21T00:00",
+                                       "--to", "06-22T00:00", "--step", "10"]),
+    # a week of time series with the box as glass (byte mode), reflected light (bounce pass, --sky-density 2 bins),
+    # every quantity: gpu_trace bytes, gpu_bounce, gpu_reduce_dc, gpu_series with Sdc
+    "box_week_glass": (DL_DAYLIGHT, ["--clear-sky", "--lat", "52.52", "--lon", "13.41", "--from", "06-01T00:00", "--to", "06-08T00:00",
+                                     "--quantity", "radiation,irradiance,illuminance,sunhours", "--timeseries", "@TMP@/series.npy",
+                                     "--optics", "box=0,0.64,glass;ground=0.25", "--transmission", "on", "--bounces", "2",
+                                     "--bounce-samples", "256", "--sky-density", "2", "--patch-samples", "4"]),
+    # views defaults (docs/views.md:333-349)
+    "box_views": (DL_VIEWS, []),
+    # views all around at 4 degree cells: isovist volume, reach 6/20/50, the box as a target group, jitter on
+    "box_views360": (DL_VIEWS, ["--fov", "360", "--cell", "4", "--reach", "en17037", "--target", "box=landmark", "--distance",
+                                "isovist,mean,min,group"]),
+    # the urban block's sky (config 2): the direction table (577 Reinhart patches, their ground mirror, the sun-up hours)
+    # and the per-quantity weights under the synthetic urban weather, from a one-quad run (they do not depend on the
+    # geometry); the bench traces the full block with them
+    "urban_sky": (DL_DAYLIGHT, ["--epw", "@TMP@/urban.epw", "--sky-density", "2", "--quantity", "radiation,irradiance,illuminance,sunhours"]),
+}
+MESH = {"urban_sky": "quad"}   # cases on one 1 m quad instead of tests/box.obj
+
+
+def urban_weather(ref, tmp):
+    """The synthetic EPW of the urban configs: the reference's clear sky (Ineichen, TL 3) at Berlin, each hour's DNI and
+    DHI times a cloud factor c ~ Beta(2, 1.5) with 3-day AR(1) persistence (Gaussian copula, rho = exp(-1/72),
+    numpy seed 2024). Written as an 8760-row EPW with the LOCATION Berlin 52.52 N 13.41 E, UTC+1."""
+    from scipy import special, stats
+    dump = os.path.join(tmp, "sun.txt")
+    L, run = _lib(ref)
+    run(L, DL_DAYLIGHT, ["--clear-sky", "--lat", "52.52", "--lon", "13.41", "--tz", "1", "--quantity", "radiation", "--dump-sun", dump], "quad")
+    rows = [l.split() for l in open(dump) if not l.startswith("#")]
+    dni = np.array([float(r[10]) for r in rows])
+    dhi = np.array([float(r[11]) for r in rows])
+    assert len(dni) == 8760
+    rng = np.random.default_rng(2024)
+    rho = np.exp(-1 / 72)
+    z = np.zeros(8760)
+    z[0] = rng.standard_normal()
+    for t in range(1, 8760):
+        z[t] = rho * z[t - 1] + np.sqrt(1 - rho * rho) * rng.standard_normal()
+    c = stats.beta.ppf(0.5 * special.erfc(-z / np.sqrt(2)), 2.0, 1.5)
+    head = ["LOCATION,Berlin synthetic,,DEU,synthetic,000000,52.52,13.41,1.0,34.0", "DESIGN CONDITIONS,0", "TYPICAL/EXTREME PERIODS,0",
+            "GROUND TEMPERATURES,0", "HOLIDAYS/DAYLIGHT SAVINGS,No,0,0,0", "COMMENTS 1,clear sky x Beta(2 1.5) AR(1) cloud factor",
+            "COMMENTS 2,kit-sim GB300 urban configs", "DATA PERIODS,1,1,Data,Sunday, 1/ 1,12/31"]
+    with open(os.path.join(tmp, "urban.epw"), "w") as f:
+        f.write("\n".join(head) + "\n")
+        t = 0
+        for m, nd in enumerate([31, 28, 31, 30, 31, 30, 31, 31, 30, 31, 30, 31], 1):
+            for d in range(1, nd + 1):
+                for h in range(1, 25):
+                    f.write("2017,%d,%d,%d,60,?,10,5,70,101325,0,0,300,0,%.1f,%.1f\n" % (m, d, h, c[t] * dni[t], c[t] * dhi[t]))
+                    t += 1
+    np.save(os.path.join(os.path.dirname(tmp), "cloud_factor.npy"), c.astype(np.float32))
+
+
+def lib_of(ref):
+    return os.path.join(REPO, "oracle", "_ref", "libdaylight_ref.so")
+
+
+def _lib(ref):
+    L = ctypes.CDLL(lib_of(ref))
+    L.dl_mesh_load.restype = ctypes.c_void_p
+    L.dl_mesh_load.argtypes = [ctypes.c_char_p]
+    L.dl_last_error.restype = ctypes.c_char_p
+    L.dl_run.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32,
+                         ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]
+    L.dl_result_rows.argtypes = L.dl_result_cols.argtypes = [ctypes.c_void_p]
+    L.dl_result_rows.restype = L.dl_result_cols.restype = ctypes.c_int64
+    L.dl_result_values.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]
+    L.dl_result_manifest.argtypes = [ctypes.c_void_p]
+    L.dl_result_manifest.restype = ctypes.c_char_p
+    L.dl_mesh_create.restype = ctypes.c_void_p
+    L.dl_mesh_create.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                 ctypes.c_int64, ctypes.c_void_p]
+
+    def run(L, tool, argv, mesh_kind):
+        if mesh_kind == "quad":   # one 1 m roof quad facing up
+            xyz = np.array([0, 0, 10, 1, 0, 10, 1, 1, 10, 0, 1, 10], np.float64)
+            counts = np.array([4], np.int32)
+            idx = np.array([0, 1, 2, 3], np.int32)
+            mesh = L.dl_mesh_create(b"roof", xyz.ctypes.data, 4, counts.ctypes.data, 1, idx.ctypes.data, 4, None)
+        else:
+            mesh = L.dl_mesh_load(os.path.join(ref, "tests", "box.obj").encode())
+        assert mesh, L.dl_last_error()
+        args = (ctypes.c_char_p * len(argv))(*[a.encode() for a in argv])
+        sensors = (ctypes.c_void_p * 1)(mesh)
+        res = ctypes.c_void_p()
+        rc = L.dl_run(tool, len(argv), args, sensors, 1, None, 0, None, ctypes.byref(res))
+        assert rc == 0, (rc, L.dl_last_error())
+        return res
+    return L, run
+
+
+def run_case(name, ref):
+    """In a child process: KGB_RECORD must be set before the library is loaded."""
+    tool, argv = CASES[name]
+    out = os.path.join(HERE, name)
+    tmp = os.path.join(out, "_tmp")
+    os.makedirs(tmp, exist_ok=True)
+    argv = [a.replace("@TMP@", tmp) for a in argv]
+    if name == "urban_sky":
+        urban_weather(ref, tmp)
+    L, run = _lib(ref)
+    res = run(L, tool, argv, MESH.get(name, "box"))
+    rows, cols = L.dl_result_rows(res), L.dl_result_cols(res)
+    vals = np.zeros(rows * cols, np.float64)
+    L.dl_result_values(res, vals.ctypes.data, vals.size)
+    np.save(os.path.join(out, "result.npy"), vals.reshape(rows, cols))
+    with open(os.path.join(out, "manifest.json"), "w") as f:
+        f.write(L.dl_result_manifest(res).decode())
+    shutil.rmtree(tmp, ignore_errors=True)
+
+
+def published(ref):
+    """The example outputs the reference's docs print for tests/box.obj (numbers only, as printed)."""
+    out = {}
+    txt = open(os.path.join(ref, "docs", "daylight.md")).read()
+    i = txt.index("daylight tests/box.obj --clear-sky --lat 52.52 --lon 13.41 --quantity radiation,sunhours")
+    blk = txt[i:].split("```")[0].strip().splitlines()[1:]
+    out["box_clearsky"] = {"source": "docs/daylight.md (tests/box.obj, a clear-sky year in Berlin)", "columns": ["radiation_front", "sunhours_front"],
+                           "values": [[float(x) for x in l.split()] for l in blk]}
+    i = txt.index("daylight tests/box.obj --quantity sunhours --lat 52.52 --lon 13.41 --tz 1 --from 06-21T00:00")
+    blk = txt[i:].split("```")[0].strip().splitlines()[1:]
+    out["box_sunhours_day"] = {"source": "docs/daylight.md (sun hours of one day)", "columns": ["sunhours_front"],
+                               "values": [[float(x) for x in l.split()] for l in blk]}
+    txt = open(os.path.join(ref, "docs", "views.md")).read()
+    i = txt.index("views tests/box.obj\n")
+    blk = txt[i:].split("```")[0].strip().splitlines()[1:]
+    out["box_views"] = {"source": "docs/views.md (tests/box.obj, defaults)",
+                        "columns": ["sky_front", "ground_front", "obstruction_front", "distance_front", "distance_min_front"],
+                        "values": [[float(x) for x in l.split()] for l in blk]}
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--case")
+    a = ap.parse_args()
+    if a.case:
+        run_case(a.case, a.ref)
+        return
+    subprocess.check_call(["make", "-s", "-j8", "-C", os.path.join(REPO, "oracle"), "ref", "REF=" + a.ref])
+    for name in CASES:
+        d = os.path.join(HERE, name)
+        shutil.rmtree(d, ignore_errors=True)
+        os.makedirs(d)
+        env = dict(os.environ, KGB_RECORD=d, KGB_ORACLE_THREADS="8")
+        subprocess.check_call([sys.executable, __file__, "--ref", a.ref, "--case", name], env=env)
+        n = sum(1 for _ in open(os.path.join(d, "calls.jsonl")))
+        print("%s: %d calls recorded" % (name, n))
+    pub = published(a.ref)
+    with open(os.path.join(HERE, "published.json"), "w") as f:
+        json.dump(pub, f, indent=1)
+    for name, p in pub.items():
+        got = np.load(os.path.join(HERE, name, "result.npy"))
+        cols = json.load(open(os.path.join(HERE, name, "manifest.json")))["columns"]
+        want = np.array(p["values"])
+        for k, c in enumerate(p["columns"]):
+            g = got[:, cols.index(c)]
+            w = want[:, k]
+            rel = np.abs(g - w) / np.maximum(np.abs(w), 1e-9)
+            print("%s %s: max rel diff vs published %.3g (max abs %.3g)" % (name, c, rel.max(), np.abs(g - w).max()))
+
+
+if __name__ == "__main__":
+    main()
