@@ -190,6 +190,10 @@ KGB_API void kgb_dims(const kgb_engine* e, uint64_t out[6]);
 /* The CUDA stream (a cudaStream_t) the engine's work runs on from now on; NULL: the engine's own stream. Calls still
  * return after their work is done; a caller times them with events on this stream. */
 KGB_API int kgb_set_stream(kgb_engine* e, void* stream);
+/* The form kgb_series computes in: 0 (default) the split-BF16 contraction on the tensor cores (tcgen05, FP32
+ * accumulation, the sun term in FP32), 1 the plain FP32 form (one thread per sensor, the reference's k_series
+ * restated), kept as the measured baseline. */
+KGB_API int kgb_set_series_form(kgb_engine* e, int form);
 /* Instrumentation for the traversal roofline: traces sensors [i0, i0+nc) exactly as kgb_trace does (same bits / bytes
  * left on the device) with counting kernels, out[0] = BVH nodes visited, out[1] = triangles tested, out[2] = rays
  * traced past the hemisphere cull, out[3] = BVH bytes (nodes + triangle records). */

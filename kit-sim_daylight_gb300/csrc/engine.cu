@@ -75,6 +75,8 @@ struct Engine {
   Buf scratch, out;
   Buf ctl;   // [0] task counter, [1] status, [2..7] three u64 counters of the instrumented kernels
   bool ownStream = true;
+  int seriesForm = 0;         // 0 split-BF16 tensor cores, 1 plain FP32
+  Buf vhi, vlo, shi, slo, csr, sunCol;
   kgb_stats stats{};
   int gridBits = 0, gridView = 0;
 };
@@ -136,7 +138,8 @@ KGB_API void kgb_destroy(kgb_engine* e) {
   Engine* g = E(e);
   if (g->st) cudaStreamSynchronize(g->st);
   delete g->sc;
-  for (Buf* b : {&g->slots, &g->P, &g->N, &g->D, &g->vis, &g->dc, &g->viewCls, &g->viewDist, &g->rowSin, &g->label, &g->scratch, &g->out, &g->ctl}) b->free();
+  for (Buf* b : {&g->slots, &g->P, &g->N, &g->D, &g->vis, &g->dc, &g->viewCls, &g->viewDist, &g->rowSin, &g->label, &g->scratch, &g->out, &g->ctl,
+                 &g->vhi, &g->vlo, &g->shi, &g->slo, &g->csr, &g->sunCol}) b->free();
   for (cudaEvent_t ev : g->ev) if (ev) cudaEventDestroy(ev);
   if (g->st && g->ownStream) cudaStreamDestroy(g->st);
   delete g;
@@ -192,6 +195,7 @@ KGB_API void kgb_trim(kgb_engine* e, int sensors) {
   Engine& g = *E(e);
   cudaStreamSynchronize(g.st);
   g.vis.free(); g.dc.free(); g.scratch.free(); g.out.free(); g.viewCls.free(); g.viewDist.free();
+  g.vhi.free(); g.vlo.free(); g.shi.free(); g.slo.free(); g.csr.free(); g.sunCol.free();
   g.viewN = 0;
   if (sensors) { g.P.free(); g.N.free(); g.label.free(); g.nLabel = 0; g.nSensors = 0; }
 }
@@ -359,10 +363,61 @@ KGB_API int kgb_series(kgb_engine* e, size_t nc, const kgb_series_in* in, float*
   a.dc = in->Sdc ? static_cast<const float*>(g.dc.p) : nullptr;
   a.Sdc = in->Sdc ? reinterpret_cast<const float*>(b + off[8]) : nullptr;
   a.E = static_cast<float*>(g.out.p);
-  launch_series_fp32(a, g.st);
-  CU(cudaGetLastError());
+  // the tensor-core form: each sun direction on a column of its own (the reference's: one sun per sun-up step)
+  std::vector<int32_t> sunOfCol(T, -1);
+  bool tc = g.seriesForm == 0;
+  for (uint32_t j = 0; tc && j < in->nSun; ++j) {
+    if (sunOfCol[size_t(in->sunStep[j])] >= 0) tc = false;
+    else sunOfCol[size_t(in->sunStep[j])] = int32_t(j);
+  }
+  if (!tc) {
+    launch_series_fp32(a, g.st);
+    CU(cudaGetLastError());
+  } else {
+    const uint32_t P = uint32_t(in->P), nBins = in->Sdc ? uint32_t(g.nBins) : 0u;
+    const size_t Kp = (size_t(P) + 1 + nBins + 63) / 64 * 64;
+    // directions per patch (CSR, each patch's directions in order)
+    std::vector<int32_t> first(P + 1, 0), dirs(in->nSky);
+    for (uint32_t d = 0; d < in->nSky; ++d) first[size_t(in->row[d]) + 1]++;
+    for (uint32_t p = 0; p < P; ++p) first[p + 1] += first[p];
+    {
+      std::vector<int32_t> at(first.begin(), first.end() - 1);
+      for (uint32_t d = 0; d < in->nSky; ++d) dirs[size_t(at[size_t(in->row[d])]++)] = int32_t(d);
+    }
+    const size_t csrBytes = (first.size() + dirs.size()) * 4;
+    if (!grow(g.vhi, nc * Kp * 2) || !grow(g.vlo, nc * Kp * 2) || !grow(g.shi, T * Kp * 2) || !grow(g.slo, T * Kp * 2) ||
+        !grow(g.csr, csrBytes) || !grow(g.sunCol, T * 4)) return 0;
+    int32_t* dFirst = static_cast<int32_t*>(g.csr.p);
+    int32_t* dDirs = dFirst + first.size();
+    CU(cudaMemcpyAsync(dFirst, first.data(), first.size() * 4, cudaMemcpyHostToDevice, g.st));
+    if (!dirs.empty()) CU(cudaMemcpyAsync(dDirs, dirs.data(), dirs.size() * 4, cudaMemcpyHostToDevice, g.st));
+    CU(cudaMemcpyAsync(g.sunCol.p, sunOfCol.data(), T * 4, cudaMemcpyHostToDevice, g.st));
+    SeriesTcPlan p{};
+    p.nc = uint32_t(nc); p.T = uint32_t(T); p.Kp = uint32_t(Kp); p.sun0 = in->sun0; p.numSMs = g.numSMs;
+    p.vhi = g.vhi.p; p.vlo = g.vlo.p; p.shi = g.shi.p; p.slo = g.slo.p;
+    p.sunOfCol = static_cast<const int32_t*>(g.sunCol.p); p.sunVec = a.sunVec; p.sunW = a.sunW;
+    p.bits = a.bits; p.bytes = a.bytes; p.N = a.N; p.E = a.E; p.status = static_cast<uint32_t*>(g.ctl.p) + 1;
+    SeriesOperands o{};
+    o.P = P; o.nBins = nBins; o.D = a.D; o.patchFirst = dFirst; o.patchDirs = dDirs; o.wsky = a.wsky; o.G = a.G; o.dc = a.dc;
+    o.S = a.S; o.g = a.g; o.Sdc = a.Sdc; o.rebuildS = true;
+    if (!reset_ctl(g)) return 0;
+    build_series_operands(p, o, g.st);
+    CU(cudaGetLastError());
+    if (const char* why = series_tc(p, g.st)) return fail(why);
+    CU(cudaGetLastError());
+    uint32_t status = 0;
+    CU(cudaMemcpyAsync(&status, static_cast<uint32_t*>(g.ctl.p) + 1, 4, cudaMemcpyDeviceToHost, g.st));
+    CU(cudaStreamSynchronize(g.st));
+    if (status & kStatusTimeout) return fail("gpu_series: the tensor-core pipeline timed out waiting (status recorded by the kernel)");
+  }
   CU(cudaMemcpyAsync(Eh, g.out.p, nc * T * 4, cudaMemcpyDeviceToHost, g.st));
   CU(cudaStreamSynchronize(g.st));
+  return 1;
+}
+
+KGB_API int kgb_set_series_form(kgb_engine* e, int form) {
+  if (form != 0 && form != 1) return fail("kgb_set_series_form: 0 (tensor cores) or 1 (plain FP32)");
+  E(e)->seriesForm = form;
   return 1;
 }
 

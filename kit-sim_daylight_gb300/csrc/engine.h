@@ -12,7 +12,7 @@ namespace kgb {
 struct Node8;
 struct TriRec;
 
-enum : uint32_t { kStatusStackOverflow = 1u };
+enum : uint32_t { kStatusStackOverflow = 1u, kStatusTimeout = 2u };
 
 // k_bits / k_bytes: sensors [first, first + n) of the engine's arrays, written to columns [out0, out0 + n) of a chunk
 // whose row stride is `stride` sensors.
@@ -114,6 +114,39 @@ struct SeriesArgs {
   float* E;
 };
 void launch_series_fp32(const SeriesArgs& a, cudaStream_t st);
+
+// time series on the tensor cores (series_tc.cu): split-BF16 operands, tcgen05 MMA, sun term in the epilogue
+struct SeriesTcPlan {
+  uint32_t nc, T, Kp, sun0;
+  int numSMs;
+  void* vhi;               // [nc x Kp] bf16
+  void* vlo;
+  void* shi;               // [T x Kp] bf16
+  void* slo;
+  const int32_t* sunOfCol; // [T]: the sun direction of column t, or -1
+  const float* sunVec;
+  const float* sunW;
+  const uint32_t* bits;
+  const uint8_t* bytes;
+  const float* N;          // the chunk's normals
+  float* E;                // [nc x T]
+  uint32_t* status;
+};
+struct SeriesOperands {
+  uint32_t P, nBins;
+  const float* D;
+  const int32_t* patchFirst;
+  const int32_t* patchDirs;
+  const float* wsky;
+  const float* G;
+  const float* dc;
+  const float* S;
+  const float* g;
+  const float* Sdc;
+  bool rebuildS;
+};
+void build_series_operands(const SeriesTcPlan& p, const SeriesOperands& o, cudaStream_t st);
+const char* series_tc(const SeriesTcPlan& p, cudaStream_t st);   // null, or what failed
 
 // host BVH builder (bvh_build.cpp): binned-SAH binary BVH, collapsed to the 8-wide quantised layout of rt.cuh
 struct BvhOut {

@@ -88,6 +88,7 @@ SIGNATURES = [
     ("kgb_bounce_flags", c_uint32, [c_int]),
     ("kgb_dims", None, [_E, POINTER(c_uint64)]),
     ("kgb_set_stream", c_int, [_E, c_void_p]),
+    ("kgb_set_series_form", c_int, [_E, c_int]),
     ("kgb_trace_counters", c_int, [_E, c_size_t, c_size_t, c_uint32, POINTER(c_uint64)]),
 ]
 
@@ -198,6 +199,10 @@ class Engine:
     def set_stream(self, stream_handle):
         """Run on this cudaStream_t (an int handle, e.g. torch.cuda.Stream().cuda_stream); None: the engine's own."""
         self._ok(self.d.kgb_set_stream(self.h, c_void_p(stream_handle) if stream_handle else None))
+
+    def set_series_form(self, form):
+        """0: split-BF16 on the tensor cores (default); 1: the plain FP32 form."""
+        self._ok(self.d.kgb_set_series_form(self.h, form))
 
     def trace_counters(self, i0, nc, flags):
         """The instrumented trace: dict(nodes, tris, rays, bvh_bytes) for the roofline (results as trace())."""
