@@ -186,6 +186,22 @@ KGB_API uint32_t kgb_bounce_flags(int cullBackfaces);
  * out[5] = 1 when the last trace wrote bytes. */
 KGB_API void kgb_dims(const kgb_engine* e, uint64_t out[6]);
 
+/* --- sky (no C ABI counterpart in the reference: it builds its sky on the host) ---------------------------------- */
+/* One time step of the sky model, the inputs of the reference's gendaymtx_step (src/sky.cpp:297): day of year (as
+ * gendaymtx computes it), sun altitude and azimuth (radians, azimuth clockwise from north), DNI and DHI (W/m2). */
+typedef struct kgb_sky_step {
+  int32_t jd, pad;
+  double alt, azi, dni, dhi;
+} kgb_sky_step;
+/* The Perez all-weather sky + AddDirect of T steps at sky density mf (1, 2, 4) on the GPU in FP64, restating
+ * gendaymtx_step (src/sky.cpp:297-474, called per step by src/run.cpp:372-446): out [T x 3 (P + 1)] floats, each step's
+ * row as gendaymtx_step writes it (ground first, then the patches; RGB). sun / sky / visible as its flags. */
+KGB_API int kgb_sky(kgb_engine* e, int32_t mf, const kgb_sky_step* steps, size_t T, double grefl, int32_t sun, int32_t sky,
+                    int32_t visible, float* out);
+/* NOAA solar positions of T steps on the GPU in FP64, restating sun_noaa (src/solar.cpp:66-105): in [T x 7] = lat, lon,
+ * tz, month, day, hour (decimal), leap; out [T x 6] = altitude (deg, refracted), azimuth (deg), up, direction x y z. */
+KGB_API int kgb_sun_noaa(kgb_engine* e, const double* in, size_t T, double* out);
+
 /* --- no reference counterpart ---------------------------------------------------------------------------------- */
 /* The CUDA stream (a cudaStream_t) the engine's work runs on from now on; NULL: the engine's own stream. Calls still
  * return after their work is done; a caller times them with events on this stream. */

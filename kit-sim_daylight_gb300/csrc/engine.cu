@@ -415,6 +415,16 @@ KGB_API int kgb_series(kgb_engine* e, size_t nc, const kgb_series_in* in, float*
   return 1;
 }
 
+KGB_API int kgb_sky(kgb_engine* e, int32_t mf, const kgb_sky_step* steps, size_t T, double grefl, int32_t sun, int32_t sky,
+                    int32_t visible, float* out) {
+  if (const char* why = sky_steps(mf, steps, T, grefl, sun, sky, visible, out, E(e)->st)) return fail(why);
+  return 1;
+}
+KGB_API int kgb_sun_noaa(kgb_engine* e, const double* in, size_t T, double* out) {
+  if (const char* why = sun_steps(in, T, out, E(e)->st)) return fail(why);
+  return 1;
+}
+
 KGB_API int kgb_set_series_form(kgb_engine* e, int form) {
   if (form != 0 && form != 1) return fail("kgb_set_series_form: 0 (tensor cores) or 1 (plain FP32)");
   E(e)->seriesForm = form;

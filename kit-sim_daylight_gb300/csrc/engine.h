@@ -148,6 +148,10 @@ struct SeriesOperands {
 void build_series_operands(const SeriesTcPlan& p, const SeriesOperands& o, cudaStream_t st);
 const char* series_tc(const SeriesTcPlan& p, cudaStream_t st);   // null, or what failed
 
+// sky (sky.cu): Perez sky of T steps, NOAA sun positions; null or what failed
+const char* sky_steps(int mf, const kgb_sky_step* steps, size_t T, double grefl, int sun, int sky, int visible, float* out, cudaStream_t st);
+const char* sun_steps(const double* in, size_t T, double* out, cudaStream_t st);
+
 // host BVH builder (bvh_build.cpp): binned-SAH binary BVH, collapsed to the 8-wide quantised layout of rt.cuh
 struct BvhOut {
   std::vector<uint32_t> nodes;   // 20 words per node

@@ -41,6 +41,10 @@ class SeriesIn(ctypes.Structure):
                 ("sunStep", POINTER(c_int32)), ("sunVec", POINTER(c_float)), ("sunW", POINTER(c_float)), ("Sdc", POINTER(c_float))]
 
 
+class SkyStep(ctypes.Structure):
+    _fields_ = [("jd", c_int32), ("pad", c_int32), ("alt", c_double), ("azi", c_double), ("dni", c_double), ("dhi", c_double)]
+
+
 class BounceIn(ctypes.Structure):
     _fields_ = [("N", c_uint32), ("M", c_uint32), ("mf", c_int32), ("north", c_double), ("cancel", CANCEL_FN), ("cancelCtx", c_void_p)]
 
@@ -88,6 +92,8 @@ SIGNATURES = [
     ("kgb_bounce_flags", c_uint32, [c_int]),
     ("kgb_dims", None, [_E, POINTER(c_uint64)]),
     ("kgb_set_stream", c_int, [_E, c_void_p]),
+    ("kgb_sky", c_int, [_E, c_int32, c_void_p, c_size_t, c_double, c_int32, c_int32, c_int32, c_void_p]),
+    ("kgb_sun_noaa", c_int, [_E, c_void_p, c_size_t, c_void_p]),
     ("kgb_set_series_form", c_int, [_E, c_int]),
     ("kgb_trace_counters", c_int, [_E, c_size_t, c_size_t, c_uint32, POINTER(c_uint64)]),
 ]
@@ -199,6 +205,24 @@ class Engine:
     def set_stream(self, stream_handle):
         """Run on this cudaStream_t (an int handle, e.g. torch.cuda.Stream().cuda_stream); None: the engine's own."""
         self._ok(self.d.kgb_set_stream(self.h, c_void_p(stream_handle) if stream_handle else None))
+
+    def sky(self, mf, steps, grefl=0.2, sun=False, sky=True, visible=False):
+        """steps: [T x 5] (jd, alt, azi, dni, dhi). Returns [T x (P + 1) x 3] floats (gendaymtx_step rows)."""
+        steps = np.asarray(steps, np.float64).reshape(-1, 5)
+        st = np.zeros(len(steps), dtype=[("jd", "<i4"), ("pad", "<i4"), ("alt", "<f8"), ("azi", "<f8"), ("dni", "<f8"), ("dhi", "<f8")])
+        st["jd"] = steps[:, 0].astype(np.int32)
+        st["alt"], st["azi"], st["dni"], st["dhi"] = steps[:, 1], steps[:, 2], steps[:, 3], steps[:, 4]
+        P = 144 * mf * mf + 1
+        out = np.zeros((len(steps), P + 1, 3), np.float32)
+        self._ok(self.d.kgb_sky(self.h, mf, st.ctypes.data_as(c_void_p), len(st), grefl, int(sun), int(sky), int(visible), _p(out)))
+        return out
+
+    def sun_noaa(self, rows):
+        """rows: [T x 7] (lat, lon, tz, month, day, hour, leap). Returns [T x 6] (alt, azi, up, x, y, z)."""
+        rows = np.ascontiguousarray(rows, np.float64).reshape(-1, 7)
+        out = np.zeros((len(rows), 6), np.float64)
+        self._ok(self.d.kgb_sun_noaa(self.h, _p(rows), len(rows), _p(out)))
+        return out
 
     def set_series_form(self, form):
         """0: split-BF16 on the tensor cores (default); 1: the plain FP32 form."""

@@ -958,6 +958,14 @@ KGB_API int kgb_download_view(kgb_engine* e, size_t nc, uint8_t* cls, float* dis
 
 KGB_API kgb_stats kgb_get_stats(const kgb_engine* e) { return reinterpret_cast<const Engine*>(e)->stats; }
 KGB_API int kgb_set_stream(kgb_engine*, void*) { return 1; }   // no device: nothing to select
+// The sky side is not restated here: its checker is the reference's own sky.cpp / solar.cpp, whose outputs
+// tests/golden/sky holds (oracle/ref_sky_golden.cpp).
+KGB_API int kgb_sky(kgb_engine*, int32_t, const kgb_sky_step*, size_t, double, int32_t, int32_t, int32_t, float*) {
+  return fail("kgb_sky: the sky's checker is the reference's own code (tests/golden/sky)");
+}
+KGB_API int kgb_sun_noaa(kgb_engine*, const double*, size_t, double*) {
+  return fail("kgb_sun_noaa: the sun's checker is the reference's own code (tests/golden/sky)");
+}
 KGB_API int kgb_set_series_form(kgb_engine*, int form) { return form == 0 || form == 1 ? 1 : fail("kgb_set_series_form: 0 or 1"); }
 KGB_API int kgb_trace_counters(kgb_engine*, size_t, size_t, uint32_t, uint64_t out[4]) {
   out[0] = out[1] = out[2] = out[3] = 0;

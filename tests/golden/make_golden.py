@@ -162,6 +162,60 @@ def published(ref):
     return out
 
 
+def sky_goldens(ref):
+    """Inputs and the reference's own outputs for the GPU sky: sun_noaa on seeded rows; gendaymtx_step on seeded steps
+    (sun positions from sun_noaa at Berlin, DNI 0..950, DHI 0..450 W/m2, night and low sun included) at sky densities
+    1, 2, 4 and the flag sets run.cpp uses (sky only; sun only; sky visible; both)."""
+    d = os.path.join(HERE, "sky")
+    shutil.rmtree(d, ignore_errors=True)
+    os.makedirs(d)
+    exe = os.path.join(REPO, "oracle", "_ref", "ref_sky_golden")
+    rng = np.random.default_rng(77)
+    n = 3000
+    lat = rng.uniform(-60, 70, n)
+    lon = rng.uniform(-180, 180, n)
+    tz = np.round(lon / 15) + rng.integers(-1, 2, n)
+    month = rng.integers(1, 13, n)
+    dim = np.array([31, 28, 31, 30, 31, 30, 31, 31, 30, 31, 30, 31])
+    leap = rng.integers(0, 2, n)
+    day = np.array([rng.integers(1, dim[m - 1] + (1 if (m == 2 and lp) else 0) + 1) for m, lp in zip(month, leap)])
+    hour = np.round(rng.uniform(0, 24, n) * 60) / 60
+    hour[:40] = np.arange(40) * 0.5 + 0.5   # exact half hours (the 0.01-day rounding's ties)
+    sun_in = np.stack([lat, lon, tz, month, day, hour, leap], axis=1).astype(np.float64)
+    sun_in.tofile(os.path.join(d, "sun_in.bin"))
+    subprocess.check_call([exe, "sun", os.path.join(d, "sun_in.bin"), os.path.join(d, "sun_out.bin"), str(n)])
+    cases = []
+    for mf, T, flags in [(1, 192, [(0, 1, 0), (1, 0, 0), (0, 1, 1), (1, 1, 0)]), (2, 96, [(0, 1, 0), (1, 0, 1)]), (4, 48, [(0, 1, 0)])]:
+        hrs = np.sort(rng.uniform(0, 8760, T))
+        month_, day_, h_ = [], [], []
+        for x in hrs:
+            dd = int(x // 24)
+            m = 1
+            while dd >= dim[m - 1]:
+                dd -= dim[m - 1]
+                m += 1
+            month_.append(m); day_.append(dd + 1); h_.append(x % 24)
+        rows = np.stack([np.full(T, 52.52), np.full(T, 13.41), np.full(T, 1.0), month_, day_, h_, np.zeros(T)], axis=1)
+        rows.astype(np.float64).tofile(os.path.join(d, "tmp_in.bin"))
+        subprocess.check_call([exe, "sun", os.path.join(d, "tmp_in.bin"), os.path.join(d, "tmp_out.bin"), str(T)])
+        sun = np.fromfile(os.path.join(d, "tmp_out.bin"), np.float64).reshape(T, 6)
+        jd = np.array([int(sum(dim[:m - 1]) + dy) for m, dy in zip(month_, day_)])
+        dni = rng.uniform(0, 950, T) * (rng.random(T) > 0.15)
+        dhi = rng.uniform(0, 450, T) * (rng.random(T) > 0.05)
+        steps = np.stack([jd, np.radians(sun[:, 0]), np.radians(sun[:, 1]), dni, dhi], axis=1).astype(np.float64)
+        name = "mf%d" % mf
+        steps.tofile(os.path.join(d, name + "_in.bin"))
+        for sun_f, sky_f, vis_f in flags:
+            tag = "%s_sun%d_sky%d_vis%d" % (name, sun_f, sky_f, vis_f)
+            subprocess.check_call([exe, "sky", os.path.join(d, name + "_in.bin"), os.path.join(d, tag + ".bin"), str(T), str(mf), str(sun_f),
+                                   str(sky_f), str(vis_f), "0.2"])
+            cases.append({"mf": mf, "T": T, "sun": sun_f, "sky": sky_f, "visible": vis_f, "grefl": 0.2, "in": name + "_in.bin", "out": tag + ".bin"})
+    for f in ("tmp_in.bin", "tmp_out.bin"):
+        os.remove(os.path.join(d, f))
+    json.dump({"sun": {"n": n, "in": "sun_in.bin", "out": "sun_out.bin"}, "sky": cases}, open(os.path.join(d, "index.json"), "w"), indent=1)
+    print("sky: %d sun rows, %d sky cases" % (n, len(cases)))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -179,6 +233,7 @@ def main():
         subprocess.check_call([sys.executable, __file__, "--ref", a.ref, "--case", name], env=env)
         n = sum(1 for _ in open(os.path.join(d, "calls.jsonl")))
         print("%s: %d calls recorded" % (name, n))
+    sky_goldens(a.ref)
     pub = published(a.ref)
     with open(os.path.join(HERE, "published.json"), "w") as f:
         json.dump(pub, f, indent=1)
