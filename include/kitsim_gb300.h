@@ -202,6 +202,54 @@ KGB_API int kgb_sky(kgb_engine* e, int32_t mf, const kgb_sky_step* steps, size_t
  * tz, month, day, hour (decimal), leap; out [T x 6] = altitude (deg, refracted), azimuth (deg), up, direction x y z. */
 KGB_API int kgb_sun_noaa(kgb_engine* e, const double* in, size_t T, double* out);
 
+/* --- serving (no reference counterpart: the reference runs one request at a time, src/run.cpp:35) ---------------- */
+/* A server keeps scenes resident and runs daylight and views requests of any size with continuous batching: requests
+ * are admitted as the HBM budget allows, cut into sensor chunks, and every iteration packs chunks of all admitted
+ * requests into one batch (daylight: one persistent any-hit launch + one multi-quantity reduce, a CUDA graph; views:
+ * the view kernels per chunk). Results equal the single-request entry points' bit for bit. A request's host arrays
+ * must stay valid until kgb_server_wait returns for it. */
+typedef struct kgb_server kgb_server;
+typedef struct kgb_daylight_request {
+  int32_t scene;
+  uint32_t nSensors, nDir, nQ; /* nQ quantities, 1..8 */
+  const float* P;              /* [nSensors x 3] recentred sensor points (offset applied) */
+  const float* N;              /* [nSensors x 3] unit normals */
+  const float* D;              /* [nDir x 3] directions */
+  const float* W;              /* [nQ x nDir] weights per quantity (gpu_reduce's W) */
+  uint32_t useCosMask;         /* bit q: quantity q weighted by max(0, N.D) */
+  uint32_t rayFlags;           /* visibility bits: KGB_RAY_DISABLE_ANYHIT set */
+  double* out;                 /* [nQ x nSensors] sums, as gpu_reduce gives them */
+} kgb_daylight_request;
+typedef struct kgb_views_request {
+  int32_t scene;
+  uint32_t nSensors;
+  const float* P;
+  const float* N;
+  const uint8_t* label;        /* [scene triangles] classes, or NULL (every hit an obstruction) */
+  kgb_view_in view;            /* the grid; its cancel hook is not used */
+  uint32_t rayFlags;
+  const double* wRow;          /* [nEl] */
+  uint32_t nClass;
+  double farDist;
+  const float* reach;
+  uint32_t nReach;
+  int32_t glazing;
+  uint32_t isoDim;
+  double* out;                 /* [nSensors x NA], gpu_reduce_view's columns */
+} kgb_views_request;
+KGB_API kgb_server* kgb_server_create(uint64_t hbmBudgetBytes);
+KGB_API void kgb_server_destroy(kgb_server* s);
+/* a resident scene (8-wide BVH) for requests; *sceneId its index */
+KGB_API int kgb_server_add_scene(kgb_server* s, const float* v, size_t nv, const uint32_t* tri, size_t nt, int32_t* sceneId);
+/* times calibration batches on scene 0 and keeps the fastest chunk and batch sizes (call while idle) */
+KGB_API int kgb_server_autotune(kgb_server* s);
+KGB_API int kgb_server_submit(kgb_server* s, const kgb_daylight_request* r, uint64_t* ticket);
+KGB_API int kgb_server_submit_views(kgb_server* s, const kgb_views_request* r, uint64_t* ticket);
+/* 1 once the request completed (its out written), 0 on failure or timeout (kgb_last_error) */
+KGB_API int kgb_server_wait(kgb_server* s, uint64_t ticket, double timeoutSec);
+/* out[10]: completed requests, latency p50, p90, p99, max (s), rays, batches, HBM bytes in use, chunk sensors, batch rays */
+KGB_API void kgb_server_stats(kgb_server* s, double* out);
+
 /* --- no reference counterpart ---------------------------------------------------------------------------------- */
 /* The CUDA stream (a cudaStream_t) the engine's work runs on from now on; NULL: the engine's own stream. Calls still
  * return after their work is done; a caller times them with events on this stream. */

@@ -105,6 +105,8 @@ float elapsed(Engine& g) {
 }
 
 }  // namespace
+
+int set_error(const std::string& message) { return fail(message); }
 }  // namespace kgb
 
 using namespace kgb;

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <cstddef>
 #include <cstdint>
+#include <string>
 #include <vector>
 #include "kitsim_gb300.h"
 
@@ -13,6 +14,9 @@ struct Node8;
 struct TriRec;
 
 enum : uint32_t { kStatusStackOverflow = 1u, kStatusTimeout = 2u };
+
+// the calling thread's message for kgb_last_error (engine.cu); returns 0 for the C ABI's failure status
+int set_error(const std::string& message);
 
 // k_bits / k_bytes: sensors [first, first + n) of the engine's arrays, written to columns [out0, out0 + n) of a chunk
 // whose row stride is `stride` sensors.

@@ -332,4 +332,30 @@ __device__ __forceinline__ bool closest(const Scene& s, const Ray& r, float tmin
   return any;
 }
 
+// One visibility word: bit k = direction w*32+k of a sensor (normal n, ray origin o) passes the hemisphere cull and every
+// hit from tmin 1e-5 on is an own-plane hit, at most 3 (the reference's __raygen__bits, trace_dev.cu:91-108, restated
+// over the ray's hit set). COUNT adds traversal counters and rays traced.
+template <bool COUNT>
+__device__ __forceinline__ uint32_t trace_word(const Scene& s, F3 n, F3 o, const float* D, uint32_t nDir, uint32_t w, bool cull,
+                                               uint32_t& overflow, Count& ctr, uint32_t& rays) {
+  uint32_t word = 0;
+  for (uint32_t k = 0; k < 32; ++k) {
+    const uint32_t d = w * 32 + k;
+    if (d >= nDir) break;
+    const F3 dir = ld3(D + 3 * d);
+    if (!(n.x * dir.x + n.y * dir.y + n.z * dir.z > 0.f)) continue;
+    const Ray r = make_ray(o, dir);
+    bool blocked = false;
+    int own = 0;
+    if (COUNT) ++rays;
+    for_hits<COUNT>(s, r, 1e-5f, INFINITY, cull, [&](const Hit& h, F3 v0, F3 v1, F3 v2, uint32_t, uint32_t) {
+      if (own_hit(v0, v1, v2, h, dir, n) && ++own <= 3) return false;
+      blocked = true;
+      return true;
+    }, overflow, &ctr);
+    if (!blocked) word |= 1u << k;
+  }
+  return word;
+}
+
 }  // namespace kgb

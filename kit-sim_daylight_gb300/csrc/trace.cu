@@ -33,23 +33,7 @@ __global__ void __launch_bounds__(256) k_bits(TraceArgs a) {
     if (i >= a.n) continue;
     const uint32_t gi = a.first + i;
     const F3 n = ld3(a.N + 3 * gi), o = offset_ray(ld3(a.P + 3 * gi), n);
-    uint32_t word = 0;
-    for (uint32_t k = 0; k < 32; ++k) {
-      const uint32_t d = w * 32 + k;
-      if (d >= a.nDir) break;
-      const F3 dir = ld3(a.D + 3 * d);
-      if (!(n.x * dir.x + n.y * dir.y + n.z * dir.z > 0.f)) continue;
-      const Ray r = make_ray(o, dir);
-      bool blocked = false;
-      int own = 0;
-      if (COUNT) ++rays;
-      for_hits<COUNT>(s, r, 1e-5f, INFINITY, cull, [&](const Hit& h, F3 v0, F3 v1, F3 v2, uint32_t, uint32_t) {
-        if (own_hit(v0, v1, v2, h, dir, n) && ++own <= 3) return false;
-        blocked = true;
-        return true;
-      }, overflow, &ctr);
-      if (!blocked) word |= 1u << k;
-    }
+    const uint32_t word = trace_word<COUNT>(s, n, o, a.D, a.nDir, w, cull, overflow, ctr, rays);
     a.bits[size_t(w) * a.stride + a.out0 + i] = word;
   }
   if (overflow) atomicOr(a.status, kStatusStackOverflow);

@@ -55,6 +55,17 @@ class ViewIn(ctypes.Structure):
                 ("groundZ", c_float), ("north", c_double), ("cancel", CANCEL_FN), ("cancelCtx", c_void_p)]
 
 
+class DaylightRequest(ctypes.Structure):
+    _fields_ = [("scene", c_int32), ("nSensors", c_uint32), ("nDir", c_uint32), ("nQ", c_uint32), ("P", c_void_p), ("N", c_void_p),
+                ("D", c_void_p), ("W", c_void_p), ("useCosMask", c_uint32), ("rayFlags", c_uint32), ("out", c_void_p)]
+
+
+class ViewsRequest(ctypes.Structure):
+    _fields_ = [("scene", c_int32), ("nSensors", c_uint32), ("P", c_void_p), ("N", c_void_p), ("label", c_void_p), ("view", ViewIn),
+                ("rayFlags", c_uint32), ("wRow", c_void_p), ("nClass", c_uint32), ("farDist", c_double), ("reach", c_void_p),
+                ("nReach", c_uint32), ("glazing", c_int32), ("isoDim", c_uint32), ("out", c_void_p)]
+
+
 RAY_DISABLE_ANYHIT, RAY_TERMINATE_ON_FIRST_HIT, RAY_CULL_BACK_FACING = 1, 4, 16
 SLOT_GLASS, SLOT_THIN, SLOT_INWARD, SLOT_TWIN = 1, 2, 4, 8
 LABEL_PASS, MAX_PANES, VIEW_GLAZED = 255, 16, 0x80
@@ -92,6 +103,14 @@ SIGNATURES = [
     ("kgb_bounce_flags", c_uint32, [c_int]),
     ("kgb_dims", None, [_E, POINTER(c_uint64)]),
     ("kgb_set_stream", c_int, [_E, c_void_p]),
+    ("kgb_server_create", c_void_p, [c_uint64]),
+    ("kgb_server_destroy", None, [c_void_p]),
+    ("kgb_server_add_scene", c_int, [c_void_p, c_void_p, c_size_t, c_void_p, c_size_t, POINTER(c_int32)]),
+    ("kgb_server_autotune", c_int, [c_void_p]),
+    ("kgb_server_submit", c_int, [c_void_p, POINTER(DaylightRequest), POINTER(c_uint64)]),
+    ("kgb_server_submit_views", c_int, [c_void_p, POINTER(ViewsRequest), POINTER(c_uint64)]),
+    ("kgb_server_wait", c_int, [c_void_p, c_uint64, c_double]),
+    ("kgb_server_stats", None, [c_void_p, POINTER(c_double)]),
     ("kgb_sky", c_int, [_E, c_int32, c_void_p, c_size_t, c_double, c_int32, c_int32, c_int32, c_void_p]),
     ("kgb_sun_noaa", c_int, [_E, c_void_p, c_size_t, c_void_p]),
     ("kgb_set_series_form", c_int, [_E, c_int]),
@@ -312,6 +331,83 @@ class Engine:
         dist = np.zeros(nc * K, np.float32)
         self._ok(self.d.kgb_download_view(self.h, nc, _p(cls), _p(dist), nc * K))
         return cls.reshape(nc, K), dist.reshape(nc, K)
+
+
+class Server:
+    """The engine's serving loop: resident scenes, continuous batching of daylight and views requests."""
+
+    def __init__(self, lib, hbm_budget_bytes):
+        self.lib, self.d = lib, lib.dll
+        self.h = self.d.kgb_server_create(int(hbm_budget_bytes))
+        if not self.h:
+            raise KgbError(lib.err())
+        self._live = {}
+
+    def close(self):
+        if self.h:
+            self.d.kgb_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_scene(self, v, tri):
+        v = _f32(v, (-1, 3))
+        tri = np.ascontiguousarray(tri, dtype=np.uint32).reshape(-1, 3)
+        sid = c_int32(-1)
+        if not self.d.kgb_server_add_scene(self.h, _p(v), len(v), _p(tri), len(tri), ctypes.byref(sid)):
+            raise KgbError(self.lib.err())
+        return sid.value
+
+    def autotune(self):
+        if not self.d.kgb_server_autotune(self.h):
+            raise KgbError(self.lib.err())
+
+    def submit(self, scene, P, N, D, W, use_cos, flags=5):
+        """Daylight request: W [nQ x nDir]; use_cos per quantity. Returns a ticket; wait() gives out [nQ x nSensors]."""
+        P, N, D = _f32(P, (-1, 3)), _f32(N, (-1, 3)), _f32(D, (-1, 3))
+        W = _f32(W).reshape(len(use_cos), len(D))
+        out = np.zeros((len(use_cos), len(P)), np.float64)
+        mask = sum(1 << q for q, c in enumerate(use_cos) if c)
+        r = DaylightRequest(scene, len(P), len(D), len(use_cos), _p(P), _p(N), _p(D), _p(W), mask, flags, _p(out))
+        t = c_uint64(0)
+        if not self.d.kgb_server_submit(self.h, ctypes.byref(r), ctypes.byref(t)):
+            raise KgbError(self.lib.err())
+        self._live[t.value] = (P, N, D, W, out, r)
+        return t.value
+
+    def submit_views(self, scene, P, N, nAz, nEl, az0, dAz, rowSin, wRow, nClass, farDist, reach=(), glazing=False, isoDim=0,
+                     label=None, world=False, cull=False, jitter=True, back=False, vground=True, nS=1, groundZ=0.0, north=0.0, flags=1):
+        P, N, rowSin = _f32(P, (-1, 3)), _f32(N, (-1, 3)), _f32(rowSin)
+        wRow = np.ascontiguousarray(wRow, np.float64)
+        reach = np.ascontiguousarray(reach, np.float32)
+        label = None if label is None else np.ascontiguousarray(label, np.uint8)
+        NA = 3 * nClass + 1 + len(reach) + int(bool(glazing)) + int(bool(isoDim))
+        out = np.zeros((len(P), NA), np.float64)
+        v = ViewIn(nAz, nEl, az0, dAz, _typed(rowSin, c_float), int(world), int(cull), int(jitter), int(back), int(vground), nS, groundZ,
+                   north, CANCEL_FN(), None)
+        r = ViewsRequest(scene, len(P), _p(P), _p(N), _p(label), v, flags, _p(wRow), nClass, farDist, _p(reach), len(reach), int(glazing),
+                         isoDim, _p(out))
+        t = c_uint64(0)
+        if not self.d.kgb_server_submit_views(self.h, ctypes.byref(r), ctypes.byref(t)):
+            raise KgbError(self.lib.err())
+        self._live[t.value] = (P, N, rowSin, wRow, reach, label, out, r)
+        return t.value
+
+    def wait(self, ticket, timeout=600.0):
+        if not self.d.kgb_server_wait(self.h, ticket, timeout):
+            raise KgbError(self.lib.err())
+        keep = self._live.pop(ticket)
+        return keep[4] if len(keep) == 6 else keep[6]
+
+    def stats(self):
+        out = (c_double * 10)()
+        self.d.kgb_server_stats(self.h, out)
+        keys = ["completed", "p50_s", "p90_s", "p99_s", "max_s", "rays", "batches", "hbm_bytes", "chunk_sensors", "batch_rays"]
+        return dict(zip(keys, list(out)))
 
 
 def slots_array(slots):
