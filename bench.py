@@ -273,18 +273,147 @@ def run_ours(args, pkg):
         torch.distributed.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------------------------- config 3: precision
+KRF, KGF, KBF = 0.265074126, 0.670114631, 0.064811243   # Radiance CIE_rf / gf / bf (bright())
+
+
+def patch_dirs(mf):
+    """Reinhart / Tregenza patch centres (gendaymtx order), float as the reference's make_patches + dir_from_altaz."""
+    tnaz = [30, 30, 24, 24, 18, 12, 6]
+    alpha = (np.pi / 2) / (7 * mf + .5)
+    alt, azi, om = [], [], []
+    for i in range(7 * mf):
+        n = tnaz[i // mf] * mf
+        for j in range(n):
+            alt.append(np.float32(alpha * (i + .5)))
+            azi.append(np.float32(2 * np.pi * j / n))
+            om.append(np.float32(2 * np.pi * (np.sin(alpha * (i + 1)) - np.sin(alpha * i)) / n))
+    alt.append(np.float32(np.pi / 2)); azi.append(np.float32(0)); om.append(np.float32(2 * np.pi * (1 - np.cos(alpha * .5))))
+    a, z = np.array(alt, np.float64), np.array(azi, np.float64)
+    D = np.stack([np.cos(a) * np.sin(z), np.cos(a) * np.cos(z), np.sin(a)], axis=1).astype(np.float32)
+    return D, np.array(om, np.float32)
+
+
+def urban_year_sky(e, mf):
+    """The urban weather year's series operands on the GPU: NOAA sun per hour (kgb_sun_noaa) and the Perez sky per
+    hour and patch (kgb_sky, FP64), as the reference's run.cpp builds them on the host (physical mode, radiometric)."""
+    w = np.load(os.path.join(GOLDEN, "urban_sky", "weather.npy")).astype(np.float64)   # [2, 8760] DNI, DHI
+    dim = [31, 28, 31, 30, 31, 30, 31, 31, 30, 31, 30, 31]
+    month = np.repeat(np.arange(1, 13), [24 * d for d in dim])
+    day = np.concatenate([np.repeat(np.arange(1, d + 1), 24) for d in dim])
+    hour = np.tile(np.arange(24) + 0.5, 365)
+    jd = np.repeat(np.arange(1, 366), 24)
+    rows = np.stack([np.full(8760, 52.52), np.full(8760, 13.41), np.full(8760, 1.0), month, day, hour, np.zeros(8760)], axis=1)
+    t0 = time.perf_counter()
+    sun = e.sun_noaa(rows)
+    steps = np.stack([jd, np.radians(sun[:, 0]), np.radians(sun[:, 1]), w[0], w[1]], axis=1)
+    sky = e.sky(mf, steps, grefl=0.2, sun=False, sky=True, visible=False)
+    sky_s = time.perf_counter() - t0
+    bright = KRF * sky[:, :, 0] + KGF * sky[:, :, 1] + KBF * sky[:, :, 2]
+    col = (w[0] + w[1]) > 1e-4
+    colOf = np.cumsum(col) - 1
+    S = np.ascontiguousarray(bright[col, 1:].T, np.float32)
+    g = np.ascontiguousarray(bright[col, 0], np.float32)
+    up = sun[:, 2] > 0
+    sunVec = sun[up, 3:6].astype(np.float32)
+    ups = np.nonzero(up)[0]
+    sunStep = np.where(col[ups], colOf[ups], 0).astype(np.int32)
+    sunW = np.where(col[ups], w[0][ups], 0).astype(np.float32)
+    return dict(S=S, g=g, sunVec=sunVec, sunStep=sunStep, sunW=sunW, sky_s=sky_s, T=int(col.sum()))
+
+
+def run_precision(args, pkg):
+    import torch
+    torch.cuda.set_device(0)
+    kgb = pkg.kgb
+    lib = pkg.load()
+    e = pkg.engine()
+    mf = 4
+    Dsky, omega = patch_dirs(mf)
+    P = len(Dsky)
+    yr = urban_year_sky(e, mf)
+    D = np.concatenate([Dsky, -Dsky, yr["sunVec"]]).astype(np.float32)
+    nSky, sun0 = P, 2 * P
+    scene = pkg.workloads.urban_block(glass_share=0.2)
+    slots = [(0.2, 0, 0, 0), (0.0, 0.64, kgb.tn_from_Tn(0.64), kgb.SLOT_GLASS), (0.2, 0, 0, 0)]
+    e.build(scene["v"], scene["tri"], scene["slot"], slots)
+    e.set_slots(slots)
+    e.set_scene(scene["P"], scene["N"], D)
+    nc_all, T = len(scene["P"]), yr["T"]
+    Wg = np.zeros(len(D), np.float32)
+    Wg[nSky:2 * nSky] = omega
+    flags = lib.ray_flags(False, True)   # a slot transmits: bytes
+    chunk = max(1, (256 << 20) // len(D))   # the reference's 256 MiB cap on the per-chunk visibility
+    sargs = dict(nSky=nSky, row=np.arange(nSky), wsky=omega, S=yr["S"], g=yr["g"], sun0=sun0, sunStep=yr["sunStep"], sunVec=yr["sunVec"],
+                 sunW=yr["sunW"])
+    tt = {"trace": 0.0, "tc": 0.0, "fp32": 0.0}
+    first = None
+    for i0 in range(0, nc_all, chunk):
+        nc = min(chunk, nc_all - i0)
+        t0 = time.perf_counter()
+        e.trace(i0, nc, flags)
+        torch.cuda.synchronize()
+        tt["trace"] += time.perf_counter() - t0
+        G = e.reduce(nc, Wg, True).astype(np.float32)
+        for form, key in ((0, "tc"), (1, "fp32")):
+            if key == "fp32" and i0 > 0 and not args.full_fp32:
+                continue   # the plain FP32 form is timed on the first chunk (it is the slow one)
+            e.set_series_form(form)
+            t0 = time.perf_counter()
+            E = e.series(nc, G=G, **sargs)
+            tt[key] += time.perf_counter() - t0
+            if i0 == 0:
+                if form == 0:
+                    first = (E, G)
+                else:
+                    fp32_first = E
+    e.set_series_form(0)
+    # accuracy: the first chunk's seeded sample against the oracle's FP64 contraction of the same FP32 weights
+    sub = np.sort(np.random.default_rng(9).choice(min(chunk, nc_all), 64, replace=False))
+    subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle"), "all"])
+    o = kgb.Engine(kgb.Lib(os.path.join(REPO, "oracle", "_build", "liboracle.so")))
+    o.build(scene["v"], scene["tri"], scene["slot"], slots)
+    o.set_slots(slots)
+    o.set_scene(scene["P"][sub], scene["N"][sub], D)
+    o.trace(0, len(sub), flags)
+    E64 = o.series(len(sub), G=first[1][sub], **sargs)
+    o.close()
+    def colerr(E):
+        cmax = np.abs(E64).max(axis=0)
+        live = cmax > 0
+        return np.abs(E[sub] - E64).max(axis=0)[live] / cmax[live]
+    ce, ce32 = colerr(first[0]), colerr(fp32_first)
+    n_fp32 = nc_all if args.full_fp32 else min(chunk, nc_all)
+    line = {"metric": "radiation solves/s", "unit": "sensor-steps/s",
+            "value": nc_all * T / tt["tc"], "fp32_value": n_fp32 * T / tt["fp32"], "speedup_vs_fp32": (nc_all * T / tt["tc"]) / (n_fp32 * T / tt["fp32"]),
+            "config": {"workload": "precision: urban block, %d sensors, %d patches + ground, %d directions, %d series columns (non-night hours), "
+                                   "20%% glass tau 0.64 (byte mode), chunks of %d sensors" % (nc_all, P, len(D), T, chunk)},
+            "dtype": "split-bf16 (3 products) on tcgen05, fp32 accumulate; sun term fp32",
+            "column_error_vs_fp64": {"max": float(ce.max()), "p99": float(np.percentile(ce, 99)), "median": float(np.median(ce)),
+                                     "columns_over_1e-6": int((ce > 1e-6).sum()), "columns": int(ce.size), "sample_sensors": len(sub)},
+            "fp32_column_error_vs_fp64": {"max": float(ce32.max()), "median": float(np.median(ce32))},
+            "trace_mrays_s": nc_all * len(D) / tt["trace"] / 1e6, "sky_build_s": yr["sky_s"], "series_tc_s": tt["tc"], "series_fp32_s_timed": tt["fp32"],
+            "E_bytes": nc_all * T * 4, "E_write_gbs": nc_all * T * 4 / tt["tc"] / 1e9}
+    print(json.dumps(line), flush=True)
+    e.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-sample", type=int, default=3000)
-    ap.add_argument("--ref-sample", type=int, default=2000)
+    ap.add_argument("--cpu-sample", type=int, default=30000)
+    ap.add_argument("--ref-sample", type=int, default=20000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--config", default="urban", choices=["urban", "precision"])
+    ap.add_argument("--full-fp32", action="store_true")
     args = ap.parse_args()
     pkg = package()
-    if args.impl == "reference":
+    if args.config == "precision":
+        run_precision(args, pkg)
+    elif args.impl == "reference":
         run_reference(args, pkg)
     else:
         run_ours(args, pkg)

@@ -81,6 +81,9 @@ def urban_weather(ref, tmp):
                     f.write("2017,%d,%d,%d,60,?,10,5,70,101325,0,0,300,0,%.1f,%.1f\n" % (m, d, h, c[t] * dni[t], c[t] * dhi[t]))
                     t += 1
     np.save(os.path.join(os.path.dirname(tmp), "cloud_factor.npy"), c.astype(np.float32))
+    # the weather as written (%.1f W/m2), for the sky side of the bench's precision config
+    w = np.stack([np.round(c * dni, 1), np.round(c * dhi, 1)]).astype(np.float32)
+    np.save(os.path.join(os.path.dirname(tmp), "weather.npy"), w)
 
 
 def lib_of(ref):
