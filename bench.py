@@ -398,6 +398,159 @@ def run_precision(args, pkg):
     e.close()
 
 
+# ---------------------------------------------------------------------------------------------- config 4: views
+def run_views(args, pkg):
+    import torch
+    torch.cuda.set_device(0)
+    lib = pkg.load()
+    e = pkg.engine()
+    city = pkg.workloads.views_city()
+    t0 = time.perf_counter()
+    e.build(city["v"], city["tri"])
+    build_s = time.perf_counter() - t0
+    e.set_labels(city["label"])
+    nc = len(city["P"])
+    e.set_scene(city["P"], city["N"], np.zeros((0, 3), np.float32))
+    flags = lib.bounce_flags(False)
+    res = {}
+    for name, fov, world, iso, reach in (("fov120", 120.0, False, 0, []), ("fov360", 360.0, True, 3, [6.0, 20.0, 50.0])):
+        nAz, nEl, dAz, rowSin, wRow = pkg.workloads.views_grid(fov, 2.0)
+        kw = dict(world=world, cull=world, jitter=True, vground=True, groundZ=city["groundZ"])
+        e.view(0, min(nc, 4096), flags, nAz, nEl, 0.0 if world else -fov / 2, dAz, rowSin, **kw)   # warm-up
+        torch.cuda.synchronize()
+        best = None
+        for _ in range(max(1, args.steps)):
+            t0 = time.perf_counter()
+            e.view(0, nc, flags, nAz, nEl, 0.0 if world else -fov / 2, dAz, rowSin, **kw)
+            t1 = time.perf_counter()
+            out = e.reduce_view(nc, wRow, 6, 1000.0, reach=reach, glazing=False, isoDim=iso)
+            t2 = time.perf_counter()
+            if best is None or t1 - t0 < best[0]:
+                best = (t1 - t0, t2 - t1)
+        K = nAz * nEl
+        res[name] = {"rays": nc * K, "trace_s": best[0], "reduce_s": best[1], "mrays_s": nc * K / best[0] / 1e6,
+                     "shares_sum_check": float(np.abs(out[:, 0] + out[:, 3] + out[:, 6] + out[:, 9] + out[:, 12] + out[:, 15] + out[:, 18] - 1).max())}
+    line = {"metric": "Mrays/s (closest hit)", "unit": "Mrays/s", "value": res["fov120"]["mrays_s"],
+            "config": {"workload": "views city: %d facade sensors, %d triangles, 3 target groups; fov 120 / 2 deg (3600 rays), fov 360 / 2 deg "
+                                   "(10800 rays, isovist volume, reach 6/20/50), jitter on" % (nc, len(city["tri"]))},
+            "fov120": res["fov120"], "fov360": res["fov360"], "bvh_build_s": build_s}
+    print(json.dumps(line), flush=True)
+    e.close()
+
+
+# ---------------------------------------------------------------------------------------------- config 5: serving
+def serving_requests(pkg, scenes, rate, window, seed=5):
+    """A seeded Poisson stream: 70 % daylight (sensors log-uniform 100..200k, sky density 145 / 577 / 2305 patches, time
+    range log-uniform 1 h .. 1 year -> its sun-up hours as sun directions, radiation + sun hours), 30 % views (fov 120
+    or 360 at 2 degree cells, sensors log-uniform 1k..50k); scenes uniform over the resident four."""
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    dirs = {mf: patch_dirs(mf) for mf in (1, 2, 4)}
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > window:
+            break
+        sc = int(rng.integers(0, len(scenes)))
+        s = scenes[sc]
+        if rng.random() < 0.7:
+            n = int(min(len(s["P"]), np.exp(rng.uniform(np.log(100), np.log(200_000)))))
+            mf = int(rng.choice([1, 2, 4]))
+            hours = float(np.exp(rng.uniform(0, np.log(8760))))
+            nSun = max(0, int(hours * 0.5))
+            Dsky, om = dirs[mf]
+            sun = pkg.workloads.hemisphere_dirs(1, nSun, int(rng.integers(1 << 30)))[2:] if nSun else np.zeros((0, 3), np.float32)
+            D = np.concatenate([Dsky, -Dsky, sun]).astype(np.float32)
+            W = np.zeros((2, len(D)), np.float32)
+            W[0, :2 * len(Dsky)] = np.concatenate([om, om]) * 0.1
+            W[0, 2 * len(Dsky):] = 0.8
+            W[1, 2 * len(Dsky):] = 1.0
+            first = int(rng.integers(0, len(s["P"]) - n + 1))
+            out.append(dict(t=t, kind="daylight", scene=sc, P=s["P"][first:first + n], N=s["N"][first:first + n], D=D, W=W, use_cos=[True, False]))
+        else:
+            n = int(min(len(s["P"]), np.exp(rng.uniform(np.log(1000), np.log(50_000)))))
+            fov = float(rng.choice([120.0, 360.0]))
+            first = int(rng.integers(0, len(s["P"]) - n + 1))
+            out.append(dict(t=t, kind="views", scene=sc, P=s["P"][first:first + n], N=s["N"][first:first + n], fov=fov))
+    return out
+
+
+def run_serving(args, pkg):
+    import torch
+    torch.cuda.set_device(0)
+    lib = pkg.load()
+    kgb = pkg.kgb
+    sizes = [500_000, 1_000_000, 2_000_000, 5_000_000]
+    scenes = [pkg.workloads.views_city(seed=10 + k, n_buildings=max(2000, n // 100), target_tris=n, n_sensors=60_000) for k, n in enumerate(sizes)]
+    srv = kgb.Server(lib, 150e9)
+    ids = [srv.add_scene(s["v"], s["tri"]) for s in scenes]
+    srv.autotune()
+    reqs = serving_requests(pkg, scenes, args.rate, args.window)
+    grids = {fov: pkg.workloads.views_grid(fov, 2.0) for fov in (120.0, 360.0)}
+    t0 = time.perf_counter()
+    tickets = []
+    for r in reqs:
+        dt = r["t"] - (time.perf_counter() - t0)
+        if dt > 0:
+            time.sleep(dt)
+        if r["kind"] == "daylight":
+            tickets.append(srv.submit(ids[r["scene"]], r["P"], r["N"], r["D"], r["W"], r["use_cos"]))
+        else:
+            nAz, nEl, dAz, rowSin, wRow = grids[r["fov"]]
+            world = r["fov"] == 360.0
+            tickets.append(srv.submit_views(ids[r["scene"]], r["P"], r["N"], nAz, nEl, 0.0 if world else -r["fov"] / 2, dAz, rowSin, wRow, 6,
+                                            1000.0, reach=[6.0, 20.0, 50.0] if world else [], isoDim=3 if world else 0, label=scenes[r["scene"]]["label"],
+                                            world=world, cull=world, groundZ=scenes[r["scene"]]["groundZ"]))
+    for t in tickets:
+        srv.wait(t, 3600)
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    sensors = sum(len(r["P"]) for r in reqs)
+    # the plain form: one request per launch, FIFO, through the single-request entry points (scenes parked and attached)
+    e = pkg.engine()
+    parked = []
+    for s in scenes:
+        e.build(s["v"], s["tri"])
+        parked.append(e.detach())
+    service = []
+    cur = None
+    for r in reqs:
+        t1 = time.perf_counter()
+        if cur != r["scene"]:
+            if cur is not None:
+                parked[cur] = e.detach()
+            e.attach(parked[r["scene"]])
+            cur = r["scene"]
+        if r["kind"] == "daylight":
+            e.set_scene(r["P"], r["N"], r["D"])
+            e.trace(0, len(r["P"]), lib.ray_flags(False, False))
+            for q, c in enumerate(r["use_cos"]):
+                e.reduce(len(r["P"]), r["W"][q], c)
+        else:
+            nAz, nEl, dAz, rowSin, wRow = grids[r["fov"]]
+            world = r["fov"] == 360.0
+            e.set_labels(scenes[r["scene"]]["label"])
+            e.set_scene(r["P"], r["N"], np.zeros((0, 3), np.float32))
+            e.view(0, len(r["P"]), lib.bounce_flags(False), nAz, nEl, 0.0 if world else -r["fov"] / 2, dAz, rowSin, world=world, cull=world,
+                   groundZ=scenes[r["scene"]]["groundZ"])
+            e.reduce_view(len(r["P"]), wRow, 6, 1000.0, reach=[6.0, 20.0, 50.0] if world else [], isoDim=3 if world else 0)
+        service.append(time.perf_counter() - t1)
+    done, lat = 0.0, []
+    for r, sv in zip(reqs, service):
+        done = max(done, r["t"]) + sv
+        lat.append(done - r["t"])
+    base_wall = done
+    e.close()
+    line = {"metric": "solves/s", "unit": "sensor solves/s", "value": sensors / wall, "p50_ms": 1e3 * st["p50_s"], "p99_ms": 1e3 * st["p99_s"],
+            "plain_one_request_per_launch": {"solves_s": sensors / base_wall, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+                                             "p99_ms": 1e3 * float(np.percentile(lat, 99))},
+            "config": {"workload": "serving: Poisson %.0f req/s for %.1f s (%d requests: %d daylight, %d views), 4 resident scenes of %s triangles, "
+                                   "150 GB HBM budget" % (args.rate, args.window, len(reqs), sum(r["kind"] == "daylight" for r in reqs),
+                                                         sum(r["kind"] == "views" for r in reqs), "/".join("%.1fM" % (len(s["tri"]) / 1e6) for s in scenes))},
+            "server": {k: st[k] for k in ("completed", "batches", "rays", "chunk_sensors", "batch_rays")}, "wall_s": wall}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -407,12 +560,18 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=30000)
     ap.add_argument("--ref-sample", type=int, default=20000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--config", default="urban", choices=["urban", "precision"])
+    ap.add_argument("--config", default="urban", choices=["urban", "precision", "views", "serving"])
+    ap.add_argument("--rate", type=float, default=200.0)
+    ap.add_argument("--window", type=float, default=2.0)
     ap.add_argument("--full-fp32", action="store_true")
     args = ap.parse_args()
     pkg = package()
     if args.config == "precision":
         run_precision(args, pkg)
+    elif args.config == "views":
+        run_views(args, pkg)
+    elif args.config == "serving":
+        run_serving(args, pkg)
     elif args.impl == "reference":
         run_reference(args, pkg)
     else:

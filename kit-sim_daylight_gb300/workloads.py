@@ -173,3 +173,104 @@ def hemisphere_dirs(n_sky, n_sun, seed=0):
     sun = np.stack([r2 * np.sin(a2), r2 * np.cos(a2), z2], axis=1)
     D = np.concatenate([sky, -sky, sun]).astype(np.float32)
     return D
+
+
+def views_city(seed=42, n_buildings=20000, target_tris=2_000_000, n_sensors=50_000):
+    """The views city: rotated boxes with gable roofs (14 triangles each) on a street grid, the facades of the first
+    buildings remeshed into ~n_sensors receiver quads (mesh sizes vary from building to building), and three target
+    groups - a water strip (label 3), park lawns (label 4) and a landmark tower (label 5) - on a ground of quads that
+    brings the scene to ~target_tris triangles. Labels: 2 obstruction, 3.. targets (the reference's views classes)."""
+    rng = np.random.default_rng(seed)
+    side = int(np.ceil(np.sqrt(n_buildings * 1.15)))
+    pitch = 40.0
+    lots = [(i, j) for j in range(side) for i in range(side)]
+    park_lots = set(rng.choice(len(lots), max(1, len(lots) // 12), replace=False).tolist())
+    centre_lot = (side // 2) * side + side // 2
+    park_lots.discard(centre_lot)
+    V, T, L = [], [], []
+    nv = 0
+
+    def add(verts, tris, label):
+        nonlocal nv
+        V.append(np.asarray(verts, np.float64))
+        T.append(np.asarray(tris, np.int64) + nv)
+        L.append(np.full(len(tris), label, np.uint8))
+        nv += len(verts)
+
+    sens = Mesh()   # receivers: facade quads of the first buildings
+    sens_target = n_sensors
+    made = 0
+    b = 0
+    for k, (i, j) in enumerate(lots):
+        x0, y0 = i * pitch, j * pitch
+        if k in park_lots:
+            add([(x0 + 2, y0 + 2, 0.05), (x0 + 38, y0 + 2, 0.05), (x0 + 38, y0 + 38, 0.05), (x0 + 2, y0 + 38, 0.05)], [(0, 1, 2), (0, 2, 3)], 4)
+            continue
+        if k == centre_lot:   # the landmark: a 30 x 30 m tower, 150 m
+            c = [(x0 + 5, y0 + 5), (x0 + 35, y0 + 5), (x0 + 35, y0 + 35), (x0 + 5, y0 + 35)]
+            vs = [(x, y, 0) for x, y in c] + [(x, y, 150) for x, y in c]
+            add(vs, [(0, 1, 5), (0, 5, 4), (1, 2, 6), (1, 6, 5), (2, 3, 7), (2, 7, 6), (3, 0, 4), (3, 4, 7), (4, 5, 6), (4, 6, 7)], 5)
+            continue
+        if b >= n_buildings:
+            continue
+        b += 1
+        w, d = sorted(rng.uniform(10, 30, 2))[::-1]
+        h = rng.uniform(8, 40)
+        rh = rng.uniform(2, 6)
+        th = rng.uniform(0, np.pi)
+        cx, cy = x0 + 20, y0 + 20
+        ct, st = np.cos(th), np.sin(th)
+        loc = [(-w / 2, -d / 2), (w / 2, -d / 2), (w / 2, d / 2), (-w / 2, d / 2)]
+        c = [(cx + ct * a - st * bb, cy + st * a + ct * bb) for a, bb in loc]
+        r0 = (cx + ct * (-w / 2), cy + st * (-w / 2))
+        r1 = (cx + ct * (w / 2), cy + st * (w / 2))
+        roof = [(x, y, h) for x, y in c] + [(r0[0], r0[1], h + rh), (r1[0], r1[1], h + rh)]
+        # roof: south slope c0 c1 R1 R0, north slope c2 c3 R0 R1, gables c3 c0 R0 and c1 c2 R1 (indices into roof)
+        rt = [(0, 1, 5), (0, 5, 4), (2, 3, 4), (2, 4, 5), (3, 0, 4), (1, 2, 5)]
+        if made < sens_target:   # facades as receivers, ~2.5 m quads
+            for q in range(4):
+                a0, a1 = c[q], c[(q + 1) % 4]
+                L_ = np.hypot(a1[0] - a0[0], a1[1] - a0[1])
+                nu, nvv = max(1, int(round(L_ / 2.5))), max(1, int(round(h / 2.5)))
+                sens.grid((a0[0], a0[1], 0), (a1[0] - a0[0], a1[1] - a0[1], 0), (0, 0, h), nu, nvv)
+                made += nu * nvv
+            add(roof, rt, 2)
+        else:
+            vs = [(x, y, 0) for x, y in c] + roof
+            wt = [(0, 1, 5), (0, 5, 4), (1, 2, 6), (1, 6, 5), (2, 3, 7), (2, 7, 6), (3, 0, 4), (3, 4, 7)]
+            add(vs, wt + [(4 + a, 4 + bb, 4 + cc) for a, bb, cc in rt], 2)
+    W = side * pitch
+    add([(0, -60, 0.05), (W, -60, 0.05), (W, -10, 0.05), (0, -10, 0.05)], [(0, 1, 2), (0, 2, 3)], 3)   # water strip
+    have = sum(len(t) for t in T) + 2 * sum(len(q) for q in sens.quads)
+    G = max(1, int(np.sqrt(max(0, target_tris - have) / 2)))
+    gm = Mesh()
+    gm.grid((-100, -160, 0), (W + 200, 0, 0), (0, W + 260, 0), G, G)
+    gp, gq, _ = gm.arrays()
+    add(gp, np.concatenate([gq[:, [0, 1, 2]], gq[:, [0, 2, 3]]], axis=1).reshape(-1, 3), 2)
+    # assemble: receivers first (they block too), then the context
+    sp, sq, _ = sens.arrays()
+    allv = np.concatenate([sp] + V)
+    centre = 0.5 * (allv.min(axis=0) + allv.max(axis=0))
+    st_tri = np.concatenate([sq[:, [0, 1, 2]], sq[:, [0, 2, 3]]], axis=1).reshape(-1, 3)
+    v = np.concatenate([sp - centre] + [x - centre for x in V]).astype(np.float32)
+    tri = np.concatenate([st_tri] + [t + len(sp) for t in T]).astype(np.uint32)
+    label = np.concatenate([np.full(len(st_tri), 2, np.uint8)] + L)
+    c_, n_ = _faces_geom(sp - centre, sq)
+    return dict(v=v, tri=tri, label=label, P=c_.astype(np.float32), N=n_.astype(np.float32), groundZ=float(0 - centre[2]), centre=centre)
+
+
+def views_grid(fov, cell, lo=-70.0, hi=50.0):
+    """The reference's field (views.cpp:122-136): nAz x nEl cells, per row sin of its bottom / top elevation, row
+    weights (solid angle, normalised so the field sums to 1)."""
+    flat = lo == hi
+    nAz = max(1, int(round(fov / cell)))
+    nEl = 1 if flat else max(1, int(round((hi - lo) / cell)))
+    dAz, dEl = fov / nAz, (hi - lo) / nEl
+    rowSin = np.zeros((nEl, 2), np.float32)
+    wRow = np.zeros(nEl)
+    for k in range(nEl):
+        top, bot = np.sin(np.radians(hi - k * dEl)), np.sin(np.radians(hi - (k + 1) * dEl))
+        rowSin[k] = (bot, top)
+        wRow[k] = np.radians(dAz) * (1 if flat else top - bot)
+    wRow /= wRow.sum() * nAz
+    return nAz, nEl, float(dAz), rowSin, wRow
