@@ -92,6 +92,7 @@ int sync_status(Engine& g) {   // wait for the stream, then read the kernels' st
   CU(cudaStreamSynchronize(g.st));
   CU(cudaGetLastError());
   if (status & kStatusStackOverflow) return fail("traversal stack overflow (BVH deeper than the kernel's stack)");
+  if (status & kStatusVisitLimit) return fail("traversal gave up: a query passed 2^20 node visits or met a node index beyond the BVH");
   return 1;
 }
 int reset_ctl(Engine& g) {

@@ -13,7 +13,7 @@ namespace kgb {
 struct Node8;
 struct TriRec;
 
-enum : uint32_t { kStatusStackOverflow = 1u, kStatusTimeout = 2u };
+enum : uint32_t { kStatusStackOverflow = 1u, kStatusTimeout = 2u, kStatusVisitLimit = 4u };
 
 // the calling thread's message for kgb_last_error (engine.cu); returns 0 for the C ABI's failure status
 int set_error(const std::string& message);

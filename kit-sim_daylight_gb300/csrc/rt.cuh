@@ -210,6 +210,7 @@ struct Scene {
 };
 
 constexpr int kStack = 48;   // node-group stack entries (one per level at most)
+constexpr uint32_t kMaxVisits = 1u << 20;   // node visits of one query past which the traversal gives up (overflow bit 2)
 
 // Traversal counters of the instrumented kernels (nodes visited, triangles tested); compiled out otherwise.
 struct Count {
@@ -224,7 +225,8 @@ __device__ __forceinline__ void for_hits(const Scene& s, const Ray& r, float tmi
   uint2 stack[kStack];   // node group: x = childBase, y = imask << 8 | remaining inner children
   int sp = 0;
   uint32_t cur = 0;      // node to visit
-  for (;;) {
+  for (uint32_t visits = 0;; ++visits) {
+    if (visits >= kMaxVisits || cur >= s.nNodes) { overflow |= 2u; return; }
     uint4 n[5];
     load_node(s.nodes, cur, n);
     if (COUNT) ctr->nodes++;
@@ -281,9 +283,11 @@ __device__ __forceinline__ bool closest(const Scene& s, const Ray& r, float tmin
   bool any = false;
   float best = tmax;
   stack[sp++] = Entry{0u, tmin};
+  uint32_t visits = 0;
   while (sp) {
     const Entry e = stack[--sp];
     if (e.t > best) continue;
+    if (++visits > kMaxVisits || e.node >= s.nNodes) { overflow |= 2u; return any; }
     uint4 n[5];
     load_node(s.nodes, e.node, n);
     float tn[8];

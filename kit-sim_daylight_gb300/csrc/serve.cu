@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(256) k_bits_batch(const BatchHdr* hdr, const S
     const uint32_t word = trace_word<false>(s, n, o, g.D, g.nDir, w, (g.rayFlags & KGB_RAY_CULL_BACK_FACING) != 0, overflow, ctr, rays);
     bitsPool[g.bitsOff + size_t(w) * g.n + i] = word;
   }
-  if (overflow) atomicOr(status, kStatusStackOverflow);
+  if (overflow) atomicOr(status, (overflow & 1u ? kStatusStackOverflow : 0u) | (overflow & 2u ? kStatusVisitLimit : 0u));
 }
 
 // every quantity of every chunk: out[outOff + q n + i] = sum over visible d, in order, of

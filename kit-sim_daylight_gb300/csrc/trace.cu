@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(256) k_bits(TraceArgs a) {
     const uint32_t word = trace_word<COUNT>(s, n, o, a.D, a.nDir, w, cull, overflow, ctr, rays);
     a.bits[size_t(w) * a.stride + a.out0 + i] = word;
   }
-  if (overflow) atomicOr(a.status, kStatusStackOverflow);
+  if (overflow) atomicOr(a.status, (overflow & 1u ? kStatusStackOverflow : 0u) | (overflow & 2u ? kStatusVisitLimit : 0u));
   if (COUNT) {
     unsigned long long* c = reinterpret_cast<unsigned long long*>(a.status + 1);   // ctl words 2..7: three u64 counters
     atomicAdd(c, (unsigned long long)ctr.nodes);
@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(256) k_bytes(TraceArgs a) {
       a.bytes[size_t(d) * a.stride + a.out0 + i] = trace_byte(s, a, o, n, ld3(a.D + 3 * d), cull, overflow);
     }
   }
-  if (overflow) atomicOr(a.status, kStatusStackOverflow);
+  if (overflow) atomicOr(a.status, (overflow & 1u ? kStatusStackOverflow : 0u) | (overflow & 2u ? kStatusVisitLimit : 0u));
 }
 
 // ---------------------------------------------------------------------------------------------------- views
@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(256) k_view(ViewArgs a) {
       a.dist[at] = t;
     }
   }
-  if (overflow) atomicOr(a.status, kStatusStackOverflow);
+  if (overflow) atomicOr(a.status, (overflow & 1u ? kStatusStackOverflow : 0u) | (overflow & 2u ? kStatusVisitLimit : 0u));
 }
 
 // ---------------------------------------------------------------------------------------------------- bounce
@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(128) k_bounce(BounceArgs a) {
       o = add(offset_ray(h.p, h.n), h.lift);
     }
   }
-  if (overflow) atomicOr(a.status, kStatusStackOverflow);
+  if (overflow) atomicOr(a.status, (overflow & 1u ? kStatusStackOverflow : 0u) | (overflow & 2u ? kStatusVisitLimit : 0u));
 }
 
 // ---------------------------------------------------------------------------------------------------- launches
