@@ -173,6 +173,8 @@ def run_ours(args, pkg):
     torch.cuda.set_device(local)
     pkg.load()
     scene = pkg.workloads.urban_block(seed=42 + rank)   # weak scaling: every rank its own block of the same shape
+    if args.sensors:   # a smaller case of the same kernel (profiling): the block's first sensors
+        scene = dict(scene, P=scene["P"][:args.sensors], N=scene["N"][:args.sensors])
     D, Ws, manifest = urban_sky()
     nc, nDir = len(scene["P"]), len(D)
     stream = torch.cuda.Stream()
@@ -250,8 +252,9 @@ def run_ours(args, pkg):
         line = {"metric": "Mrays/s", "value": world * rays / (ms / 1000) / 1e6, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded urban block; the reference's direction table and weights, tests/golden/urban_sky)",
-                "config": {"workload": "urban block: 20x20 boxes, %d sensors, %d triangles, %d directions (%d sky + %d ground + %d sun), "
-                                       "trace + 4 reduces (radiation, irradiance, illuminance, sunhours)" %
+                "config": {"workload": (("urban block: 20x20 boxes, %d sensors, %d triangles, %d directions (%d sky + %d ground + %d sun), " if not args.sensors else
+                                         "urban block, first %d sensors only (profiling case), %d triangles, %d directions (%d sky + %d ground + %d sun), ") +
+                                        "trace + 4 reduces (radiation, irradiance, illuminance, sunhours)") %
                                        (nc, len(scene["tri"]), nDir, manifest["dirs"]["sky"], manifest["dirs"]["ground"], manifest["dirs"]["sun"]),
                            "rays_per_step": rays, "l2": "flushed between steps (512 MB write)", "parallelism": "replicas (weak)" if world > 1 else "1 GPU"},
                 "e2e": {"value": world * rays / (ms_e2e / 1000) / 1e6, "unit": "Mrays/s",
@@ -560,6 +563,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=30000)
     ap.add_argument("--ref-sample", type=int, default=20000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sensors", type=int, default=0, help="urban: trace only the block's first N sensors (a small case for profiling)")
     ap.add_argument("--config", default="urban", choices=["urban", "precision", "views", "serving"])
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--window", type=float, default=2.0)

@@ -60,7 +60,7 @@ struct Engine {
   SceneObj* sc = nullptr;
   Buf slots;
   uint32_t nSlots = 0;
-  Buf P, N, D;
+  Buf P, N, D, rayTab;   // rayTab: 48 bytes per direction (the direction-only part of each ray)
   size_t nSensors = 0, nDir = 0, nWords = 0;
   Buf vis;
   bool bytes = false;
@@ -76,7 +76,7 @@ struct Engine {
   Buf ctl;   // [0] task counter, [1] status, [2..7] three u64 counters of the instrumented kernels
   bool ownStream = true;
   int seriesForm = 0;         // 0 split-BF16 tensor cores, 1 plain FP32
-  Buf vhi, vlo, shi, slo, csr, sunCol;
+  Buf vop, sop, csr, sunCol;
   kgb_stats stats{};
   int gridBits = 0, gridView = 0;
 };
@@ -141,8 +141,8 @@ KGB_API void kgb_destroy(kgb_engine* e) {
   Engine* g = E(e);
   if (g->st) cudaStreamSynchronize(g->st);
   delete g->sc;
-  for (Buf* b : {&g->slots, &g->P, &g->N, &g->D, &g->vis, &g->dc, &g->viewCls, &g->viewDist, &g->rowSin, &g->label, &g->scratch, &g->out, &g->ctl,
-                 &g->vhi, &g->vlo, &g->shi, &g->slo, &g->csr, &g->sunCol}) b->free();
+  for (Buf* b : {&g->slots, &g->P, &g->N, &g->D, &g->rayTab, &g->vis, &g->dc, &g->viewCls, &g->viewDist, &g->rowSin, &g->label, &g->scratch, &g->out, &g->ctl,
+                 &g->vop, &g->sop, &g->csr, &g->sunCol}) b->free();
   for (cudaEvent_t ev : g->ev) if (ev) cudaEventDestroy(ev);
   if (g->st && g->ownStream) cudaStreamDestroy(g->st);
   delete g;
@@ -198,7 +198,7 @@ KGB_API void kgb_trim(kgb_engine* e, int sensors) {
   Engine& g = *E(e);
   cudaStreamSynchronize(g.st);
   g.vis.free(); g.dc.free(); g.scratch.free(); g.out.free(); g.viewCls.free(); g.viewDist.free();
-  g.vhi.free(); g.vlo.free(); g.shi.free(); g.slo.free(); g.csr.free(); g.sunCol.free();
+  g.vop.free(); g.sop.free(); g.csr.free(); g.sunCol.free();
   g.viewN = 0;
   if (sensors) { g.P.free(); g.N.free(); g.label.free(); g.nLabel = 0; g.nSensors = 0; }
 }
@@ -241,7 +241,10 @@ KGB_API uint64_t kgb_free_bytes(void) {
 KGB_API int kgb_set_scene(kgb_engine* e, const float* P, const float* N, size_t nSensors, const float* D, size_t nDir) {
   Engine& g = *E(e);
   g.nSensors = nSensors; g.nDir = nDir; g.nWords = (nDir + 31) / 32;
-  if (!upload(g.P, P, nSensors * 12, g.st) || !upload(g.N, N, nSensors * 12, g.st) || !upload(g.D, D, nDir * 12, g.st)) return 0;
+  if (!upload(g.P, P, nSensors * 12, g.st) || !upload(g.N, N, nSensors * 12, g.st) || !upload(g.D, D, nDir * 12, g.st) ||
+      !grow(g.rayTab, nDir * 48)) return 0;
+  launch_ray_table(static_cast<const float*>(g.D.p), uint32_t(nDir), g.rayTab.p, g.st);
+  CU(cudaGetLastError());
   CU(cudaStreamSynchronize(g.st));
   return 1;
 }
@@ -263,11 +266,12 @@ static int trace_impl(Engine& g, size_t i0, size_t nc, uint32_t rayFlags, uint64
   if (!grow(g.vis, g.bytes ? g.nDir * nc : g.nWords * nc * 4)) return 0;
   g.i0 = i0; g.visN = nc;
   if (nc == 0 || g.nWords == 0) return 1;
-  if (!g.gridBits) g.gridBits = g.numSMs * 4;
+  if (!g.gridBits) g.gridBits = g.numSMs * bits_blocks_per_sm();
   const bool any = g.bytes;
   const double targetMs = any ? 30 : 150;
   const size_t nMin = any ? std::max<size_t>(1, (size_t(1) << 13) / g.nWords) : 1024;
-  size_t done = 0, n = counters ? nc : std::min(any ? nMin : size_t(4096), nc);
+  const size_t nMax = std::max<size_t>(32, size_t(0xffffffffu) / g.nWords * 32);   // warp tasks are counted in 32 bits
+  size_t done = 0, n = std::min(counters ? nc : std::min(any ? nMin : size_t(4096), nc), nMax);
   TraceArgs a{};
   a.nodes = static_cast<const Node8*>(g.sc->nodes.p); a.tris = static_cast<const TriRec*>(g.sc->tris.p); a.nNodes = g.sc->nNodes;
   a.P = static_cast<const float*>(g.P.p); a.N = static_cast<const float*>(g.N.p); a.D = static_cast<const float*>(g.D.p);
@@ -276,10 +280,11 @@ static int trace_impl(Engine& g, size_t i0, size_t nc, uint32_t rayFlags, uint64
   a.bytes = any ? static_cast<uint8_t*>(g.vis.p) : nullptr;
   a.slots = static_cast<const kgb_slot*>(g.slots.p); a.nSlots = g.nSlots;
   a.counter = static_cast<uint32_t*>(g.ctl.p); a.status = static_cast<uint32_t*>(g.ctl.p) + 1;
+  a.rayTab = static_cast<const RayDir*>(g.rayTab.p);
   while (done < nc) {
     a.first = uint32_t(i0 + done); a.n = uint32_t(n); a.out0 = uint32_t(done);
     if (!reset_ctl(g)) return 0;
-    const size_t tasks = (n + 31) / 32 * g.nWords;
+    const size_t tasks = (n + 31) / 32 * g.nWords;   // warp tasks: 32 sensors x one 32-direction word
     const int grid = int(std::min<size_t>(size_t(g.gridBits), (tasks + 7) / 8));
     CU(cudaEventRecord(g.ev[0], g.st));
     if (any) launch_bytes(a, grid, g.st); else launch_bits(a, grid, g.st, counters != nullptr);
@@ -294,7 +299,7 @@ static int trace_impl(Engine& g, size_t i0, size_t nc, uint32_t rayFlags, uint64
     g.stats.traceMs += ms; g.stats.rays += n * g.nDir; g.stats.launches++;
     done += n;
     const double want = double(n) * targetMs / std::max(ms, 1e-3);
-    n = std::min({std::max<size_t>(want > 1e12 ? size_t(1) << 40 : size_t(want), nMin), any ? 2 * n : nc, nc - done});
+    n = std::min({std::max<size_t>(want > 1e12 ? size_t(1) << 40 : size_t(want), nMin), any ? 2 * n : nc, nc - done, nMax});
   }
   return 1;
 }
@@ -327,7 +332,7 @@ KGB_API int kgb_reduce(kgb_engine* e, size_t nc, const float* W, int useCos, dou
   const float* N = static_cast<const float*>(g.N.p) + 3 * g.i0;
   if (g.bytes) launch_reduce_bytes(static_cast<const uint8_t*>(g.vis.p), uint32_t(nc), uint32_t(g.nDir), N, static_cast<const float*>(g.D.p),
                                    static_cast<const float*>(g.scratch.p), useCos, static_cast<double*>(g.out.p), g.st);
-  else launch_reduce_bits(static_cast<const uint32_t*>(g.vis.p), uint32_t(nc), uint32_t(g.nWords), N, static_cast<const float*>(g.D.p),
+  else launch_reduce_bits(static_cast<const uint32_t*>(g.vis.p), uint32_t(nc), uint32_t(g.nWords), uint32_t(g.nDir), N, static_cast<const float*>(g.D.p),
                           static_cast<const float*>(g.scratch.p), useCos, static_cast<double*>(g.out.p), g.st);
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(out, g.out.p, nc * 8, cudaMemcpyDeviceToHost, g.st));
@@ -388,7 +393,7 @@ KGB_API int kgb_series(kgb_engine* e, size_t nc, const kgb_series_in* in, float*
       for (uint32_t d = 0; d < in->nSky; ++d) dirs[size_t(at[size_t(in->row[d])]++)] = int32_t(d);
     }
     const size_t csrBytes = (first.size() + dirs.size()) * 4;
-    if (!grow(g.vhi, nc * Kp * 2) || !grow(g.vlo, nc * Kp * 2) || !grow(g.shi, T * Kp * 2) || !grow(g.slo, T * Kp * 2) ||
+    if (!grow(g.vop, 3 * nc * Kp * 2) || !grow(g.sop, 3 * T * Kp * 2) ||
         !grow(g.csr, csrBytes) || !grow(g.sunCol, T * 4)) return 0;
     int32_t* dFirst = static_cast<int32_t*>(g.csr.p);
     int32_t* dDirs = dFirst + first.size();
@@ -397,7 +402,7 @@ KGB_API int kgb_series(kgb_engine* e, size_t nc, const kgb_series_in* in, float*
     CU(cudaMemcpyAsync(g.sunCol.p, sunOfCol.data(), T * 4, cudaMemcpyHostToDevice, g.st));
     SeriesTcPlan p{};
     p.nc = uint32_t(nc); p.T = uint32_t(T); p.Kp = uint32_t(Kp); p.sun0 = in->sun0; p.numSMs = g.numSMs;
-    p.vhi = g.vhi.p; p.vlo = g.vlo.p; p.shi = g.shi.p; p.slo = g.slo.p;
+    p.v = g.vop.p; p.s = g.sop.p;
     p.sunOfCol = static_cast<const int32_t*>(g.sunCol.p); p.sunVec = a.sunVec; p.sunW = a.sunW;
     p.bits = a.bits; p.bytes = a.bytes; p.N = a.N; p.E = a.E; p.status = static_cast<uint32_t*>(g.ctl.p) + 1;
     SeriesOperands o{};
@@ -461,6 +466,14 @@ KGB_API int kgb_bounce(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, c
     CU(cudaEventRecord(g.ev[0], g.st));
     launch_bounce(a, g.st);
     CU(cudaEventRecord(g.ev[1], g.st));
+    uint32_t ctl[4] = {};
+    CU(cudaMemcpyAsync(ctl, g.ctl.p, 16, cudaMemcpyDeviceToHost, g.st));
+    CU(cudaStreamSynchronize(g.st));
+    CU(cudaGetLastError());
+    const unsigned long long segments = (unsigned long long)ctl[2] | ((unsigned long long)ctl[3] << 32);
+    if (ctl[1] & kStatusTimeout)
+      return fail("gpu_bounce: a launch of " + std::to_string(n) + " samples x " + std::to_string(nc) + " sensors passed its 10 s limit after " +
+                  std::to_string(segments) + " path segments");
     if (!sync_status(g)) return 0;
     const double ms = elapsed(g);
     g.stats.bounceMs += ms; g.stats.paths += n * nc; g.stats.bounceLaunches++;

@@ -12,6 +12,7 @@ namespace kgb {
 
 struct Node8;
 struct TriRec;
+struct RayDir;
 
 enum : uint32_t { kStatusStackOverflow = 1u, kStatusTimeout = 2u, kStatusVisitLimit = 4u };
 
@@ -35,6 +36,7 @@ struct TraceArgs {
   uint32_t nSlots;
   uint32_t* counter;
   uint32_t* status;
+  const RayDir* rayTab;   // the directions' precomputed ray parts (k_bits), or null
 };
 
 struct ViewArgs {
@@ -71,14 +73,16 @@ struct BounceArgs {
   uint32_t* status;
 };
 
+void launch_ray_table(const float* D, uint32_t nDir, void* tab, cudaStream_t st);   // 48 bytes per direction
+int bits_blocks_per_sm();
 void launch_bits(const TraceArgs& a, int grid, cudaStream_t st, bool count = false);
 void launch_bytes(const TraceArgs& a, int grid, cudaStream_t st);
 void launch_view(const ViewArgs& a, int grid, cudaStream_t st);
 void launch_bounce(const BounceArgs& a, cudaStream_t st);
 
 // reductions (reduce.cu)
-void launch_reduce_bits(const uint32_t* bits, uint32_t nc, uint32_t nWords, const float* N, const float* D, const float* W, int useCos,
-                        double* out, cudaStream_t st);
+void launch_reduce_bits(const uint32_t* bits, uint32_t nc, uint32_t nWords, uint32_t nDir, const float* N, const float* D, const float* W,
+                        int useCos, double* out, cudaStream_t st);
 void launch_reduce_bytes(const uint8_t* bytes, uint32_t nc, uint32_t nDir, const float* N, const float* D, const float* W, int useCos,
                          double* out, cudaStream_t st);
 void launch_reduce_dc(const float* dc, uint32_t nc, uint32_t nBins, const float* W, double* out, cudaStream_t st);
@@ -123,10 +127,8 @@ void launch_series_fp32(const SeriesArgs& a, cudaStream_t st);
 struct SeriesTcPlan {
   uint32_t nc, T, Kp, sun0;
   int numSMs;
-  void* vhi;               // [nc x Kp] bf16
-  void* vlo;
-  void* shi;               // [T x Kp] bf16
-  void* slo;
+  void* v;                 // [3 x nc x Kp] bf16: the pieces hi, mid, lo of V, one after the other
+  void* s;                 // [3 x T x Kp] bf16: the same of S^T
   const int32_t* sunOfCol; // [T]: the sun direction of column t, or -1
   const float* sunVec;
   const float* sunW;

@@ -13,8 +13,36 @@ namespace kgb {
 
 __device__ __forceinline__ float dotf(F3 a, F3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }   // per-op rounding (gpu.cu:69-72)
 
-__global__ void __launch_bounds__(256) k_reduce_bits(const uint32_t* __restrict__ bits, uint32_t nc, uint32_t nWords, const float* __restrict__ N,
-                                                     const float* __restrict__ D, const float* __restrict__ W, int useCos, double* __restrict__ out) {
+// GB300's FP64 pipe is narrow (a few lanes per clock per SM), so each term of a sum costs one FP64 instruction:
+//  - the float factor x > 0 becomes a double exactly by integer operations: its exponent rebiased (+896) and its
+//    mantissa moved up 29 bits (normal floats; a subnormal takes the conversion instruction);
+//  - the weights are read as doubles, converted once per block into shared memory;
+//  - the product of two floats is exact in double, so fma(x, w, acc) equals acc + x * w rounded once, as the
+//    reference's separate multiply and add;
+//  - a zero factor adds +0, which leaves the sum as it is: it is skipped.
+__device__ __forceinline__ double widen(float x) {
+  const uint32_t b = __float_as_uint(x);
+  return x >= 1.17549435e-38f ? __hiloint2double(int((b >> 3) + (896u << 20)), int(b << 29)) : (double)x;
+}
+
+constexpr uint32_t kReduceSmemDirs = 24576;   // weights held as doubles in shared memory (192 KB) up to this many
+
+template <bool SMEM>
+__device__ __forceinline__ const double* weights_to_smem(const float* W, uint32_t n, double* sW) {
+  if (!SMEM) return nullptr;
+  for (uint32_t d = threadIdx.x; d < n; d += blockDim.x) sW[d] = (double)__ldg(W + d);
+  __syncthreads();
+  return sW;
+}
+template <bool SMEM>
+__device__ __forceinline__ double weight(const double* sW, const float* W, uint32_t d) { return SMEM ? sW[d] : (double)__ldg(W + d); }
+
+template <bool SMEM>
+__global__ void __launch_bounds__(256) k_reduce_bits(const uint32_t* __restrict__ bits, uint32_t nc, uint32_t nWords, uint32_t nDir,
+                                                     const float* __restrict__ N, const float* __restrict__ D, const float* __restrict__ W,
+                                                     int useCos, double* __restrict__ out) {
+  extern __shared__ double sW[];
+  const double* w64 = weights_to_smem<SMEM>(W, nDir, sW);
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nc) return;
   const F3 n = ld3(N + 3 * size_t(i));
@@ -25,14 +53,17 @@ __global__ void __launch_bounds__(256) k_reduce_bits(const uint32_t* __restrict_
       const uint32_t d = w * 32 + (__ffs(m) - 1);
       m &= m - 1;
       const float c = useCos ? fmaxf(dotf(n, ld3(D + 3 * d)), 0.f) : 1.f;
-      acc += (double)(c * 1.f) * (double)__ldg(W + d);
+      if (c != 0.f) acc = __fma_rn(widen(c), weight<SMEM>(w64, W, d), acc);
     }
   }
   out[i] = acc;
 }
 
+template <bool SMEM>
 __global__ void __launch_bounds__(256) k_reduce_bytes(const uint8_t* __restrict__ bytes, uint32_t nc, uint32_t nDir, const float* __restrict__ N,
                                                       const float* __restrict__ D, const float* __restrict__ W, int useCos, double* __restrict__ out) {
+  extern __shared__ double sW[];
+  const double* w64 = weights_to_smem<SMEM>(W, nDir, sW);
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nc) return;
   const F3 n = ld3(N + 3 * size_t(i));
@@ -42,7 +73,8 @@ __global__ void __launch_bounds__(256) k_reduce_bytes(const uint8_t* __restrict_
     if (!b) continue;
     const float at = float(b) / 255.f;
     const float c = useCos ? fmaxf(dotf(n, ld3(D + 3 * d)), 0.f) : 1.f;
-    acc += (double)(c * at) * (double)__ldg(W + d);
+    const float x = c * at;
+    if (x != 0.f) acc = __fma_rn(widen(x), weight<SMEM>(w64, W, d), acc);
   }
   out[i] = acc;
 }
@@ -151,13 +183,26 @@ __global__ void __launch_bounds__(256) k_iso(ViewReduceArgs a) {
   if (!lane) a.out[size_t(i) * a.NA + a.NA - 1] = v;
 }
 
-void launch_reduce_bits(const uint32_t* bits, uint32_t nc, uint32_t nWords, const float* N, const float* D, const float* W, int useCos,
-                        double* out, cudaStream_t st) {
-  k_reduce_bits<<<(nc + 255) / 256, 256, 0, st>>>(bits, nc, nWords, N, D, W, useCos, out);
+// The weights go to shared memory as doubles when they fit (kReduceSmemDirs); the kernels' sums are the same either way.
+static bool reduce_smem_ready() {
+  static bool ok = [] {
+    const int bytes = int(kReduceSmemDirs * sizeof(double));
+    return cudaFuncSetAttribute(k_reduce_bits<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess &&
+           cudaFuncSetAttribute(k_reduce_bytes<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess;
+  }();
+  return ok;
+}
+void launch_reduce_bits(const uint32_t* bits, uint32_t nc, uint32_t nWords, uint32_t nDir, const float* N, const float* D, const float* W,
+                        int useCos, double* out, cudaStream_t st) {
+  if (nDir <= kReduceSmemDirs && reduce_smem_ready())
+    k_reduce_bits<true><<<(nc + 255) / 256, 256, nDir * sizeof(double), st>>>(bits, nc, nWords, nDir, N, D, W, useCos, out);
+  else k_reduce_bits<false><<<(nc + 255) / 256, 256, 0, st>>>(bits, nc, nWords, nDir, N, D, W, useCos, out);
 }
 void launch_reduce_bytes(const uint8_t* bytes, uint32_t nc, uint32_t nDir, const float* N, const float* D, const float* W, int useCos,
                          double* out, cudaStream_t st) {
-  k_reduce_bytes<<<(nc + 255) / 256, 256, 0, st>>>(bytes, nc, nDir, N, D, W, useCos, out);
+  if (nDir <= kReduceSmemDirs && reduce_smem_ready())
+    k_reduce_bytes<true><<<(nc + 255) / 256, 256, nDir * sizeof(double), st>>>(bytes, nc, nDir, N, D, W, useCos, out);
+  else k_reduce_bytes<false><<<(nc + 255) / 256, 256, 0, st>>>(bytes, nc, nDir, N, D, W, useCos, out);
 }
 void launch_reduce_dc(const float* dc, uint32_t nc, uint32_t nBins, const float* W, double* out, cudaStream_t st) {
   k_reduce_dc<<<(nc + 255) / 256, 256, 0, st>>>(dc, nc, nBins, W, out);

@@ -99,6 +99,30 @@ __device__ __forceinline__ Ray make_ray(F3 o, F3 d) {
   return r;
 }
 
+// The direction-only part of a ray (everything but the origin), 48 bytes, computed once per direction table by
+// make_ray itself: a = d.xyz, Sx | b = inv.xyz, Sy | c = Sz, kx | ky << 8 | kz << 16 | oct << 24, 0, 0.
+struct __align__(16) RayDir { float4 a, b, c; };
+__device__ __forceinline__ RayDir ray_dir_of(F3 d) {
+  const Ray r = make_ray(f3(0.f, 0.f, 0.f), d);
+  RayDir t;
+  t.a = make_float4(r.d.x, r.d.y, r.d.z, r.Sx);
+  t.b = make_float4(r.inv.x, r.inv.y, r.inv.z, r.Sy);
+  t.c = make_float4(r.Sz, __uint_as_float(uint32_t(r.kx) | uint32_t(r.ky) << 8 | uint32_t(r.kz) << 16 | r.oct << 24), 0.f, 0.f);
+  return t;
+}
+// make_ray(o, d) from direction d's precomputed part: the same values, with o * inv the only arithmetic.
+__device__ __forceinline__ Ray ray_from(const RayDir* tab, uint32_t d, F3 o) {
+  const float4 a = __ldg(&tab[d].a), b = __ldg(&tab[d].b), c = __ldg(&tab[d].c);
+  Ray r;
+  r.o = o; r.d = f3(a.x, a.y, a.z);
+  const uint32_t k = __float_as_uint(c.y);
+  r.kx = int(k & 0xffu); r.ky = int((k >> 8) & 0xffu); r.kz = int((k >> 16) & 0xffu); r.oct = k >> 24;
+  r.Sx = a.w; r.Sy = b.w; r.Sz = c.x;
+  r.inv = f3(b.x, b.y, b.z);
+  r.oinv = f3(o.x * r.inv.x, o.y * r.inv.y, o.z * r.inv.z);
+  return r;
+}
+
 struct Hit { float t, u, v; uint32_t prim; bool front; };
 
 // Woop, Benthin, Wald 2013 (JCGT 2(1)) with a tie rule on edges: the same operation sequence as the oracle's hit_tri.
@@ -159,11 +183,30 @@ __device__ __forceinline__ bool own_hit(F3 v0, F3 v1, F3 v2, const Hit& hh, F3 d
 __device__ __forceinline__ F3 through(const TriHit& h) { return sub(offset_ray(h.p, mul(-1.f, h.n)), h.lift); }
 
 // ------------------------------------------------------------------------------------------------ BVH8 traversal
-__device__ __forceinline__ float ubyte(uint32_t w, int k) { return float((w >> (8 * k)) & 0xffu); }
 __device__ __forceinline__ uint32_t byte_of(uint32_t w, int k) { return (w >> (8 * k)) & 0xffu; }
 
-// Child boxes of a node against the ray in [tmin, tmax]: returns the mask of hit children (bit k), their entry
-// distances in tn[8]. Conservative: the boxes were expanded at build; the exit distance is widened by 2^-20.
+// Byte b of w as a float, exactly: the bit pattern 0x4B0000qq is 2^23 + q, and the subtraction of 2^23 is exact.
+// One byte permute and one add instead of a bit-field extract and an integer-to-float conversion.
+__device__ __forceinline__ float qf(uint32_t w, int b) {
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | uint32_t(b))) - 8388608.f;
+}
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
+// Child boxes of a node against the ray in [tmin, tmax] (tmin >= 0): returns the mask of hit children (bit k), their
+// entry distances in tn[8]. Conservative: the boxes were expanded at build; the exit distance is widened by 2^-20.
+// Per axis the near plane is the low one when the ray's inverse direction is non-negative (the slab distance
+// fma(q, adj, o) is then non-decreasing in q), else the high one: the words of near and far planes are picked once
+// per node, so each child costs six plane distances, one 3-input max and one 3-input min. Empty child slots need
+// no test: a leaf slot without triangles that the box test lets through tests nothing.
 __device__ __forceinline__ uint32_t node_hits(const uint4* n, const Ray& r, float tmin, float tmax, float* tn) {
   const float px = __uint_as_float(n[0].x), py = __uint_as_float(n[0].y), pz = __uint_as_float(n[0].z);
   const uint32_t ew = n[0].w;
@@ -171,22 +214,22 @@ __device__ __forceinline__ uint32_t node_hits(const uint4* n, const Ray& r, floa
   const float adjx = sx * r.inv.x, adjy = sy * r.inv.y, adjz = sz * r.inv.z;
   const float ox = __fmaf_rn(px, r.inv.x, -r.oinv.x), oy = __fmaf_rn(py, r.inv.y, -r.oinv.y), oz = __fmaf_rn(pz, r.inv.z, -r.oinv.z);
   // quantised bounds: qlo.x = n2.x,n2.y  qlo.y = n2.z,n2.w  qlo.z = n3.x,n3.y  qhi.x = n3.z,n3.w  qhi.y = n4.x,n4.y  qhi.z = n4.z,n4.w
+  const bool nx = r.inv.x < 0.f, ny = r.inv.y < 0.f, nz = r.inv.z < 0.f;
+  const uint32_t nearX[2] = {nx ? n[3].z : n[2].x, nx ? n[3].w : n[2].y}, farX[2] = {nx ? n[2].x : n[3].z, nx ? n[2].y : n[3].w};
+  const uint32_t nearY[2] = {ny ? n[4].x : n[2].z, ny ? n[4].y : n[2].w}, farY[2] = {ny ? n[2].z : n[4].x, ny ? n[2].w : n[4].y};
+  const uint32_t nearZ[2] = {nz ? n[4].z : n[3].x, nz ? n[4].w : n[3].y}, farZ[2] = {nz ? n[3].x : n[4].z, nz ? n[3].y : n[4].w};
   uint32_t mask = 0;
-  const uint32_t meta0 = n[1].z, meta1 = n[1].w, imask = ew >> 24;
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
     const int h = k >> 2, b = k & 3;
-    const uint32_t qlx = byte_of(h ? n[2].y : n[2].x, b), qly = byte_of(h ? n[2].w : n[2].z, b), qlz = byte_of(h ? n[3].y : n[3].x, b);
-    const uint32_t qhx = byte_of(h ? n[3].w : n[3].z, b), qhy = byte_of(h ? n[4].y : n[4].x, b), qhz = byte_of(h ? n[4].w : n[4].z, b);
-    const float t0x = __fmaf_rn(float(qlx), adjx, ox), t1x = __fmaf_rn(float(qhx), adjx, ox);
-    const float t0y = __fmaf_rn(float(qly), adjy, oy), t1y = __fmaf_rn(float(qhy), adjy, oy);
-    const float t0z = __fmaf_rn(float(qlz), adjz, oz), t1z = __fmaf_rn(float(qhz), adjz, oz);
-    const float tnear = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
-    float tfar = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
-    tfar = fminf(__fmaf_rn(fabsf(tfar), 9.5367431640625e-7f, tfar), tmax);
-    const uint32_t meta = byte_of(k < 4 ? meta0 : meta1, k & 3);
-    const bool live = ((imask >> k) & 1u) || meta != 0u;
-    if (live && tnear <= tfar) { mask |= 1u << k; tn[k] = tnear; }
+    const float tnx = __fmaf_rn(qf(nearX[h], b), adjx, ox), tfx = __fmaf_rn(qf(farX[h], b), adjx, ox);
+    const float tny = __fmaf_rn(qf(nearY[h], b), adjy, oy), tfy = __fmaf_rn(qf(farY[h], b), adjy, oy);
+    const float tnz = __fmaf_rn(qf(nearZ[h], b), adjz, oz), tfz = __fmaf_rn(qf(farZ[h], b), adjz, oz);
+    const float tnear = max3f(tnx, tny, fmaxf(tnz, tmin));
+    // exit widened to tfar (1 + 2^-20): for tfar >= 0 the value fma(|tfar|, 2^-20, tfar), and a negative tfar
+    // fails against tnear >= tmin >= 0 either way
+    const float tfar = fminf(__fmul_rn(min3f(tfx, tfy, tfz), 1.00000095367431640625f), tmax);
+    if (tnear <= tfar) { mask |= 1u << k; tn[k] = tnear; }
   }
   return mask;
 }
@@ -208,6 +251,13 @@ struct Scene {
   const TriRec* tris;
   uint32_t nNodes;    // 0: empty scene, every ray misses
 };
+
+// the GPU's nanosecond clock (kernels with a wall-time limit read it)
+__device__ __forceinline__ uint64_t clock_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
 
 constexpr int kStack = 48;   // node-group stack entries (one per level at most)
 constexpr uint32_t kMaxVisits = 1u << 20;   // node visits of one query past which the traversal gives up (overflow bit 2)
@@ -339,8 +389,9 @@ __device__ __forceinline__ bool closest(const Scene& s, const Ray& r, float tmin
 // One visibility word: bit k = direction w*32+k of a sensor (normal n, ray origin o) passes the hemisphere cull and every
 // hit from tmin 1e-5 on is an own-plane hit, at most 3 (the reference's __raygen__bits, trace_dev.cu:91-108, restated
 // over the ray's hit set). COUNT adds traversal counters and rays traced.
+// tab: the directions' precomputed RayDir entries, or null (the rays are made from D).
 template <bool COUNT>
-__device__ __forceinline__ uint32_t trace_word(const Scene& s, F3 n, F3 o, const float* D, uint32_t nDir, uint32_t w, bool cull,
+__device__ __forceinline__ uint32_t trace_word(const Scene& s, F3 n, F3 o, const float* D, const RayDir* tab, uint32_t nDir, uint32_t w, bool cull,
                                                uint32_t& overflow, Count& ctr, uint32_t& rays) {
   uint32_t word = 0;
   for (uint32_t k = 0; k < 32; ++k) {
@@ -348,7 +399,7 @@ __device__ __forceinline__ uint32_t trace_word(const Scene& s, F3 n, F3 o, const
     if (d >= nDir) break;
     const F3 dir = ld3(D + 3 * d);
     if (!(n.x * dir.x + n.y * dir.y + n.z * dir.z > 0.f)) continue;
-    const Ray r = make_ray(o, dir);
+    const Ray r = tab ? ray_from(tab, d, o) : make_ray(o, dir);
     bool blocked = false;
     int own = 0;
     if (COUNT) ++rays;

@@ -4,19 +4,28 @@
 //
 // with k over the sky patches (V = the cos- and transmission-weighted visibility per patch, S = the patch radiance per
 // step), then the ground (V = G, S = g) and the reflected-light bins (V = dc, S = Sdc): the reference's k_series +
-// k_series_dc (gpu.cu:116-169) as one dense contraction. Each operand is split x = hi + lo in bf16 (16 significant
-// bits) and three products run per K block (hi.hi + hi.lo + lo.hi, fp32 accumulation in tensor memory); the sun term
-// (one direction per step, exact in the reference's float arithmetic) is added in the epilogue, where each output is
-// finished in registers and streamed to HBM with 128-byte row stores.
+// k_series_dc (gpu.cu:116-169) as one dense contraction.
+//
+// Precision (within 1e-6 of an FP64 contraction per output column):
+//  - each FP32 operand is split x = hi + mid + lo exactly into three bf16 pieces (24 significant bits), and six
+//    products run per K step: hi.hi, then the corrections hi.mid + mid.hi + hi.lo + mid.mid + lo.hi (the dropped
+//    mid.lo, lo.mid, lo.lo are 2^-24 of the product and below);
+//  - the tensor core's FP32 accumulation truncates, so a long accumulation chain drifts low by about a quarter ulp per
+//    instruction (1e-5 over 2305 patches). hi.hi, which carries the sum, is therefore accumulated in TMEM over chunks
+//    of 128 K only (8 instructions), and the chunk sums are added in FP32 round-to-nearest by the epilogue; the
+//    corrections (2^-8 of the sum) keep one chain per tile in a second accumulator;
+//  - the sun term (one direction per step, exact in the reference's float arithmetic) is added in the epilogue, where
+//    each output is finished in registers and streamed to HBM with 128-byte row stores.
 //
 // Kernel k_series_tc, one CTA per SM, persistent over 128 x 128 output tiles (sensors x steps, steps fastest so that
 // the CTAs running at once share a few V panels and all of S in L2):
-//   warp 0      TMA producer: per 64-wide K block, V_hi, V_lo (128 x 64) and S_hi, S_lo (128 x 64) bf16 tiles,
-//               128-byte swizzled, into a 3-stage shared-memory ring (64 KB a stage)
-//   warp 1      MMA issuer (one thread): 12 tcgen05.mma (M 128, N 128, K 16) per stage into one of two TMEM
-//               accumulators (128 columns each), tcgen05.commit to free the stage / to hand the tile to the epilogue
-//   warps 2-5   epilogue: tcgen05.ld 32 columns at a time (warp w reads TMEM lanes 32 (w % 4) ..), the sun term,
-//               a per-warp shared-memory transpose, coalesced stores of E rows
+//   warp 0      TMA producer: per 64-wide K block, the three pieces of V (128 x 64) and of S (128 x 64), bf16,
+//               128-byte swizzled, into a 2-stage shared-memory ring (96 KB a stage)
+//   warp 1      MMA issuer (one thread): 24 tcgen05.mma (M 128, N 128, K 16) per stage: hi.hi into the chunk
+//               accumulator H[chunk % 2], the corrections into the tile accumulator C[tile % 2] (TMEM: H0 H1 C0 C1,
+//               128 columns each); tcgen05.commit frees the stage, hands a finished chunk or tile to the epilogue
+//   warps 2-5   epilogue: per chunk, tcgen05.ld of H (warp w reads TMEM lanes 32 (w % 4) ..) added into 128 FP32
+//               registers; per tile, C and the sun term, a per-warp shared-memory transpose, coalesced stores of E rows
 // Every wait on an mbarrier is bounded: past the limit the kernel records kStatusTimeout and leaves its loops (the
 // TMEM it holds is released on the way out).
 #include <cuda.h>
@@ -29,14 +38,15 @@
 
 namespace kgb {
 
-constexpr int BM = 128, BN = 128, BK = 64, STAGES = 3;
+constexpr int BM = 128, BN = 128, BK = 64, STAGES = 2, PIECES = 3;
+constexpr int CHUNK_BLOCKS = 2;                      // K blocks (of BK) per hi.hi accumulation chunk: 8 instructions
 constexpr int TILE_BYTES = BM * BK * 2;              // 16 KB: one bf16 operand tile (rows x 128 B)
-constexpr int STAGE_BYTES = 4 * TILE_BYTES;          // V_hi, V_lo, S_hi, S_lo
+constexpr int STAGE_BYTES = 2 * PIECES * TILE_BYTES; // V hi mid lo, S hi mid lo
 constexpr int EPI_WARPS = 4;
 constexpr int THREADS = 32 * (2 + EPI_WARPS);
 constexpr int STAGE_PAD = 33;                        // floats per row of the per-warp transpose buffer
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + EPI_WARPS * 32 * STAGE_PAD * 4 + 1024 /* align */ + 256 /* barriers */;
-constexpr uint32_t TMEM_COLS = 2 * BN;               // two accumulators
+constexpr uint32_t TMEM_COLS = 4 * BN;               // H0 H1 (chunk sums of hi.hi), C0 C1 (corrections of a tile)
 constexpr uint64_t kWaitLimitNs = 4000000000ull;   // 4 s: no wait of a healthy run comes near it
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
@@ -124,28 +134,35 @@ __device__ __forceinline__ float dotf_rn(const float* n, const float* d) {
   return __fadd_rn(__fadd_rn(__fmul_rn(n[0], d[0]), __fmul_rn(n[1], d[1])), __fmul_rn(n[2], d[2]));
 }
 
-__global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant__ CUtensorMap mapVhi, const __grid_constant__ CUtensorMap mapVlo,
-                                                          const __grid_constant__ CUtensorMap mapShi, const __grid_constant__ CUtensorMap mapSlo,
+// mapV: the three pieces of V stacked as rows [3 nc x Kp]; mapS: the pieces of S^T stacked as [3 T x Kp]. Piece p of
+// an operand tile at rows r0 is at rows r0 + p nc (p T); rows past a piece's end read the next piece's rows (or the
+// zero fill), which only reach accumulator rows and columns that are never stored.
+__global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant__ CUtensorMap mapV, const __grid_constant__ CUtensorMap mapS,
                                                           SeriesTcArgs a) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   float* stageBuf = reinterpret_cast<float*>(smem + STAGES * STAGE_BYTES);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES + EPI_WARPS * 32 * STAGE_PAD * 4);
-  uint64_t* full = bars;               // [STAGES] TMA -> MMA
-  uint64_t* empty = bars + STAGES;     // [STAGES] MMA -> TMA
-  uint64_t* accFull = bars + 2 * STAGES;       // [2] MMA -> epilogue
-  uint64_t* accEmpty = bars + 2 * STAGES + 2;  // [2] epilogue -> MMA
-  uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 4);
+  uint64_t* full = bars;                 // [STAGES] TMA -> MMA
+  uint64_t* empty = bars + STAGES;       // [STAGES] MMA -> TMA
+  uint64_t* hFull = bars + 2 * STAGES;   // [2] MMA -> epilogue: a chunk sum of hi.hi is complete
+  uint64_t* hEmpty = hFull + 2;          // [2] epilogue -> MMA
+  uint64_t* cFull = hFull + 4;           // [2] MMA -> epilogue: the tile's corrections are complete
+  uint64_t* cEmpty = hFull + 6;          // [2] epilogue -> MMA
+  uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(hFull + 8);
   __shared__ volatile uint32_t abortFlag;
 
   const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
-    for (int b = 0; b < 2; ++b) { mbar_init(&accFull[b], 1); mbar_init(&accEmpty[b], EPI_WARPS * 32); }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&hFull[b], 1); mbar_init(&hEmpty[b], EPI_WARPS * 32);
+      mbar_init(&cFull[b], 1); mbar_init(&cEmpty[b], EPI_WARPS * 32);
+    }
     abortFlag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 1) {   // TMEM: two accumulators of BN fp32 columns x 128 lanes
+  if (warp == 1) {   // TMEM: four accumulators of BN fp32 columns x 128 lanes
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmemSlot)), "r"(TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
@@ -154,6 +171,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmemBase = *tmemSlot;
   const uint32_t kBlocks = a.Kp / BK;
+  const uint32_t nChunks = (kBlocks + CHUNK_BLOCKS - 1) / CHUNK_BLOCKS;
   const uint32_t nTilesAll = a.mTiles * a.nTiles;
 
   if (warp == 0) {
@@ -166,10 +184,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
           uint8_t* s = smem + stage * STAGE_BYTES;
           mbar_expect_tx(&full[stage], STAGE_BYTES);
           const int k0 = int(kb) * BK;
-          tma_load_2d(s, &mapVhi, k0, m0, &full[stage]);
-          tma_load_2d(s + TILE_BYTES, &mapVlo, k0, m0, &full[stage]);
-          tma_load_2d(s + 2 * TILE_BYTES, &mapShi, k0, n0, &full[stage]);
-          tma_load_2d(s + 3 * TILE_BYTES, &mapSlo, k0, n0, &full[stage]);
+#pragma unroll
+          for (int p = 0; p < PIECES; ++p) {
+            tma_load_2d(s + p * TILE_BYTES, &mapV, k0, m0 + p * int(a.nc), &full[stage]);
+            tma_load_2d(s + (PIECES + p) * TILE_BYTES, &mapS, k0, n0 + p * int(a.T), &full[stage]);
+          }
           if (++stage == STAGES) { stage = 0; phase ^= 1; }
         }
       }
@@ -177,52 +196,87 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
     __syncwarp();
   } else if (warp == 1) {
     if (lane == 0) {   // ---------------- MMA issuer
-      uint32_t stage = 0, phase = 0, local = 0;
+      uint32_t stage = 0, phase = 0, local = 0, chunk = 0;
       for (uint32_t tile = blockIdx.x; tile < nTilesAll && !abortFlag; tile += gridDim.x, ++local) {
-        const uint32_t buf = local & 1, use = local >> 1;
-        if (!mbar_wait(&accEmpty[buf], (use & 1) ^ 1, a.status)) { abortFlag = 1; break; }
+        const uint32_t cbuf = local & 1, cuse = local >> 1;
+        if (!mbar_wait(&cEmpty[cbuf], (cuse & 1) ^ 1, a.status)) { abortFlag = 1; break; }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t dTmem = tmemBase + buf * BN;
-        for (uint32_t kb = 0; kb < kBlocks; ++kb) {
-          if (!mbar_wait(&full[stage], phase, a.status)) { abortFlag = 1; break; }
+        const uint32_t cT = tmemBase + (2 + cbuf) * BN;
+        uint32_t hT = tmemBase, hbuf = 0;
+        bool ok = true;
+        for (uint32_t kb = 0; kb < kBlocks && ok; ++kb) {
+          const uint32_t kc = kb % CHUNK_BLOCKS;
+          if (kc == 0) {   // a new chunk of hi.hi
+            hbuf = chunk & 1;
+            if (!mbar_wait(&hEmpty[hbuf], ((chunk >> 1) & 1) ^ 1, a.status)) { ok = false; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            hT = tmemBase + hbuf * BN;
+          }
+          if (!mbar_wait(&full[stage], phase, a.status)) { ok = false; break; }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint8_t* s = smem + stage * STAGE_BYTES;
-          const uint64_t dVhi = smem_desc(s), dVlo = smem_desc(s + TILE_BYTES), dShi = smem_desc(s + 2 * TILE_BYTES),
-                         dSlo = smem_desc(s + 3 * TILE_BYTES);
+          const uint64_t v0 = smem_desc(s), v1 = smem_desc(s + TILE_BYTES), v2 = smem_desc(s + 2 * TILE_BYTES);
+          const uint64_t s0 = smem_desc(s + 3 * TILE_BYTES), s1 = smem_desc(s + 4 * TILE_BYTES), s2 = smem_desc(s + 5 * TILE_BYTES);
 #pragma unroll
           for (int k = 0; k < BK / 16; ++k) {   // 16 bf16 = 32 bytes along K: +2 in the descriptor's address field
             const uint64_t off = uint64_t(2 * k);
-            mma_bf16(dTmem, dVhi + off, dShi + off, (kb | k) != 0);
-            mma_bf16(dTmem, dVhi + off, dSlo + off, 1);
-            mma_bf16(dTmem, dVlo + off, dShi + off, 1);
+            mma_bf16(hT, v0 + off, s0 + off, (kc | uint32_t(k)) != 0);
+            mma_bf16(cT, v0 + off, s1 + off, (kb | uint32_t(k)) != 0);
+            mma_bf16(cT, v1 + off, s0 + off, 1);
+            mma_bf16(cT, v0 + off, s2 + off, 1);
+            mma_bf16(cT, v1 + off, s1 + off, 1);
+            mma_bf16(cT, v2 + off, s0 + off, 1);
           }
           mma_commit(&empty[stage]);   // the stage is free once these MMAs have read it
           if (++stage == STAGES) { stage = 0; phase ^= 1; }
+          if (kc == CHUNK_BLOCKS - 1 || kb == kBlocks - 1) { mma_commit(&hFull[hbuf]); ++chunk; }
         }
-        mma_commit(&accFull[buf]);     // the tile's accumulator is complete
+        if (!ok) { abortFlag = 1; break; }
+        mma_commit(&cFull[cbuf]);      // the tile's corrections are complete
       }
     }
     __syncwarp();
   } else {   // ---------------- epilogue: warps 2..5
     const uint32_t q = warp & 3;                       // TMEM lane quarter this warp may read
+    const uint32_t laneBase = (q * 32u) << 16;
     float* tb = stageBuf + (warp - 2) * 32 * STAGE_PAD;
-    uint32_t local = 0;
+    uint32_t local = 0, chunk = 0;
     for (uint32_t tile = blockIdx.x; tile < nTilesAll; tile += gridDim.x, ++local) {
-      const uint32_t buf = local & 1, use = local >> 1;
-      bool ok = mbar_wait(&accFull[buf], use & 1, a.status);
-      ok = __all_sync(~0u, ok);
+      float acc[BN];
+#pragma unroll
+      for (int c = 0; c < BN; ++c) acc[c] = 0.f;
+      bool ok = true;
+      for (uint32_t ch = 0; ch < nChunks; ++ch, ++chunk) {
+        const uint32_t hbuf = chunk & 1;
+        ok = __all_sync(~0u, mbar_wait(&hFull[hbuf], (chunk >> 1) & 1, a.status));
+        if (!ok || abortFlag) { ok = false; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+        for (int g = 0; g < BN / 32; ++g) {
+          float v[32];
+          tmem_ld32(tmemBase + laneBase + hbuf * BN + g * 32, v);
+#pragma unroll
+          for (int c = 0; c < 32; ++c) acc[g * 32 + c] = __fadd_rn(acc[g * 32 + c], v[c]);
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        mbar_arrive(&hEmpty[hbuf]);
+      }
+      const uint32_t cbuf = local & 1;
+      if (ok) ok = __all_sync(~0u, mbar_wait(&cFull[cbuf], (local >> 1) & 1, a.status));
       if (!ok || abortFlag) { abortFlag = 1; break; }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t m0 = (tile / a.nTiles) * BM, n0 = (tile % a.nTiles) * BN;
       const uint32_t row = m0 + q * 32 + lane;         // this thread's sensor
       float nrm[3] = {0.f, 0.f, 0.f};
       if (row < a.nc) { nrm[0] = a.N[3 * row]; nrm[1] = a.N[3 * row + 1]; nrm[2] = a.N[3 * row + 2]; }
-      for (uint32_t c0 = 0; c0 < BN; c0 += 32) {
+#pragma unroll
+      for (int g = 0; g < BN / 32; ++g) {
         float v[32];
-        tmem_ld32(tmemBase + ((q * 32u) << 16) + buf * BN + c0, v);
-#pragma unroll 4
+        tmem_ld32(tmemBase + laneBase + (2 + cbuf) * BN + g * 32, v);
+#pragma unroll
         for (int c = 0; c < 32; ++c) {
-          const uint32_t t = n0 + c0 + c;
+          float x = __fadd_rn(acc[g * 32 + c], v[c]);
+          const uint32_t t = n0 + g * 32 + c;
           if (t < a.T && row < a.nc) {
             const int j = __ldg(a.sunOfCol + t);
             if (j >= 0) {
@@ -230,14 +284,14 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
               float at;
               if (a.bytes) { const uint32_t b = a.bytes[size_t(d) * a.nc + row]; at = b ? float(b) / 255.f : 0.f; }
               else at = float((a.bits[size_t(d >> 5) * a.nc + row] >> (d & 31)) & 1u);
-              if (at != 0.f) v[c] = __fadd_rn(v[c], __fmul_rn(__fmul_rn(fmaxf(dotf_rn(nrm, a.sunVec + 3 * j), 0.f), at), a.sunW[j]));
+              if (at != 0.f) x = __fadd_rn(x, __fmul_rn(__fmul_rn(fmaxf(dotf_rn(nrm, a.sunVec + 3 * j), 0.f), at), a.sunW[j]));
             }
           }
-          tb[lane * STAGE_PAD + c] = v[c];
+          tb[lane * STAGE_PAD + c] = x;
         }
         __syncwarp();
         // the warp's 32 rows x 32 columns: one 128-byte row segment per store instruction
-        const uint32_t t = n0 + c0 + lane;
+        const uint32_t t = n0 + g * 32 + lane;
         for (int r = 0; r < 32; ++r) {
           const uint32_t rr = m0 + q * 32 + r;
           if (rr < a.nc && t < a.T) a.E[size_t(rr) * a.T + t] = tb[r * STAGE_PAD + lane];
@@ -245,7 +299,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
         __syncwarp();
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      mbar_arrive(&accEmpty[buf]);
+      mbar_arrive(&cEmpty[cbuf]);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -258,7 +312,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
 
 // ------------------------------------------------------------------------------------------------ operand builds
 // V per chunk: V[i, k] = sum over the sky directions d of patch k (in d order) of max(0, N_i . D_d) T_d wsky_d (float),
-// then G_i (k = P), then dc(b, i) (k = P + 1 + b); split into bf16 hi + lo, rows of Kp (zero padded). A block computes 32
+// then G_i (k = P), then dc(b, i) (k = P + 1 + b); split exactly into bf16 hi + mid + lo, rows of Kp (zero padded). A block computes 32
 // sensors x 64 columns: lanes = sensors (coalesced visibility reads), then the rows leave through shared memory.
 struct VBuildArgs {
   const uint32_t* bits;
@@ -271,9 +325,16 @@ struct VBuildArgs {
   const float* wsky;
   const float* G;
   const float* dc;             // [nBins x nc] or null
-  __nv_bfloat16* vhi;
-  __nv_bfloat16* vlo;
+  __nv_bfloat16* v;            // [3 x nc x Kp]: hi, mid, lo
 };
+
+// x = hi + mid + lo exactly (each difference is exact in FP32), each piece round-to-nearest bf16
+__device__ __forceinline__ void split3(float x, __nv_bfloat16& hi, __nv_bfloat16& mid, __nv_bfloat16& lo) {
+  hi = __float2bfloat16_rn(x);
+  const float r = __fsub_rn(x, __bfloat162float(hi));
+  mid = __float2bfloat16_rn(r);
+  lo = __float2bfloat16_rn(__fsub_rn(r, __bfloat162float(mid)));
+}
 
 __global__ void __launch_bounds__(256) k_build_v(VBuildArgs a) {
   __shared__ float tile[64][33];
@@ -306,18 +367,20 @@ __global__ void __launch_bounds__(256) k_build_v(VBuildArgs a) {
     if (ii >= a.nc) continue;
     for (uint32_t h = 0; h < 2; ++h) {
       const uint32_t kk = h * 32 + lane;
-      const float x = tile[kk][r];
-      const __nv_bfloat16 hi = __float2bfloat16_rn(x);
-      const __nv_bfloat16 lo = __float2bfloat16_rn(x - __bfloat162float(hi));
-      a.vhi[size_t(ii) * a.Kp + k0 + kk] = hi;
-      a.vlo[size_t(ii) * a.Kp + k0 + kk] = lo;
+      __nv_bfloat16 hi, mid, lo;
+      split3(tile[kk][r], hi, mid, lo);
+      const size_t at = size_t(ii) * a.Kp + k0 + kk, piece = size_t(a.nc) * a.Kp;
+      a.v[at] = hi;
+      a.v[at + piece] = mid;
+      a.v[at + 2 * piece] = lo;
     }
   }
 }
 
-// S^T per chunk (K-major rows of the steps): St[t, k] = S[k, t] (k < P), g[t] (k = P), Sdc[k - P - 1, t]; hi + lo.
+// S^T per chunk (K-major rows of the steps): St[t, k] = S[k, t] (k < P), g[t] (k = P), Sdc[k - P - 1, t]; hi + mid + lo
+// into [3 x T x Kp].
 __global__ void __launch_bounds__(256) k_build_st(const float* S, const float* g, const float* Sdc, uint32_t P, uint32_t nBins, uint32_t T,
-                                                  uint32_t Kp, __nv_bfloat16* shi, __nv_bfloat16* slo) {
+                                                  uint32_t Kp, __nv_bfloat16* st) {
   __shared__ float tile[32][33];
   const uint32_t t0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
   const uint32_t tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 8 rows of 32
@@ -335,10 +398,12 @@ __global__ void __launch_bounds__(256) k_build_st(const float* S, const float* g
   for (uint32_t r = ty; r < 32; r += 8) {
     const uint32_t t = t0 + r, k = k0 + tx;
     if (t >= T) continue;
-    const float x = tile[tx][r];
-    const __nv_bfloat16 hi = __float2bfloat16_rn(x);
-    shi[size_t(t) * Kp + k] = hi;
-    slo[size_t(t) * Kp + k] = __float2bfloat16_rn(x - __bfloat162float(hi));
+    __nv_bfloat16 hi, mid, lo;
+    split3(tile[tx][r], hi, mid, lo);
+    const size_t at = size_t(t) * Kp + k, piece = size_t(T) * Kp;
+    st[at] = hi;
+    st[at + piece] = mid;
+    st[at + 2 * piece] = lo;
   }
 }
 
@@ -370,10 +435,10 @@ static bool make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t K
 const char* series_tc(const SeriesTcPlan& p, cudaStream_t st) {
   if (p.nc == 0 || p.T == 0) return nullptr;
   if (p.Kp % BK) return "series_tc: K not padded to 64";
-  CUtensorMap mVhi, mVlo, mShi, mSlo;
-  if (!make_map(&mVhi, p.vhi, p.nc, p.Kp) || !make_map(&mVlo, p.vlo, p.nc, p.Kp) || !make_map(&mShi, p.shi, p.T, p.Kp) ||
-      !make_map(&mSlo, p.slo, p.T, p.Kp))
+  CUtensorMap mV, mS;
+  if (!make_map(&mV, p.v, uint64_t(PIECES) * p.nc, p.Kp) || !make_map(&mS, p.s, uint64_t(PIECES) * p.T, p.Kp))
     return "series_tc: cuTensorMapEncodeTiled failed";
+  if (uint64_t(PIECES) * p.nc + BM > 0x7fffffffull || uint64_t(PIECES) * p.T + BN > 0x7fffffffull) return "series_tc: chunk too large";
   static bool attr = false;
   if (!attr) {
     if (cudaFuncSetAttribute(k_series_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) != cudaSuccess)
@@ -386,7 +451,7 @@ const char* series_tc(const SeriesTcPlan& p, cudaStream_t st) {
   a.sunOfCol = p.sunOfCol; a.sunVec = p.sunVec; a.sunW = p.sunW; a.sun0 = p.sun0;
   a.bits = p.bits; a.bytes = p.bytes; a.N = p.N; a.E = p.E; a.status = p.status;
   const int grid = int(std::min<uint32_t>(uint32_t(p.numSMs), a.mTiles * a.nTiles));
-  k_series_tc<<<grid, THREADS, SMEM_BYTES, st>>>(mVhi, mVlo, mShi, mSlo, a);
+  k_series_tc<<<grid, THREADS, SMEM_BYTES, st>>>(mV, mS, a);
   return nullptr;
 }
 
@@ -394,11 +459,10 @@ void build_series_operands(const SeriesTcPlan& p, const SeriesOperands& o, cudaS
   VBuildArgs v{};
   v.bits = p.bits; v.bytes = p.bytes; v.nc = p.nc; v.P = o.P; v.nBins = o.nBins; v.Kp = p.Kp; v.N = p.N; v.D = o.D;
   v.patchFirst = o.patchFirst; v.patchDirs = o.patchDirs; v.wsky = o.wsky; v.G = o.G; v.dc = o.dc;
-  v.vhi = static_cast<__nv_bfloat16*>(p.vhi); v.vlo = static_cast<__nv_bfloat16*>(p.vlo);
+  v.v = static_cast<__nv_bfloat16*>(p.v);
   k_build_v<<<dim3((p.nc + 31) / 32, p.Kp / 64), 256, 0, st>>>(v);
   if (o.rebuildS)
-    k_build_st<<<dim3((p.T + 31) / 32, p.Kp / 32), 256, 0, st>>>(o.S, o.g, o.Sdc, o.P, o.nBins, p.T, p.Kp, static_cast<__nv_bfloat16*>(p.shi),
-                                                                 static_cast<__nv_bfloat16*>(p.slo));
+    k_build_st<<<dim3((p.T + 31) / 32, p.Kp / 32), 256, 0, st>>>(o.S, o.g, o.Sdc, o.P, o.nBins, p.T, p.Kp, static_cast<__nv_bfloat16*>(p.s));
 }
 
 }  // namespace kgb

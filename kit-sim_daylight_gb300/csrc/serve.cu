@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(256) k_bits_batch(const BatchHdr* hdr, const S
     if (i >= g.n) continue;
     const Scene s{g.nodes, g.tris, g.nNodes};
     const F3 n = ld3(g.N + 3 * i), o = offset_ray(ld3(g.P + 3 * i), n);
-    const uint32_t word = trace_word<false>(s, n, o, g.D, g.nDir, w, (g.rayFlags & KGB_RAY_CULL_BACK_FACING) != 0, overflow, ctr, rays);
+    const uint32_t word = trace_word<false>(s, n, o, g.D, nullptr, g.nDir, w, (g.rayFlags & KGB_RAY_CULL_BACK_FACING) != 0, overflow, ctr, rays);
     bitsPool[g.bitsOff + size_t(w) * g.n + i] = word;
   }
   if (overflow) atomicOr(status, (overflow & 1u ? kStatusStackOverflow : 0u) | (overflow & 2u ? kStatusVisitLimit : 0u));

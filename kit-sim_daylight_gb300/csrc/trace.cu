@@ -33,7 +33,7 @@ __global__ void __launch_bounds__(256) k_bits(TraceArgs a) {
     if (i >= a.n) continue;
     const uint32_t gi = a.first + i;
     const F3 n = ld3(a.N + 3 * gi), o = offset_ray(ld3(a.P + 3 * gi), n);
-    const uint32_t word = trace_word<COUNT>(s, n, o, a.D, a.nDir, w, cull, overflow, ctr, rays);
+    const uint32_t word = trace_word<COUNT>(s, n, o, a.D, a.rayTab, a.nDir, w, cull, overflow, ctr, rays);
     a.bits[size_t(w) * a.stride + a.out0 + i] = word;
   }
   if (overflow) atomicOr(a.status, (overflow & 1u ? kStatusStackOverflow : 0u) | (overflow & 2u ? kStatusVisitLimit : 0u));
@@ -237,6 +237,8 @@ __device__ __forceinline__ uint32_t sky_bin(F3 d, uint32_t mf, uint32_t nBins, f
   return b + uint32_t(az * (float(n) / 6.28318531f) + .5f) % n;
 }
 
+constexpr uint64_t kBounceLimitNs = 10000000000ull;   // 10 s: past it a thread stops its paths and records kStatusTimeout
+
 __global__ void __launch_bounds__(128) k_bounce(BounceArgs a) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
@@ -247,14 +249,18 @@ __global__ void __launch_bounds__(128) k_bounce(BounceArgs a) {
   const U3 rot = pcg3d(gi, ~0u, ~0u);
   const float r0 = u01(rot.x), r1 = u01(rot.y), weight = 3.14159265f / float(a.M);
   float* row = a.dc + i;
-  uint32_t overflow = 0;
-  for (uint32_t smp = a.s0; smp < a.s1; ++smp) {
+  uint32_t overflow = 0, segments = 0;
+  const uint64_t start = clock_ns();
+  bool late = false;
+  for (uint32_t smp = a.s0; smp < a.s1 && !late; ++smp) {
     const float u = float(smp) / float(a.M) + r0, v = u01(__brev(smp)) + r1;
     F3 o = o0, d = cosine_dir(nn, u - floorf(u), v - floorf(v));
     float w = 1.f;
     uint32_t diffuse = 0, k = 0;
     bool reflected = false;
     for (uint32_t seg = 0; seg < a.nBounce + 16; ++seg) {
+      if (clock_ns() - start > kBounceLimitNs) { late = true; break; }   // a launch is sized to ~100 ms
+      ++segments;
       ClosestOut c;
       if (!closest(s, make_ray(o, d), 1e-5f, FLT_MAX, cull, c, overflow)) {
         if (reflected) { float* p = row + size_t(sky_bin(d, a.mf, a.nBins, a.alpha, a.cosN, a.sinN)) * a.nc; *p = *p + w * weight; }
@@ -285,10 +291,24 @@ __global__ void __launch_bounds__(128) k_bounce(BounceArgs a) {
       o = add(offset_ray(h.p, h.n), h.lift);
     }
   }
-  if (overflow) atomicOr(a.status, (overflow & 1u ? kStatusStackOverflow : 0u) | (overflow & 2u ? kStatusVisitLimit : 0u));
+  atomicAdd(reinterpret_cast<unsigned long long*>(a.status + 1), (unsigned long long)segments);   // ctl words 2-3
+  if (overflow || late)
+    atomicOr(a.status, (overflow & 1u ? kStatusStackOverflow : 0u) | (overflow & 2u ? kStatusVisitLimit : 0u) | (late ? kStatusTimeout : 0u));
 }
 
 // ---------------------------------------------------------------------------------------------------- launches
+__global__ void __launch_bounds__(256) k_ray_table(const float* D, uint32_t nDir, RayDir* tab) {
+  const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d < nDir) tab[d] = ray_dir_of(ld3(D + 3 * d));
+}
+void launch_ray_table(const float* D, uint32_t nDir, void* tab, cudaStream_t st) {
+  if (nDir) k_ray_table<<<(nDir + 255) / 256, 256, 0, st>>>(D, nDir, static_cast<RayDir*>(tab));
+}
+int bits_blocks_per_sm() {   // resident blocks of k_bits per SM (its persistent grid fills the GPU once)
+  int b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_bits<false>, 256, 0) != cudaSuccess || b < 1) b = 1;
+  return b;
+}
 void launch_bits(const TraceArgs& a, int grid, cudaStream_t st, bool count) {
   if (count) k_bits<true><<<grid, 256, 0, st>>>(a);
   else k_bits<false><<<grid, 256, 0, st>>>(a);

@@ -214,9 +214,9 @@ def test_errors_are_the_references(engine_lib, kgb, pkg):
         # an empty scene: every hemisphere direction is visible
         e.build(np.zeros((0, 3)), np.zeros((0, 3)))
         e.trace(0, 10, e.lib.ray_flags(False, False))
-        W = np.ones(16, np.float32)
         N = s["N"][:10]
         D = pkg.workloads.hemisphere_dirs(8, 8, 1)
+        W = np.ones(len(D), np.float32)   # one weight per direction (sky, ground, sun)
         up = ((N[:, 0:1] * D[None, :, 0] + N[:, 1:2] * D[None, :, 1]) + N[:, 2:3] * D[None, :, 2]) > 0
         assert np.array_equal(e.reduce(10, W, False), up.sum(axis=1).astype(np.float64))
     finally:

@@ -8,7 +8,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-COLUMN_TOL = 2e-6   # normwise per-column bound asserted here; the measured values are printed
+COLUMN_TOL = 1e-6   # normwise per-column bound of the tensor-core form against FP64 (measured values are printed)
 
 
 def _setup(pkg, kgb, lib, s, D, nc):
