@@ -154,6 +154,19 @@ KGB_API int kgb_set_labels(kgb_engine* e, const uint8_t* label, size_t n);
 KGB_API int kgb_trace(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags);
 /* replaces gpu_reduce (src/internal.h:154): out[i] = sum_d T(i,d) * (useCos ? max(0, N_i.D_d) : 1) * W[d] (double) */
 KGB_API int kgb_reduce(kgb_engine* e, size_t nc, const float* W, int useCos, double* out);
+/* No counterpart in the reference. kgb_reduce for a caller that must not allocate device memory at the time of the
+ * call: a host that reserved the GPU's memory for its own pool up front, or a plugin host that forbids device
+ * allocation once its processing loop runs (a failed or extra cudaMalloc there breaks the host). Same arguments,
+ * kernels and results as kgb_reduce, bit for bit; the weights and the sums are staged in one fixed 1 MiB array of
+ * device memory that belongs to the library (every GPU that loads the library holds it until the process exits)
+ * instead of in engine buffers that kgb_reduce may have to grow. Limit: nDir weights (4 bytes each, rounded up to
+ * 256 bytes) plus nc sums (8 bytes each) must fit in 1 MiB, e.g. at most 128,260 sensors per call with 5610
+ * directions; a larger call fails with a message giving the limit. The first call on a device looks the array's
+ * address up (cudaGetSymbolAddress): make that first call before any stream capture. Every call uses the same
+ * array, so calls whose work overlaps on the GPU (other threads, other engines on the device) race; each call waits
+ * for its own work before it returns. Nothing in the array needs clearing between calls: the weights are copied in
+ * and every sum is written before it is read. */
+KGB_API int kgb_reduce_noalloc(kgb_engine* e, size_t nc, const float* W, int useCos, double* out);
 /* replaces gpu_series (src/internal.h:171): E[i*T + t] (host, nc x T floats) */
 KGB_API int kgb_series(kgb_engine* e, size_t nc, const kgb_series_in* in, float* E);
 /* replaces gpu_bounce (src/internal.h:179) */

@@ -108,6 +108,16 @@ float elapsed(Engine& g) {
 }  // namespace
 
 int set_error(const std::string& message) { return fail(message); }
+
+void engine_reduce_inputs(kgb_engine* e, ReduceInputs& in) {
+  const Engine& g = *E(e);
+  in.device = g.device; in.st = g.st;
+  in.visN = g.visN; in.nDir = g.nDir; in.nWords = g.nWords; in.bytes = g.bytes;
+  in.bitsVis = g.bytes ? nullptr : static_cast<const uint32_t*>(g.vis.p);
+  in.bytesVis = g.bytes ? static_cast<const uint8_t*>(g.vis.p) : nullptr;
+  in.N = static_cast<const float*>(g.N.p) + 3 * g.i0;
+  in.D = static_cast<const float*>(g.D.p);
+}
 }  // namespace kgb
 
 using namespace kgb;

@@ -154,6 +154,19 @@ struct SeriesOperands {
 void build_series_operands(const SeriesTcPlan& p, const SeriesOperands& o, cudaStream_t st);
 const char* series_tc(const SeriesTcPlan& p, cudaStream_t st);   // null, or what failed
 
+// What a reduce of the last trace reads, for the reduce entry points outside engine.cu (reduce_noalloc.cu).
+struct ReduceInputs {
+  int device;
+  cudaStream_t st;
+  size_t visN, nDir, nWords;   // sensors of the last trace, directions, 32-direction words
+  bool bytes;                  // the last trace wrote transmittance bytes (else bits)
+  const uint32_t* bitsVis;
+  const uint8_t* bytesVis;
+  const float* N;              // the traced chunk's normals
+  const float* D;
+};
+void engine_reduce_inputs(kgb_engine* e, ReduceInputs& in);
+
 // sky (sky.cu): Perez sky of T steps, NOAA sun positions; null or what failed
 const char* sky_steps(int mf, const kgb_sky_step* steps, size_t T, double grefl, int sun, int sky, int visible, float* out, cudaStream_t st);
 const char* sun_steps(const double* in, size_t T, double* out, cudaStream_t st);

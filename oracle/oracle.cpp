@@ -620,6 +620,8 @@ KGB_API int kgb_reduce(kgb_engine* e, size_t nc, const float* W, int useCos, dou
   });
   return 1;
 }
+// The restatement has no device memory to stage in: the no-allocation reduce is its reduce.
+KGB_API int kgb_reduce_noalloc(kgb_engine* e, size_t nc, const float* W, int useCos, double* out) { return kgb_reduce(e, nc, W, useCos, out); }
 
 // gpu.cu:116-169 (k_series, k_series_dc) as an FP64 contraction of the same FP32 per-direction weights: the reference
 // the engine's FP32 and split-BF16 forms are measured against. E is float(the double sum).
