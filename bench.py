@@ -311,52 +311,68 @@ def urban_year_sky(e, mf):
     sun = e.sun_noaa(rows)
     steps = np.stack([jd, np.radians(sun[:, 0]), np.radians(sun[:, 1]), w[0], w[1]], axis=1)
     sky = e.sky(mf, steps, grefl=0.2, sun=False, sky=True, visible=False)
+    sunbin = e.sky(mf, steps, grefl=0.2, sun=True, sky=False, visible=False)   # the sun as gendaymtx bins it (AddDirect)
     sky_s = time.perf_counter() - t0
     bright = KRF * sky[:, :, 0] + KGF * sky[:, :, 1] + KBF * sky[:, :, 2]
+    bright_sun = KRF * sunbin[:, :, 0] + KGF * sunbin[:, :, 1] + KBF * sunbin[:, :, 2]
     col = (w[0] + w[1]) > 1e-4
     colOf = np.cumsum(col) - 1
     S = np.ascontiguousarray(bright[col, 1:].T, np.float32)
     g = np.ascontiguousarray(bright[col, 0], np.float32)
+    # reflected light (run.cpp:411-419): bin 0 the ground, bin 1 + p the patch radiance plus the binned sun
+    Sdc = np.concatenate([g[None, :], (S.astype(np.float64) + bright_sun[col, 1:].T).astype(np.float32)]).astype(np.float32)
     up = sun[:, 2] > 0
     sunVec = sun[up, 3:6].astype(np.float32)
     ups = np.nonzero(up)[0]
     sunStep = np.where(col[ups], colOf[ups], 0).astype(np.int32)
     sunW = np.where(col[ups], w[0][ups], 0).astype(np.float32)
-    return dict(S=S, g=g, sunVec=sunVec, sunStep=sunStep, sunW=sunW, sky_s=sky_s, T=int(col.sum()))
+    return dict(S=S, g=g, Sdc=Sdc, sunVec=sunVec, sunStep=sunStep, sunW=sunW, sky_s=sky_s, T=int(col.sum()))
 
 
 def run_precision(args, pkg):
+    """Config 3: the urban block at 2305 patches, 20 % glass (byte mode), one diffuse bounce of 1024 paths per sensor,
+    and the hourly series of the non-night hours with reflected light, chunk by chunk as the reference's run() does
+    (run.cpp:623-688: trace, bounce, ground reduce, series). The split-BF16 tensor-core series is timed against the
+    plain FP32 form on the same inputs, and its error per output column is measured against the oracle's FP64
+    contraction on a contiguous 64-sensor range (the same global indices, so the same reflected-light paths)."""
     import torch
     torch.cuda.set_device(0)
     kgb = pkg.kgb
     lib = pkg.load()
     e = pkg.engine()
-    mf = 4
+    mf, M = 4, 1024
     Dsky, omega = patch_dirs(mf)
     P = len(Dsky)
     yr = urban_year_sky(e, mf)
     D = np.concatenate([Dsky, -Dsky, yr["sunVec"]]).astype(np.float32)
     nSky, sun0 = P, 2 * P
     scene = pkg.workloads.urban_block(glass_share=0.2)
+    if args.sensors:   # a smaller case of the same kernels (profiling): the block's first sensors
+        scene = dict(scene, P=scene["P"][:args.sensors], N=scene["N"][:args.sensors])
     slots = [(0.2, 0, 0, 0), (0.0, 0.64, kgb.tn_from_Tn(0.64), kgb.SLOT_GLASS), (0.2, 0, 0, 0)]
-    e.build(scene["v"], scene["tri"], scene["slot"], slots)
+    e.build(scene["v"], scene["tri"], scene["slot"], slots, per_slot=True)
     e.set_slots(slots)
     e.set_scene(scene["P"], scene["N"], D)
     nc_all, T = len(scene["P"]), yr["T"]
     Wg = np.zeros(len(D), np.float32)
     Wg[nSky:2 * nSky] = omega
     flags = lib.ray_flags(False, True)   # a slot transmits: bytes
+    bflags = lib.bounce_flags(False)
     chunk = max(1, (256 << 20) // len(D))   # the reference's 256 MiB cap on the per-chunk visibility
     sargs = dict(nSky=nSky, row=np.arange(nSky), wsky=omega, S=yr["S"], g=yr["g"], sun0=sun0, sunStep=yr["sunStep"], sunVec=yr["sunVec"],
-                 sunW=yr["sunW"])
-    tt = {"trace": 0.0, "tc": 0.0, "fp32": 0.0}
-    first = None
+                 sunW=yr["sunW"], Sdc=yr["Sdc"])
+    tt = {"trace": 0.0, "bounce": 0.0, "tc": 0.0, "fp32": 0.0}
+    first = fp32_first = None
+    t_all = time.perf_counter()
     for i0 in range(0, nc_all, chunk):
         nc = min(chunk, nc_all - i0)
         t0 = time.perf_counter()
         e.trace(i0, nc, flags)
         torch.cuda.synchronize()
         tt["trace"] += time.perf_counter() - t0
+        t0 = time.perf_counter()
+        e.bounce(i0, nc, bflags, N=1, M=M, mf=mf, north=0.0)
+        tt["bounce"] += time.perf_counter() - t0
         G = e.reduce(nc, Wg, True).astype(np.float32)
         for form, key in ((0, "tc"), (1, "fp32")):
             if key == "fp32" and i0 > 0 and not args.full_fp32:
@@ -371,15 +387,19 @@ def run_precision(args, pkg):
                 else:
                     fp32_first = E
     e.set_series_form(0)
-    # accuracy: the first chunk's seeded sample against the oracle's FP64 contraction of the same FP32 weights
-    sub = np.sort(np.random.default_rng(9).choice(min(chunk, nc_all), 64, replace=False))
+    pipeline_s = time.perf_counter() - t_all
+    # accuracy: a contiguous 64-sensor range of the first chunk, traced and bounced by the oracle at the same global
+    # indices, its series in FP64 from the same FP32 inputs
+    s0 = int(np.random.default_rng(9).integers(0, min(chunk, nc_all) - 64))
+    sub = np.arange(s0, s0 + 64)
     subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle"), "all"])
     o = kgb.Engine(kgb.Lib(os.path.join(REPO, "oracle", "_build", "liboracle.so")))
-    o.build(scene["v"], scene["tri"], scene["slot"], slots)
+    o.build(scene["v"], scene["tri"], scene["slot"], slots, per_slot=True)
     o.set_slots(slots)
-    o.set_scene(scene["P"][sub], scene["N"][sub], D)
-    o.trace(0, len(sub), flags)
-    E64 = o.series(len(sub), G=first[1][sub], **sargs)
+    o.set_scene(scene["P"], scene["N"], D)
+    o.trace(s0, 64, flags)
+    o.bounce(s0, 64, bflags, N=1, M=M, mf=mf, north=0.0)
+    E64 = o.series(64, G=first[1][sub], **sargs)
     o.close()
     def colerr(E):
         cmax = np.abs(E64).max(axis=0)
@@ -387,16 +407,20 @@ def run_precision(args, pkg):
         return np.abs(E[sub] - E64).max(axis=0)[live] / cmax[live]
     ce, ce32 = colerr(first[0]), colerr(fp32_first)
     n_fp32 = nc_all if args.full_fp32 else min(chunk, nc_all)
+    paths = nc_all * M
     line = {"metric": "radiation solves/s", "unit": "sensor-steps/s",
             "value": nc_all * T / tt["tc"], "fp32_value": n_fp32 * T / tt["fp32"], "speedup_vs_fp32": (nc_all * T / tt["tc"]) / (n_fp32 * T / tt["fp32"]),
             "config": {"workload": "precision: urban block, %d sensors, %d patches + ground, %d directions, %d series columns (non-night hours), "
-                                   "20%% glass tau 0.64 (byte mode), chunks of %d sensors" % (nc_all, P, len(D), T, chunk)},
-            "dtype": "split-bf16 (3 products) on tcgen05, fp32 accumulate; sun term fp32",
+                                   "20%% glass tau 0.64 (byte mode), 1 bounce x %d paths (%d reflected-light bins in K), chunks of %d sensors"
+                                   % (nc_all, P, len(D), T, M, P + 1, chunk)},
+            "dtype": "split-bf16 (3 pieces, 6 products) on tcgen05, fp32 accumulate per 64-K chunk, chunks Kahan-summed; sun term fp32",
             "column_error_vs_fp64": {"max": float(ce.max()), "p99": float(np.percentile(ce, 99)), "median": float(np.median(ce)),
                                      "columns_over_1e-6": int((ce > 1e-6).sum()), "columns": int(ce.size), "sample_sensors": len(sub)},
             "fp32_column_error_vs_fp64": {"max": float(ce32.max()), "median": float(np.median(ce32))},
-            "trace_mrays_s": nc_all * len(D) / tt["trace"] / 1e6, "sky_build_s": yr["sky_s"], "series_tc_s": tt["tc"], "series_fp32_s_timed": tt["fp32"],
-            "E_bytes": nc_all * T * 4, "E_write_gbs": nc_all * T * 4 / tt["tc"] / 1e9}
+            "trace_mrays_s": nc_all * len(D) / tt["trace"] / 1e6, "bounce_mpaths_s": paths / tt["bounce"] / 1e6, "sky_build_s": yr["sky_s"],
+            "trace_s": tt["trace"], "bounce_s": tt["bounce"], "series_tc_s": tt["tc"], "series_fp32_s_timed": tt["fp32"],
+            "pipeline_s": pipeline_s - (tt["fp32"] if not args.full_fp32 else 0.0),
+            "E_bytes": nc_all * T * 4, "note": "series times include the E download to host memory (pageable), as the reference's gpu_series"}
     print(json.dumps(line), flush=True)
     e.close()
 
@@ -563,7 +587,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=30000)
     ap.add_argument("--ref-sample", type=int, default=20000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--sensors", type=int, default=0, help="urban: trace only the block's first N sensors (a small case for profiling)")
+    ap.add_argument("--sensors", type=int, default=0, help="urban / precision: only the block's first N sensors (a small case for profiling)")
     ap.add_argument("--config", default="urban", choices=["urban", "precision", "views", "serving"])
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--window", type=float, default=2.0)

@@ -65,7 +65,7 @@ struct Engine {
   Buf vis;
   bool bytes = false;
   size_t i0 = 0, visN = 0;
-  Buf dc;
+  Buf dc, contrib;   // contrib: one (bin, contribution) pair per path of a bounce launch
   size_t nBins = 0, dcN = 0, dcI0 = 0;
   Buf viewCls, viewDist, rowSin;
   size_t viewN = 0, viewK = 0, viewI0 = 0;
@@ -151,7 +151,7 @@ KGB_API void kgb_destroy(kgb_engine* e) {
   Engine* g = E(e);
   if (g->st) cudaStreamSynchronize(g->st);
   delete g->sc;
-  for (Buf* b : {&g->slots, &g->P, &g->N, &g->D, &g->rayTab, &g->vis, &g->dc, &g->viewCls, &g->viewDist, &g->rowSin, &g->label, &g->scratch, &g->out, &g->ctl,
+  for (Buf* b : {&g->slots, &g->P, &g->N, &g->D, &g->rayTab, &g->vis, &g->dc, &g->contrib, &g->viewCls, &g->viewDist, &g->rowSin, &g->label, &g->scratch, &g->out, &g->ctl,
                  &g->vop, &g->sop, &g->csr, &g->sunCol}) b->free();
   for (cudaEvent_t ev : g->ev) if (ev) cudaEventDestroy(ev);
   if (g->st && g->ownStream) cudaStreamDestroy(g->st);
@@ -207,7 +207,7 @@ KGB_API int kgb_build(kgb_engine* e, const float* v, size_t nv, const uint32_t* 
 KGB_API void kgb_trim(kgb_engine* e, int sensors) {
   Engine& g = *E(e);
   cudaStreamSynchronize(g.st);
-  g.vis.free(); g.dc.free(); g.scratch.free(); g.out.free(); g.viewCls.free(); g.viewDist.free();
+  g.vis.free(); g.dc.free(); g.contrib.free(); g.scratch.free(); g.out.free(); g.viewCls.free(); g.viewDist.free();
   g.vop.free(); g.sop.free(); g.csr.free(); g.sunCol.free();
   g.viewN = 0;
   if (sensors) { g.P.free(); g.N.free(); g.label.free(); g.nLabel = 0; g.nSensors = 0; }
@@ -450,7 +450,8 @@ KGB_API int kgb_set_series_form(kgb_engine* e, int form) {
 }
 
 // gpu.cu:533-568: the whole chunk over sample ranges [done, done + n): n from 2^13 / nc (1..64), then ~100 ms, at most
-// doubling; cancel between launches. Each thread adds to its sensor's rows in sample order: deterministic.
+// doubling; cancel between launches. One thread per path, then per sensor the paths' contributions are added in
+// sample order: deterministic, whatever the launch boundaries.
 KGB_API int kgb_bounce(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, const kgb_bounce_in* b) {
   Engine& g = *E(e);
   if (i0 + nc > g.nSensors) return fail("gpu_bounce: sensor range exceeds the scene");
@@ -468,9 +469,12 @@ KGB_API int kgb_bounce(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, c
   a.alpha = float((KGB_PI_D / 2.) / (7 * mf + .5)); a.cosN = float(std::cos(rad)); a.sinN = float(std::sin(rad));
   a.rayFlags = rayFlags; a.slots = static_cast<const kgb_slot*>(g.slots.p); a.nSlots = g.nSlots;
   a.dc = static_cast<float*>(g.dc.p); a.status = static_cast<uint32_t*>(g.ctl.p) + 1;
+  const size_t nCap = std::max<size_t>(1, (size_t(256) << 20) / (8 * nc));   // per-path results of a launch: at most 256 MiB
   for (size_t done = 0, n = std::clamp<size_t>((size_t(1) << 13) / nc, 1, 64); done < b->M;) {
     if (b->cancel && b->cancel(b->cancelCtx)) return fail("cancelled");
-    n = std::min<size_t>(n, b->M - done);
+    n = std::min({n, size_t(b->M) - done, nCap});
+    if (!grow(g.contrib, n * nc * 8)) return 0;
+    a.contrib = static_cast<uint2*>(g.contrib.p);
     a.s0 = uint32_t(done); a.s1 = uint32_t(done + n);
     if (!reset_ctl(g)) return 0;
     CU(cudaEventRecord(g.ev[0], g.st));

@@ -70,6 +70,7 @@ struct BounceArgs {
   const kgb_slot* slots;
   uint32_t nSlots;
   float* dc;
+  uint2* contrib;     // [(s1 - s0) x n]: each path's sky bin (or none) and contribution
   uint32_t* status;
 };
 

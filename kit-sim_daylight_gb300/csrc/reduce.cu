@@ -14,25 +14,23 @@ namespace kgb {
 __device__ __forceinline__ float dotf(F3 a, F3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }   // per-op rounding (gpu.cu:69-72)
 
 // GB300's FP64 pipe is narrow (a few lanes per clock per SM), so each term of a sum costs one FP64 instruction:
-//  - the float factor x > 0 becomes a double exactly by integer operations: its exponent rebiased (+896) and its
-//    mantissa moved up 29 bits (normal floats; a subnormal takes the conversion instruction);
+//  - the float factor x > 0 becomes a double exactly by integer operations (widen, rt.cuh);
 //  - the weights are read as doubles, converted once per block into shared memory;
 //  - the product of two floats is exact in double, so fma(x, w, acc) equals acc + x * w rounded once, as the
 //    reference's separate multiply and add;
 //  - a zero factor adds +0, which leaves the sum as it is: it is skipped.
-__device__ __forceinline__ double widen(float x) {
-  const uint32_t b = __float_as_uint(x);
-  return x >= 1.17549435e-38f ? __hiloint2double(int((b >> 3) + (896u << 20)), int(b << 29)) : (double)x;
-}
 
 constexpr uint32_t kReduceSmemDirs = 24576;   // weights held as doubles in shared memory (192 KB) up to this many
 
 template <bool SMEM>
 __device__ __forceinline__ const double* weights_to_smem(const float* W, uint32_t n, double* sW) {
-  if (!SMEM) return nullptr;
-  for (uint32_t d = threadIdx.x; d < n; d += blockDim.x) sW[d] = (double)__ldg(W + d);
-  __syncthreads();
-  return sW;
+  if constexpr (SMEM) {
+    for (uint32_t d = threadIdx.x; d < n; d += blockDim.x) sW[d] = (double)__ldg(W + d);
+    __syncthreads();
+    return sW;
+  } else {
+    return nullptr;
+  }
 }
 template <bool SMEM>
 __device__ __forceinline__ double weight(const double* sW, const float* W, uint32_t d) { return SMEM ? sW[d] : (double)__ldg(W + d); }

@@ -70,6 +70,13 @@ __device__ __forceinline__ void glass_TR(float c, float tn, float& T, float& R) 
   R = .5f * rs * (1.f + (1.f - 2.f * rs) * d2) / (1.f - rs * rs * d2) + .5f * rp * (1.f + (1.f - 2.f * rp) * d2) / (1.f - rp * rp * d2);
 }
 
+// x >= 0 as a double, exactly, without the FP64 pipe for a normal float: the exponent rebiased (+896) and the
+// mantissa moved up 29 bits by integer operations (zero and subnormals take the conversion instruction).
+__device__ __forceinline__ double widen(float x) {
+  const uint32_t b = __float_as_uint(x);
+  return x >= 1.17549435e-38f ? __hiloint2double(int((b >> 3) + (896u << 20)), int(b << 29)) : (double)x;
+}
+
 // ------------------------------------------------------------------------------------------------ the ray
 struct Ray {
   F3 o, d;
@@ -201,18 +208,53 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
   return r;
 }
 
+// Two floats in one 64-bit register pair, for the packed FP32 instructions (add / mul / fma .f32x2, sm_100 and
+// later): each half is rounded exactly as the scalar instruction rounds it.
+__device__ __forceinline__ unsigned long long pk2(float a, float b) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void up2(unsigned long long r, float& a, float& b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r)); }
+__device__ __forceinline__ unsigned long long add2(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b, unsigned long long c) {
+  unsigned long long r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+__device__ __forceinline__ unsigned long long mul2(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+// Bytes b and b + 1 of w as the bit patterns 2^23 + q (see qf), packed.
+__device__ __forceinline__ unsigned long long qf2raw(uint32_t w, int b) {
+  return pk2(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | uint32_t(b))), __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | uint32_t(b + 1))));
+}
+
 // Child boxes of a node against the ray in [tmin, tmax] (tmin >= 0): returns the mask of hit children (bit k), their
 // entry distances in tn[8]. Conservative: the boxes were expanded at build; the exit distance is widened by 2^-20.
 // Per axis the near plane is the low one when the ray's inverse direction is non-negative (the slab distance
 // fma(q, adj, o) is then non-decreasing in q), else the high one: the words of near and far planes are picked once
-// per node, so each child costs six plane distances, one 3-input max and one 3-input min. Empty child slots need
+// per node. Children go in pairs through the packed instructions: per pair and plane two byte permutes, one packed
+// add (the exact byte value) and one packed fma; per child one 3-input max and one 3-input min. Empty child slots need
 // no test: a leaf slot without triangles that the box test lets through tests nothing.
+// CLIP: the exit is also clipped at tmax (closest hit, where tmax shrinks to the best hit). Without it boxes beyond
+// tmax pass as well, which is conservative: the triangle test applies tmax (the any-hit walks run to infinity).
+template <bool CLIP = true>
 __device__ __forceinline__ uint32_t node_hits(const uint4* n, const Ray& r, float tmin, float tmax, float* tn) {
   const float px = __uint_as_float(n[0].x), py = __uint_as_float(n[0].y), pz = __uint_as_float(n[0].z);
   const uint32_t ew = n[0].w;
   const float sx = __uint_as_float((ew & 0xffu) << 23), sy = __uint_as_float(((ew >> 8) & 0xffu) << 23), sz = __uint_as_float(((ew >> 16) & 0xffu) << 23);
   const float adjx = sx * r.inv.x, adjy = sy * r.inv.y, adjz = sz * r.inv.z;
   const float ox = __fmaf_rn(px, r.inv.x, -r.oinv.x), oy = __fmaf_rn(py, r.inv.y, -r.oinv.y), oz = __fmaf_rn(pz, r.inv.z, -r.oinv.z);
+  const unsigned long long AX = pk2(adjx, adjx), AY = pk2(adjy, adjy), AZ = pk2(adjz, adjz);
+  const unsigned long long OX = pk2(ox, ox), OY = pk2(oy, oy), OZ = pk2(oz, oz);
+  const unsigned long long MAGIC = pk2(-8388608.f, -8388608.f), WIDEN = pk2(1.00000095367431640625f, 1.00000095367431640625f);
   // quantised bounds: qlo.x = n2.x,n2.y  qlo.y = n2.z,n2.w  qlo.z = n3.x,n3.y  qhi.x = n3.z,n3.w  qhi.y = n4.x,n4.y  qhi.z = n4.z,n4.w
   const bool nx = r.inv.x < 0.f, ny = r.inv.y < 0.f, nz = r.inv.z < 0.f;
   const uint32_t nearX[2] = {nx ? n[3].z : n[2].x, nx ? n[3].w : n[2].y}, farX[2] = {nx ? n[2].x : n[3].z, nx ? n[2].y : n[3].w};
@@ -220,16 +262,25 @@ __device__ __forceinline__ uint32_t node_hits(const uint4* n, const Ray& r, floa
   const uint32_t nearZ[2] = {nz ? n[4].z : n[3].x, nz ? n[4].w : n[3].y}, farZ[2] = {nz ? n[3].x : n[4].z, nz ? n[3].y : n[4].w};
   uint32_t mask = 0;
 #pragma unroll
-  for (int k = 0; k < 8; ++k) {
+  for (int k = 0; k < 8; k += 2) {
     const int h = k >> 2, b = k & 3;
-    const float tnx = __fmaf_rn(qf(nearX[h], b), adjx, ox), tfx = __fmaf_rn(qf(farX[h], b), adjx, ox);
-    const float tny = __fmaf_rn(qf(nearY[h], b), adjy, oy), tfy = __fmaf_rn(qf(farY[h], b), adjy, oy);
-    const float tnz = __fmaf_rn(qf(nearZ[h], b), adjz, oz), tfz = __fmaf_rn(qf(farZ[h], b), adjz, oz);
-    const float tnear = max3f(tnx, tny, fmaxf(tnz, tmin));
-    // exit widened to tfar (1 + 2^-20): for tfar >= 0 the value fma(|tfar|, 2^-20, tfar), and a negative tfar
-    // fails against tnear >= tmin >= 0 either way
-    const float tfar = fminf(__fmul_rn(min3f(tfx, tfy, tfz), 1.00000095367431640625f), tmax);
-    if (tnear <= tfar) { mask |= 1u << k; tn[k] = tnear; }
+    float tnx[2], tny[2], tnz[2], tfx[2], tfy[2], tfz[2];
+    up2(fma2(add2(qf2raw(nearX[h], b), MAGIC), AX, OX), tnx[0], tnx[1]);
+    up2(fma2(add2(qf2raw(farX[h], b), MAGIC), AX, OX), tfx[0], tfx[1]);
+    up2(fma2(add2(qf2raw(nearY[h], b), MAGIC), AY, OY), tny[0], tny[1]);
+    up2(fma2(add2(qf2raw(farY[h], b), MAGIC), AY, OY), tfy[0], tfy[1]);
+    up2(fma2(add2(qf2raw(nearZ[h], b), MAGIC), AZ, OZ), tnz[0], tnz[1]);
+    up2(fma2(add2(qf2raw(farZ[h], b), MAGIC), AZ, OZ), tfz[0], tfz[1]);
+    // exit widened to tfar (1 + 2^-20): for tfar >= 0 the value fma(|tfar|, 2^-20, tfar), and a negative tfar fails
+    // against tnear >= tmin >= 0 either way
+    float tf[2];
+    up2(mul2(pk2(min3f(tfx[0], tfy[0], tfz[0]), min3f(tfx[1], tfy[1], tfz[1])), WIDEN), tf[0], tf[1]);
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const float tnear = max3f(tnx[e], tny[e], fmaxf(tnz[e], tmin));
+      const float tfar = CLIP ? fminf(tf[e], tmax) : tf[e];
+      if (tnear <= tfar) { mask |= 1u << (k + e); tn[k + e] = tnear; }
+    }
   }
   return mask;
 }
@@ -281,7 +332,7 @@ __device__ __forceinline__ void for_hits(const Scene& s, const Ray& r, float tmi
     load_node(s.nodes, cur, n);
     if (COUNT) ctr->nodes++;
     float tn[8];
-    const uint32_t hit = node_hits(n, r, tmin, tmax, tn);
+    const uint32_t hit = node_hits<false>(n, r, tmin, tmax, tn);
     const uint32_t imask = n[0].w >> 24;
     uint32_t leaves = hit & ~imask;
     while (leaves) {
@@ -341,7 +392,7 @@ __device__ __forceinline__ bool closest(const Scene& s, const Ray& r, float tmin
     uint4 n[5];
     load_node(s.nodes, e.node, n);
     float tn[8];
-    const uint32_t hit = node_hits(n, r, tmin, best, tn);
+    const uint32_t hit = node_hits<true>(n, r, tmin, best, tn);
     const uint32_t imask = n[0].w >> 24;
     uint32_t leaves = hit & ~imask;
     while (leaves) {

@@ -11,21 +11,24 @@
 //    products run per K step: hi.hi, then the corrections hi.mid + mid.hi + hi.lo + mid.mid + lo.hi (the dropped
 //    mid.lo, lo.mid, lo.lo are 2^-24 of the product and below);
 //  - the tensor core's FP32 accumulation truncates, so a long accumulation chain drifts low by about a quarter ulp per
-//    instruction (1e-5 over 2305 patches). hi.hi, which carries the sum, is therefore accumulated in TMEM over chunks
-//    of 128 K only (8 instructions), and the chunk sums are added in FP32 round-to-nearest by the epilogue; the
-//    corrections (2^-8 of the sum) keep one chain per tile in a second accumulator;
+//    instruction (1e-5 over 2305 patches). Every accumulation chain is therefore short: per 64-wide K block (a chunk)
+//    hi.hi goes into one TMEM accumulator and the five corrections into another, both from zero (4 and 20 MMAs), and
+//    the epilogue adds both chunk sums into FP32 registers with Kahan compensation;
 //  - the sun term (one direction per step, exact in the reference's float arithmetic) is added in the epilogue, where
-//    each output is finished in registers and streamed to HBM with 128-byte row stores.
+//    each output is finished in registers and stored with 16-byte row stores.
 //
-// Kernel k_series_tc, one CTA per SM, persistent over 128 x 128 output tiles (sensors x steps, steps fastest so that
+// Kernel k_series_tc, one CTA per SM, persistent over 128 x 64 output tiles (sensors x steps, steps fastest so that
 // the CTAs running at once share a few V panels and all of S in L2):
-//   warp 0      TMA producer: per 64-wide K block, the three pieces of V (128 x 64) and of S (128 x 64), bf16,
-//               128-byte swizzled, into a 2-stage shared-memory ring (96 KB a stage)
-//   warp 1      MMA issuer (one thread): 24 tcgen05.mma (M 128, N 128, K 16) per stage: hi.hi into the chunk
-//               accumulator H[chunk % 2], the corrections into the tile accumulator C[tile % 2] (TMEM: H0 H1 C0 C1,
-//               128 columns each); tcgen05.commit frees the stage, hands a finished chunk or tile to the epilogue
-//   warps 2-5   epilogue: per chunk, tcgen05.ld of H (warp w reads TMEM lanes 32 (w % 4) ..) added into 128 FP32
-//               registers; per tile, C and the sun term, a per-warp shared-memory transpose, coalesced stores of E rows
+//   warp 0      TMA producer: per 64-wide K block, the three pieces of V (128 x 64) and of S (64 x 64), bf16,
+//               128-byte swizzled, into a 3-stage shared-memory ring (72 KB a stage)
+//   warp 1      MMA issuer (one thread): 24 tcgen05.mma (M 128, N 64, K 16) per stage: hi.hi into H[chunk % 2], the
+//               corrections into C[chunk % 2] (TMEM: H0 H1 C0 C1, 64 columns each); tcgen05.commit frees the stage
+//               and hands a finished chunk to the epilogue
+//   warps 2-5   epilogue, one per TMEM lane quarter (warp w reads lanes 32 (w % 4) ..), a thread per output row: per
+//               chunk, tcgen05.ld of H and C added into the row's 64 Kahan-compensated FP32 sums (128 registers); per
+//               tile, the sun term, and the row of E stored 16 bytes at a time
+// The 64-column tile keeps the Kahan sums in registers: six warps per CTA leave a scheduler at most two warps, so a
+// thread may hold up to 255 registers (the register file is split between the SM's four schedulers).
 // Every wait on an mbarrier is bounded: past the limit the kernel records kStatusTimeout and leaves its loops (the
 // TMEM it holds is released on the way out).
 #include <cuda.h>
@@ -38,15 +41,15 @@
 
 namespace kgb {
 
-constexpr int BM = 128, BN = 128, BK = 64, STAGES = 2, PIECES = 3;
-constexpr int CHUNK_BLOCKS = 2;                      // K blocks (of BK) per hi.hi accumulation chunk: 8 instructions
-constexpr int TILE_BYTES = BM * BK * 2;              // 16 KB: one bf16 operand tile (rows x 128 B)
-constexpr int STAGE_BYTES = 2 * PIECES * TILE_BYTES; // V hi mid lo, S hi mid lo
-constexpr int EPI_WARPS = 4;
+constexpr int BM = 128, BN = 64, BK = 64, STAGES = 3, PIECES = 3;
+constexpr int CHUNK_BLOCKS = 1;                      // K blocks (of BK) per accumulation chunk: 4 hi.hi + 20 correction MMAs
+constexpr int V_TILE = BM * BK * 2;                  // 16 KB: one bf16 V tile (128 rows x 128 B)
+constexpr int S_TILE = BN * BK * 2;                  // 8 KB: one bf16 S^T tile (64 rows x 128 B)
+constexpr int STAGE_BYTES = PIECES * (V_TILE + S_TILE); // V hi mid lo, S hi mid lo
+constexpr int EPI_WARPS = 4;                        // one per TMEM lane quarter, the tile's 64 columns each
 constexpr int THREADS = 32 * (2 + EPI_WARPS);
-constexpr int STAGE_PAD = 33;                        // floats per row of the per-warp transpose buffer
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + EPI_WARPS * 32 * STAGE_PAD * 4 + 1024 /* align */ + 256 /* barriers */;
-constexpr uint32_t TMEM_COLS = 4 * BN;               // H0 H1 (chunk sums of hi.hi), C0 C1 (corrections of a tile)
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /* align */ + 256 /* barriers */;
+constexpr uint32_t TMEM_COLS = 4 * BN;               // H0 H1 (hi.hi of a chunk), C0 C1 (its corrections)
 constexpr uint64_t kWaitLimitNs = 4000000000ull;   // 4 s: no wait of a healthy run comes near it
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
@@ -116,6 +119,18 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
   for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
 }
 
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]),
+        "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+
 struct SeriesTcArgs {
   uint32_t nc, T, Kp, mTiles, nTiles;
   // sun term of the epilogue (the reference's k_series tail, gpu.cu:145-148): column t's sun direction, if any
@@ -141,15 +156,12 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
                                                           SeriesTcArgs a) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  float* stageBuf = reinterpret_cast<float*>(smem + STAGES * STAGE_BYTES);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES + EPI_WARPS * 32 * STAGE_PAD * 4);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
   uint64_t* full = bars;                 // [STAGES] TMA -> MMA
   uint64_t* empty = bars + STAGES;       // [STAGES] MMA -> TMA
-  uint64_t* hFull = bars + 2 * STAGES;   // [2] MMA -> epilogue: a chunk sum of hi.hi is complete
+  uint64_t* hFull = bars + 2 * STAGES;   // [2] MMA -> epilogue: a chunk's two sums (hi.hi, corrections) are complete
   uint64_t* hEmpty = hFull + 2;          // [2] epilogue -> MMA
-  uint64_t* cFull = hFull + 4;           // [2] MMA -> epilogue: the tile's corrections are complete
-  uint64_t* cEmpty = hFull + 6;          // [2] epilogue -> MMA
-  uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(hFull + 8);
+  uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(hFull + 4);
   __shared__ volatile uint32_t abortFlag;
 
   const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x & 31;
@@ -157,7 +169,6 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
     for (int s = 0; s < STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&hFull[b], 1); mbar_init(&hEmpty[b], EPI_WARPS * 32);
-      mbar_init(&cFull[b], 1); mbar_init(&cEmpty[b], EPI_WARPS * 32);
     }
     abortFlag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -186,8 +197,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
           const int k0 = int(kb) * BK;
 #pragma unroll
           for (int p = 0; p < PIECES; ++p) {
-            tma_load_2d(s + p * TILE_BYTES, &mapV, k0, m0 + p * int(a.nc), &full[stage]);
-            tma_load_2d(s + (PIECES + p) * TILE_BYTES, &mapS, k0, n0 + p * int(a.T), &full[stage]);
+            tma_load_2d(s + p * V_TILE, &mapV, k0, m0 + p * int(a.nc), &full[stage]);
+            tma_load_2d(s + PIECES * V_TILE + p * S_TILE, &mapS, k0, n0 + p * int(a.T), &full[stage]);
           }
           if (++stage == STAGES) { stage = 0; phase ^= 1; }
         }
@@ -196,32 +207,31 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
     __syncwarp();
   } else if (warp == 1) {
     if (lane == 0) {   // ---------------- MMA issuer
-      uint32_t stage = 0, phase = 0, local = 0, chunk = 0;
-      for (uint32_t tile = blockIdx.x; tile < nTilesAll && !abortFlag; tile += gridDim.x, ++local) {
-        const uint32_t cbuf = local & 1, cuse = local >> 1;
-        if (!mbar_wait(&cEmpty[cbuf], (cuse & 1) ^ 1, a.status)) { abortFlag = 1; break; }
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t cT = tmemBase + (2 + cbuf) * BN;
-        uint32_t hT = tmemBase, hbuf = 0;
+      uint32_t stage = 0, phase = 0, chunk = 0;
+      for (uint32_t tile = blockIdx.x; tile < nTilesAll && !abortFlag; tile += gridDim.x) {
+        uint32_t hT = tmemBase, cT = tmemBase + 2 * BN, hbuf = 0;
         bool ok = true;
         for (uint32_t kb = 0; kb < kBlocks && ok; ++kb) {
           const uint32_t kc = kb % CHUNK_BLOCKS;
-          if (kc == 0) {   // a new chunk of hi.hi
+          if (kc == 0) {   // a new chunk: hi.hi into H[buf], the corrections into C[buf], both from zero
             hbuf = chunk & 1;
             if (!mbar_wait(&hEmpty[hbuf], ((chunk >> 1) & 1) ^ 1, a.status)) { ok = false; break; }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             hT = tmemBase + hbuf * BN;
+            cT = tmemBase + (2 + hbuf) * BN;
           }
           if (!mbar_wait(&full[stage], phase, a.status)) { ok = false; break; }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint8_t* s = smem + stage * STAGE_BYTES;
-          const uint64_t v0 = smem_desc(s), v1 = smem_desc(s + TILE_BYTES), v2 = smem_desc(s + 2 * TILE_BYTES);
-          const uint64_t s0 = smem_desc(s + 3 * TILE_BYTES), s1 = smem_desc(s + 4 * TILE_BYTES), s2 = smem_desc(s + 5 * TILE_BYTES);
+          const uint64_t v0 = smem_desc(s), v1 = smem_desc(s + V_TILE), v2 = smem_desc(s + 2 * V_TILE);
+          const uint8_t* st = s + PIECES * V_TILE;
+          const uint64_t s0 = smem_desc(st), s1 = smem_desc(st + S_TILE), s2 = smem_desc(st + 2 * S_TILE);
 #pragma unroll
           for (int k = 0; k < BK / 16; ++k) {   // 16 bf16 = 32 bytes along K: +2 in the descriptor's address field
             const uint64_t off = uint64_t(2 * k);
-            mma_bf16(hT, v0 + off, s0 + off, (kc | uint32_t(k)) != 0);
-            mma_bf16(cT, v0 + off, s1 + off, (kb | uint32_t(k)) != 0);
+            const uint32_t acc = (kc | uint32_t(k)) != 0;
+            mma_bf16(hT, v0 + off, s0 + off, acc);
+            mma_bf16(cT, v0 + off, s1 + off, acc);
             mma_bf16(cT, v1 + off, s0 + off, 1);
             mma_bf16(cT, v0 + off, s2 + off, 1);
             mma_bf16(cT, v1 + off, s1 + off, 1);
@@ -232,19 +242,18 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
           if (kc == CHUNK_BLOCKS - 1 || kb == kBlocks - 1) { mma_commit(&hFull[hbuf]); ++chunk; }
         }
         if (!ok) { abortFlag = 1; break; }
-        mma_commit(&cFull[cbuf]);      // the tile's corrections are complete
       }
     }
     __syncwarp();
   } else {   // ---------------- epilogue: warps 2..5
-    const uint32_t q = warp & 3;                       // TMEM lane quarter this warp may read
+    const uint32_t q = warp & 3;                       // the TMEM lane quarter this warp may read
     const uint32_t laneBase = (q * 32u) << 16;
-    float* tb = stageBuf + (warp - 2) * 32 * STAGE_PAD;
-    uint32_t local = 0, chunk = 0;
-    for (uint32_t tile = blockIdx.x; tile < nTilesAll; tile += gridDim.x, ++local) {
-      float acc[BN];
+    uint32_t chunk = 0;
+    for (uint32_t tile = blockIdx.x; tile < nTilesAll; tile += gridDim.x) {
+      // the chunks' sums (hi.hi and corrections), added with Kahan compensation (acc - cmp is the running sum)
+      float acc[BN], cmp[BN];
 #pragma unroll
-      for (int c = 0; c < BN; ++c) acc[c] = 0.f;
+      for (int c = 0; c < BN; ++c) { acc[c] = 0.f; cmp[c] = 0.f; }
       bool ok = true;
       for (uint32_t ch = 0; ch < nChunks; ++ch, ++chunk) {
         const uint32_t hbuf = chunk & 1;
@@ -252,31 +261,38 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
         if (!ok || abortFlag) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-        for (int g = 0; g < BN / 32; ++g) {
-          float v[32];
-          tmem_ld32(tmemBase + laneBase + hbuf * BN + g * 32, v);
+        for (int part = 0; part < 2; ++part) {   // the chunk's hi.hi sum, then its corrections
 #pragma unroll
-          for (int c = 0; c < 32; ++c) acc[g * 32 + c] = __fadd_rn(acc[g * 32 + c], v[c]);
+          for (int g = 0; g < BN / 16; ++g) {
+            float v[16];
+            tmem_ld16(tmemBase + laneBase + (2 * part + hbuf) * BN + g * 16, v);
+#pragma unroll
+            for (int c = 0; c < 16; ++c) {
+              const int j = g * 16 + c;
+              const float y = __fsub_rn(v[c], cmp[j]);
+              const float t = __fadd_rn(acc[j], y);
+              cmp[j] = __fsub_rn(__fsub_rn(t, acc[j]), y);
+              acc[j] = t;
+            }
+          }
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         mbar_arrive(&hEmpty[hbuf]);
       }
-      const uint32_t cbuf = local & 1;
-      if (ok) ok = __all_sync(~0u, mbar_wait(&cFull[cbuf], (local >> 1) & 1, a.status));
       if (!ok || abortFlag) { abortFlag = 1; break; }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t m0 = (tile / a.nTiles) * BM, n0 = (tile % a.nTiles) * BN;
       const uint32_t row = m0 + q * 32 + lane;         // this thread's sensor
       float nrm[3] = {0.f, 0.f, 0.f};
       if (row < a.nc) { nrm[0] = a.N[3 * row]; nrm[1] = a.N[3 * row + 1]; nrm[2] = a.N[3 * row + 2]; }
+      float* Erow = a.E + size_t(row) * a.T;
+      const bool vec = (a.T & 3u) == 0;                  // 16-byte row stores when rows are 16-byte aligned
 #pragma unroll
-      for (int g = 0; g < BN / 32; ++g) {
-        float v[32];
-        tmem_ld32(tmemBase + laneBase + (2 + cbuf) * BN + g * 32, v);
+      for (int g = 0; g < BN / 16; ++g) {
+        float v[16];
 #pragma unroll
-        for (int c = 0; c < 32; ++c) {
-          float x = __fadd_rn(acc[g * 32 + c], v[c]);
-          const uint32_t t = n0 + g * 32 + c;
+        for (int c = 0; c < 16; ++c) {
+          float x = __fsub_rn(acc[g * 16 + c], cmp[g * 16 + c]);
+          const uint32_t t = n0 + g * 16 + c;
           if (t < a.T && row < a.nc) {
             const int j = __ldg(a.sunOfCol + t);
             if (j >= 0) {
@@ -287,19 +303,19 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
               if (at != 0.f) x = __fadd_rn(x, __fmul_rn(__fmul_rn(fmaxf(dotf_rn(nrm, a.sunVec + 3 * j), 0.f), at), a.sunW[j]));
             }
           }
-          tb[lane * STAGE_PAD + c] = x;
+          v[c] = x;
         }
-        __syncwarp();
-        // the warp's 32 rows x 32 columns: one 128-byte row segment per store instruction
-        const uint32_t t = n0 + g * 32 + lane;
-        for (int r = 0; r < 32; ++r) {
-          const uint32_t rr = m0 + q * 32 + r;
-          if (rr < a.nc && t < a.T) a.E[size_t(rr) * a.T + t] = tb[r * STAGE_PAD + lane];
+        if (row < a.nc) {
+          const uint32_t t0 = n0 + g * 16;
+          if (vec && t0 + 16 <= a.T) {
+#pragma unroll
+            for (int c = 0; c < 16; c += 4) *reinterpret_cast<float4*>(Erow + t0 + c) = make_float4(v[c], v[c + 1], v[c + 2], v[c + 3]);
+          } else {
+#pragma unroll
+            for (int c = 0; c < 16; ++c) if (t0 + c < a.T) Erow[t0 + c] = v[c];
+          }
         }
-        __syncwarp();
       }
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      mbar_arrive(&cEmpty[cbuf]);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -420,13 +436,13 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// A [rows x Kp] bf16, K contiguous: boxes of 64 (128 B) x 128 rows, 128-byte swizzle, zero fill past the rows.
-static bool make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t Kp) {
+// A [rows x Kp] bf16, K contiguous: boxes of 64 (128 B) x boxRows rows, 128-byte swizzle, zero fill past the rows.
+static bool make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t Kp, uint32_t boxRows) {
   auto fn = encode_fn();
   if (!fn) return false;
   const cuuint64_t dims[2] = {Kp, rows};
   const cuuint64_t strides[1] = {Kp * 2};
-  const cuuint32_t box[2] = {BK, BM};
+  const cuuint32_t box[2] = {BK, boxRows};
   const cuuint32_t estr[2] = {1, 1};
   return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
             CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
@@ -436,7 +452,7 @@ const char* series_tc(const SeriesTcPlan& p, cudaStream_t st) {
   if (p.nc == 0 || p.T == 0) return nullptr;
   if (p.Kp % BK) return "series_tc: K not padded to 64";
   CUtensorMap mV, mS;
-  if (!make_map(&mV, p.v, uint64_t(PIECES) * p.nc, p.Kp) || !make_map(&mS, p.s, uint64_t(PIECES) * p.T, p.Kp))
+  if (!make_map(&mV, p.v, uint64_t(PIECES) * p.nc, p.Kp, BM) || !make_map(&mS, p.s, uint64_t(PIECES) * p.T, p.Kp, BN))
     return "series_tc: cuTensorMapEncodeTiled failed";
   if (uint64_t(PIECES) * p.nc + BM > 0x7fffffffull || uint64_t(PIECES) * p.T + BN > 0x7fffffffull) return "series_tc: chunk too large";
   static bool attr = false;

@@ -38,7 +38,8 @@ struct __align__(16) Seg {
   const float* P;      // the chunk's first sensor
   const float* N;
   const float* D;
-  const float* W;      // [nQ x nDir]
+  const RayDir* tab;   // the directions' precomputed ray parts
+  const double* W;     // [nQ x nDir], the request's float weights widened
   uint32_t nNodes, nDir, nWords, n;
   uint32_t rayFlags, nQ, useCosMask, taskBase;
   uint32_t sensBase, bitsOff, outOff, pad;
@@ -72,14 +73,15 @@ __global__ void __launch_bounds__(256) k_bits_batch(const BatchHdr* hdr, const S
     if (i >= g.n) continue;
     const Scene s{g.nodes, g.tris, g.nNodes};
     const F3 n = ld3(g.N + 3 * i), o = offset_ray(ld3(g.P + 3 * i), n);
-    const uint32_t word = trace_word<false>(s, n, o, g.D, nullptr, g.nDir, w, (g.rayFlags & KGB_RAY_CULL_BACK_FACING) != 0, overflow, ctr, rays);
+    const uint32_t word = trace_word<false>(s, n, o, g.D, g.tab, g.nDir, w, (g.rayFlags & KGB_RAY_CULL_BACK_FACING) != 0, overflow, ctr, rays);
     bitsPool[g.bitsOff + size_t(w) * g.n + i] = word;
   }
   if (overflow) atomicOr(status, (overflow & 1u ? kStatusStackOverflow : 0u) | (overflow & 2u ? kStatusVisitLimit : 0u));
 }
 
 // every quantity of every chunk: out[outOff + q n + i] = sum over visible d, in order, of
-// double(float(useCos_q ? max(0, N_i . D_d) : 1)) x W_q[d] (the single-request reduce's arithmetic, per quantity)
+// double(float(useCos_q ? max(0, N_i . D_d) : 1)) x W_q[d] (the single-request reduce's arithmetic, per quantity:
+// one fma per term, the float factor widened exactly, a zero factor skipped)
 __global__ void __launch_bounds__(256) k_reduce_batch(const BatchHdr* hdr, const Seg* segs, const uint32_t* bitsPool, double* outPool) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= hdr->nSens) return;
@@ -97,8 +99,10 @@ __global__ void __launch_bounds__(256) k_reduce_batch(const BatchHdr* hdr, const
       const F3 dir = ld3(g.D + 3 * d);
       const float c = fmaxf(__fadd_rn(__fadd_rn(__fmul_rn(n.x, dir.x), __fmul_rn(n.y, dir.y)), __fmul_rn(n.z, dir.z)), 0.f);
 #pragma unroll
-      for (uint32_t q = 0; q < kMaxQ; ++q)
-        if (q < g.nQ) acc[q] = __dadd_rn(acc[q], __dmul_rn((double)((((g.useCosMask >> q) & 1u) ? c : 1.f) * 1.f), (double)__ldg(g.W + size_t(q) * g.nDir + d)));
+      for (uint32_t q = 0; q < kMaxQ; ++q) {
+        const float x = ((g.useCosMask >> q) & 1u) ? c : 1.f;
+        if (q < g.nQ && x != 0.f) acc[q] = __fma_rn(widen(x), __ldg(g.W + size_t(q) * g.nDir + d), acc[q]);
+      }
     }
   }
   for (uint32_t q = 0; q < g.nQ; ++q) outPool[g.outOff + size_t(q) * g.n + i] = acc[q];
@@ -124,8 +128,9 @@ struct Request {
   std::vector<float> rowSin;
   std::vector<double> wRow;
   std::vector<float> reach;
+  std::vector<double> w64;    // daylight: the weights widened to double (the source of their upload)
   uint32_t nSensors = 0, nextSensor = 0, doneSensors = 0;
-  void* dev = nullptr;        // P, N, D, W (daylight) | P, N, rowSin, wRow, label, cls, dist, out (views)
+  void* dev = nullptr;        // P, N, D, ray table, W (daylight) | P, N, rowSin, wRow, label, cls, dist, out (views)
   uint64_t devBytes = 0;
   Clock::time_point tSubmit, tDone;
   bool done = false, failed = false;
@@ -176,9 +181,21 @@ bool cuok(cudaError_t e, std::string& err, const char* what) {
   return false;
 }
 
-uint64_t daylight_bytes(const kgb_daylight_request& r) {
-  return uint64_t(r.nSensors) * 24 + uint64_t(r.nDir) * 12 + uint64_t(r.nQ) * r.nDir * 4 + 1024;
+// a daylight request's device arrays: P, N (12 B per sensor each), D (12 B per direction), its ray table (48 B per
+// direction), its weights as doubles [nQ x nDir]; 256-byte aligned pieces
+struct DayLayout { size_t offN, offD, offTab, offW, total; };
+DayLayout day_layout(const kgb_daylight_request& d) {
+  const auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
+  DayLayout L;
+  L.offN = size_t(d.nSensors) * 12;
+  L.offD = up(2 * L.offN);
+  L.offTab = up(L.offD + size_t(d.nDir) * 12);
+  L.offW = up(L.offTab + size_t(d.nDir) * 48);
+  L.total = up(L.offW + size_t(d.nQ) * d.nDir * 8);
+  return L;
 }
+
+uint64_t daylight_bytes(const kgb_daylight_request& r) { return day_layout(r).total; }
 uint32_t views_NA(const kgb_views_request& r) { return 3 * r.nClass + 1 + r.nReach + (r.glazing ? 1 : 0) + (r.isoDim ? 1 : 0); }
 uint64_t views_bytes(const kgb_views_request& r, uint32_t chunk, uint32_t nTris) {
   const uint64_t K = uint64_t(r.view.nAz) * r.view.nEl;
@@ -231,14 +248,18 @@ void finish(Server& s, Request* r, bool ok, const std::string& err) {
 bool upload(Server& s, Request* r, std::string& err) {
   if (r->kind == 0) {
     const kgb_daylight_request& d = r->d;
-    const size_t offN = size_t(d.nSensors) * 12, offD = offN * 2, offW = offD + size_t(d.nDir) * 12;
-    r->devBytes = offW + size_t(d.nQ) * d.nDir * 4 + 256;
+    const DayLayout L = day_layout(d);
+    r->devBytes = L.total;
     if (!cuok(cudaMalloc(&r->dev, r->devBytes), err, "request memory")) return false;
     char* b = static_cast<char*>(r->dev);
-    cudaMemcpyAsync(b, d.P, offN, cudaMemcpyHostToDevice, s.st);
-    cudaMemcpyAsync(b + offN, d.N, offN, cudaMemcpyHostToDevice, s.st);
-    cudaMemcpyAsync(b + offD, d.D, size_t(d.nDir) * 12, cudaMemcpyHostToDevice, s.st);
-    cudaMemcpyAsync(b + offW, d.W, size_t(d.nQ) * d.nDir * 4, cudaMemcpyHostToDevice, s.st);
+    r->w64.resize(size_t(d.nQ) * d.nDir);
+    const float* W = static_cast<const float*>(d.W);
+    for (size_t k = 0; k < r->w64.size(); ++k) r->w64[k] = double(W[k]);
+    cudaMemcpyAsync(b, d.P, L.offN, cudaMemcpyHostToDevice, s.st);
+    cudaMemcpyAsync(b + L.offN, d.N, L.offN, cudaMemcpyHostToDevice, s.st);
+    cudaMemcpyAsync(b + L.offD, d.D, size_t(d.nDir) * 12, cudaMemcpyHostToDevice, s.st);
+    cudaMemcpyAsync(b + L.offW, r->w64.data(), r->w64.size() * 8, cudaMemcpyHostToDevice, s.st);
+    launch_ray_table(reinterpret_cast<const float*>(b + L.offD), d.nDir, b + L.offTab, s.st);
   } else {
     const kgb_views_request& v = r->v;
     const DScene& sc = s.scenes[size_t(v.scene)];
@@ -311,11 +332,12 @@ bool run_daylight_batch(Server& s, const std::vector<Part>& parts, std::string& 
     const kgb_daylight_request& d = p.r->d;
     const DScene& sc = s.scenes[size_t(d.scene)];
     const char* b = static_cast<const char*>(p.r->dev);
-    const size_t offN = size_t(d.nSensors) * 12, offD = offN * 2, offW = offD + size_t(d.nDir) * 12;
+    const DayLayout L = day_layout(d);
     Seg& g = s.hSegs[k];
     g.nodes = static_cast<const Node8*>(sc.nodes); g.tris = static_cast<const TriRec*>(sc.tris); g.nNodes = sc.nNodes;
-    g.P = reinterpret_cast<const float*>(b) + 3 * size_t(p.i0); g.N = reinterpret_cast<const float*>(b + offN) + 3 * size_t(p.i0);
-    g.D = reinterpret_cast<const float*>(b + offD); g.W = reinterpret_cast<const float*>(b + offW);
+    g.P = reinterpret_cast<const float*>(b) + 3 * size_t(p.i0); g.N = reinterpret_cast<const float*>(b + L.offN) + 3 * size_t(p.i0);
+    g.D = reinterpret_cast<const float*>(b + L.offD); g.tab = reinterpret_cast<const RayDir*>(b + L.offTab);
+    g.W = reinterpret_cast<const double*>(b + L.offW);
     g.nDir = d.nDir; g.nWords = (d.nDir + 31) / 32; g.n = p.n; g.rayFlags = d.rayFlags; g.nQ = d.nQ; g.useCosMask = d.useCosMask;
     g.taskBase = tasks; g.sensBase = sens; g.bitsOff = uint32_t(bits); g.outOff = uint32_t(out);
     tasks += (p.n + 31) / 32 * g.nWords;

@@ -77,7 +77,7 @@ __device__ __forceinline__ double tcos_d(const double* costab, double x) {   // 
 __global__ void __launch_bounds__(128) k_sky(SkyArgs a) {
   extern __shared__ double sh[];   // [P] terms, then [P] sun dot products
   __shared__ double sPar[5], sScal[6];
-  __shared__ int sIdx, sNight;
+  __shared__ int sNight;
   const uint32_t t = blockIdx.x;
   const kgb_sky_step st = a.steps[t];
   float* parr = a.out + size_t(t) * 3 * (a.P + 1);
@@ -133,7 +133,6 @@ __global__ void __launch_bounds__(128) k_sky(SkyArgs a) {
       sPar[3] = -exp(delta * (x[12] + x[13] * sz)) + x[14] + delta * x[15];
     }
     sScal[0] = sz; sScal[1] = diff_illum; sScal[2] = dir_illum; sScal[3] = altitude; sScal[4] = st.azi;
-    sIdx = index;
   }
   __syncthreads();
   if (sNight) {

@@ -237,63 +237,79 @@ __device__ __forceinline__ uint32_t sky_bin(F3 d, uint32_t mf, uint32_t nBins, f
   return b + uint32_t(az * (float(n) / 6.28318531f) + .5f) % n;
 }
 
-constexpr uint64_t kBounceLimitNs = 10000000000ull;   // 10 s: past it a thread stops its paths and records kStatusTimeout
+constexpr uint64_t kBounceLimitNs = 10000000000ull;   // 10 s: past it a path stops and records kStatusTimeout
+constexpr uint32_t kNoBin = 0xffffffffu;
 
-__global__ void __launch_bounds__(128) k_bounce(BounceArgs a) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
+// One path per thread: sensor i = t % n, sample s0 + t / n. A path adds to at most one sky bin (where it escapes after
+// a reflection): it leaves that bin and its contribution (w x pi / M) in contrib[t], and k_bounce_accum adds them to
+// each sensor's rows in sample order, as the reference's per-sensor loop over samples does.
+__global__ void __launch_bounds__(128) k_bounce_paths(BounceArgs a) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= a.n * (a.s1 - a.s0)) return;
+  const uint32_t i = t % a.n, smp = a.s0 + t / a.n;
   const Scene s{a.nodes, a.tris, a.nNodes};
   const bool cull = (a.rayFlags & KGB_RAY_CULL_BACK_FACING) != 0;
   const uint32_t gi = a.i0 + i;
   const F3 nn = ld3(a.N + 3 * gi), o0 = offset_ray(ld3(a.P + 3 * gi), nn);
   const U3 rot = pcg3d(gi, ~0u, ~0u);
   const float r0 = u01(rot.x), r1 = u01(rot.y), weight = 3.14159265f / float(a.M);
-  float* row = a.dc + i;
-  uint32_t overflow = 0, segments = 0;
+  uint32_t overflow = 0, segments = 0, bin = kNoBin;
+  float gain = 0.f;
   const uint64_t start = clock_ns();
   bool late = false;
-  for (uint32_t smp = a.s0; smp < a.s1 && !late; ++smp) {
-    const float u = float(smp) / float(a.M) + r0, v = u01(__brev(smp)) + r1;
-    F3 o = o0, d = cosine_dir(nn, u - floorf(u), v - floorf(v));
-    float w = 1.f;
-    uint32_t diffuse = 0, k = 0;
-    bool reflected = false;
-    for (uint32_t seg = 0; seg < a.nBounce + 16; ++seg) {
-      if (clock_ns() - start > kBounceLimitNs) { late = true; break; }   // a launch is sized to ~100 ms
-      ++segments;
-      ClosestOut c;
-      if (!closest(s, make_ray(o, d), 1e-5f, FLT_MAX, cull, c, overflow)) {
-        if (reflected) { float* p = row + size_t(sky_bin(d, a.mf, a.nBins, a.alpha, a.cosN, a.sinN)) * a.nc; *p = *p + w * weight; }
-        break;
-      }
-      const kgb_slot sl = c.slot < a.nSlots ? a.slots[c.slot] : kgb_slot{0.2f, 0.f, 0.f, 0u};
-      TriHit h;
-      if (!tri_geom(c.v0, c.v1, c.v2, c.h, h)) break;
-      if (seg == 0 && own_plane(h, c.h.t, d, nn)) { o = through(h); continue; }
-      if ((sl.flags & (KGB_SLOT_THIN | KGB_SLOT_TWIN)) == KGB_SLOT_THIN && h.front == ((sl.flags & KGB_SLOT_INWARD) != 0)) { o = through(h); continue; }
-      const bool mirror = (sl.flags & KGB_SLOT_GLASS) != 0;
-      float T = sl.tau, R = sl.rho;
-      if (mirror) { glass_TR(fabsf(dot(d, h.n)), sl.tn, T, R); if (!(sl.tau > 0.f)) T = 0.f; }
-      else if (diffuse == a.nBounce) R = 0.f;
-      if (!(T + R > 0.f)) break;
-      const U3 rr = pcg3d(gi, smp, k++);
-      w *= T + R;
-      if (u01(rr.x) * (T + R) < T) { o = through(h); continue; }
-      reflected = true;
-      if (mirror) d = sub(d, mul(2.f * dot(d, h.n), h.n));
-      else {
-        d = cosine_dir(h.n, u01(rr.y), u01(rr.z));
-        if (++diffuse >= 2) {
-          if (u01(pcg3d(gi, smp, k++).x) >= w) break;
-          w = 1.f;
-        }
-      }
-      o = add(offset_ray(h.p, h.n), h.lift);
+  const float u = float(smp) / float(a.M) + r0, v = u01(__brev(smp)) + r1;
+  F3 o = o0, d = cosine_dir(nn, u - floorf(u), v - floorf(v));
+  float w = 1.f;
+  uint32_t diffuse = 0, k = 0;
+  bool reflected = false;
+  for (uint32_t seg = 0; seg < a.nBounce + 16; ++seg) {
+    if (clock_ns() - start > kBounceLimitNs) { late = true; break; }
+    ++segments;
+    ClosestOut c;
+    if (!closest(s, make_ray(o, d), 1e-5f, FLT_MAX, cull, c, overflow)) {
+      if (reflected) { bin = sky_bin(d, a.mf, a.nBins, a.alpha, a.cosN, a.sinN); gain = w * weight; }
+      break;
     }
+    const kgb_slot sl = c.slot < a.nSlots ? a.slots[c.slot] : kgb_slot{0.2f, 0.f, 0.f, 0u};
+    TriHit h;
+    if (!tri_geom(c.v0, c.v1, c.v2, c.h, h)) break;
+    if (seg == 0 && own_plane(h, c.h.t, d, nn)) { o = through(h); continue; }
+    if ((sl.flags & (KGB_SLOT_THIN | KGB_SLOT_TWIN)) == KGB_SLOT_THIN && h.front == ((sl.flags & KGB_SLOT_INWARD) != 0)) { o = through(h); continue; }
+    const bool mirror = (sl.flags & KGB_SLOT_GLASS) != 0;
+    float T = sl.tau, R = sl.rho;
+    if (mirror) { glass_TR(fabsf(dot(d, h.n)), sl.tn, T, R); if (!(sl.tau > 0.f)) T = 0.f; }
+    else if (diffuse == a.nBounce) R = 0.f;
+    if (!(T + R > 0.f)) break;
+    const U3 rr = pcg3d(gi, smp, k++);
+    w *= T + R;
+    if (u01(rr.x) * (T + R) < T) { o = through(h); continue; }
+    reflected = true;
+    if (mirror) d = sub(d, mul(2.f * dot(d, h.n), h.n));
+    else {
+      d = cosine_dir(h.n, u01(rr.y), u01(rr.z));
+      if (++diffuse >= 2) {
+        if (u01(pcg3d(gi, smp, k++).x) >= w) break;
+        w = 1.f;
+      }
+    }
+    o = add(offset_ray(h.p, h.n), h.lift);
   }
-  atomicAdd(reinterpret_cast<unsigned long long*>(a.status + 1), (unsigned long long)segments);   // ctl words 2-3
+  a.contrib[t] = make_uint2(late ? kNoBin : bin, __float_as_uint(gain));
+  const uint32_t sum = __reduce_add_sync(__activemask(), segments);
+  if ((threadIdx.x & 31) == __ffs(__activemask()) - 1) atomicAdd(reinterpret_cast<unsigned long long*>(a.status + 1), (unsigned long long)sum);
   if (overflow || late)
     atomicOr(a.status, (overflow & 1u ? kStatusStackOverflow : 0u) | (overflow & 2u ? kStatusVisitLimit : 0u) | (late ? kStatusTimeout : 0u));
+}
+
+// Per sensor, the launch's samples in order: row[bin] = row[bin] + contribution (the reference's float additions).
+__global__ void __launch_bounds__(256) k_bounce_accum(BounceArgs a) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  float* row = a.dc + i;
+  for (uint32_t q = 0; q < a.s1 - a.s0; ++q) {
+    const uint2 c = a.contrib[size_t(q) * a.n + i];
+    if (c.x != kNoBin) { float* p = row + size_t(c.x) * a.nc; *p = *p + __uint_as_float(c.y); }
+  }
 }
 
 // ---------------------------------------------------------------------------------------------------- launches
@@ -315,6 +331,10 @@ void launch_bits(const TraceArgs& a, int grid, cudaStream_t st, bool count) {
 }
 void launch_bytes(const TraceArgs& a, int grid, cudaStream_t st) { k_bytes<<<grid, 256, 0, st>>>(a); }
 void launch_view(const ViewArgs& a, int grid, cudaStream_t st) { k_view<<<grid, 256, 0, st>>>(a); }
-void launch_bounce(const BounceArgs& a, cudaStream_t st) { k_bounce<<<(a.n + 127) / 128, 128, 0, st>>>(a); }
+void launch_bounce(const BounceArgs& a, cudaStream_t st) {
+  const size_t paths = size_t(a.n) * (a.s1 - a.s0);
+  k_bounce_paths<<<unsigned((paths + 127) / 128), 128, 0, st>>>(a);
+  k_bounce_accum<<<(a.n + 255) / 256, 256, 0, st>>>(a);
+}
 
 }  // namespace kgb
