@@ -66,13 +66,22 @@ __global__ void __launch_bounds__(256) k_reduce_bytes(const uint8_t* __restrict_
   if (i >= nc) return;
   const F3 n = ld3(N + 3 * size_t(i));
   double acc = 0;
-  for (uint32_t d = 0; d < nDir; ++d) {
-    const uint32_t b = bytes[size_t(d) * nc + i];
-    if (!b) continue;
-    const float at = float(b) / 255.f;
-    const float c = useCos ? fmaxf(dotf(n, ld3(D + 3 * d)), 0.f) : 1.f;
-    const float x = c * at;
-    if (x != 0.f) acc = __fma_rn(widen(x), weight<SMEM>(w64, W, d), acc);
+  // 16 directions' bytes are loaded before any is used (16 loads in flight per thread: a chunk of the reference's
+  // size leaves few threads per SM), then added in direction order
+  constexpr uint32_t G = 16;
+  for (uint32_t d0 = 0; d0 < nDir; d0 += G) {
+    uint32_t bb[G];
+#pragma unroll
+    for (uint32_t k = 0; k < G; ++k) bb[k] = d0 + k < nDir ? uint32_t(__ldg(bytes + size_t(d0 + k) * nc + i)) : 0u;
+#pragma unroll
+    for (uint32_t k = 0; k < G; ++k) {
+      if (!bb[k]) continue;
+      const uint32_t d = d0 + k;
+      const float at = float(bb[k]) / 255.f;
+      const float c = useCos ? fmaxf(dotf(n, ld3(D + 3 * d)), 0.f) : 1.f;
+      const float x = c * at;
+      if (x != 0.f) acc = __fma_rn(widen(x), weight<SMEM>(w64, W, d), acc);
+    }
   }
   out[i] = acc;
 }
