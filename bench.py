@@ -180,6 +180,7 @@ def run_ours(args, pkg):
     stream = torch.cuda.Stream()
     e = pkg.engine()
     e.set_stream(stream.cuda_stream)
+    e.set_builder(args.builder)
     e.build(scene["v"], scene["tri"])
     flags = e.lib.ray_flags(False, False)
     # pinned host copies of the step's inputs (e2e) and outputs
@@ -256,7 +257,8 @@ def run_ours(args, pkg):
                                          "urban block, first %d sensors only (profiling case), %d triangles, %d directions (%d sky + %d ground + %d sun), ") +
                                         "trace + 4 reduces (radiation, irradiance, illuminance, sunhours)") %
                                        (nc, len(scene["tri"]), nDir, manifest["dirs"]["sky"], manifest["dirs"]["ground"], manifest["dirs"]["sun"]),
-                           "rays_per_step": rays, "l2": "flushed between steps (512 MB write)", "parallelism": "replicas (weak)" if world > 1 else "1 GPU"},
+                           "rays_per_step": rays, "l2": "flushed between steps (512 MB write)", "parallelism": "replicas (weak)" if world > 1 else "1 GPU",
+                           "bvh": "device LBVH" if args.builder else "host binned SAH"},
                 "e2e": {"value": world * rays / (ms_e2e / 1000) / 1e6, "unit": "Mrays/s",
                         "h2d_bytes_per_step": int(P.nbytes + N.nbytes + Dp.nbytes + sum(W.nbytes for W, _ in Wp)),
                         "d2h_bytes_per_step": int(8 * nc * len(Wp))},
@@ -457,10 +459,29 @@ def run_views(args, pkg):
         K = nAz * nEl
         res[name] = {"rays": nc * K, "trace_s": best[0], "reduce_s": best[1], "mrays_s": nc * K / best[0] / 1e6,
                      "shares_sum_check": float(np.abs(out[:, 0] + out[:, 3] + out[:, 6] + out[:, 9] + out[:, 12] + out[:, 15] + out[:, 18] - 1).max())}
+    # the device builder on the same city: build time, and the fov 120 trace on its tree (same results, other boxes)
+    e.set_builder(1)
+    e.build(city["v"], city["tri"])   # warm-up (module load, allocations)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e.build(city["v"], city["tri"])
+    torch.cuda.synchronize()
+    gpu_build_s = time.perf_counter() - t0
+    e.set_labels(city["label"])
+    e.set_scene(city["P"], city["N"], np.zeros((0, 3), np.float32))
+    nAz, nEl, dAz, rowSin, wRow = pkg.workloads.views_grid(120.0, 2.0)
+    kw = dict(world=False, cull=False, jitter=True, vground=True, groundZ=city["groundZ"])
+    best = None
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        e.view(0, nc, flags, nAz, nEl, -60.0, dAz, rowSin, **kw)
+        t1 = time.perf_counter()
+        best = t1 - t0 if best is None else min(best, t1 - t0)
+    device_tree = {"build_s": gpu_build_s, "fov120_mrays_s": nc * nAz * nEl / best / 1e6, "gas_bytes": e.stats()["gasBytes"]}
     line = {"metric": "Mrays/s (closest hit)", "unit": "Mrays/s", "value": res["fov120"]["mrays_s"],
             "config": {"workload": "views city: %d facade sensors, %d triangles, 3 target groups; fov 120 / 2 deg (3600 rays), fov 360 / 2 deg "
                                    "(10800 rays, isovist volume, reach 6/20/50), jitter on" % (nc, len(city["tri"]))},
-            "fov120": res["fov120"], "fov360": res["fov360"], "bvh_build_s": build_s}
+            "fov120": res["fov120"], "fov360": res["fov360"], "bvh_build_s": build_s, "device_builder": device_tree}
     print(json.dumps(line), flush=True)
     e.close()
 
@@ -589,6 +610,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sensors", type=int, default=0, help="urban / precision: only the block's first N sensors (a small case for profiling)")
     ap.add_argument("--config", default="urban", choices=["urban", "precision", "views", "serving"])
+    ap.add_argument("--builder", type=int, default=0, choices=[0, 1], help="urban: 0 host binned-SAH tree, 1 device LBVH")
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--window", type=float, default=2.0)
     ap.add_argument("--full-fp32", action="store_true")

@@ -271,6 +271,11 @@ KGB_API int kgb_set_stream(kgb_engine* e, void* stream);
  * accumulation, the sun term in FP32), 1 the plain FP32 form (one thread per sensor, the reference's k_series
  * restated), kept as the measured baseline. */
 KGB_API int kgb_set_series_form(kgb_engine* e, int form);
+/* No counterpart in the reference (its gpu_build builds an OptiX GAS on the device): which builder the following
+ * kgb_build calls use. 0: binned-SAH binary tree on the host, collapsed to 8-wide nodes (the default); 1: on the
+ * device, a Morton-ordered radix tree (LBVH) collapsed to the same 8-wide records. Every result is the same either way
+ * (both trees are conservative); the device builder is much faster on large scenes, the SAH tree traces faster. */
+KGB_API int kgb_set_builder(kgb_engine* e, int which);
 /* Instrumentation for the traversal roofline: traces sensors [i0, i0+nc) exactly as kgb_trace does (same bits / bytes
  * left on the device) with counting kernels, out[0] = BVH nodes visited, out[1] = triangles tested, out[2] = rays
  * traced past the hemisphere cull, out[3] = BVH bytes (nodes + triangle records). */

@@ -1,0 +1,402 @@
+// Device builder of the engine's acceleration structure (the reference's gpu_build, gpu.cu:386-457, builds an OptiX
+// GAS on the device; this is the GB300 counterpart): a linear BVH over Morton codes (Karras 2012), collapsed to the
+// 8-wide quantised nodes and 48-byte triangle records that rt.cuh reads, the same layout as the host builder
+// (bvh_build.cpp) makes.
+//
+//   1. |coordinates| maximum -> eps = max(1, M) / 65536 (the host builder's expansion)
+//   2. per triangle: box (expanded by eps), centroid; centroid bounds
+//   3. 63-bit Morton codes of the centroids, radix-sorted with the triangle index (stable: ties keep index order)
+//   4. binary radix tree (Karras 2012): internal node i's range and split from common prefixes of the sorted codes
+//   5. boxes bottom-up: each leaf walks towards the root, the second arrival at a node unites its children's boxes
+//   6. collapse to 8-wide nodes level by level: a wide node adopts the children of its largest-area inner child until
+//      it has 8 (the host builder's rule); subtrees of at most 3 triangles become leaves; a prefix sum over the level
+//      gives each node its block of inner children and of triangle records, so the layout is deterministic
+//   7. each node's child boxes quantised outwards to 8 bits against a power-of-two step per axis (double arithmetic,
+//      as the host builder)
+// Conservative exactly as the host builder: any conservative BVH gives the traversal the brute-force hit set, so the
+// results do not depend on which builder made the scene.
+#include "engine.h"
+
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace kgb {
+namespace {
+
+constexpr uint32_t kLeafMax = 3;   // triangles per leaf, as the host builder
+
+__device__ __forceinline__ uint32_t ord(float f) {   // order-preserving float -> uint
+  const uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float unord(uint32_t u) { return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u); }
+
+__global__ void k_maxabs(const float* v, size_t n, uint32_t* out) {
+  uint32_t m = 0;
+  for (size_t k = blockIdx.x * size_t(blockDim.x) + threadIdx.x; k < n; k += size_t(gridDim.x) * blockDim.x)
+    m = max(m, __float_as_uint(fabsf(v[k])));   // non-negative floats order as their bits
+  for (int s = 16; s; s >>= 1) m = max(m, __shfl_xor_sync(~0u, m, s));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+// triangle boxes (expanded), centroids (of the unexpanded box, as the host), centroid bounds (ordered uints)
+__global__ void k_prims(const float* v, const uint32_t* tri, uint32_t nt, float eps, float4* lo, float4* hi, float4* cen, uint32_t* cb) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t cmin[3] = {~0u, ~0u, ~0u}, cmax[3] = {0u, 0u, 0u};
+  if (t < nt) {
+    float l[3], h[3], c[3];
+    for (int a = 0; a < 3; ++a) {
+      const float x0 = v[3 * tri[3 * t] + a], x1 = v[3 * tri[3 * t + 1] + a], x2 = v[3 * tri[3 * t + 2] + a];
+      const float mn = fminf(x0, fminf(x1, x2)), mx = fmaxf(x0, fmaxf(x1, x2));
+      l[a] = __fsub_rn(mn, eps); h[a] = __fadd_rn(mx, eps);
+      c[a] = __fadd_rn(__fmul_rn(0.5f, mn), __fmul_rn(0.5f, mx));
+      cmin[a] = cmax[a] = ord(c[a]);
+    }
+    lo[t] = make_float4(l[0], l[1], l[2], 0.f);
+    hi[t] = make_float4(h[0], h[1], h[2], 0.f);
+    cen[t] = make_float4(c[0], c[1], c[2], 0.f);
+  }
+  for (int a = 0; a < 3; ++a) {
+    for (int s = 16; s; s >>= 1) {
+      cmin[a] = min(cmin[a], __shfl_xor_sync(~0u, cmin[a], s));
+      cmax[a] = max(cmax[a], __shfl_xor_sync(~0u, cmax[a], s));
+    }
+    if ((threadIdx.x & 31) == 0) { atomicMin(&cb[a], cmin[a]); atomicMax(&cb[3 + a], cmax[a]); }
+  }
+}
+
+__device__ __forceinline__ uint64_t spread21(uint64_t x) {   // 21 bits -> every third bit of 63
+  x &= 0x1fffffull;
+  x = (x | (x << 32)) & 0x1f00000000ffffull;
+  x = (x | (x << 16)) & 0x1f0000ff0000ffull;
+  x = (x | (x << 8)) & 0x100f00f00f00f00full;
+  x = (x | (x << 4)) & 0x10c30c30c30c30c3ull;
+  x = (x | (x << 2)) & 0x1249249249249249ull;
+  return x;
+}
+__global__ void k_morton(const float4* cen, uint32_t nt, const uint32_t* cb, uint64_t* key, uint32_t* val) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  const float4 c = cen[t];
+  const float cc[3] = {c.x, c.y, c.z};
+  uint64_t code = 0;
+  for (int a = 0; a < 3; ++a) {
+    const float lo = unord(cb[a]), hi = unord(cb[3 + a]);
+    const float ext = hi - lo;
+    float u = ext > 0.f ? (cc[a] - lo) / ext : 0.f;
+    u = fminf(fmaxf(u, 0.f), 1.f);
+    code |= spread21(uint64_t(fminf(u * 2097152.f, 2097151.f))) << (2 - a);
+  }
+  key[t] = code;
+  val[t] = t;
+}
+
+// Karras 2012: internal node i (0 <= i < n - 1) over sorted keys; ties broken by position. A child c >= 0 is an
+// internal node, c < 0 the leaf ~c (a position in the sorted order).
+__device__ __forceinline__ int delta(const uint64_t* k, int n, int i, long long j) {
+  if (j < 0 || j >= n) return -1;
+  const uint64_t a = k[i], b = k[size_t(j)];
+  return a == b ? 64 + __clz(uint32_t(i) ^ uint32_t(j)) : __clzll(a ^ b);
+}
+__global__ void k_karras(const uint64_t* k, int n, int* left, int* right, int* parent, int* leafParent, int2* range) {
+  const int i = int(blockIdx.x * blockDim.x + threadIdx.x);
+  if (i >= n - 1) return;
+  const int d = delta(k, n, i, i + 1) - delta(k, n, i, i - 1) >= 0 ? 1 : -1;
+  const int dmin = delta(k, n, i, i - d);
+  long long lmax = 2;
+  while (lmax < 2ll * n && delta(k, n, i, i + lmax * d) > dmin) lmax *= 2;   // at most log2(2n) doublings
+  long long l = 0;
+  for (long long t = lmax / 2; t >= 1; t /= 2)
+    if (delta(k, n, i, i + (l + t) * d) > dmin) l += t;
+  const int j = int(i + l * d);
+  const int dnode = delta(k, n, i, j);
+  long long s = 0;
+  for (long long div = 2;; div *= 2) {
+    const long long t = (l + div - 1) / div;
+    if (delta(k, n, i, i + (s + t) * d) > dnode) s += t;
+    if (t <= 1) break;
+  }
+  const int gamma = int(i + s * d + min(d, 0));
+  const int first = min(i, j), last = max(i, j);
+  const int L = first == gamma ? ~gamma : gamma, R = last == gamma + 1 ? ~(gamma + 1) : gamma + 1;
+  left[i] = L;
+  right[i] = R;
+  range[i] = make_int2(first, last);
+  if (L >= 0) parent[L] = i; else leafParent[~L] = i;
+  if (R >= 0) parent[R] = i; else leafParent[~R] = i;
+  if (i == 0) parent[0] = -1;
+}
+
+// boxes bottom-up: the second thread to arrive at a node unites its children (no waiting: the first one stops)
+__global__ void k_boxes(int n, const uint32_t* order, const float4* plo, const float4* phi, const int* left, const int* right,
+                        const int* parent, const int* leafParent, float4* nlo, float4* nhi, uint32_t* arrivals) {
+  const int p = int(blockIdx.x * blockDim.x + threadIdx.x);
+  if (p >= n) return;
+  int node = leafParent[p];
+  while (node >= 0) {
+    __threadfence();
+    if (atomicAdd(&arrivals[node], 1u) == 0) return;
+    __threadfence();
+    float4 lo = make_float4(INFINITY, INFINITY, INFINITY, 0.f), hi = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
+    const int ch[2] = {left[node], right[node]};
+    for (int c : ch) {
+      const float4 a = c >= 0 ? __ldcg(&nlo[c]) : plo[order[~c]], b = c >= 0 ? __ldcg(&nhi[c]) : phi[order[~c]];
+      lo = make_float4(fminf(lo.x, a.x), fminf(lo.y, a.y), fminf(lo.z, a.z), 0.f);
+      hi = make_float4(fmaxf(hi.x, b.x), fmaxf(hi.y, b.y), fmaxf(hi.z, b.z), 0.f);
+    }
+    __stcg(&nlo[node], lo);
+    __stcg(&nhi[node], hi);
+    node = parent[node];
+  }
+}
+
+struct Tree {
+  const uint32_t* order;   // sorted position -> triangle
+  const float4 *plo, *phi, *nlo, *nhi;
+  const int *left, *right;
+  const int2* range;
+};
+__device__ __forceinline__ uint32_t count_of(const Tree& T, int c) { return c >= 0 ? uint32_t(T.range[c].y - T.range[c].x + 1) : 1u; }
+__device__ __forceinline__ uint32_t first_of(const Tree& T, int c) { return c >= 0 ? uint32_t(T.range[c].x) : uint32_t(~c); }
+__device__ __forceinline__ bool leaf_of(const Tree& T, int c) { return count_of(T, c) <= kLeafMax; }
+__device__ __forceinline__ void box_of(const Tree& T, int c, float4& lo, float4& hi) {
+  if (c >= 0) { lo = T.nlo[c]; hi = T.nhi[c]; } else { lo = T.plo[T.order[~c]]; hi = T.phi[T.order[~c]]; }
+}
+__device__ __forceinline__ float area_of(const Tree& T, int c) {
+  float4 lo, hi;
+  box_of(T, c, lo, hi);
+  const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+  return dx < 0.f ? 0.f : dx * dy + dy * dz + dz * dx;
+}
+
+// level pass 1: each wide node's children (the host builder's greedy opening), inner-child and triangle counts
+__global__ void k_collapse_count(Tree T, const int* wideSrc, uint32_t b, uint32_t e, int* kids, uint32_t* nInner, uint32_t* nTri) {
+  const uint32_t w = b + blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= e) return;
+  const int src = wideSrc[w];
+  int ch[8];
+  int n = 0;
+  if (leaf_of(T, src)) ch[n++] = src;   // a leaf root: one leaf child
+  else {
+    ch[n++] = T.left[src]; ch[n++] = T.right[src];
+    while (n < 8) {
+      int best = -1;
+      float bestA = -1.f;
+      for (int k = 0; k < n; ++k)
+        if (!leaf_of(T, ch[k])) { const float a = area_of(T, ch[k]); if (a > bestA) { bestA = a; best = k; } }
+      if (best < 0) break;
+      const int c = ch[best];
+      ch[best] = T.left[c];
+      ch[n++] = T.right[c];
+    }
+  }
+  uint32_t ni = 0, nt = 0;
+  for (int k = 0; k < 8; ++k) {
+    kids[size_t(w - b) * 8 + k] = k < n ? ch[k] : INT32_MIN;
+    if (k < n) { if (leaf_of(T, ch[k])) nt += count_of(T, ch[k]); else ++ni; }
+  }
+  nInner[w - b] = ni;
+  nTri[w - b] = nt;
+}
+
+// the host builder's quant_axis: step s = 2^(eb - 127) with p + 255 s covering the extent
+__device__ __forceinline__ void quant_axis(float p, float hi, uint32_t& eb, float& s) {
+  const double ext = fmax(double(hi) - double(p), 1e-30);
+  int e = 0;
+  frexp(ext / 255.0, &e);
+  e = max(-126, min(127, e));
+  for (int it = 0; it < 300; ++it) {   // e rises to 127 at most
+    s = ldexpf(1.f, e);
+    if (double(p) + 255.0 * double(s) >= double(hi) || e >= 127) break;
+    ++e;
+  }
+  eb = uint32_t(e + 127);
+}
+
+// level pass 2: node records, triangle records, the next level's sources
+__global__ void k_collapse_emit(Tree T, const float* v, const uint32_t* tri, const uint32_t* slot, const uint8_t* translucent, uint32_t b,
+                                uint32_t e, const int* kids, const uint32_t* innerOff, const uint32_t* triOff, uint32_t triBase0,
+                                uint32_t* nodes, float* tris, int* wideSrc) {
+  const uint32_t w = b + blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= e) return;
+  int ch[8];
+  int n = 0;
+  for (int k = 0; k < 8; ++k) { ch[k] = kids[size_t(w - b) * 8 + k]; if (ch[k] != INT32_MIN) n = k + 1; }
+  float4 blo = make_float4(INFINITY, INFINITY, INFINITY, 0.f), bhi = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
+  for (int k = 0; k < n; ++k) {
+    float4 lo, hi;
+    box_of(T, ch[k], lo, hi);
+    blo = make_float4(fminf(blo.x, lo.x), fminf(blo.y, lo.y), fminf(blo.z, lo.z), 0.f);
+    bhi = make_float4(fmaxf(bhi.x, hi.x), fmaxf(bhi.y, hi.y), fmaxf(bhi.z, hi.z), 0.f);
+  }
+  const float p[3] = {blo.x, blo.y, blo.z}, ph[3] = {bhi.x, bhi.y, bhi.z};
+  uint32_t eb[3];
+  float s[3];
+  for (int a = 0; a < 3; ++a) quant_axis(p[a], ph[a], eb[a], s[a]);
+  const uint32_t childBase = e + innerOff[w - b], triBase = triBase0 + triOff[w - b];
+  uint32_t imask = 0, meta[8] = {}, q[6][8] = {}, inner = 0, tOff = 0;
+  for (int k = 0; k < n; ++k) {
+    float4 lo, hi;
+    box_of(T, ch[k], lo, hi);
+    const float cl[3] = {lo.x, lo.y, lo.z}, chh[3] = {hi.x, hi.y, hi.z};
+    for (int a = 0; a < 3; ++a) {
+      const double ql = floor((double(cl[a]) - double(p[a])) / double(s[a]));
+      const double qh = ceil((double(chh[a]) - double(p[a])) / double(s[a]));
+      q[a][k] = uint32_t(fmax(0.0, fmin(255.0, ql)));
+      q[3 + a][k] = uint32_t(fmax(0.0, fmin(255.0, qh)));
+    }
+    if (!leaf_of(T, ch[k])) {
+      imask |= 1u << k;
+      wideSrc[childBase + inner++] = ch[k];
+    } else {
+      const uint32_t cnt = count_of(T, ch[k]), f = first_of(T, ch[k]);
+      meta[k] = (cnt << 5) | tOff;
+      for (uint32_t j = 0; j < cnt; ++j) {
+        const uint32_t t = T.order[f + j];
+        float* r = tris + size_t(triBase + tOff + j) * 12;
+        for (int vtx = 0; vtx < 3; ++vtx)
+          for (int a = 0; a < 3; ++a) r[4 * vtx + a] = v[3 * tri[3 * t + vtx] + a];
+        r[3] = __uint_as_float(t);
+        r[7] = __uint_as_float(translucent && translucent[t] ? 1u : 0u);
+        r[11] = __uint_as_float(slot ? slot[t] : 0u);
+      }
+      tOff += cnt;
+    }
+  }
+  uint32_t* rec = nodes + size_t(w) * 20;
+  rec[0] = __float_as_uint(p[0]); rec[1] = __float_as_uint(p[1]); rec[2] = __float_as_uint(p[2]);
+  rec[3] = eb[0] | (eb[1] << 8) | (eb[2] << 16) | (imask << 24);
+  rec[4] = childBase;
+  rec[5] = triBase;
+  rec[6] = meta[0] | (meta[1] << 8) | (meta[2] << 16) | (meta[3] << 24);
+  rec[7] = meta[4] | (meta[5] << 8) | (meta[6] << 16) | (meta[7] << 24);
+  for (int f = 0; f < 6; ++f) {
+    rec[8 + 2 * f] = q[f][0] | (q[f][1] << 8) | (q[f][2] << 16) | (q[f][3] << 24);
+    rec[9 + 2 * f] = q[f][4] | (q[f][5] << 8) | (q[f][6] << 16) | (q[f][7] << 24);
+  }
+}
+
+struct DevBuf {
+  void* p = nullptr;
+  ~DevBuf() { if (p) cudaFree(p); }
+  template <class T> T* as() { return static_cast<T*>(p); }
+};
+#define KGB_TRY(x) do { const cudaError_t e_ = (x); if (e_ != cudaSuccess) return std::string(#x ": ") + cudaGetErrorString(e_); } while (0)
+
+}  // namespace
+
+// Builds on the device from host arrays; *nodesOut / *trisOut are new device buffers (cudaMalloc) the caller owns,
+// also when the build fails after allocating them. Returns "" or what failed.
+std::string build_bvh8_gpu(const float* v, size_t nv, const uint32_t* tri, size_t nt, const uint32_t* slot, const uint8_t* translucent,
+                           cudaStream_t st, void** nodesOut, void** trisOut, uint32_t* nNodesOut, uint64_t* tempBytes) {
+  *nodesOut = *trisOut = nullptr;
+  *nNodesOut = 0;
+  if (!nt) return "";
+  if (nt >= (size_t(1) << 31) - 1) return "more than 2^31 triangles";
+  const int n = int(nt);
+  DevBuf dv, dtri, dslot, dtr, plo, phi, cen, cb, keys, keys2, vals, vals2, left, right, parent, leafParent, range, nlo, nhi, arr, wideSrc, kids,
+      nInner, nTri, offI, offT, tmp, maxabs;
+  const size_t tiles = (nt + 255) / 256;
+  KGB_TRY(cudaMalloc(&dv.p, nv * 12));
+  KGB_TRY(cudaMalloc(&dtri.p, nt * 12));
+  KGB_TRY(cudaMemcpyAsync(dv.p, v, nv * 12, cudaMemcpyHostToDevice, st));
+  KGB_TRY(cudaMemcpyAsync(dtri.p, tri, nt * 12, cudaMemcpyHostToDevice, st));
+  if (slot) { KGB_TRY(cudaMalloc(&dslot.p, nt * 4)); KGB_TRY(cudaMemcpyAsync(dslot.p, slot, nt * 4, cudaMemcpyHostToDevice, st)); }
+  if (translucent) { KGB_TRY(cudaMalloc(&dtr.p, nt)); KGB_TRY(cudaMemcpyAsync(dtr.p, translucent, nt, cudaMemcpyHostToDevice, st)); }
+  // 1. eps
+  KGB_TRY(cudaMalloc(&maxabs.p, 4));
+  KGB_TRY(cudaMemsetAsync(maxabs.p, 0, 4, st));
+  k_maxabs<<<1024, 256, 0, st>>>(dv.as<float>(), nv * 3, maxabs.as<uint32_t>());
+  uint32_t mbits = 0;
+  KGB_TRY(cudaMemcpyAsync(&mbits, maxabs.p, 4, cudaMemcpyDeviceToHost, st));
+  KGB_TRY(cudaStreamSynchronize(st));
+  float M;
+  std::memcpy(&M, &mbits, 4);
+  M = std::max(1.f, M);
+  const float eps = M * (1.f / 65536.f);
+  // 2. boxes, centroids, centroid bounds
+  KGB_TRY(cudaMalloc(&plo.p, nt * 16)); KGB_TRY(cudaMalloc(&phi.p, nt * 16)); KGB_TRY(cudaMalloc(&cen.p, nt * 16));
+  KGB_TRY(cudaMalloc(&cb.p, 24));
+  const uint32_t cbInit[6] = {~0u, ~0u, ~0u, 0u, 0u, 0u};
+  KGB_TRY(cudaMemcpyAsync(cb.p, cbInit, 24, cudaMemcpyHostToDevice, st));
+  k_prims<<<unsigned(tiles), 256, 0, st>>>(dv.as<float>(), dtri.as<uint32_t>(), uint32_t(nt), eps, plo.as<float4>(), phi.as<float4>(), cen.as<float4>(),
+                                           cb.as<uint32_t>());
+  // 3. Morton codes, sorted
+  KGB_TRY(cudaMalloc(&keys.p, nt * 8)); KGB_TRY(cudaMalloc(&keys2.p, nt * 8));
+  KGB_TRY(cudaMalloc(&vals.p, nt * 4)); KGB_TRY(cudaMalloc(&vals2.p, nt * 4));
+  k_morton<<<unsigned(tiles), 256, 0, st>>>(cen.as<float4>(), uint32_t(nt), cb.as<uint32_t>(), keys.as<uint64_t>(), vals.as<uint32_t>());
+  size_t sortBytes = 0, scanBytes = 0;
+  KGB_TRY(cub::DeviceRadixSort::SortPairs(nullptr, sortBytes, keys.as<uint64_t>(), keys2.as<uint64_t>(), vals.as<uint32_t>(), vals2.as<uint32_t>(),
+                                          n, 0, 63, st));
+  KGB_TRY(cub::DeviceScan::ExclusiveSum(nullptr, scanBytes, static_cast<uint32_t*>(nullptr), static_cast<uint32_t*>(nullptr), n, st));
+  const size_t tmpBytes = std::max(sortBytes, scanBytes);
+  KGB_TRY(cudaMalloc(&tmp.p, tmpBytes));
+  size_t sortUse = tmpBytes;
+  KGB_TRY(cub::DeviceRadixSort::SortPairs(tmp.p, sortUse, keys.as<uint64_t>(), keys2.as<uint64_t>(), vals.as<uint32_t>(), vals2.as<uint32_t>(), n,
+                                          0, 63, st));
+  // 4. radix tree
+  const size_t ni = std::max<size_t>(1, nt - 1);
+  KGB_TRY(cudaMalloc(&left.p, ni * 4)); KGB_TRY(cudaMalloc(&right.p, ni * 4)); KGB_TRY(cudaMalloc(&parent.p, ni * 4));
+  KGB_TRY(cudaMalloc(&leafParent.p, nt * 4)); KGB_TRY(cudaMalloc(&range.p, ni * 8));
+  KGB_TRY(cudaMalloc(&nlo.p, ni * 16)); KGB_TRY(cudaMalloc(&nhi.p, ni * 16)); KGB_TRY(cudaMalloc(&arr.p, ni * 4));
+  KGB_TRY(cudaMemsetAsync(arr.p, 0, ni * 4, st));
+  if (n == 1) KGB_TRY(cudaMemsetAsync(leafParent.p, 0xff, 4, st));   // the single leaf is the root
+  else {
+    k_karras<<<unsigned((ni + 255) / 256), 256, 0, st>>>(keys2.as<uint64_t>(), n, left.as<int>(), right.as<int>(), parent.as<int>(), leafParent.as<int>(),
+                                                         range.as<int2>());
+    // 5. boxes
+    k_boxes<<<unsigned(tiles), 256, 0, st>>>(n, vals2.as<uint32_t>(), plo.as<float4>(), phi.as<float4>(), left.as<int>(), right.as<int>(),
+                                             parent.as<int>(), leafParent.as<int>(), nlo.as<float4>(), nhi.as<float4>(), arr.as<uint32_t>());
+  }
+  // 6-7. collapse level by level into the output buffers
+  void* nodes = nullptr;
+  void* tris = nullptr;
+  const size_t maxNodes = std::max<size_t>(1, nt);   // a wide node has at least two children but the root
+  KGB_TRY(cudaMalloc(&nodes, maxNodes * 80));
+  if (cudaMalloc(&tris, nt * 48) != cudaSuccess) { cudaFree(nodes); return "cudaMalloc(tris) failed"; }
+  *nodesOut = nodes;
+  *trisOut = tris;
+  KGB_TRY(cudaMalloc(&wideSrc.p, maxNodes * 4));
+  KGB_TRY(cudaMalloc(&kids.p, maxNodes * 32));
+  KGB_TRY(cudaMalloc(&nInner.p, maxNodes * 4)); KGB_TRY(cudaMalloc(&nTri.p, maxNodes * 4));
+  KGB_TRY(cudaMalloc(&offI.p, maxNodes * 4)); KGB_TRY(cudaMalloc(&offT.p, maxNodes * 4));
+  const int root = n == 1 ? ~0 : 0;
+  KGB_TRY(cudaMemcpyAsync(wideSrc.p, &root, 4, cudaMemcpyHostToDevice, st));
+  Tree T{vals2.as<uint32_t>(), plo.as<float4>(), phi.as<float4>(), nlo.as<float4>(), nhi.as<float4>(), left.as<int>(), right.as<int>(),
+         range.as<int2>()};
+  uint32_t b = 0, e = 1, triBase = 0;
+  for (int level = 0; b < e; ++level) {
+    if (level > 4096) return "bvh collapse: too many levels";
+    const uint32_t cnt = e - b, blocks = (cnt + 127) / 128;
+    k_collapse_count<<<blocks, 128, 0, st>>>(T, wideSrc.as<int>(), b, e, kids.as<int>(), nInner.as<uint32_t>(), nTri.as<uint32_t>());
+    size_t sb = tmpBytes;
+    KGB_TRY(cub::DeviceScan::ExclusiveSum(tmp.p, sb, nInner.as<uint32_t>(), offI.as<uint32_t>(), int(cnt), st));
+    KGB_TRY(cub::DeviceScan::ExclusiveSum(tmp.p, sb, nTri.as<uint32_t>(), offT.as<uint32_t>(), int(cnt), st));
+    uint32_t lastI[2], lastT[2];
+    KGB_TRY(cudaMemcpyAsync(&lastI[0], offI.as<uint32_t>() + cnt - 1, 4, cudaMemcpyDeviceToHost, st));
+    KGB_TRY(cudaMemcpyAsync(&lastI[1], nInner.as<uint32_t>() + cnt - 1, 4, cudaMemcpyDeviceToHost, st));
+    KGB_TRY(cudaMemcpyAsync(&lastT[0], offT.as<uint32_t>() + cnt - 1, 4, cudaMemcpyDeviceToHost, st));
+    KGB_TRY(cudaMemcpyAsync(&lastT[1], nTri.as<uint32_t>() + cnt - 1, 4, cudaMemcpyDeviceToHost, st));
+    k_collapse_emit<<<blocks, 128, 0, st>>>(T, dv.as<float>(), dtri.as<uint32_t>(), dslot.as<uint32_t>(), dtr.as<uint8_t>(), b, e, kids.as<int>(),
+                                            offI.as<uint32_t>(), offT.as<uint32_t>(), triBase, static_cast<uint32_t*>(nodes), static_cast<float*>(tris),
+                                            wideSrc.as<int>());
+    KGB_TRY(cudaGetLastError());
+    KGB_TRY(cudaStreamSynchronize(st));
+    const uint64_t next = uint64_t(e) + lastI[0] + lastI[1];
+    if (next > maxNodes) return "bvh collapse: node count beyond its bound";
+    triBase += lastT[0] + lastT[1];
+    b = e;
+    e = uint32_t(next);
+  }
+  if (triBase != nt) return "bvh collapse: " + std::to_string(triBase) + " triangle records for " + std::to_string(nt) + " triangles";
+  *nNodesOut = e;
+  *tempBytes = nt * (12 + 16 * 3 + 8 * 2 + 4 * 2 + 4 * 4 + 8 + 32 + 4) + maxNodes * (4 + 32 + 16) + tmpBytes;
+  return "";
+}
+
+}  // namespace kgb

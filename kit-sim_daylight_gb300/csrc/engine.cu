@@ -13,6 +13,8 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <thread>
+#include <vector>
 
 namespace kgb {
 namespace {
@@ -38,6 +40,81 @@ int grow(Buf& b, size_t bytes) {
   b.cap = std::max<size_t>(bytes, 256);
   return 1;
 }
+// Device -> pageable host copy of a large result through two pinned staging buffers: slice k + 1 streams over the
+// link while the host copies slice k into place with a few threads (a pageable cudaMemcpy moves a few tens of GB/s).
+struct Staging {
+  void* h[2] = {nullptr, nullptr};
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  static constexpr size_t kSlice = size_t(32) << 20;
+  void free() {
+    for (int k = 0; k < 2; ++k) {
+      if (h[k]) cudaFreeHost(h[k]);
+      if (ev[k]) cudaEventDestroy(ev[k]);
+      h[k] = nullptr; ev[k] = nullptr;
+    }
+  }
+};
+void host_copy(void* dst, const void* src, size_t bytes) {
+  constexpr size_t kPart = size_t(4) << 20;
+  const int nt = int(std::min<size_t>(4, (bytes + kPart - 1) / kPart));
+  if (nt <= 1) { std::memcpy(dst, src, bytes); return; }
+  std::vector<std::thread> th;
+  const size_t per = (bytes + nt - 1) / nt;
+  for (int t = 0; t < nt; ++t) {
+    const size_t a = size_t(t) * per, b = std::min(bytes, a + per);
+    if (a < b) th.emplace_back([=] { std::memcpy(static_cast<char*>(dst) + a, static_cast<const char*>(src) + a, b - a); });
+  }
+  for (auto& x : th) x.join();
+}
+int download_large(Staging& s, void* dst, const void* src, size_t bytes, cudaStream_t st) {
+  if (bytes < 2 * Staging::kSlice) {   // small results: one plain copy
+    CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    return 1;
+  }
+  for (int k = 0; k < 2; ++k) {
+    if (!s.h[k]) CU(cudaMallocHost(&s.h[k], Staging::kSlice));
+    if (!s.ev[k]) CU(cudaEventCreateWithFlags(&s.ev[k], cudaEventDisableTiming));
+  }
+  const size_t n = (bytes + Staging::kSlice - 1) / Staging::kSlice;
+  const auto slice = [&](size_t k) { return std::min(Staging::kSlice, bytes - k * Staging::kSlice); };
+  CU(cudaMemcpyAsync(s.h[0], src, slice(0), cudaMemcpyDeviceToHost, st));
+  CU(cudaEventRecord(s.ev[0], st));
+  for (size_t k = 0; k < n; ++k) {
+    const int b = int(k & 1);
+    if (k + 1 < n) {
+      CU(cudaMemcpyAsync(s.h[b ^ 1], static_cast<const char*>(src) + (k + 1) * Staging::kSlice, slice(k + 1), cudaMemcpyDeviceToHost, st));
+      CU(cudaEventRecord(s.ev[b ^ 1], st));
+    }
+    CU(cudaEventSynchronize(s.ev[b]));
+    host_copy(static_cast<char*>(dst) + k * Staging::kSlice, s.h[b], slice(k));
+  }
+  return 1;
+}
+
+// Host -> device copy of a large input through the same staging slices (the host fills slice k while slice k - 1
+// is in flight); the copies are queued on the stream, in order.
+int upload_large(Staging& s, void* dst, const void* src, size_t bytes, cudaStream_t st) {
+  if (bytes < 2 * Staging::kSlice) {
+    CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+    return 1;
+  }
+  for (int k = 0; k < 2; ++k) {
+    if (!s.h[k]) CU(cudaMallocHost(&s.h[k], Staging::kSlice));
+    if (!s.ev[k]) CU(cudaEventCreateWithFlags(&s.ev[k], cudaEventDisableTiming));
+  }
+  const size_t n = (bytes + Staging::kSlice - 1) / Staging::kSlice;
+  for (size_t k = 0; k < n; ++k) {
+    const int b = int(k & 1);
+    const size_t len = std::min(Staging::kSlice, bytes - k * Staging::kSlice);
+    CU(cudaEventSynchronize(s.ev[b]));   // the slice's previous copy has left it
+    host_copy(s.h[b], static_cast<const char*>(src) + k * Staging::kSlice, len);
+    CU(cudaMemcpyAsync(static_cast<char*>(dst) + k * Staging::kSlice, s.h[b], len, cudaMemcpyHostToDevice, st));
+    CU(cudaEventRecord(s.ev[b], st));
+  }
+  return 1;
+}
+
 int upload(Buf& b, const void* h, size_t bytes, cudaStream_t st) {
   if (!grow(b, bytes)) return 0;
   if (bytes) CU(cudaMemcpyAsync(b.p, h, bytes, cudaMemcpyHostToDevice, st));
@@ -77,8 +154,10 @@ struct Engine {
   bool ownStream = true;
   int seriesForm = 0;         // 0 split-BF16 tensor cores, 1 plain FP32
   Buf vop, sop, csr, sunCol;
+  Staging staging;   // pinned slices for the series download
   kgb_stats stats{};
   int gridBits = 0, gridView = 0;
+  int builder = 0;            // 0 host binned SAH, 1 device LBVH (kgb_set_builder)
 };
 
 namespace {
@@ -153,6 +232,7 @@ KGB_API void kgb_destroy(kgb_engine* e) {
   delete g->sc;
   for (Buf* b : {&g->slots, &g->P, &g->N, &g->D, &g->rayTab, &g->vis, &g->dc, &g->contrib, &g->viewCls, &g->viewDist, &g->rowSin, &g->label, &g->scratch, &g->out, &g->ctl,
                  &g->vop, &g->sop, &g->csr, &g->sunCol}) b->free();
+  g->staging.free();
   for (cudaEvent_t ev : g->ev) if (ev) cudaEventDestroy(ev);
   if (g->st && g->ownStream) cudaStreamDestroy(g->st);
   delete g;
@@ -188,18 +268,33 @@ KGB_API int kgb_build(kgb_engine* e, const float* v, size_t nv, const uint32_t* 
     translucent.resize(nt);
     for (size_t k = 0; k < nt; ++k) translucent[k] = slots[slot[k]].tau > 0 ? 1 : 0;
   }
-  BvhOut b;
-  build_bvh8(v, nv, tri, nt, slotted ? slot : nullptr, slotted ? translucent.data() : nullptr, b);
   SceneObj& s = *g.sc;
-  if (!upload(s.nodes, b.nodes.data(), b.nodes.size() * 4, g.st) || !upload(s.tris, b.tris.data(), b.tris.size() * 4, g.st)) return 0;
-  s.nNodes = b.nNodes;
+  if (g.builder == 1) {   // on the device
+    void* nodes = nullptr;
+    void* tris = nullptr;
+    uint32_t nNodes = 0;
+    uint64_t temp = 0;
+    const std::string why = build_bvh8_gpu(v, nv, tri, nt, slotted ? slot : nullptr, slotted ? translucent.data() : nullptr, g.st, &nodes, &tris,
+                                           &nNodes, &temp);
+    s.nodes.p = nodes; s.nodes.cap = std::max<size_t>(1, nt) * 80;
+    s.tris.p = tris; s.tris.cap = nt * 48;
+    if (!why.empty()) return fail("gpu_build: " + why);
+    s.nNodes = nNodes;
+    s.bytes = uint64_t(nNodes) * 80 + uint64_t(nt) * 48;
+    g.stats.buildTempBytes = temp;
+  } else {   // on the host (binned SAH)
+    BvhOut b;
+    build_bvh8(v, nv, tri, nt, slotted ? slot : nullptr, slotted ? translucent.data() : nullptr, b);
+    if (!upload(s.nodes, b.nodes.data(), b.nodes.size() * 4, g.st) || !upload(s.tris, b.tris.data(), b.tris.size() * 4, g.st)) return 0;
+    s.nNodes = b.nNodes;
+    s.bytes = b.nodes.size() * 4 + b.tris.size() * 4;
+    g.stats.buildTempBytes = uint64_t(nt) * 64;
+  }
   s.nTris = uint32_t(nt);
-  s.bytes = b.nodes.size() * 4 + b.tris.size() * 4;
   CU(cudaEventRecord(g.ev[1], g.st));
   CU(cudaStreamSynchronize(g.st));
   g.stats.buildMs += elapsed(g);
   g.stats.gasBytes = s.bytes;
-  g.stats.buildTempBytes = uint64_t(nt) * 64;
   g.stats.buildOutputBytes = s.bytes;
   return 1;
 }
@@ -367,7 +462,8 @@ KGB_API int kgb_series(kgb_engine* e, size_t nc, const kgb_series_in* in, float*
   for (int k = 0; k < 9; ++k) { off[k] = total; total += (len[k] + 255) & ~size_t(255); }
   if (!grow(g.scratch, total) || !grow(g.out, nc * T * 4)) return 0;
   char* b = static_cast<char*>(g.scratch.p);
-  for (int k = 0; k < 9; ++k) if (len[k]) CU(cudaMemcpyAsync(b + off[k], src[k], len[k], cudaMemcpyHostToDevice, g.st));
+  for (int k = 0; k < 9; ++k)
+    if (len[k] && !upload_large(g.staging, b + off[k], src[k], len[k], g.st)) return 0;
   SeriesArgs a{};
   a.bits = g.bytes ? nullptr : static_cast<const uint32_t*>(g.vis.p);
   a.bytes = g.bytes ? static_cast<const uint8_t*>(g.vis.p) : nullptr;
@@ -428,9 +524,7 @@ KGB_API int kgb_series(kgb_engine* e, size_t nc, const kgb_series_in* in, float*
     CU(cudaStreamSynchronize(g.st));
     if (status & kStatusTimeout) return fail("gpu_series: the tensor-core pipeline timed out waiting (status recorded by the kernel)");
   }
-  CU(cudaMemcpyAsync(Eh, g.out.p, nc * T * 4, cudaMemcpyDeviceToHost, g.st));
-  CU(cudaStreamSynchronize(g.st));
-  return 1;
+  return download_large(g.staging, Eh, g.out.p, nc * T * 4, g.st);
 }
 
 KGB_API int kgb_sky(kgb_engine* e, int32_t mf, const kgb_sky_step* steps, size_t T, double grefl, int32_t sun, int32_t sky,
@@ -440,6 +534,12 @@ KGB_API int kgb_sky(kgb_engine* e, int32_t mf, const kgb_sky_step* steps, size_t
 }
 KGB_API int kgb_sun_noaa(kgb_engine* e, const double* in, size_t T, double* out) {
   if (const char* why = sun_steps(in, T, out, E(e)->st)) return fail(why);
+  return 1;
+}
+
+KGB_API int kgb_set_builder(kgb_engine* e, int which) {
+  if (which != 0 && which != 1) return fail("kgb_set_builder: 0 (host binned SAH) or 1 (device LBVH)");
+  E(e)->builder = which;
   return 1;
 }
 

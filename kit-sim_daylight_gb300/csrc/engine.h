@@ -179,5 +179,8 @@ struct BvhOut {
   uint32_t nNodes = 0;
 };
 void build_bvh8(const float* v, size_t nv, const uint32_t* tri, size_t nt, const uint32_t* slot, const uint8_t* translucent, BvhOut& out);
+// device builder (bvh_gpu.cu): the same records, built on the GPU from a Morton-ordered radix tree; "" or what failed
+std::string build_bvh8_gpu(const float* v, size_t nv, const uint32_t* tri, size_t nt, const uint32_t* slot, const uint8_t* translucent,
+                           cudaStream_t st, void** nodesOut, void** trisOut, uint32_t* nNodesOut, uint64_t* tempBytes);
 
 }  // namespace kgb

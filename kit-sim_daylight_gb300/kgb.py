@@ -113,6 +113,7 @@ SIGNATURES = [
     ("kgb_server_stats", None, [c_void_p, POINTER(c_double)]),
     ("kgb_sky", c_int, [_E, c_int32, c_void_p, c_size_t, c_double, c_int32, c_int32, c_int32, c_void_p]),
     ("kgb_sun_noaa", c_int, [_E, c_void_p, c_size_t, c_void_p]),
+    ("kgb_set_builder", c_int, [_E, c_int]),
     ("kgb_set_series_form", c_int, [_E, c_int]),
     ("kgb_trace_counters", c_int, [_E, c_size_t, c_size_t, c_uint32, POINTER(c_uint64)]),
 ]
@@ -242,6 +243,10 @@ class Engine:
         out = np.zeros((len(rows), 6), np.float64)
         self._ok(self.d.kgb_sun_noaa(self.h, _p(rows), len(rows), _p(out)))
         return out
+
+    def set_builder(self, which):
+        """0: host binned-SAH tree (default); 1: device LBVH. Applies to the following build() calls."""
+        self._ok(self.d.kgb_set_builder(self.h, int(which)))
 
     def set_series_form(self, form):
         """0: split-BF16 on the tensor cores (default); 1: the plain FP32 form."""

@@ -977,6 +977,8 @@ KGB_API int kgb_sky(kgb_engine*, int32_t, const kgb_sky_step*, size_t, double, i
 KGB_API int kgb_sun_noaa(kgb_engine*, const double*, size_t, double*) {
   return fail("kgb_sun_noaa: the sun's checker is the reference's own code (tests/golden/sky)");
 }
+// The restatement has one builder (its binary SAH tree): every builder choice gives the same results.
+KGB_API int kgb_set_builder(kgb_engine*, int which) { return which == 0 || which == 1 ? 1 : fail("kgb_set_builder: 0 or 1"); }
 KGB_API int kgb_set_series_form(kgb_engine*, int form) { return form == 0 || form == 1 ? 1 : fail("kgb_set_series_form: 0 or 1"); }
 KGB_API int kgb_trace_counters(kgb_engine*, size_t, size_t, uint32_t, uint64_t out[4]) {
   out[0] = out[1] = out[2] = out[3] = 0;
