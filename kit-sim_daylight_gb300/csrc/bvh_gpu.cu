@@ -1,5 +1,6 @@
 // Device builder of the engine's acceleration structure (the reference's gpu_build, gpu.cu:386-457, builds an OptiX
-// GAS on the device; this is the GB300 counterpart): a linear BVH over Morton codes (Karras 2012), collapsed to the
+// GAS on the device; this is the GB300 counterpart): a linear BVH over Morton codes (Karras 2012), refined by treelet
+// restructuring, collapsed to the
 // 8-wide quantised nodes and 48-byte triangle records that rt.cuh reads, the same layout as the host builder
 // (bvh_build.cpp) makes.
 //
@@ -7,9 +8,12 @@
 //   2. per triangle: box (expanded by eps), centroid; centroid bounds
 //   3. 63-bit Morton codes of the centroids, radix-sorted with the triangle index (stable: ties keep index order)
 //   4. binary radix tree (Karras 2012): internal node i's range and split from common prefixes of the sorted codes
-//   5. boxes bottom-up: each leaf walks towards the root, the second arrival at a node unites its children's boxes
+//   5. boxes, triangle counts and SAH costs bottom-up (each leaf walks towards the root, the second arrival at a node
+//      refits it from its children), then three such passes that also restructure each node's treelet of up to 7
+//      leaves to its least-SAH topology (Karras & Aila 2013)
 //   6. collapse to 8-wide nodes level by level: a wide node adopts the children of its largest-area inner child until
-//      it has 8 (the host builder's rule); subtrees of at most 3 triangles become leaves; a prefix sum over the level
+//      it has 8 (the host builder's rule); subtrees of at most 3 triangles become leaves (their triangles gathered by a
+//      walk: restructured subtrees are no longer ranges of the sorted order); a prefix sum over the level
 //      gives each node its block of inner children and of triangle records, so the layout is deterministic
 //   7. each node's child boxes quantised outwards to 8 bits against a power-of-two step per axis (double arithmetic,
 //      as the host builder)
@@ -29,6 +33,7 @@ namespace kgb {
 namespace {
 
 constexpr uint32_t kLeafMax = 3;   // triangles per leaf, as the host builder
+constexpr int kTreeletPasses = 3;  // bottom-up passes of treelet restructuring
 
 __device__ __forceinline__ uint32_t ord(float f) {   // order-preserving float -> uint
   const uint32_t u = __float_as_uint(f);
@@ -132,26 +137,134 @@ __global__ void k_karras(const uint64_t* k, int n, int* left, int* right, int* p
   if (i == 0) parent[0] = -1;
 }
 
-// boxes bottom-up: the second thread to arrive at a node unites its children (no waiting: the first one stops)
-__global__ void k_boxes(int n, const uint32_t* order, const float4* plo, const float4* phi, const int* left, const int* right,
-                        const int* parent, const int* leafParent, float4* nlo, float4* nhi, uint32_t* arrivals) {
+// SAH constants of the binary tree's cost (relative): a box test, a triangle test
+constexpr float kCi = 1.2f, kCt = 1.0f;
+
+__device__ __forceinline__ float box_area(float4 lo, float4 hi) {
+  const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+  return dx < 0.f ? 0.f : dx * dy + dy * dz + dz * dx;
+}
+
+// the binary tree being built: child c >= 0 an internal node, c < 0 the leaf ~c (a sorted position)
+struct Tree2 {
+  int *left, *right, *parent, *leafParent;
+  float4 *nlo, *nhi;
+  uint32_t* count;   // triangles under an internal node
+  float* cost;       // SAH cost of its subtree (a set of at most 3 triangles costs as one leaf)
+  const uint32_t* order;
+  const float4 *plo, *phi;
+};
+__device__ __forceinline__ void child_info(const Tree2& T, int c, float4& lo, float4& hi, uint32_t& cnt, float& cst) {
+  if (c >= 0) { lo = __ldcg(&T.nlo[c]); hi = __ldcg(&T.nhi[c]); cnt = __ldcg(&T.count[c]); cst = __ldcg(&T.cost[c]); }
+  else { lo = T.plo[T.order[~c]]; hi = T.phi[T.order[~c]]; cnt = 1; cst = kCt * box_area(lo, hi); }
+}
+// box, count and cost of internal node x from its children
+__device__ __forceinline__ void refit(const Tree2& T, int x) {
+  float4 a, b, c, d;
+  uint32_t na, nb;
+  float ca, cb;
+  child_info(T, __ldcg(&T.left[x]), a, b, na, ca);
+  child_info(T, __ldcg(&T.right[x]), c, d, nb, cb);
+  const float4 lo = make_float4(fminf(a.x, c.x), fminf(a.y, c.y), fminf(a.z, c.z), 0.f);
+  const float4 hi = make_float4(fmaxf(b.x, d.x), fmaxf(b.y, d.y), fmaxf(b.z, d.z), 0.f);
+  const uint32_t n = na + nb;
+  const float A = box_area(lo, hi);
+  __stcg(&T.nlo[x], lo);
+  __stcg(&T.nhi[x], hi);
+  __stcg(&T.count[x], n);
+  __stcg(&T.cost[x], n <= kLeafMax ? kCt * A * float(n) : kCi * A + ca + cb);
+}
+
+// Treelet restructuring (Karras & Aila 2013): the treelet of node x has up to 7 leaves (grown by opening the
+// largest-area internal leaf); a dynamic program over the subsets of its leaves finds the binary topology of least SAH
+// cost, and the treelet's internal nodes are rewired to it when that is cheaper. Subsets of at most 3 triangles cost
+// as the one 8-wide leaf they become.
+__device__ void optimize_treelet(const Tree2& T, int x) {
+  int leaf[7], inner[6];
+  int m = 0, ni = 0;
+  inner[ni++] = x;
+  leaf[m++] = __ldcg(&T.left[x]);
+  leaf[m++] = __ldcg(&T.right[x]);
+  while (m < 7) {
+    int best = -1;
+    float bestA = -1.f;
+    for (int k = 0; k < m; ++k) {
+      const int c = leaf[k];
+      if (c < 0 || __ldcg(&T.count[c]) <= kLeafMax) continue;
+      const float A = box_area(__ldcg(&T.nlo[c]), __ldcg(&T.nhi[c]));
+      if (A > bestA) { bestA = A; best = k; }
+    }
+    if (best < 0) break;
+    const int c = leaf[best];
+    inner[ni++] = c;
+    leaf[best] = __ldcg(&T.left[c]);
+    leaf[m++] = __ldcg(&T.right[c]);
+  }
+  if (m < 4) return;
+  float4 llo[7], lhi[7];
+  uint32_t lcnt[7];
+  float lcost[7];
+  for (int k = 0; k < m; ++k) child_info(T, leaf[k], llo[k], lhi[k], lcnt[k], lcost[k]);
+  float cst[128];
+  uint8_t part[128];
+  const uint32_t full = (1u << m) - 1u;
+  for (uint32_t S = 1; S <= full; ++S) {   // a proper subset precedes its superset
+    float4 lo = make_float4(INFINITY, INFINITY, INFINITY, 0.f), hi = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
+    uint32_t n = 0;
+    for (int k = 0; k < m; ++k)
+      if (S >> k & 1u) {
+        lo = make_float4(fminf(lo.x, llo[k].x), fminf(lo.y, llo[k].y), fminf(lo.z, llo[k].z), 0.f);
+        hi = make_float4(fmaxf(hi.x, lhi[k].x), fmaxf(hi.y, lhi[k].y), fmaxf(hi.z, lhi[k].z), 0.f);
+        n += lcnt[k];
+      }
+    const uint32_t low = S & (0u - S);
+    if (S == low) { cst[S] = lcost[__ffs(S) - 1]; part[S] = 0; continue; }
+    float best = INFINITY;
+    uint32_t bp = low;
+    for (uint32_t P = (S - 1) & S; P; P = (P - 1) & S)
+      if (P & low) { const float c = cst[P] + cst[S ^ P]; if (c < best) { best = c; bp = P; } }
+    const float A = box_area(lo, hi);
+    cst[S] = n <= kLeafMax ? kCt * A * float(n) : kCi * A + best;
+    part[S] = uint8_t(bp);
+  }
+  if (!(cst[full] < __ldcg(&T.cost[x]) * 0.9999f)) return;   // keep the tree unless the treelet improves
+  // rewire top-down (x stays the root), then refit bottom-up in reverse order of assignment
+  uint32_t setOf[6];
+  int nodeOf[6], order[6];
+  int sp = 0, next = 1, done = 0;
+  setOf[0] = full; nodeOf[0] = x; sp = 1;
+  while (sp) {
+    --sp;
+    const uint32_t S = setOf[sp];
+    const int node = nodeOf[sp];
+    order[done++] = node;
+    const uint32_t P[2] = {part[S], S ^ part[S]};
+    int id[2];
+    for (int h = 0; h < 2; ++h) {
+      if (__popc(P[h]) == 1) id[h] = leaf[__ffs(P[h]) - 1];
+      else { id[h] = inner[next++]; setOf[sp] = P[h]; nodeOf[sp] = id[h]; ++sp; }
+      if (id[h] >= 0) __stcg(&T.parent[id[h]], node); else __stcg(&T.leafParent[~id[h]], node);
+    }
+    __stcg(&T.left[node], id[0]);
+    __stcg(&T.right[node], id[1]);
+  }
+  for (int k = done - 1; k >= 0; --k) refit(T, order[k]);
+}
+
+// bottom-up pass: the second thread to arrive at a node refits it from its children and, when asked, restructures
+// its treelet (every node below is final by then); the first one stops: no thread waits
+__global__ void k_bottom_up(Tree2 T, int n, uint32_t* arrivals, int optimize) {
   const int p = int(blockIdx.x * blockDim.x + threadIdx.x);
   if (p >= n) return;
-  int node = leafParent[p];
+  int node = __ldcg(&T.leafParent[p]);
   while (node >= 0) {
     __threadfence();
     if (atomicAdd(&arrivals[node], 1u) == 0) return;
     __threadfence();
-    float4 lo = make_float4(INFINITY, INFINITY, INFINITY, 0.f), hi = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
-    const int ch[2] = {left[node], right[node]};
-    for (int c : ch) {
-      const float4 a = c >= 0 ? __ldcg(&nlo[c]) : plo[order[~c]], b = c >= 0 ? __ldcg(&nhi[c]) : phi[order[~c]];
-      lo = make_float4(fminf(lo.x, a.x), fminf(lo.y, a.y), fminf(lo.z, a.z), 0.f);
-      hi = make_float4(fmaxf(hi.x, b.x), fmaxf(hi.y, b.y), fmaxf(hi.z, b.z), 0.f);
-    }
-    __stcg(&nlo[node], lo);
-    __stcg(&nhi[node], hi);
-    node = parent[node];
+    refit(T, node);
+    if (optimize && __ldcg(&T.count[node]) > kLeafMax) optimize_treelet(T, node);
+    __threadfence();
+    node = __ldcg(&T.parent[node]);
   }
 }
 
@@ -159,19 +272,32 @@ struct Tree {
   const uint32_t* order;   // sorted position -> triangle
   const float4 *plo, *phi, *nlo, *nhi;
   const int *left, *right;
-  const int2* range;
+  const uint32_t* count;
 };
-__device__ __forceinline__ uint32_t count_of(const Tree& T, int c) { return c >= 0 ? uint32_t(T.range[c].y - T.range[c].x + 1) : 1u; }
-__device__ __forceinline__ uint32_t first_of(const Tree& T, int c) { return c >= 0 ? uint32_t(T.range[c].x) : uint32_t(~c); }
+__device__ __forceinline__ uint32_t count_of(const Tree& T, int c) { return c >= 0 ? T.count[c] : 1u; }
 __device__ __forceinline__ bool leaf_of(const Tree& T, int c) { return count_of(T, c) <= kLeafMax; }
+// the triangles under a subtree of at most kLeafMax triangles, left to right
+__device__ __forceinline__ uint32_t gather(const Tree& T, int c, uint32_t* out) {
+  int st[2 * kLeafMax];
+  int sp = 0;
+  uint32_t n = 0;
+  st[sp++] = c;
+  while (sp && n < kLeafMax) {
+    const int x = st[--sp];
+    if (x < 0) { out[n++] = T.order[~x]; continue; }
+    if (sp + 2 > int(2 * kLeafMax)) break;
+    st[sp++] = T.right[x];
+    st[sp++] = T.left[x];
+  }
+  return n;
+}
 __device__ __forceinline__ void box_of(const Tree& T, int c, float4& lo, float4& hi) {
   if (c >= 0) { lo = T.nlo[c]; hi = T.nhi[c]; } else { lo = T.plo[T.order[~c]]; hi = T.phi[T.order[~c]]; }
 }
 __device__ __forceinline__ float area_of(const Tree& T, int c) {
   float4 lo, hi;
   box_of(T, c, lo, hi);
-  const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
-  return dx < 0.f ? 0.f : dx * dy + dy * dz + dz * dx;
+  return box_area(lo, hi);
 }
 
 // level pass 1: each wide node's children (the host builder's greedy opening), inner-child and triangle counts
@@ -254,10 +380,11 @@ __global__ void k_collapse_emit(Tree T, const float* v, const uint32_t* tri, con
       imask |= 1u << k;
       wideSrc[childBase + inner++] = ch[k];
     } else {
-      const uint32_t cnt = count_of(T, ch[k]), f = first_of(T, ch[k]);
+      uint32_t tt[kLeafMax];
+      const uint32_t cnt = gather(T, ch[k], tt);
       meta[k] = (cnt << 5) | tOff;
       for (uint32_t j = 0; j < cnt; ++j) {
-        const uint32_t t = T.order[f + j];
+        const uint32_t t = tt[j];
         float* r = tris + size_t(triBase + tOff + j) * 12;
         for (int vtx = 0; vtx < 3; ++vtx)
           for (int a = 0; a < 3; ++a) r[4 * vtx + a] = v[3 * tri[3 * t + vtx] + a];
@@ -299,8 +426,8 @@ std::string build_bvh8_gpu(const float* v, size_t nv, const uint32_t* tri, size_
   if (!nt) return "";
   if (nt >= (size_t(1) << 31) - 1) return "more than 2^31 triangles";
   const int n = int(nt);
-  DevBuf dv, dtri, dslot, dtr, plo, phi, cen, cb, keys, keys2, vals, vals2, left, right, parent, leafParent, range, nlo, nhi, arr, wideSrc, kids,
-      nInner, nTri, offI, offT, tmp, maxabs;
+  DevBuf dv, dtri, dslot, dtr, plo, phi, cen, cb, keys, keys2, vals, vals2, left, right, parent, leafParent, range, nlo, nhi, arr, cnt, cost, wideSrc,
+      kids, nInner, nTri, offI, offT, tmp, maxabs;
   const size_t tiles = (nt + 255) / 256;
   KGB_TRY(cudaMalloc(&dv.p, nv * 12));
   KGB_TRY(cudaMalloc(&dtri.p, nt * 12));
@@ -344,14 +471,18 @@ std::string build_bvh8_gpu(const float* v, size_t nv, const uint32_t* tri, size_
   KGB_TRY(cudaMalloc(&left.p, ni * 4)); KGB_TRY(cudaMalloc(&right.p, ni * 4)); KGB_TRY(cudaMalloc(&parent.p, ni * 4));
   KGB_TRY(cudaMalloc(&leafParent.p, nt * 4)); KGB_TRY(cudaMalloc(&range.p, ni * 8));
   KGB_TRY(cudaMalloc(&nlo.p, ni * 16)); KGB_TRY(cudaMalloc(&nhi.p, ni * 16)); KGB_TRY(cudaMalloc(&arr.p, ni * 4));
-  KGB_TRY(cudaMemsetAsync(arr.p, 0, ni * 4, st));
+  KGB_TRY(cudaMalloc(&cnt.p, ni * 4)); KGB_TRY(cudaMalloc(&cost.p, ni * 4));
+  Tree2 T2{left.as<int>(), right.as<int>(), parent.as<int>(), leafParent.as<int>(), nlo.as<float4>(), nhi.as<float4>(), cnt.as<uint32_t>(),
+           cost.as<float>(), vals2.as<uint32_t>(), plo.as<float4>(), phi.as<float4>()};
   if (n == 1) KGB_TRY(cudaMemsetAsync(leafParent.p, 0xff, 4, st));   // the single leaf is the root
   else {
     k_karras<<<unsigned((ni + 255) / 256), 256, 0, st>>>(keys2.as<uint64_t>(), n, left.as<int>(), right.as<int>(), parent.as<int>(), leafParent.as<int>(),
                                                          range.as<int2>());
-    // 5. boxes
-    k_boxes<<<unsigned(tiles), 256, 0, st>>>(n, vals2.as<uint32_t>(), plo.as<float4>(), phi.as<float4>(), left.as<int>(), right.as<int>(),
-                                             parent.as<int>(), leafParent.as<int>(), nlo.as<float4>(), nhi.as<float4>(), arr.as<uint32_t>());
+    // 5. boxes, counts, costs; then passes of treelet restructuring
+    for (int pass = 0; pass <= kTreeletPasses; ++pass) {
+      KGB_TRY(cudaMemsetAsync(arr.p, 0, ni * 4, st));
+      k_bottom_up<<<unsigned(tiles), 256, 0, st>>>(T2, n, arr.as<uint32_t>(), pass > 0 ? 1 : 0);
+    }
   }
   // 6-7. collapse level by level into the output buffers
   void* nodes = nullptr;
@@ -368,7 +499,7 @@ std::string build_bvh8_gpu(const float* v, size_t nv, const uint32_t* tri, size_
   const int root = n == 1 ? ~0 : 0;
   KGB_TRY(cudaMemcpyAsync(wideSrc.p, &root, 4, cudaMemcpyHostToDevice, st));
   Tree T{vals2.as<uint32_t>(), plo.as<float4>(), phi.as<float4>(), nlo.as<float4>(), nhi.as<float4>(), left.as<int>(), right.as<int>(),
-         range.as<int2>()};
+         cnt.as<uint32_t>()};
   uint32_t b = 0, e = 1, triBase = 0;
   for (int level = 0; b < e; ++level) {
     if (level > 4096) return "bvh collapse: too many levels";
@@ -395,7 +526,7 @@ std::string build_bvh8_gpu(const float* v, size_t nv, const uint32_t* tri, size_
   }
   if (triBase != nt) return "bvh collapse: " + std::to_string(triBase) + " triangle records for " + std::to_string(nt) + " triangles";
   *nNodesOut = e;
-  *tempBytes = nt * (12 + 16 * 3 + 8 * 2 + 4 * 2 + 4 * 4 + 8 + 32 + 4) + maxNodes * (4 + 32 + 16) + tmpBytes;
+  *tempBytes = nt * (12 + 16 * 3 + 8 * 2 + 4 * 2 + 4 * 4 + 8 + 32 + 4 + 8) + maxNodes * (4 + 32 + 16) + tmpBytes;
   return "";
 }
 

@@ -157,7 +157,7 @@ struct Engine {
   Staging staging;   // pinned slices for the series download
   kgb_stats stats{};
   int gridBits = 0, gridView = 0;
-  int builder = 0;            // 0 host binned SAH, 1 device LBVH (kgb_set_builder)
+  int builder = 1;            // 1 device LBVH with treelet restructuring (default), 0 host binned SAH (kgb_set_builder)
 };
 
 namespace {

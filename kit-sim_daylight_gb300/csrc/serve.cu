@@ -559,20 +559,20 @@ KGB_API void kgb_server_destroy(kgb_server* h) {
 KGB_API int kgb_server_add_scene(kgb_server* h, const float* v, size_t nv, const uint32_t* tri, size_t nt, int32_t* sceneId) {
   Server* s = reinterpret_cast<Server*>(h);
   for (size_t k = 0; k < 3 * nt; ++k) if (tri[k] >= nv) { set_error("kgb_server_add_scene: a triangle's vertex index exceeds the vertices"); return 0; }
-  BvhOut b;
-  build_bvh8(v, nv, tri, nt, nullptr, nullptr, b);
   DScene d;
-  std::string err;
-  d.nNodes = b.nNodes;
-  d.nTris = uint32_t(nt);
-  d.bytes = b.nodes.size() * 4 + b.tris.size() * 4;
   std::lock_guard<std::mutex> lk(s->m);
-  if (nt && (!cuok(cudaMalloc(&d.nodes, b.nodes.size() * 4), err, "scene") || !cuok(cudaMalloc(&d.tris, b.tris.size() * 4), err, "scene") ||
-             !cuok(cudaMemcpy(d.nodes, b.nodes.data(), b.nodes.size() * 4, cudaMemcpyHostToDevice), err, "scene") ||
-             !cuok(cudaMemcpy(d.tris, b.tris.data(), b.tris.size() * 4, cudaMemcpyHostToDevice), err, "scene"))) {
-    set_error(err);
-    return 0;
+  if (nt) {   // the device builder (bvh_gpu.cu), on the server's stream
+    uint64_t temp = 0;
+    const std::string why = build_bvh8_gpu(v, nv, tri, nt, nullptr, nullptr, s->st, &d.nodes, &d.tris, &d.nNodes, &temp);
+    if (!why.empty()) {
+      if (d.nodes) cudaFree(d.nodes);
+      if (d.tris) cudaFree(d.tris);
+      set_error("kgb_server_add_scene: " + why);
+      return 0;
+    }
   }
+  d.nTris = uint32_t(nt);
+  d.bytes = uint64_t(d.nNodes) * 80 + uint64_t(nt) * 48;
   s->used += d.bytes;
   s->scenes.push_back(d);
   *sceneId = int32_t(s->scenes.size() - 1);

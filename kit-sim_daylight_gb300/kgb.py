@@ -245,7 +245,7 @@ class Engine:
         return out
 
     def set_builder(self, which):
-        """0: host binned-SAH tree (default); 1: device LBVH. Applies to the following build() calls."""
+        """1: device LBVH with treelet restructuring (default); 0: host binned-SAH tree. Applies to the following build() calls."""
         self._ok(self.d.kgb_set_builder(self.h, int(which)))
 
     def set_series_form(self, form):

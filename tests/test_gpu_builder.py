@@ -1,6 +1,6 @@
-"""The device BVH builder (kgb_set_builder(1): Morton-ordered radix tree on the GPU, collapsed to the same 8-wide
-records as the host builder). Every result must equal the oracle's bit for bit, as with the host builder: the tree
-only changes which boxes are visited, never the hit set. Covered: visibility bits and transmittance bytes on seeded
+"""Both BVH builders (kgb_set_builder: 1 the device LBVH with treelet restructuring, the default; 0 the host binned
+SAH tree), collapsed to the same 8-wide records. Every result must equal the oracle's bit for bit with either: the
+tree only changes which boxes are visited, never the hit set. Covered: visibility bits and transmittance bytes on seeded
 cities, closest-hit view classes and distances, reflected-light rows (slot records), scenes of 0 to 4 triangles and
 triangles sharing one centroid (equal Morton codes, the tie rule of the radix tree)."""
 import numpy as np
@@ -9,9 +9,12 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def engines(engine_lib, oracle, kgb):
+BUILDERS = [1, 0]
+
+
+def engines(engine_lib, oracle, kgb, builder):
     e, o = kgb.Engine(engine_lib), kgb.Engine(oracle)
-    e.set_builder(1)
+    e.set_builder(builder)
     return e, o
 
 
@@ -20,11 +23,12 @@ def bits_of(eng, nc, flags):
     return eng.download_bits(nc)
 
 
+@pytest.mark.parametrize("builder", BUILDERS)
 @pytest.mark.parametrize("seed", [1, 2, 3])
-def test_device_tree_bits(engine_lib, oracle, kgb, pkg, seed):
+def test_tree_bits(engine_lib, oracle, kgb, pkg, seed, builder):
     s = pkg.workloads.random_city(seed)
     D = pkg.workloads.hemisphere_dirs(145, 300, seed)
-    e, o = engines(engine_lib, oracle, kgb)
+    e, o = engines(engine_lib, oracle, kgb, builder)
     try:
         for x in (e, o):
             x.build(s["v"], s["tri"])
@@ -39,13 +43,14 @@ def test_device_tree_bits(engine_lib, oracle, kgb, pkg, seed):
         e.close(); o.close()
 
 
-def test_device_tree_bytes_and_bounce(engine_lib, oracle, kgb, pkg):
+@pytest.mark.parametrize("builder", BUILDERS)
+def test_tree_bytes_and_bounce(engine_lib, oracle, kgb, pkg, builder):
     s = pkg.workloads.random_city(9, porous=True, glass=True, thin=True)
     tn = kgb.tn_from_Tn(0.64)
     slots = [(0.2, 0, 0, 0), (0.3, 0.5, 0, 0), (0.0, 0.64, tn, kgb.SLOT_GLASS), (0.25, 0, 0, 0), (0.2, 0, 0, 0), (0.2, 0, 0, 0),
              (0.2, 0, 0, 0), (0.1, 0.6, 0, kgb.SLOT_THIN)]
     D = pkg.workloads.hemisphere_dirs(145, 300, 9)
-    e, o = engines(engine_lib, oracle, kgb)
+    e, o = engines(engine_lib, oracle, kgb, builder)
     try:
         for x in (e, o):
             x.build(s["v"], s["tri"], s["slot"], slots, per_slot=True)
@@ -66,11 +71,12 @@ def test_device_tree_bytes_and_bounce(engine_lib, oracle, kgb, pkg):
         e.close(); o.close()
 
 
-def test_device_tree_views(engine_lib, oracle, kgb, pkg):
+@pytest.mark.parametrize("builder", BUILDERS)
+def test_tree_views(engine_lib, oracle, kgb, pkg, builder):
     s = pkg.workloads.random_city(7, glass=True)
     label = np.random.default_rng(2).integers(2, 6, len(s["tri"])).astype(np.uint8)
     nAz, nEl, dAz, rowSin, wRow = pkg.workloads.views_grid(120.0, 4.0)
-    e, o = engines(engine_lib, oracle, kgb)
+    e, o = engines(engine_lib, oracle, kgb, builder)
     try:
         out = []
         for x in (e, o):
@@ -85,8 +91,9 @@ def test_device_tree_views(engine_lib, oracle, kgb, pkg):
         e.close(); o.close()
 
 
+@pytest.mark.parametrize("builder", BUILDERS)
 @pytest.mark.parametrize("nt", [0, 1, 2, 3, 4, 97])
-def test_device_tree_small_and_tied(engine_lib, oracle, kgb, nt):
+def test_tree_small_and_tied(engine_lib, oracle, kgb, nt, builder):
     rng = np.random.default_rng(nt)
     if nt == 97:   # every triangle with the same centroid: equal Morton codes throughout
         c = np.array([0.5, 0.5, 2.0], np.float32)
@@ -101,7 +108,7 @@ def test_device_tree_small_and_tied(engine_lib, oracle, kgb, nt):
     z = rng.uniform(0.05, 1, 256)
     a = rng.uniform(0, 2 * np.pi, 256)
     D = np.stack([np.sqrt(1 - z * z) * np.cos(a), np.sqrt(1 - z * z) * np.sin(a), z], axis=1).astype(np.float32)
-    e, o = engines(engine_lib, oracle, kgb)
+    e, o = engines(engine_lib, oracle, kgb, builder)
     try:
         got = []
         for x in (e, o):
