@@ -434,6 +434,8 @@ def run_views(args, pkg):
     lib = pkg.load()
     e = pkg.engine()
     city = pkg.workloads.views_city()
+    if args.sensors:   # a smaller case of the same kernels (profiling): the city's first sensors
+        city = dict(city, P=city["P"][:args.sensors], N=city["N"][:args.sensors])
     e.build(np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32), np.array([[0, 1, 2]], np.uint32))   # warm-up of the device builder
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -610,7 +612,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=30000)
     ap.add_argument("--ref-sample", type=int, default=20000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--sensors", type=int, default=0, help="urban / precision: only the block's first N sensors (a small case for profiling)")
+    ap.add_argument("--sensors", type=int, default=0, help="urban / precision / views: only the first N sensors (a small case for profiling)")
     ap.add_argument("--config", default="urban", choices=["urban", "precision", "views", "serving"])
     ap.add_argument("--builder", type=int, default=1, choices=[0, 1], help="urban: 1 device LBVH with treelets (default), 0 host binned-SAH tree")
     ap.add_argument("--rate", type=float, default=200.0)

@@ -156,7 +156,7 @@ struct Engine {
   Buf vop, sop, csr, sunCol;
   Staging staging;   // pinned slices for the series download
   kgb_stats stats{};
-  int gridBits = 0, gridView = 0;
+  int gridBits = 0, gridBytes = 0, gridView = 0;
   int builder = 1;            // 1 device LBVH with treelet restructuring (default), 0 host binned SAH (kgb_set_builder)
 };
 
@@ -372,9 +372,11 @@ static int trace_impl(Engine& g, size_t i0, size_t nc, uint32_t rayFlags, uint64
   g.i0 = i0; g.visN = nc;
   if (nc == 0 || g.nWords == 0) return 1;
   if (!g.gridBits) g.gridBits = g.numSMs * bits_blocks_per_sm();
+  if (!g.gridBytes) g.gridBytes = g.numSMs * bytes_blocks_per_sm();
   const bool any = g.bytes;
   const double targetMs = any ? 30 : 150;
-  const size_t nMin = any ? std::max<size_t>(1, (size_t(1) << 13) / g.nWords) : 1024;
+  // byte mode: the reference starts at 2^13 threads and at most doubles; here at least four tasks per resident warp
+  const size_t nMin = any ? std::max<size_t>((size_t(1) << 13) / g.nWords, (size_t(4) * g.gridBytes * 8 * 32 + g.nWords - 1) / g.nWords) : 1024;
   const size_t nMax = std::max<size_t>(32, size_t(0xffffffffu) / g.nWords * 32);   // warp tasks are counted in 32 bits
   size_t done = 0, n = std::min(counters ? nc : std::min(any ? nMin : size_t(4096), nc), nMax);
   TraceArgs a{};
@@ -390,7 +392,7 @@ static int trace_impl(Engine& g, size_t i0, size_t nc, uint32_t rayFlags, uint64
     a.first = uint32_t(i0 + done); a.n = uint32_t(n); a.out0 = uint32_t(done);
     if (!reset_ctl(g)) return 0;
     const size_t tasks = (n + 31) / 32 * g.nWords;   // warp tasks: 32 sensors x one 32-direction word
-    const int grid = int(std::min<size_t>(size_t(g.gridBits), (tasks + 7) / 8));
+    const int grid = int(std::min<size_t>(size_t(any ? g.gridBytes : g.gridBits), (tasks + 7) / 8));
     CU(cudaEventRecord(g.ev[0], g.st));
     if (any) launch_bytes(a, grid, g.st); else launch_bits(a, grid, g.st, counters != nullptr);
     CU(cudaEventRecord(g.ev[1], g.st));
@@ -570,7 +572,9 @@ KGB_API int kgb_bounce(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, c
   a.rayFlags = rayFlags; a.slots = static_cast<const kgb_slot*>(g.slots.p); a.nSlots = g.nSlots;
   a.dc = static_cast<float*>(g.dc.p); a.status = static_cast<uint32_t*>(g.ctl.p) + 1;
   const size_t nCap = std::max<size_t>(1, (size_t(256) << 20) / (8 * nc));   // per-path results of a launch: at most 256 MiB
-  for (size_t done = 0, n = std::clamp<size_t>((size_t(1) << 13) / nc, 1, 64); done < b->M;) {
+  // the reference starts at 2^13 / nc samples (1..64); here also at least ~4 paths per resident thread (a path a thread)
+  const size_t fill = (size_t(4) * size_t(g.numSMs) * 2048 + nc - 1) / nc;
+  for (size_t done = 0, n = std::max(std::clamp<size_t>((size_t(1) << 13) / nc, 1, 64), fill); done < b->M;) {
     if (b->cancel && b->cancel(b->cancelCtx)) return fail("cancelled");
     n = std::min({n, size_t(b->M) - done, nCap});
     if (!grow(g.contrib, n * nc * 8)) return 0;
@@ -645,7 +649,7 @@ KGB_API int kgb_view(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, con
   if (!grow(g.viewCls, K * nc) || !grow(g.viewDist, K * nc * 4) || !upload(g.rowSin, v->rowSin, size_t(v->nEl) * 8, g.st)) return 0;
   g.viewN = nc; g.viewK = K; g.viewI0 = i0; g.view = *v; g.view.rowSin = nullptr;
   if (nc == 0 || K == 0) { CU(cudaStreamSynchronize(g.st)); return 1; }
-  if (!g.gridView) g.gridView = g.numSMs * 4;
+  if (!g.gridView) g.gridView = g.numSMs * view_blocks_per_sm();
   const double rad = v->north * KGB_PI_D / 180;
   ViewArgs a{};
   a.nodes = static_cast<const Node8*>(g.sc->nodes.p); a.tris = static_cast<const TriRec*>(g.sc->tris.p); a.nNodes = g.sc->nNodes;
@@ -658,7 +662,9 @@ KGB_API int kgb_view(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, con
   a.label = g.nLabel ? static_cast<const uint8_t*>(g.label.p) : nullptr;
   a.cls = static_cast<uint8_t*>(g.viewCls.p); a.dist = static_cast<float*>(g.viewDist.p);
   a.counter = static_cast<uint32_t*>(g.ctl.p); a.status = static_cast<uint32_t*>(g.ctl.p) + 1;
-  const size_t nMin = std::max<size_t>(1, (size_t(1) << 13) / nWords);
+  // gpu.cu:590: sub-launches of at least 2^13 threads there; here at least four (32 sensors x word) tasks for each
+  // resident warp, so that no launch leaves the GPU idle; then ~40 ms, at most doubling, as the reference
+  const size_t nMin = std::max<size_t>((size_t(1) << 13) / nWords, (size_t(4) * g.gridView * 8 * 32 + nWords - 1) / nWords);
   size_t n = std::max(*launch, nMin);
   for (size_t done = 0; done < nc;) {
     if (v->cancel && v->cancel(v->cancelCtx)) return fail("cancelled");
@@ -677,7 +683,7 @@ KGB_API int kgb_view(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, con
     const double want = double(m) * 40 / std::max(ms, 1e-3);
     n = std::max(nMin, std::min(2 * n, want > 1e12 ? size_t(1) << 40 : size_t(want)));
   }
-  *launch = n;
+  *launch = n;   // the caller passes it to the next chunk
   return 1;
 }
 

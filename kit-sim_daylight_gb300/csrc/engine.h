@@ -75,6 +75,8 @@ struct BounceArgs {
 };
 
 void launch_ray_table(const float* D, uint32_t nDir, void* tab, cudaStream_t st);   // 48 bytes per direction
+int bytes_blocks_per_sm();
+int view_blocks_per_sm();
 int bits_blocks_per_sm();
 void launch_bits(const TraceArgs& a, int grid, cudaStream_t st, bool count = false);
 void launch_bytes(const TraceArgs& a, int grid, cudaStream_t st);

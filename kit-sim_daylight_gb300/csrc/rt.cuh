@@ -373,8 +373,9 @@ __device__ __forceinline__ void for_hits(const Scene& s, const Ray& r, float tmi
   }
 }
 
-// The closest hit in [tmin, tmax], ties broken by the smaller primitive index. Children are visited near to far; a
-// node whose entry lies beyond the best hit so far is skipped.
+// The closest hit in [tmin, tmax], ties broken by the smaller primitive index. Children are visited near to far: the
+// nearest inner child next, the others pushed far to near; a node whose entry lies beyond the best hit so far is
+// skipped. The visiting order changes nothing but the work: the result is the closest hit of the whole hit set.
 struct ClosestOut { Hit h; F3 v0, v1, v2; uint32_t flags, slot; };
 __device__ __forceinline__ bool closest(const Scene& s, const Ray& r, float tmin, float tmax, bool cull, ClosestOut& out, uint32_t& overflow) {
   if (!s.nNodes) return false;
@@ -383,14 +384,11 @@ __device__ __forceinline__ bool closest(const Scene& s, const Ray& r, float tmin
   int sp = 0;
   bool any = false;
   float best = tmax;
-  stack[sp++] = Entry{0u, tmin};
-  uint32_t visits = 0;
-  while (sp) {
-    const Entry e = stack[--sp];
-    if (e.t > best) continue;
-    if (++visits > kMaxVisits || e.node >= s.nNodes) { overflow |= 2u; return any; }
+  uint32_t cur = 0, visits = 0;
+  for (;;) {
+    if (++visits > kMaxVisits || cur >= s.nNodes) { overflow |= 2u; return any; }
     uint4 n[5];
-    load_node(s.nodes, e.node, n);
+    load_node(s.nodes, cur, n);
     float tn[8];
     const uint32_t hit = node_hits<true>(n, r, tmin, best, tn);
     const uint32_t imask = n[0].w >> 24;
@@ -415,26 +413,32 @@ __device__ __forceinline__ bool closest(const Scene& s, const Ray& r, float tmin
         }
       }
     }
-    // inner children, pushed far to near so the nearest is popped first
+    // inner children still in front of the best hit, sorted far to near: the nearest is visited next
     uint32_t inner = hit & imask;
-    const int cnt = __popc(inner);
-    if (sp + cnt > kStack * 4) { overflow = 1; continue; }
     Entry ch[8];
     int m = 0;
     while (inner) {
       const int k = __ffs(inner) - 1;
       inner &= inner - 1;
-      ch[m++] = Entry{n[1].x + __popc(imask & ((1u << k) - 1u)), tn[k]};
-    }
-    for (int a = 1; a < m; ++a) {   // insertion sort, descending t
-      const Entry x = ch[a];
-      int b = a - 1;
+      if (tn[k] > best) continue;
+      const Entry x{n[1].x + __popc(imask & ((1u << k) - 1u)), tn[k]};
+      int b = m - 1;
       while (b >= 0 && ch[b].t < x.t) { ch[b + 1] = ch[b]; --b; }
       ch[b + 1] = x;
+      ++m;
     }
-    for (int a = 0; a < m; ++a) stack[sp++] = ch[a];
+    if (m) {
+      if (sp + m - 1 > kStack * 4) { overflow |= 1u; m = 1; }
+      for (int a = 0; a < m - 1; ++a) stack[sp++] = ch[a];
+      cur = ch[m - 1].node;
+      continue;
+    }
+    for (;;) {   // the next pushed node still in front of the best hit
+      if (!sp) return any;
+      const Entry e = stack[--sp];
+      if (e.t <= best) { cur = e.node; break; }
+    }
   }
-  return any;
 }
 
 // One visibility word: bit k = direction w*32+k of a sensor (normal n, ray origin o) passes the hemisphere cull and every

@@ -149,7 +149,7 @@ __device__ __forceinline__ F3 view_cell(uint32_t d, uint32_t col, float rsx, flo
   return f3(c * sa, c * ca, s);
 }
 
-__global__ void __launch_bounds__(256) k_view(ViewArgs a) {
+__global__ void __launch_bounds__(256, 3) k_view(ViewArgs a) {   // 3 blocks an SM: more warps to hide latency beat the few spills
   const Scene s{a.nodes, a.tris, a.nNodes};
   const bool cull = (a.rayFlags & KGB_RAY_CULL_BACK_FACING) != 0;
   const uint32_t lane = threadIdx.x & 31;
@@ -319,6 +319,16 @@ __global__ void __launch_bounds__(256) k_ray_table(const float* D, uint32_t nDir
 }
 void launch_ray_table(const float* D, uint32_t nDir, void* tab, cudaStream_t st) {
   if (nDir) k_ray_table<<<(nDir + 255) / 256, 256, 0, st>>>(D, nDir, static_cast<RayDir*>(tab));
+}
+int bytes_blocks_per_sm() {   // resident blocks of k_bytes per SM
+  int b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_bytes, 256, 0) != cudaSuccess || b < 1) b = 1;
+  return b;
+}
+int view_blocks_per_sm() {   // resident blocks of k_view per SM
+  int b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_view, 256, 0) != cudaSuccess || b < 1) b = 1;
+  return b;
 }
 int bits_blocks_per_sm() {   // resident blocks of k_bits per SM (its persistent grid fills the GPU once)
   int b = 0;
