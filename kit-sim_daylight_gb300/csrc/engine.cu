@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <thread>
@@ -56,7 +57,7 @@ struct Staging {
 };
 void host_copy(void* dst, const void* src, size_t bytes) {
   constexpr size_t kPart = size_t(4) << 20;
-  const int nt = int(std::min<size_t>(4, (bytes + kPart - 1) / kPart));
+  const int nt = int(std::min<size_t>(8, (bytes + kPart - 1) / kPart));
   if (nt <= 1) { std::memcpy(dst, src, bytes); return; }
   std::vector<std::thread> th;
   const size_t per = (bytes + nt - 1) / nt;
@@ -175,7 +176,7 @@ int sync_status(Engine& g) {   // wait for the stream, then read the kernels' st
   return 1;
 }
 int reset_ctl(Engine& g) {
-  CU(cudaMemsetAsync(g.ctl.p, 0, 32, g.st));
+  CU(cudaMemsetAsync(g.ctl.p, 0, 128, g.st));
   return 1;
 }
 float elapsed(Engine& g) {
@@ -218,7 +219,7 @@ KGB_API kgb_engine* kgb_init(void) {
   g->numSMs = prop.multiProcessorCount;
   if (cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking) != cudaSuccess) return bad("cudaStreamCreate failed");
   if (cudaEventCreate(&g->ev[0]) != cudaSuccess || cudaEventCreate(&g->ev[1]) != cudaSuccess) return bad("cudaEventCreate failed");
-  if (!grow(g->ctl, 64)) return bad(g_err);
+  if (!grow(g->ctl, 128)) return bad(g_err);
   g->sc = new SceneObj;
   const kgb_slot one{0.2f, 0.f, 0.f, 0u};
   if (!kgb_set_slots(reinterpret_cast<kgb_engine*>(g), &one, 1)) return bad(g_err);
@@ -584,14 +585,23 @@ KGB_API int kgb_bounce(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, c
     CU(cudaEventRecord(g.ev[0], g.st));
     launch_bounce(a, g.st);
     CU(cudaEventRecord(g.ev[1], g.st));
-    uint32_t ctl[4] = {};
-    CU(cudaMemcpyAsync(ctl, g.ctl.p, 16, cudaMemcpyDeviceToHost, g.st));
+    uint32_t ctl[32] = {};
+    CU(cudaMemcpyAsync(ctl, g.ctl.p, 128, cudaMemcpyDeviceToHost, g.st));
     CU(cudaStreamSynchronize(g.st));
     CU(cudaGetLastError());
     const unsigned long long segments = (unsigned long long)ctl[2] | ((unsigned long long)ctl[3] << 32);
+    std::string where;
+    if (ctl[16]) {   // the first path whose walk gave up
+      const auto f = [&](int k) { float x; std::memcpy(&x, &ctl[k], 4); char b[32]; std::snprintf(b, sizeof b, "%.9g", x); return std::string(b); };
+      where = "; first walk that gave up: sensor " + std::to_string(ctl[17]) + " sample " + std::to_string(ctl[18]) + " segment " +
+              std::to_string(ctl[19]) + ", origin (" + f(20) + ", " + f(21) + ", " + f(22) + "), direction (" + f(23) + ", " + f(24) + ", " +
+              f(25) + ")";
+    }
     if (ctl[1] & kStatusTimeout)
       return fail("gpu_bounce: a launch of " + std::to_string(n) + " samples x " + std::to_string(nc) + " sensors passed its 10 s limit after " +
-                  std::to_string(segments) + " path segments");
+                  std::to_string(segments) + " path segments" + where);
+    if (ctl[1] & kStatusVisitLimit)
+      return fail("gpu_bounce: traversal gave up (more node visits than the BVH has nodes, or a node index beyond it)" + where);
     if (!sync_status(g)) return 0;
     const double ms = elapsed(g);
     g.stats.bounceMs += ms; g.stats.paths += n * nc; g.stats.bounceLaunches++;

@@ -197,39 +197,77 @@ __device__ __forceinline__ uint32_t byte_of(uint32_t w, int k) { return (w >> (8
 __device__ __forceinline__ float qf(uint32_t w, int b) {
   return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | uint32_t(b))) - 8388608.f;
 }
+// The helpers below hold inline PTX; their host branches (plain C++, the same values) let tests and tools compile
+// this header for the CPU.
 __device__ __forceinline__ float max3f(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
   float r;
   asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
   return r;
+#else
+  return fmaxf(fmaxf(a, b), c);
+#endif
 }
 __device__ __forceinline__ float min3f(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
   float r;
   asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
   return r;
+#else
+  return fminf(fminf(a, b), c);
+#endif
 }
 
 // Two floats in one 64-bit register pair, for the packed FP32 instructions (add / mul / fma .f32x2, sm_100 and
 // later): each half is rounded exactly as the scalar instruction rounds it.
 __device__ __forceinline__ unsigned long long pk2(float a, float b) {
+#if defined(__CUDA_ARCH__)
   unsigned long long r;
   asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
   return r;
+#else
+  return (unsigned long long)__float_as_uint(a) | ((unsigned long long)__float_as_uint(b) << 32);
+#endif
 }
-__device__ __forceinline__ void up2(unsigned long long r, float& a, float& b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r)); }
+__device__ __forceinline__ void up2(unsigned long long r, float& a, float& b) {
+#if defined(__CUDA_ARCH__)
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+#else
+  a = __uint_as_float(uint32_t(r)); b = __uint_as_float(uint32_t(r >> 32));
+#endif
+}
 __device__ __forceinline__ unsigned long long add2(unsigned long long a, unsigned long long b) {
+#if defined(__CUDA_ARCH__)
   unsigned long long r;
   asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
   return r;
+#else
+  float a0, a1, b0, b1;
+  up2(a, a0, a1); up2(b, b0, b1);
+  return pk2(a0 + b0, a1 + b1);
+#endif
 }
 __device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b, unsigned long long c) {
+#if defined(__CUDA_ARCH__)
   unsigned long long r;
   asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
   return r;
+#else
+  float a0, a1, b0, b1, c0, c1;
+  up2(a, a0, a1); up2(b, b0, b1); up2(c, c0, c1);
+  return pk2(fmaf(a0, b0, c0), fmaf(a1, b1, c1));
+#endif
 }
 __device__ __forceinline__ unsigned long long mul2(unsigned long long a, unsigned long long b) {
+#if defined(__CUDA_ARCH__)
   unsigned long long r;
   asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
   return r;
+#else
+  float a0, a1, b0, b1;
+  up2(a, a0, a1); up2(b, b0, b1);
+  return pk2(a0 * b0, a1 * b1);
+#endif
 }
 // Bytes b and b + 1 of w as the bit patterns 2^23 + q (see qf), packed.
 __device__ __forceinline__ unsigned long long qf2raw(uint32_t w, int b) {
@@ -305,13 +343,20 @@ struct Scene {
 
 // the GPU's nanosecond clock (kernels with a wall-time limit read it)
 __device__ __forceinline__ uint64_t clock_ns() {
+#if defined(__CUDA_ARCH__)
   uint64_t t;
   asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
   return t;
+#else
+  return 0;
+#endif
 }
 
 constexpr int kStack = 48;   // node-group stack entries (one per level at most)
-constexpr uint32_t kMaxVisits = 1u << 20;   // node visits of one query past which the traversal gives up (overflow bit 2)
+// Node visits of one query past which the traversal gives up (overflow bit 2): a query visits a node of a tree at
+// most once, so more than the node count (or 2^20) means a damaged walk; it ends at once instead of running on.
+constexpr uint32_t kMaxVisits = 1u << 20;
+__device__ __forceinline__ uint32_t visit_cap(const Scene& s) { return min(kMaxVisits, s.nNodes + 8u); }
 
 // Traversal counters of the instrumented kernels (nodes visited, triangles tested); compiled out otherwise.
 struct Count {
@@ -326,8 +371,9 @@ __device__ __forceinline__ void for_hits(const Scene& s, const Ray& r, float tmi
   uint2 stack[kStack];   // node group: x = childBase, y = imask << 8 | remaining inner children
   int sp = 0;
   uint32_t cur = 0;      // node to visit
+  const uint32_t cap = visit_cap(s);
   for (uint32_t visits = 0;; ++visits) {
-    if (visits >= kMaxVisits || cur >= s.nNodes) { overflow |= 2u; return; }
+    if (visits >= cap || cur >= s.nNodes) { overflow |= 2u; return; }
     uint4 n[5];
     load_node(s.nodes, cur, n);
     if (COUNT) ctr->nodes++;
@@ -385,8 +431,9 @@ __device__ __forceinline__ bool closest(const Scene& s, const Ray& r, float tmin
   bool any = false;
   float best = tmax;
   uint32_t cur = 0, visits = 0;
+  const uint32_t cap = visit_cap(s);
   for (;;) {
-    if (++visits > kMaxVisits || cur >= s.nNodes) { overflow |= 2u; return any; }
+    if (++visits > cap || cur >= s.nNodes) { overflow |= 2u; return any; }
     uint4 n[5];
     load_node(s.nodes, cur, n);
     float tn[8];

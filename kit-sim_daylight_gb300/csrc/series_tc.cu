@@ -17,8 +17,8 @@
 //  - the sun term (one direction per step, exact in the reference's float arithmetic) is added in the epilogue, where
 //    each output is finished in registers and stored with 16-byte row stores.
 //
-// Kernel k_series_tc, one CTA per SM, persistent over 128 x 64 output tiles (sensors x steps, steps fastest so that
-// the CTAs running at once share a few V panels and all of S in L2):
+// Kernel k_series_tc, one CTA per SM, persistent over 128 x 64 output tiles (sensors x steps) in bands of 16 step-tiles
+// (tile_coords), so that the CTAs running at once share a few V panels and the band's S panels in L2:
 //   warp 0      TMA producer: per 64-wide K block, the three pieces of V (128 x 64) and of S (64 x 64), bf16,
 //               128-byte swizzled, into a 3-stage shared-memory ring (72 KB a stage)
 //   warp 1      MMA issuer (one thread): 24 tcgen05.mma (M 128, N 64, K 16) per stage: hi.hi into H[chunk % 2], the
@@ -145,6 +145,17 @@ struct SeriesTcArgs {
   uint32_t* status;
 };
 
+// Tile order: bands of kBand step-tiles; within a band every row of tiles, steps fastest. The CTAs running at once share
+// a few V panels and the band's S panels (16 x 64 steps x K x 6 B, some 30 MB at K 4672), which stay in L2 for the
+// band; S is read from DRAM about once and V once per band (a steps-fastest order over all steps re-read S per row).
+constexpr uint32_t kBand = 16;
+__device__ __forceinline__ void tile_coords(uint32_t tile, uint32_t mTiles, uint32_t nTiles, uint32_t& m, uint32_t& n) {
+  const uint32_t perBand = mTiles * kBand, band = tile / perBand, idx = tile - band * perBand;
+  const uint32_t width = min(kBand, nTiles - band * kBand);
+  m = idx / width;
+  n = band * kBand + idx % width;
+}
+
 __device__ __forceinline__ float dotf_rn(const float* n, const float* d) {
   return __fadd_rn(__fadd_rn(__fmul_rn(n[0], d[0]), __fmul_rn(n[1], d[1])), __fmul_rn(n[2], d[2]));
 }
@@ -189,7 +200,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
     if (lane == 0) {   // ---------------- TMA producer
       uint32_t stage = 0, phase = 0;
       for (uint32_t tile = blockIdx.x; tile < nTilesAll && !abortFlag; tile += gridDim.x) {
-        const int m0 = int(tile / a.nTiles) * BM, n0 = int(tile % a.nTiles) * BN;
+        uint32_t tm, tn;
+        tile_coords(tile, a.mTiles, a.nTiles, tm, tn);
+        const int m0 = int(tm) * BM, n0 = int(tn) * BN;
         for (uint32_t kb = 0; kb < kBlocks; ++kb) {
           if (!mbar_wait(&empty[stage], phase ^ 1, a.status)) { abortFlag = 1; break; }
           uint8_t* s = smem + stage * STAGE_BYTES;
@@ -280,7 +293,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
         mbar_arrive(&hEmpty[hbuf]);
       }
       if (!ok || abortFlag) { abortFlag = 1; break; }
-      const uint32_t m0 = (tile / a.nTiles) * BM, n0 = (tile % a.nTiles) * BN;
+      uint32_t tm, tn;
+      tile_coords(tile, a.mTiles, a.nTiles, tm, tn);
+      const uint32_t m0 = tm * BM, n0 = tn * BN;
       const uint32_t row = m0 + q * 32 + lane;         // this thread's sensor
       float nrm[3] = {0.f, 0.f, 0.f};
       if (row < a.nc) { nrm[0] = a.N[3 * row]; nrm[1] = a.N[3 * row + 1]; nrm[2] = a.N[3 * row + 2]; }

@@ -118,7 +118,7 @@ __device__ uint8_t trace_byte(const Scene& s, const TraceArgs& a, F3 o, F3 n, F3
   return (uint8_t)__float2uint_rn(T * 255.f);
 }
 
-__global__ void __launch_bounds__(256, 3) k_bytes(TraceArgs a) {   // 3 blocks an SM (a few spills), measured faster
+__global__ void __launch_bounds__(256) k_bytes(TraceArgs a) {
   const Scene s{a.nodes, a.tris, a.nNodes};
   const bool cull = (a.rayFlags & KGB_RAY_CULL_BACK_FACING) != 0;
   const uint32_t lane = threadIdx.x & 31;
@@ -243,7 +243,7 @@ constexpr uint32_t kNoBin = 0xffffffffu;
 // One path per thread: sensor i = t % n, sample s0 + t / n. A path adds to at most one sky bin (where it escapes after
 // a reflection): it leaves that bin and its contribution (w x pi / M) in contrib[t], and k_bounce_accum adds them to
 // each sensor's rows in sample order, as the reference's per-sensor loop over samples does.
-__global__ void __launch_bounds__(128, 6) k_bounce_paths(BounceArgs a) {   // 6 blocks an SM (a few spills), measured faster
+__global__ void __launch_bounds__(128) k_bounce_paths(BounceArgs a) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= a.n * (a.s1 - a.s0)) return;
   const uint32_t i = t % a.n, smp = a.s0 + t / a.n;
@@ -266,7 +266,17 @@ __global__ void __launch_bounds__(128, 6) k_bounce_paths(BounceArgs a) {   // 6 
     if (clock_ns() - start > kBounceLimitNs) { late = true; break; }
     ++segments;
     ClosestOut c;
-    if (!closest(s, make_ray(o, d), 1e-5f, FLT_MAX, cull, c, overflow)) {
+    const bool found = closest(s, make_ray(o, d), 1e-5f, FLT_MAX, cull, c, overflow);
+    if (overflow & 2u) {   // the walk gave up: the first such path leaves its ray for the error message
+      uint32_t* diag = a.status + 15;   // ctl words 16..
+      if (atomicCAS(diag, 0u, 1u) == 0u) {
+        diag[1] = gi; diag[2] = smp; diag[3] = seg;
+        diag[4] = __float_as_uint(o.x); diag[5] = __float_as_uint(o.y); diag[6] = __float_as_uint(o.z);
+        diag[7] = __float_as_uint(d.x); diag[8] = __float_as_uint(d.y); diag[9] = __float_as_uint(d.z);
+      }
+      break;
+    }
+    if (!found) {
       if (reflected) { bin = sky_bin(d, a.mf, a.nBins, a.alpha, a.cosN, a.sinN); gain = w * weight; }
       break;
     }
