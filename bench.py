@@ -553,9 +553,10 @@ def run_serving(args, pkg):
                                             1000.0, reach=[6.0, 20.0, 50.0] if world else [], isoDim=3 if world else 0, label=scenes[r["scene"]]["label"],
                                             world=world, cull=world, groundZ=scenes[r["scene"]]["groundZ"]))
     for t in tickets:
-        srv.wait(t, 3600)
+        srv.wait(t, 240)
     wall = time.perf_counter() - t0
     st = srv.stats()
+    tm = srv.timing()
     srv.close()
     sensors = sum(len(r["P"]) for r in reqs)
     # the plain form: one request per launch, FIFO, through the single-request entry points (scenes parked and attached)
@@ -599,7 +600,9 @@ def run_serving(args, pkg):
             "config": {"workload": "serving: Poisson %.0f req/s for %.1f s (%d requests: %d daylight, %d views), 4 resident scenes of %s triangles, "
                                    "150 GB HBM budget" % (args.rate, args.window, len(reqs), sum(r["kind"] == "daylight" for r in reqs),
                                                          sum(r["kind"] == "views" for r in reqs), "/".join("%.1fM" % (len(s["tri"]) / 1e6) for s in scenes))},
-            "server": {k: st[k] for k in ("completed", "batches", "rays", "chunk_sensors", "batch_rays")}, "wall_s": wall}
+            "server": {k: st[k] for k in ("completed", "items", "rays", "chunk_sensors", "batch_rays")}, "wall_s": wall,
+            "gpu": {"daylight_s": tm["day_gpu_s"], "daylight_mrays_s": tm["day_rays"] / max(tm["day_gpu_s"], 1e-9) / 1e6, "views_s": tm["views_gpu_s"],
+                    "views_mrays_s": tm["views_rays"] / max(tm["views_gpu_s"], 1e-9) / 1e6, "queued_s": tm["queued_s"]}}
     print(json.dumps(line), flush=True)
 
 

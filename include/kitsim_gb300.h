@@ -217,10 +217,11 @@ KGB_API int kgb_sun_noaa(kgb_engine* e, const double* in, size_t T, double* out)
 
 /* --- serving (no reference counterpart: the reference runs one request at a time, src/run.cpp:35) ---------------- */
 /* A server keeps scenes resident and runs daylight and views requests of any size with continuous batching: requests
- * are admitted as the HBM budget allows, cut into sensor chunks, and every iteration packs chunks of all admitted
- * requests into one batch (daylight: one persistent any-hit launch + one multi-quantity reduce, a CUDA graph; views:
- * the view kernels per chunk). Results equal the single-request entry points' bit for bit. A request's host arrays
- * must stay valid until kgb_server_wait returns for it. */
+ * are admitted as the HBM budget allows and cut into work items that run back to back on one stream, two queued at a
+ * time, picked by a priority (remaining work over age plus 0.3 s): daylight batches packing chunks of any number of
+ * requests (one persistent any-hit launch + one multi-quantity reduce, a CUDA graph) and views chunks (the view
+ * kernels on a range of one request's sensors). Results equal the single-request entry points' bit for bit. A
+ * request's host arrays must stay valid until kgb_server_wait returns for it. */
 typedef struct kgb_server kgb_server;
 typedef struct kgb_daylight_request {
   int32_t scene;
@@ -256,12 +257,19 @@ KGB_API void kgb_server_destroy(kgb_server* s);
 KGB_API int kgb_server_add_scene(kgb_server* s, const float* v, size_t nv, const uint32_t* tri, size_t nt, int32_t* sceneId);
 /* times calibration batches on scene 0 and keeps the fastest chunk and batch sizes (call while idle) */
 KGB_API int kgb_server_autotune(kgb_server* s);
+/* sets by hand what the autotuner picks (call while idle; 0 keeps a value): sensors per daylight chunk (32..2^20), rays
+ * per daylight batch (2^16..2^32) and rays per views chunk (2^16..2^31, default 2^27) */
+KGB_API int kgb_server_set_tuning(kgb_server* s, uint32_t chunkSensors, uint64_t batchRays, uint64_t viewRays);
 KGB_API int kgb_server_submit(kgb_server* s, const kgb_daylight_request* r, uint64_t* ticket);
 KGB_API int kgb_server_submit_views(kgb_server* s, const kgb_views_request* r, uint64_t* ticket);
 /* 1 once the request completed (its out written), 0 on failure or timeout (kgb_last_error) */
 KGB_API int kgb_server_wait(kgb_server* s, uint64_t ticket, double timeoutSec);
-/* out[10]: completed requests, latency p50, p90, p99, max (s), rays, batches, HBM bytes in use, chunk sensors, batch rays */
+/* out[10]: completed requests, latency p50, p90, p99, max (s), rays, work items (daylight batches and views chunks), HBM
+ * bytes in use, chunk sensors, batch rays */
 KGB_API void kgb_server_stats(kgb_server* s, double* out);
+/* out[5]: GPU seconds and rays of daylight batches, the same of views chunks (events around each item on the work
+ * stream), and wall seconds with work queued on it */
+KGB_API void kgb_server_timing(kgb_server* s, double* out);
 
 /* --- no reference counterpart ---------------------------------------------------------------------------------- */
 /* The CUDA stream (a cudaStream_t) the engine's work runs on from now on; NULL: the engine's own stream. Calls still

@@ -1,17 +1,25 @@
 // The serving loop: device-resident scenes, and daylight / views requests of any size admitted against an HBM budget
-// and run with continuous batching. A request is cut into chunks of sensors. Every iteration of the server thread
-// admits what the budget allows, then packs chunks of the admitted requests (round robin, so a short request is not held
-// behind a long one) into one batch:
-//  - daylight chunks: ONE persistent any-hit launch over every chunk of the batch (k_bits_batch: tasks of 32 sensors x
-//    one 32-direction word, each task finds its chunk in the batch's segment table) and ONE reduce launch giving every
-//    quantity of every chunk (k_reduce_batch). The batch's pipeline (segment table up, counter reset, the two kernels,
-//    the sums down) is a CUDA graph captured once and replayed per batch: its pointers never change, the table does;
-//  - views chunks: the view kernels (k_view, k_view_reduce, k_iso) on each chunk, between the daylight batches.
-// A request completes when its last chunk has; its results are bit-identical to the request run alone through the
-// single-request entry points (same kernels, same per-sensor arithmetic and summation order).
+// and run with continuous batching.
 //
-// The autotuner times calibration batches on the first scene at start-up and keeps the fastest chunk size and batch
-// size (rays per batch) for the daylight pipeline.
+// Requests are cut into work items that run one after another on one work stream, two of them queued at a time so that
+// the GPU never waits for the host:
+//  - a daylight batch: chunks of sensors of any number of admitted daylight requests, traced by ONE persistent any-hit
+//    launch (k_bits_batch: tasks of 32 sensors x one 32-direction word, each task finds its chunk in the batch's
+//    segment table) and reduced by ONE launch giving every quantity of every chunk (k_reduce_batch). The batch's
+//    pipeline (segment table up, counter reset, the two kernels, the sums and the status down into pinned memory) is a
+//    CUDA graph built once per slot and replayed per batch, its copy sizes and the reduce's grid set per batch;
+//  - a views chunk: the view kernels (k_view, k_view_reduce, k_iso) on a range of one request's sensors, sized by rays.
+// The scheduler picks the next item by a priority over every request with sensors not yet issued: its remaining work
+// (rays times a running estimate of seconds per ray of its kind, measured from the items' own GPU time) divided by its
+// age plus 0.3 s. Short requests overtake long ones, and a long one's priority grows as it waits, which keeps the p50
+// near one item's time while bounding the p99. A daylight batch is packed in that order, a chunk at a time.
+// Admitted requests' inputs go up on a separate upload stream into stream-ordered allocations from the server's own
+// memory pool, so neither uploads nor frees wait for the work stream. A request completes when its last item has; its
+// results are bit-identical to the request run alone through the single-request entry points (same kernels, same
+// per-sensor arithmetic and summation order).
+//
+// The autotuner times calibration batches on the first scene at start-up and keeps the chunk size and batch size
+// (rays per batch) for the daylight pipeline: the fastest, or a smaller batch within 5 % of it.
 #include "engine.h"
 #include "rt.cuh"
 
@@ -108,16 +116,22 @@ __global__ void __launch_bounds__(256) k_reduce_batch(const BatchHdr* hdr, const
   for (uint32_t q = 0; q < g.nQ; ++q) outPool[g.outOff + size_t(q) * g.n + i] = acc[q];
 }
 
+
 // ------------------------------------------------------------------------------------------------ host side
 namespace {
 using Clock = std::chrono::steady_clock;
+
+constexpr int kSlots = 2;                       // work items of each kind that can be in flight at once
+constexpr size_t kDepth = 2;                    // work items queued on the work stream at once
+constexpr uint32_t kMaxViewChunk = 65536;       // sensors in one views chunk
+constexpr uint32_t kMaxNA = 3 * KGB_VIEW_CLASSES + 1 + 8 + 1 + 1;   // views columns
+constexpr double kAgeSeconds = 0.3;             // the priority's age offset
 
 struct DScene {
   void* nodes = nullptr;
   void* tris = nullptr;
   uint32_t nNodes = 0, nTris = 0;
   uint64_t bytes = 0;
-  void* label = nullptr;   // views labels of the last views request on this scene (device, nTris)
 };
 
 struct Request {
@@ -127,37 +141,72 @@ struct Request {
   kgb_views_request v{};
   std::vector<float> rowSin;
   std::vector<double> wRow;
-  std::vector<float> reach;
   std::vector<double> w64;    // daylight: the weights widened to double (the source of their upload)
   uint32_t nSensors = 0, nextSensor = 0, doneSensors = 0;
-  void* dev = nullptr;        // P, N, D, ray table, W (daylight) | P, N, rowSin, wRow, label, cls, dist, out (views)
+  uint64_t raysPerSensor = 0;
+  void* dev = nullptr;        // P, N, D, ray table, W (daylight) | P, N, rowSin, wRow, label (views)
   uint64_t devBytes = 0;
   Clock::time_point tSubmit, tDone;
   bool done = false, failed = false;
   std::string err;
 };
+
+struct Part { Request* r; uint32_t i0, n; };
+
+// a daylight batch slot: its pinned and device buffers, its graph and the nodes set per batch
+struct DaySlot {
+  Seg* hSegs = nullptr;         // pinned [kMaxSegs]
+  BatchHdr* hHdr = nullptr;     // pinned
+  uint32_t* hStatus = nullptr;  // pinned
+  double* hOut = nullptr;       // pinned [outPoolDoubles]
+  Seg* dSegs = nullptr;
+  BatchHdr* dHdr = nullptr;
+  uint32_t* dCtl = nullptr;     // counter, status
+  uint32_t* dBits = nullptr;
+  double* dOut = nullptr;
+  cudaGraph_t graph = nullptr;      // kept: the nodes set per batch belong to it
+  cudaGraphExec_t exec = nullptr;
+  cudaGraphNode_t nSegs = nullptr, nReduce = nullptr, nOut = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  std::vector<Part> parts;
+  uint64_t rays = 0;
+};
+// a views chunk slot: its status and columns come back into pinned memory
+struct ViewSlot {
+  uint32_t* dCtl = nullptr;
+  uint32_t* hStatus = nullptr;
+  double* hOut = nullptr;       // pinned [kMaxViewChunk x kMaxNA]
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  Part part{nullptr, 0, 0};
+  uint32_t NA = 0;
+};
 }  // namespace
 
 struct Server {
-  int device = 0, numSMs = 0;
-  cudaStream_t st = nullptr;
+  int device = 0, numSMs = 0, gridBits = 0, gridView = 0;
+  cudaStream_t st = nullptr;    // work stream: daylight batches and views chunks in the scheduler's order
+  cudaStream_t up = nullptr;    // uploads of admitted requests' inputs
+  cudaEvent_t upDone = nullptr;
+  bool upPending = false;       // uploads issued that the work stream has not been made to wait for
+  cudaMemPool_t pool = nullptr; // requests' device memory
   uint64_t budget = 0, used = 0;
   std::vector<DScene> scenes;
-  // batch pools (fixed for the graph)
+  // tuning
   uint32_t chunkSensors = 8192;
-  uint64_t batchRays = uint64_t(1) << 30;
+  uint64_t batchRays = uint64_t(1) << 28;
+  uint64_t viewRays = uint64_t(1) << 27;
+  // batch pools (fixed for the graphs)
   size_t bitsPoolWords = 0, outPoolDoubles = 0;
-  uint32_t* dBits = nullptr;
-  double* dOut = nullptr;
-  double* hOut = nullptr;            // pinned
-  Seg* hSegs = nullptr;              // pinned [kMaxSegs]
-  BatchHdr* hHdr = nullptr;          // pinned
-  Seg* dSegs = nullptr;
-  BatchHdr* dHdr = nullptr;
-  uint32_t* dCtl = nullptr;          // counter, status
-  cudaGraphExec_t graph = nullptr;
-  int gridBits = 0;
   uint32_t maxSensPerBatch = 0;
+  uint64_t poolBytes = 0;
+  DaySlot day[kSlots];
+  ViewSlot view[kSlots];
+  uint8_t* dCls = nullptr;      // views scratch for one chunk (chunks run in stream order): classes, distances, columns
+  float* dDist = nullptr;
+  double* dViewOut = nullptr;
+  uint64_t viewCap = 0;         // rays the scratch holds
+  std::deque<std::pair<int, int>> inflight;   // (kind, slot), in launch order
+  double cost[2] = {1e-10, 3e-10};            // seconds per ray of daylight and views work (running estimate)
   // requests
   std::mutex m;
   std::condition_variable cv, doneCv;
@@ -165,12 +214,13 @@ struct Server {
   std::vector<Request*> active;
   std::map<uint64_t, Request*> all;
   uint64_t nextTicket = 1;
-  size_t rr = 0;
   bool stop = false;
   std::thread th;
   std::vector<double> latencies;   // seconds, completed requests
-  uint64_t batches = 0, rays = 0;
-  std::string fatal;
+  uint64_t items = 0, rays = 0;
+  double gpuSec[2] = {0, 0}, kindRays[2] = {0, 0};   // GPU seconds and rays of daylight batches and views chunks
+  double queuedSec = 0;                             // wall seconds with at least one item on the work stream
+  Clock::time_point queuedSince;
 };
 
 namespace {
@@ -180,63 +230,103 @@ bool cuok(cudaError_t e, std::string& err, const char* what) {
   err = std::string(what) + ": " + cudaGetErrorString(e);
   return false;
 }
+size_t up256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // a daylight request's device arrays: P, N (12 B per sensor each), D (12 B per direction), its ray table (48 B per
 // direction), its weights as doubles [nQ x nDir]; 256-byte aligned pieces
 struct DayLayout { size_t offN, offD, offTab, offW, total; };
 DayLayout day_layout(const kgb_daylight_request& d) {
-  const auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
   DayLayout L;
   L.offN = size_t(d.nSensors) * 12;
-  L.offD = up(2 * L.offN);
-  L.offTab = up(L.offD + size_t(d.nDir) * 12);
-  L.offW = up(L.offTab + size_t(d.nDir) * 48);
-  L.total = up(L.offW + size_t(d.nQ) * d.nDir * 8);
+  L.offD = up256(2 * L.offN);
+  L.offTab = up256(L.offD + size_t(d.nDir) * 12);
+  L.offW = up256(L.offTab + size_t(d.nDir) * 48);
+  L.total = up256(L.offW + size_t(d.nQ) * d.nDir * 8);
   return L;
 }
-
-uint64_t daylight_bytes(const kgb_daylight_request& r) { return day_layout(r).total; }
+// a views request's device arrays: P, N, rowSin [nEl x 2], wRow [nEl], labels [scene triangles] (when given)
+struct ViewLayout { size_t offN, offRow, offW, offLab, total; };
+ViewLayout view_layout(const kgb_views_request& v, uint32_t nTris) {
+  ViewLayout L;
+  L.offN = size_t(v.nSensors) * 12;
+  L.offRow = up256(2 * L.offN);
+  L.offW = up256(L.offRow + size_t(v.view.nEl) * 8);
+  L.offLab = up256(L.offW + size_t(v.view.nEl) * 8);
+  L.total = up256(L.offLab + (v.label ? nTris : 0));
+  return L;
+}
 uint32_t views_NA(const kgb_views_request& r) { return 3 * r.nClass + 1 + r.nReach + (r.glazing ? 1 : 0) + (r.isoDim ? 1 : 0); }
-uint64_t views_bytes(const kgb_views_request& r, uint32_t chunk, uint32_t nTris) {
-  const uint64_t K = uint64_t(r.view.nAz) * r.view.nEl;
-  return uint64_t(r.nSensors) * 24 + uint64_t(r.view.nEl) * 16 + (r.label ? nTris : 0) + uint64_t(chunk) * (5 * K + 8 * views_NA(r)) + 4096;
+uint64_t request_bytes(const Server& s, const Request* r) {
+  return r->kind == 0 ? day_layout(r->d).total : view_layout(r->v, s.scenes[size_t(r->v.scene)].nTris).total;
 }
 
-// graph of one daylight batch: table up, counter reset, trace, reduce, sums down
-bool capture(Server& s, std::string& err) {
-  cudaGraph_t gph;
-  if (!cuok(cudaStreamBeginCapture(s.st, cudaStreamCaptureModeThreadLocal), err, "capture")) return false;
-  cudaMemcpyAsync(s.dHdr, s.hHdr, sizeof(BatchHdr), cudaMemcpyHostToDevice, s.st);
-  cudaMemcpyAsync(s.dSegs, s.hSegs, sizeof(Seg) * kMaxSegs, cudaMemcpyHostToDevice, s.st);
-  cudaMemsetAsync(s.dCtl, 0, 8, s.st);
-  k_bits_batch<<<s.gridBits, 256, 0, s.st>>>(s.dHdr, s.dSegs, s.dBits, s.dCtl, s.dCtl + 1);
-  k_reduce_batch<<<(s.maxSensPerBatch + 255) / 256, 256, 0, s.st>>>(s.dHdr, s.dSegs, s.dBits, s.dOut);
-  cudaMemcpyAsync(s.hOut, s.dOut, sizeof(double) * s.outPoolDoubles, cudaMemcpyDeviceToHost, s.st);
-  if (!cuok(cudaStreamEndCapture(s.st, &gph), err, "capture end")) return false;
-  if (s.graph) cudaGraphExecDestroy(s.graph);
-  const bool ok = cuok(cudaGraphInstantiate(&s.graph, gph, 0), err, "graph instantiate");
-  cudaGraphDestroy(gph);
+// one slot's graph: table up, counter reset, trace, reduce, sums and status down
+bool build_graph(Server& s, DaySlot& d, std::string& err) {
+  if (d.exec) { cudaGraphExecDestroy(d.exec); d.exec = nullptr; }
+  if (d.graph) { cudaGraphDestroy(d.graph); d.graph = nullptr; }
+  if (!cuok(cudaGraphCreate(&d.graph, 0), err, "graph")) return false;
+  cudaGraph_t g = d.graph;
+  cudaGraphNode_t nHdr, nCtl, nBits, nStatus;
+  uint32_t* status = d.dCtl + 1;
+  void* aBits[] = {&d.dHdr, &d.dSegs, &d.dBits, &d.dCtl, &status};
+  void* aRed[] = {&d.dHdr, &d.dSegs, &d.dBits, &d.dOut};
+  cudaKernelNodeParams kb{};
+  kb.func = reinterpret_cast<void*>(k_bits_batch); kb.gridDim = dim3(unsigned(s.gridBits)); kb.blockDim = dim3(256); kb.kernelParams = aBits;
+  cudaKernelNodeParams kr{};
+  kr.func = reinterpret_cast<void*>(k_reduce_batch); kr.gridDim = dim3((s.maxSensPerBatch + 255) / 256); kr.blockDim = dim3(256);
+  kr.kernelParams = aRed;
+  cudaMemsetParams ms{};
+  ms.dst = d.dCtl; ms.value = 0; ms.elementSize = 4; ms.width = 2; ms.height = 1;
+  bool ok = cuok(cudaGraphAddMemcpyNode1D(&nHdr, g, nullptr, 0, d.dHdr, d.hHdr, sizeof(BatchHdr), cudaMemcpyHostToDevice), err, "graph") &&
+            cuok(cudaGraphAddMemcpyNode1D(&d.nSegs, g, &nHdr, 1, d.dSegs, d.hSegs, sizeof(Seg) * kMaxSegs, cudaMemcpyHostToDevice), err, "graph") &&
+            cuok(cudaGraphAddMemsetNode(&nCtl, g, &d.nSegs, 1, &ms), err, "graph") &&
+            cuok(cudaGraphAddKernelNode(&nBits, g, &nCtl, 1, &kb), err, "graph") &&
+            cuok(cudaGraphAddKernelNode(&d.nReduce, g, &nBits, 1, &kr), err, "graph") &&
+            cuok(cudaGraphAddMemcpyNode1D(&d.nOut, g, &d.nReduce, 1, d.hOut, d.dOut, sizeof(double) * s.outPoolDoubles, cudaMemcpyDeviceToHost), err, "graph") &&
+            cuok(cudaGraphAddMemcpyNode1D(&nStatus, g, &d.nOut, 1, d.hStatus, status, 4, cudaMemcpyDeviceToHost), err, "graph") &&
+            cuok(cudaGraphInstantiate(&d.exec, g, 0), err, "graph instantiate");
   return ok;
 }
 
+void free_pools(Server& s) {
+  for (DaySlot& d : s.day) {
+    if (d.exec) cudaGraphExecDestroy(d.exec);
+    if (d.graph) cudaGraphDestroy(d.graph);
+    cudaFree(d.dBits); cudaFree(d.dOut);
+    if (d.hOut) cudaFreeHost(d.hOut);
+    d.graph = nullptr; d.exec = nullptr; d.dBits = nullptr; d.dOut = nullptr; d.hOut = nullptr;
+  }
+  cudaFree(s.dCls); cudaFree(s.dDist);
+  s.dCls = nullptr; s.dDist = nullptr;
+  s.used -= s.poolBytes;
+  s.poolBytes = 0;
+}
+
+// the pools that depend on the tuning: each day slot's bits and sums (device) and sums (pinned), and its graph; the
+// views scratch
 bool make_pools(Server& s, std::string& err) {
-  if (s.dBits) { cudaFree(s.dBits); cudaFree(s.dOut); s.used -= s.bitsPoolWords * 4 + s.outPoolDoubles * 8; }
+  free_pools(s);
   s.maxSensPerBatch = std::min<uint32_t>(kMaxSegs * s.chunkSensors, 1u << 20);
   // bits of a batch: rays / 32 words, plus a word per sensor and segment for the rounding up of each chunk's words
   s.bitsPoolWords = size_t(s.batchRays / 32) + size_t(s.maxSensPerBatch) * 2;
   s.outPoolDoubles = size_t(s.maxSensPerBatch) * kMaxQ;
-  if (!cuok(cudaMalloc(&s.dBits, s.bitsPoolWords * 4), err, "batch pool") || !cuok(cudaMalloc(&s.dOut, s.outPoolDoubles * 8), err, "batch pool"))
+  s.viewCap = std::max<uint64_t>(s.viewRays, uint64_t(1) << 16);
+  for (DaySlot& d : s.day)
+    if (!cuok(cudaMalloc(&d.dBits, s.bitsPoolWords * 4), err, "batch pool") || !cuok(cudaMalloc(&d.dOut, s.outPoolDoubles * 8), err, "batch pool") ||
+        !cuok(cudaMallocHost(&d.hOut, s.outPoolDoubles * 8), err, "pinned pool") || !build_graph(s, d, err))
+      return false;
+  if (!cuok(cudaMalloc(&s.dCls, s.viewCap), err, "views scratch") || !cuok(cudaMalloc(&s.dDist, s.viewCap * 4), err, "views scratch"))
     return false;
-  s.used += s.bitsPoolWords * 4 + s.outPoolDoubles * 8;
-  if (s.hOut) cudaFreeHost(s.hOut);
-  if (!cuok(cudaMallocHost(&s.hOut, s.outPoolDoubles * 8), err, "pinned pool")) return false;
-  return capture(s, err);
+  s.poolBytes = kSlots * (s.bitsPoolWords * 4 + s.outPoolDoubles * 8) + s.viewCap * 5;
+  s.used += s.poolBytes;
+  return true;
 }
 
 void finish(Server& s, Request* r, bool ok, const std::string& err) {
-  if (r->dev) cudaFree(r->dev);
+  if (r->dev) cudaFreeAsync(r->dev, s.st);   // after every item queued on the work stream, the last users of it
   s.used -= r->devBytes;
   r->dev = nullptr;
+  r->devBytes = 0;
   r->tDone = Clock::now();
   r->failed = !ok;
   r->err = err;
@@ -244,193 +334,293 @@ void finish(Server& s, Request* r, bool ok, const std::string& err) {
   if (ok) s.latencies.push_back(std::chrono::duration<double>(r->tDone - r->tSubmit).count());
 }
 
-// device copies of a request's inputs
+// a request's inputs up on the upload stream, into memory from the server's pool (r->devBytes, reserved at admission)
 bool upload(Server& s, Request* r, std::string& err) {
+  if (!cuok(cudaMallocFromPoolAsync(&r->dev, r->devBytes, s.pool, s.up), err, "request memory")) { r->dev = nullptr; return false; }
+  char* b = static_cast<char*>(r->dev);
+  bool ok = true;
   if (r->kind == 0) {
     const kgb_daylight_request& d = r->d;
     const DayLayout L = day_layout(d);
-    r->devBytes = L.total;
-    if (!cuok(cudaMalloc(&r->dev, r->devBytes), err, "request memory")) return false;
-    char* b = static_cast<char*>(r->dev);
     r->w64.resize(size_t(d.nQ) * d.nDir);
     const float* W = static_cast<const float*>(d.W);
     for (size_t k = 0; k < r->w64.size(); ++k) r->w64[k] = double(W[k]);
-    cudaMemcpyAsync(b, d.P, L.offN, cudaMemcpyHostToDevice, s.st);
-    cudaMemcpyAsync(b + L.offN, d.N, L.offN, cudaMemcpyHostToDevice, s.st);
-    cudaMemcpyAsync(b + L.offD, d.D, size_t(d.nDir) * 12, cudaMemcpyHostToDevice, s.st);
-    cudaMemcpyAsync(b + L.offW, r->w64.data(), r->w64.size() * 8, cudaMemcpyHostToDevice, s.st);
-    launch_ray_table(reinterpret_cast<const float*>(b + L.offD), d.nDir, b + L.offTab, s.st);
+    ok = cuok(cudaMemcpyAsync(b, d.P, L.offN, cudaMemcpyHostToDevice, s.up), err, "upload") &&
+         cuok(cudaMemcpyAsync(b + L.offN, d.N, L.offN, cudaMemcpyHostToDevice, s.up), err, "upload") &&
+         cuok(cudaMemcpyAsync(b + L.offD, d.D, size_t(d.nDir) * 12, cudaMemcpyHostToDevice, s.up), err, "upload") &&
+         cuok(cudaMemcpyAsync(b + L.offW, r->w64.data(), r->w64.size() * 8, cudaMemcpyHostToDevice, s.up), err, "upload");
+    if (ok) launch_ray_table(reinterpret_cast<const float*>(b + L.offD), d.nDir, b + L.offTab, s.up);
   } else {
     const kgb_views_request& v = r->v;
-    const DScene& sc = s.scenes[size_t(v.scene)];
-    const uint64_t K = uint64_t(v.view.nAz) * v.view.nEl;
-    const size_t offN = size_t(v.nSensors) * 12, offRow = (offN * 2 + 255) & ~size_t(255), offW = offRow + size_t(v.view.nEl) * 8;
-    const size_t offLab = (offW + size_t(v.view.nEl) * 8 + 255) & ~size_t(255), offCls = (offLab + (v.label ? sc.nTris : 0) + 255) & ~size_t(255);
-    const size_t offDist = (offCls + s.chunkSensors * K + 255) & ~size_t(255), offOut = (offDist + s.chunkSensors * K * 4 + 255) & ~size_t(255);
-    r->devBytes = offOut + size_t(s.chunkSensors) * views_NA(v) * 8;
-    if (!cuok(cudaMalloc(&r->dev, r->devBytes), err, "request memory")) return false;
-    char* b = static_cast<char*>(r->dev);
-    cudaMemcpyAsync(b, v.P, offN, cudaMemcpyHostToDevice, s.st);
-    cudaMemcpyAsync(b + offN, v.N, offN, cudaMemcpyHostToDevice, s.st);
-    cudaMemcpyAsync(b + offRow, r->rowSin.data(), size_t(v.view.nEl) * 8, cudaMemcpyHostToDevice, s.st);
-    cudaMemcpyAsync(b + offW, r->wRow.data(), size_t(v.view.nEl) * 8, cudaMemcpyHostToDevice, s.st);
-    if (v.label) cudaMemcpyAsync(b + offLab, v.label, sc.nTris, cudaMemcpyHostToDevice, s.st);
+    const ViewLayout L = view_layout(v, s.scenes[size_t(v.scene)].nTris);
+    ok = cuok(cudaMemcpyAsync(b, v.P, L.offN, cudaMemcpyHostToDevice, s.up), err, "upload") &&
+         cuok(cudaMemcpyAsync(b + L.offN, v.N, L.offN, cudaMemcpyHostToDevice, s.up), err, "upload") &&
+         cuok(cudaMemcpyAsync(b + L.offRow, r->rowSin.data(), size_t(v.view.nEl) * 8, cudaMemcpyHostToDevice, s.up), err, "upload") &&
+         cuok(cudaMemcpyAsync(b + L.offW, r->wRow.data(), size_t(v.view.nEl) * 8, cudaMemcpyHostToDevice, s.up), err, "upload") &&
+         (!v.label || cuok(cudaMemcpyAsync(b + L.offLab, v.label, s.scenes[size_t(v.scene)].nTris, cudaMemcpyHostToDevice, s.up), err, "upload"));
   }
-  s.used += r->devBytes;
-  return true;
+  s.upPending = true;
+  return ok && cuok(cudaGetLastError(), err, "upload");
 }
 
-// one views chunk of a request: the single-request view kernels on its device arrays
-bool run_views_chunk(Server& s, Request* r, uint32_t i0, uint32_t nc, std::string& err) {
-  const kgb_views_request& v = r->v;
-  const DScene& sc = s.scenes[size_t(v.scene)];
-  const uint64_t K = uint64_t(v.view.nAz) * v.view.nEl;
-  const size_t offN = size_t(v.nSensors) * 12, offRow = (offN * 2 + 255) & ~size_t(255), offW = offRow + size_t(v.view.nEl) * 8;
-  const size_t offLab = (offW + size_t(v.view.nEl) * 8 + 255) & ~size_t(255), offCls = (offLab + (v.label ? sc.nTris : 0) + 255) & ~size_t(255);
-  const size_t offDist = (offCls + s.chunkSensors * K + 255) & ~size_t(255), offOut = (offDist + s.chunkSensors * K * 4 + 255) & ~size_t(255);
-  char* b = static_cast<char*>(r->dev);
-  const double rad = v.view.north * KGB_PI_D / 180;
-  ViewArgs a{};
-  a.nodes = static_cast<const Node8*>(sc.nodes); a.tris = static_cast<const TriRec*>(sc.tris); a.nNodes = sc.nNodes;
-  a.P = reinterpret_cast<const float*>(b); a.N = reinterpret_cast<const float*>(b + offN);
-  a.first = i0; a.n = nc; a.out0 = 0; a.stride = nc; a.i0 = i0;
-  a.K = uint32_t(K); a.nWords = uint32_t((K + 31) / 32); a.nAz = v.view.nAz; a.nEl = v.view.nEl; a.rayFlags = v.rayFlags;
-  a.rowSin = reinterpret_cast<const float*>(b + offRow); a.az0 = v.view.az0; a.dAz = v.view.dAz; a.groundZ = v.view.groundZ;
-  a.cosN = float(std::cos(rad)); a.sinN = float(std::sin(rad));
-  a.world = v.view.world ? 1 : 0; a.cull = v.view.cull ? 1 : 0; a.jitter = v.view.jitter ? 1 : 0; a.nS = v.view.nS; a.back = v.view.back ? 1 : 0;
-  a.vground = v.view.vground ? 1 : 0;
-  a.label = v.label ? reinterpret_cast<const uint8_t*>(b + offLab) : nullptr;
-  a.cls = reinterpret_cast<uint8_t*>(b + offCls); a.dist = reinterpret_cast<float*>(b + offDist);
-  a.counter = s.dCtl; a.status = s.dCtl + 1;
-  cudaMemsetAsync(s.dCtl, 0, 8, s.st);
-  launch_view(a, s.numSMs * 4, s.st);
-  ViewReduceArgs ra{};
-  ra.cls = a.cls; ra.dist = a.dist; ra.nc = nc; ra.K = uint32_t(K); ra.nAz = v.view.nAz; ra.nEl = v.view.nEl; ra.nClass = v.nClass;
-  ra.nReach = v.nReach; ra.glazing = v.glazing ? 1 : 0; ra.iso = v.isoDim ? 1 : 0; ra.NA = views_NA(v);
-  ra.wRow = reinterpret_cast<const double*>(b + offW); ra.farDist = float(v.farDist); ra.lnFar = std::log(v.farDist);
-  for (uint32_t k = 0; k < v.nReach; ++k) ra.reach[k] = v.reach[k];
-  ra.isoDim = v.isoDim; ra.world = a.world; ra.jitter = a.jitter; ra.i0 = i0; ra.nS = v.view.nS; ra.back = a.back;
-  ra.az0 = v.view.az0; ra.dAz = v.view.dAz; ra.rowSin = a.rowSin; ra.out = reinterpret_cast<double*>(b + offOut);
-  launch_reduce_view(ra, s.st);
-  cudaMemcpyAsync(v.out + size_t(i0) * ra.NA, ra.out, size_t(nc) * ra.NA * 8, cudaMemcpyDeviceToHost, s.st);
-  uint32_t status = 0;
-  cudaMemcpyAsync(&status, s.dCtl + 1, 4, cudaMemcpyDeviceToHost, s.st);
-  if (!cuok(cudaStreamSynchronize(s.st), err, "views chunk")) return false;
-  if (status) { err = "views chunk: traversal stack overflow"; return false; }
-  s.rays += uint64_t(nc) * K;
-  return true;
-}
-
-struct Part { Request* r; uint32_t i0, n; };
-
-// one daylight batch through the graph; parts' results scattered into their requests' outputs
-bool run_daylight_batch(Server& s, const std::vector<Part>& parts, std::string& err) {
-  uint32_t tasks = 0, sens = 0;
-  size_t bits = 0, out = 0;
-  for (size_t k = 0; k < parts.size(); ++k) {
-    const Part& p = parts[k];
-    const kgb_daylight_request& d = p.r->d;
-    const DScene& sc = s.scenes[size_t(d.scene)];
-    const char* b = static_cast<const char*>(p.r->dev);
-    const DayLayout L = day_layout(d);
-    Seg& g = s.hSegs[k];
-    g.nodes = static_cast<const Node8*>(sc.nodes); g.tris = static_cast<const TriRec*>(sc.tris); g.nNodes = sc.nNodes;
-    g.P = reinterpret_cast<const float*>(b) + 3 * size_t(p.i0); g.N = reinterpret_cast<const float*>(b + L.offN) + 3 * size_t(p.i0);
-    g.D = reinterpret_cast<const float*>(b + L.offD); g.tab = reinterpret_cast<const RayDir*>(b + L.offTab);
-    g.W = reinterpret_cast<const double*>(b + L.offW);
-    g.nDir = d.nDir; g.nWords = (d.nDir + 31) / 32; g.n = p.n; g.rayFlags = d.rayFlags; g.nQ = d.nQ; g.useCosMask = d.useCosMask;
-    g.taskBase = tasks; g.sensBase = sens; g.bitsOff = uint32_t(bits); g.outOff = uint32_t(out);
-    tasks += (p.n + 31) / 32 * g.nWords;
-    sens += p.n;
-    bits += size_t(g.nWords) * p.n;
-    out += size_t(d.nQ) * p.n;
-  }
-  if (bits > s.bitsPoolWords || out > s.outPoolDoubles || sens > s.maxSensPerBatch) { err = "internal: batch beyond its pools"; return false; }
-  s.hHdr->nSegs = uint32_t(parts.size()); s.hHdr->nTasks = tasks; s.hHdr->nSens = sens;
-  if (!cuok(cudaGraphLaunch(s.graph, s.st), err, "batch graph") || !cuok(cudaStreamSynchronize(s.st), err, "batch")) return false;
-  uint32_t status = 0;
-  cudaMemcpy(&status, s.dCtl + 1, 4, cudaMemcpyDeviceToHost);
-  if (status) { err = "batch: traversal stack overflow"; return false; }
-  for (size_t k = 0; k < parts.size(); ++k) {
-    const Part& p = parts[k];
-    const Seg& g = s.hSegs[k];
-    for (uint32_t q = 0; q < g.nQ; ++q)
-      std::memcpy(p.r->d.out + size_t(q) * p.r->nSensors + p.i0, s.hOut + g.outOff + size_t(q) * p.n, size_t(p.n) * 8);
-    s.rays += uint64_t(p.n) * g.nDir;
-  }
-  ++s.batches;
-  return true;
-}
-
-// one iteration: admit, pack, run; false when there was nothing to do
-bool step(Server& s) {
+// admission: pending requests in arrival order while the budget allows (a lone request always runs), inputs uploaded
+void admit(Server& s) {
   std::vector<Request*> admitted;
   {
-    std::unique_lock<std::mutex> lk(s.m);
+    std::lock_guard<std::mutex> lk(s.m);
     while (!s.pending.empty()) {
       Request* r = s.pending.front();
-      const uint64_t need = r->kind == 0 ? daylight_bytes(r->d) : views_bytes(r->v, s.chunkSensors, s.scenes[size_t(r->v.scene)].nTris);
-      if (s.used + need > s.budget && !s.active.empty()) break;   // wait for memory (a lone request always runs)
+      const uint64_t need = request_bytes(s, r);
+      if (s.used + need > s.budget && !s.active.empty()) break;
       s.pending.pop_front();
+      r->devBytes = need;
+      s.used += need;
       admitted.push_back(r);
       s.active.push_back(r);
     }
   }
+  if (admitted.empty()) return;
   for (Request* r : admitted) {
     std::string err;
-    if (!upload(s, r, err)) { std::lock_guard<std::mutex> lk(s.m); finish(s, r, false, err); s.doneCv.notify_all(); }
-  }
-  std::vector<Request*> act;
-  {
-    std::lock_guard<std::mutex> lk(s.m);
-    for (Request* r : s.active) if (!r->done) act.push_back(r);
-  }
-  if (act.empty()) return false;
-  // pack: round robin over the active requests, a chunk each per turn, until the batch is full
-  std::vector<Part> parts;
-  std::vector<Part> views;
-  uint64_t raysInBatch = 0;
-  size_t bitsInBatch = 0, outInBatch = 0;
-  uint32_t sensInBatch = 0;
-  bool progress = true;
-  const size_t n = act.size();
-  while (progress && parts.size() < kMaxSegs && raysInBatch < s.batchRays) {
-    progress = false;
-    for (size_t j = 0; j < n && parts.size() < kMaxSegs && raysInBatch < s.batchRays; ++j) {
-      Request* r = act[(s.rr + j) % n];
-      if (r->nextSensor >= r->nSensors) continue;
-      const uint32_t c = std::min(s.chunkSensors, r->nSensors - r->nextSensor);
-      if (r->kind == 1) {
-        if (views.empty()) { views.push_back(Part{r, r->nextSensor, c}); r->nextSensor += c; progress = true; }
-        continue;
-      }
-      const size_t words = size_t((r->d.nDir + 31) / 32) * c;
-      if (bitsInBatch + words > s.bitsPoolWords || outInBatch + size_t(r->d.nQ) * c > s.outPoolDoubles || sensInBatch + c > s.maxSensPerBatch) continue;
-      parts.push_back(Part{r, r->nextSensor, c});
-      r->nextSensor += c;
-      raysInBatch += uint64_t(c) * r->d.nDir;
-      sensInBatch += c;
-      bitsInBatch += words;
-      outInBatch += size_t(r->d.nQ) * c;
-      progress = true;
+    if (!upload(s, r, err)) {
+      cudaStreamSynchronize(s.up);   // none of its copies still in flight when its memory goes back
+      std::lock_guard<std::mutex> lk(s.m);
+      finish(s, r, false, err);
+      s.active.erase(std::remove(s.active.begin(), s.active.end(), r), s.active.end());
     }
   }
-  s.rr = (s.rr + 1) % std::max<size_t>(1, n);
-  std::string err;
-  const auto account = [&](const Part& p, bool ok) {
-    std::lock_guard<std::mutex> lk(s.m);
-    p.r->doneSensors += p.n;
-    if (!ok && !p.r->done) finish(s, p.r, false, err);
-    else if (p.r->doneSensors == p.r->nSensors && !p.r->done) finish(s, p.r, true, "");
-    s.active.erase(std::remove_if(s.active.begin(), s.active.end(), [](Request* q) { return q->done; }), s.active.end());
-  };
-  if (!parts.empty()) {
-    const bool ok = run_daylight_batch(s, parts, err);
-    for (const Part& p : parts) account(p, ok);
-  }
-  for (const Part& p : views) account(p, run_views_chunk(s, p.r, p.i0, p.n, err));
+  cudaEventRecord(s.upDone, s.up);
   s.doneCv.notify_all();
-  return !parts.empty() || !views.empty();
+}
+
+// the work stream waits for the uploads issued so far before its next item
+bool order_after_uploads(Server& s, std::string& err) {
+  if (!s.upPending) return true;
+  s.upPending = false;
+  return cuok(cudaStreamWaitEvent(s.st, s.upDone, 0), err, "upload wait");
+}
+
+double priority(const Server& s, const Request* r, Clock::time_point now) {
+  const double rem = double(r->nSensors - r->nextSensor) * double(r->raysPerSensor) * s.cost[r->kind];
+  return rem / (std::chrono::duration<double>(now - r->tSubmit).count() + kAgeSeconds);
+}
+
+// a daylight batch of the given parts into slot k, launched on the work stream
+bool launch_day(Server& s, int k, const std::vector<Part>& parts, std::string& err) {
+  DaySlot& d = s.day[k];
+  uint32_t tasks = 0, sens = 0;
+  size_t bits = 0, out = 0;
+  d.rays = 0;
+  for (size_t j = 0; j < parts.size(); ++j) {
+    const Part& p = parts[j];
+    const kgb_daylight_request& q = p.r->d;
+    const DScene& sc = s.scenes[size_t(q.scene)];
+    const char* b = static_cast<const char*>(p.r->dev);
+    const DayLayout L = day_layout(q);
+    Seg& g = d.hSegs[j];
+    g.nodes = static_cast<const Node8*>(sc.nodes); g.tris = static_cast<const TriRec*>(sc.tris); g.nNodes = sc.nNodes;
+    g.P = reinterpret_cast<const float*>(b) + 3 * size_t(p.i0); g.N = reinterpret_cast<const float*>(b + L.offN) + 3 * size_t(p.i0);
+    g.D = reinterpret_cast<const float*>(b + L.offD); g.tab = reinterpret_cast<const RayDir*>(b + L.offTab);
+    g.W = reinterpret_cast<const double*>(b + L.offW);
+    g.nDir = q.nDir; g.nWords = (q.nDir + 31) / 32; g.n = p.n; g.rayFlags = q.rayFlags; g.nQ = q.nQ; g.useCosMask = q.useCosMask;
+    g.taskBase = tasks; g.sensBase = sens; g.bitsOff = uint32_t(bits); g.outOff = uint32_t(out);
+    tasks += (p.n + 31) / 32 * g.nWords;
+    sens += p.n;
+    bits += size_t(g.nWords) * p.n;
+    out += size_t(q.nQ) * p.n;
+    d.rays += uint64_t(p.n) * q.nDir;
+  }
+  if (parts.empty() || parts.size() > kMaxSegs || bits > s.bitsPoolWords || out > s.outPoolDoubles || sens > s.maxSensPerBatch) {
+    err = "internal: batch beyond its pools";
+    return false;
+  }
+  d.hHdr->nSegs = uint32_t(parts.size()); d.hHdr->nTasks = tasks; d.hHdr->nSens = sens;
+  d.parts = parts;
+  void* aRed[] = {&d.dHdr, &d.dSegs, &d.dBits, &d.dOut};
+  cudaKernelNodeParams kr{};
+  kr.func = reinterpret_cast<void*>(k_reduce_batch); kr.gridDim = dim3((sens + 255) / 256); kr.blockDim = dim3(256); kr.kernelParams = aRed;
+  const bool ok =
+      cuok(cudaGraphExecMemcpyNodeSetParams1D(d.exec, d.nSegs, d.dSegs, d.hSegs, sizeof(Seg) * parts.size(), cudaMemcpyHostToDevice), err, "batch table") &&
+      cuok(cudaGraphExecKernelNodeSetParams(d.exec, d.nReduce, &kr), err, "batch reduce") &&
+      cuok(cudaGraphExecMemcpyNodeSetParams1D(d.exec, d.nOut, d.hOut, d.dOut, sizeof(double) * out, cudaMemcpyDeviceToHost), err, "batch sums") &&
+      order_after_uploads(s, err) && cuok(cudaEventRecord(d.ev[0], s.st), err, "batch") && cuok(cudaGraphLaunch(d.exec, s.st), err, "batch graph") &&
+      cuok(cudaEventRecord(d.ev[1], s.st), err, "batch");
+  if (!ok) d.parts.clear();
+  return ok;
+}
+
+// a views chunk of one request into slot k: the single-request view kernels on its device arrays and the views scratch
+bool launch_views(Server& s, int k, const Part& p, std::string& err) {
+  ViewSlot& vs = s.view[k];
+  const kgb_views_request& v = p.r->v;
+  const DScene& sc = s.scenes[size_t(v.scene)];
+  const ViewLayout L = view_layout(v, sc.nTris);
+  const uint64_t K = p.r->raysPerSensor;
+  const char* b = static_cast<const char*>(p.r->dev);
+  const double rad = v.view.north * KGB_PI_D / 180;
+  ViewArgs a{};
+  a.nodes = static_cast<const Node8*>(sc.nodes); a.tris = static_cast<const TriRec*>(sc.tris); a.nNodes = sc.nNodes;
+  a.P = reinterpret_cast<const float*>(b); a.N = reinterpret_cast<const float*>(b + L.offN);
+  a.first = p.i0; a.n = p.n; a.out0 = 0; a.stride = p.n; a.i0 = p.i0;
+  a.K = uint32_t(K); a.nWords = uint32_t((K + 31) / 32); a.nAz = v.view.nAz; a.nEl = v.view.nEl; a.rayFlags = v.rayFlags;
+  a.rowSin = reinterpret_cast<const float*>(b + L.offRow); a.az0 = v.view.az0; a.dAz = v.view.dAz; a.groundZ = v.view.groundZ;
+  a.cosN = float(std::cos(rad)); a.sinN = float(std::sin(rad));
+  a.world = v.view.world ? 1 : 0; a.cull = v.view.cull ? 1 : 0; a.jitter = v.view.jitter ? 1 : 0; a.nS = v.view.nS; a.back = v.view.back ? 1 : 0;
+  a.vground = v.view.vground ? 1 : 0;
+  a.label = v.label ? reinterpret_cast<const uint8_t*>(b + L.offLab) : nullptr;
+  a.cls = s.dCls; a.dist = s.dDist;
+  a.counter = vs.dCtl; a.status = vs.dCtl + 1;
+  ViewReduceArgs ra{};
+  ra.cls = a.cls; ra.dist = a.dist; ra.nc = p.n; ra.K = uint32_t(K); ra.nAz = v.view.nAz; ra.nEl = v.view.nEl; ra.nClass = v.nClass;
+  ra.nReach = v.nReach; ra.glazing = v.glazing ? 1 : 0; ra.iso = v.isoDim ? 1 : 0; ra.NA = views_NA(v);
+  ra.wRow = reinterpret_cast<const double*>(b + L.offW); ra.farDist = float(v.farDist); ra.lnFar = std::log(v.farDist);
+  for (uint32_t j = 0; j < v.nReach; ++j) ra.reach[j] = v.reach[j];
+  ra.isoDim = v.isoDim; ra.world = a.world; ra.jitter = a.jitter; ra.i0 = p.i0; ra.nS = v.view.nS; ra.back = a.back;
+  ra.az0 = v.view.az0; ra.dAz = v.view.dAz; ra.rowSin = a.rowSin; ra.out = s.dViewOut;
+  vs.part = p;
+  vs.NA = ra.NA;
+  const size_t tasks = (size_t(p.n) + 31) / 32 * a.nWords;
+  const int grid = int(std::min<size_t>(size_t(s.gridView), (tasks + 7) / 8));
+  if (!order_after_uploads(s, err) || !cuok(cudaEventRecord(vs.ev[0], s.st), err, "views") || !cuok(cudaMemsetAsync(vs.dCtl, 0, 8, s.st), err, "views"))
+    return false;
+  launch_view(a, grid, s.st);
+  launch_reduce_view(ra, s.st);
+  return cuok(cudaGetLastError(), err, "views launch") &&
+         cuok(cudaMemcpyAsync(vs.hOut, s.dViewOut, size_t(p.n) * ra.NA * 8, cudaMemcpyDeviceToHost, s.st), err, "views") &&
+         cuok(cudaMemcpyAsync(vs.hStatus, vs.dCtl + 1, 4, cudaMemcpyDeviceToHost, s.st), err, "views") &&
+         cuok(cudaEventRecord(vs.ev[1], s.st), err, "views");
+}
+
+// sensors of a views request in one chunk: the views rays the scratch holds, at most kMaxViewChunk
+uint32_t views_chunk(const Server& s, const Request* r) {
+  const uint64_t n = std::min<uint64_t>(kMaxViewChunk, std::max<uint64_t>(1, s.viewRays / r->raysPerSensor));
+  return uint32_t(std::min<uint64_t>(n, r->nSensors - r->nextSensor));
+}
+
+void account(Server& s, Request* r, uint32_t n, bool ok, const std::string& err) {
+  std::lock_guard<std::mutex> lk(s.m);
+  r->doneSensors += n;
+  if (!r->done && !ok) finish(s, r, false, err);
+  else if (!r->done && r->doneSensors == r->nSensors) finish(s, r, true, "");
+  s.active.erase(std::remove_if(s.active.begin(), s.active.end(), [](Request* q) { return q->done; }), s.active.end());
+}
+
+bool slot_busy(const Server& s, int kind, int k) {
+  for (const auto& f : s.inflight) if (f.first == kind && f.second == k) return true;
+  return false;
+}
+
+// the next work item by priority; false when there is nothing to launch
+bool launch_next(Server& s) {
+  const Clock::time_point now = Clock::now();
+  std::vector<std::pair<double, Request*>> cand;
+  {
+    std::lock_guard<std::mutex> lk(s.m);
+    for (Request* r : s.active)
+      if (!r->done && r->nextSensor < r->nSensors) cand.emplace_back(priority(s, r, now), r);
+  }
+  if (cand.empty()) return false;
+  std::sort(cand.begin(), cand.end(), [](const auto& a, const auto& b) { return a.first < b.first || (a.first == b.first && a.second->ticket < b.second->ticket); });
+  const int kind = cand.front().second->kind;
+  int k = 0;
+  while (k < kSlots && slot_busy(s, kind, k)) ++k;
+  if (k == kSlots) return false;
+  std::string err;
+  if (kind == 1) {
+    Request* r = cand.front().second;
+    const uint32_t n = views_chunk(s, r);
+    if (uint64_t(n) * r->raysPerSensor > s.viewCap) {
+      r->nextSensor = r->nSensors;
+      account(s, r, 0, false, "views: one sensor's rays exceed the views scratch (raise the views chunk rays)");
+      return true;
+    }
+    const Part p{r, r->nextSensor, n};
+    r->nextSensor += n;
+    if (!launch_views(s, k, p, err)) { account(s, r, n, false, err); return true; }
+    s.inflight.emplace_back(1, k);
+    std::lock_guard<std::mutex> lk(s.m);
+    ++s.items;
+    return true;
+  }
+  // daylight: chunks of the daylight candidates in priority order until the batch is full
+  std::vector<Part> parts;
+  uint64_t rays = 0;
+  size_t bits = 0, out = 0;
+  uint32_t sens = 0;
+  for (const auto& c : cand) {
+    Request* r = c.second;
+    if (r->kind != 0) continue;
+    const size_t perSensor = (r->d.nDir + 31) / 32;
+    while (r->nextSensor < r->nSensors && parts.size() < kMaxSegs && rays < s.batchRays) {
+      // a chunk, cut to what is left of the batch's rays and of its pools
+      const uint64_t fit = std::min({uint64_t(s.chunkSensors), uint64_t(r->nSensors - r->nextSensor),
+                                     (s.batchRays - rays + r->d.nDir - 1) / r->d.nDir, uint64_t((s.bitsPoolWords - bits) / perSensor),
+                                     uint64_t((s.outPoolDoubles - out) / r->d.nQ), uint64_t(s.maxSensPerBatch - sens)});
+      if (fit == 0) break;
+      const uint32_t n = uint32_t(fit);
+      const size_t words = perSensor * n;
+      parts.push_back(Part{r, r->nextSensor, n});
+      r->nextSensor += n;
+      rays += uint64_t(n) * r->d.nDir;
+      bits += words;
+      out += size_t(r->d.nQ) * n;
+      sens += n;
+    }
+    if (parts.size() >= kMaxSegs || rays >= s.batchRays) break;
+    if (parts.empty()) {   // not one sensor of the top request fits an empty batch: it can never run
+      r->nextSensor = r->nSensors;
+      account(s, r, 0, false, "daylight: one sensor's direction words exceed the batch pools (raise the batch rays)");
+      return true;
+    }
+  }
+  if (parts.empty()) return false;
+  if (!launch_day(s, k, parts, err)) {
+    for (const Part& p : parts) account(s, p.r, p.n, false, err);
+    return true;
+  }
+  s.inflight.emplace_back(0, k);
+  std::lock_guard<std::mutex> lk(s.m);
+  ++s.items;
+  return true;
+}
+
+// the oldest item, whose end event has been reached (or failed): results out to the requests, the cost estimate updated
+void complete(Server& s, int kind, int k, cudaError_t q) {
+  std::string err;
+  bool ok = cuok(q, err, kind == 0 ? "batch" : "views chunk");
+  cudaEvent_t* ev = kind == 0 ? s.day[k].ev : s.view[k].ev;
+  float ms = 0;
+  const uint64_t rays = kind == 0 ? s.day[k].rays : uint64_t(s.view[k].part.n) * s.view[k].part.r->raysPerSensor;
+  if (ok && cudaEventElapsedTime(&ms, ev[0], ev[1]) == cudaSuccess && rays && ms > 0) {
+    s.cost[kind] = 0.7 * s.cost[kind] + 0.3 * (double(ms) * 1e-3 / double(rays));
+    std::lock_guard<std::mutex> lk(s.m);
+    s.gpuSec[kind] += double(ms) * 1e-3;
+    s.kindRays[kind] += double(rays);
+  }
+  if (kind == 0) {
+    DaySlot& d = s.day[k];
+    if (ok && *d.hStatus) { ok = false; err = "batch: traversal stack overflow or visit limit"; }
+    for (size_t j = 0; j < d.parts.size(); ++j) {
+      const Part& p = d.parts[j];
+      const Seg& g = d.hSegs[j];
+      if (ok && !p.r->done)
+        for (uint32_t qq = 0; qq < g.nQ; ++qq)
+          std::memcpy(p.r->d.out + size_t(qq) * p.r->nSensors + p.i0, d.hOut + g.outOff + size_t(qq) * p.n, size_t(p.n) * 8);
+      account(s, p.r, p.n, ok, err);
+    }
+    d.parts.clear();
+  } else {
+    ViewSlot& vs = s.view[k];
+    const Part& p = vs.part;
+    if (ok && *vs.hStatus) { ok = false; err = "views chunk: traversal stack overflow"; }
+    if (ok && !p.r->done) std::memcpy(p.r->v.out + size_t(p.i0) * vs.NA, vs.hOut, size_t(p.n) * vs.NA * 8);
+    account(s, p.r, p.n, ok, err);
+  }
+  {
+    std::lock_guard<std::mutex> lk(s.m);
+    if (ok) s.rays += rays;
+  }
+  s.doneCv.notify_all();
 }
 
 void loop(Server* s) {
@@ -438,15 +628,47 @@ void loop(Server* s) {
   for (;;) {
     {
       std::unique_lock<std::mutex> lk(s->m);
-      s->cv.wait(lk, [&] { return s->stop || !s->pending.empty() || !s->active.empty(); });
+      s->cv.wait(lk, [&] { return s->stop || !s->pending.empty() || !s->active.empty() || !s->inflight.empty(); });
       if (s->stop) return;
     }
-    step(*s);
+    admit(*s);
+    const bool idle = s->inflight.empty();
+    while (s->inflight.size() < kDepth && launch_next(*s)) {}
+    if (idle && !s->inflight.empty()) s->queuedSince = Clock::now();
+    if (s->inflight.empty()) {   // admitted requests that all failed, or nothing launchable yet
+      std::unique_lock<std::mutex> lk(s->m);
+      s->cv.wait_for(lk, std::chrono::milliseconds(1));
+      continue;
+    }
+    const std::pair<int, int> f = s->inflight.front();
+    const cudaError_t q = cudaEventQuery(f.first == 0 ? s->day[f.second].ev[1] : s->view[f.second].ev[1]);
+    if (q == cudaErrorNotReady) { std::this_thread::sleep_for(std::chrono::microseconds(100)); continue; }
+    s->inflight.pop_front();
+    if (s->inflight.empty()) {
+      std::lock_guard<std::mutex> lk(s->m);
+      s->queuedSec += std::chrono::duration<double>(Clock::now() - s->queuedSince).count();
+    }
+    complete(*s, f.first, f.second, q);
   }
 }
 
+// one daylight batch through slot 0, waited for (the autotuner's calibration); its parts' outputs written
+bool run_batch_now(Server& s, const std::vector<Part>& parts, double& sec, std::string& err) {
+  const auto t0 = Clock::now();
+  if (!launch_day(s, 0, parts, err)) return false;
+  const cudaError_t q = cudaEventSynchronize(s.day[0].ev[1]);
+  sec = std::chrono::duration<double>(Clock::now() - t0).count();
+  if (!cuok(q, err, "calibration batch")) return false;
+  if (*s.day[0].hStatus) { err = "calibration batch: traversal stack overflow"; return false; }
+  float ms = 0;
+  if (cudaEventElapsedTime(&ms, s.day[0].ev[0], s.day[0].ev[1]) == cudaSuccess && s.day[0].rays && ms > 0) s.cost[0] = double(ms) * 1e-3 / double(s.day[0].rays);
+  s.day[0].parts.clear();
+  return true;
+}
+
 // the autotuner: calibration batches of one synthetic request on scene 0 (its first sensors against a fixed
-// direction table), keeping the chunk size and batch size with the most rays per second
+// direction table); keeps the chunk size and batch size with the most rays per second, or the smallest batch within
+// 5 % of that rate (a smaller batch is a shorter wait for requests that arrive while it runs)
 bool autotune(Server& s, std::string& err) {
   const DScene& sc = s.scenes[0];
   if (!sc.nNodes) return true;
@@ -456,7 +678,7 @@ bool autotune(Server& s, std::string& err) {
   // sensors on a horizontal grid over the middle of the scene's first node box, looking up; directions over the sky
   float p0[3];
   std::vector<uint32_t> node(20);
-  cudaMemcpy(node.data(), sc.nodes, 80, cudaMemcpyDeviceToHost);
+  if (!cuok(cudaMemcpy(node.data(), sc.nodes, 80, cudaMemcpyDeviceToHost), err, "autotune")) return false;
   std::memcpy(p0, node.data(), 12);
   for (uint32_t i = 0; i < nSens; ++i) {
     P[3 * i] = p0[0] * 0.5f + float(i % 256); P[3 * i + 1] = p0[1] * 0.5f + float(i / 256); P[3 * i + 2] = 1.f;
@@ -466,11 +688,10 @@ bool autotune(Server& s, std::string& err) {
     const double z = 0.05 + 0.9 * (d + 0.5) / nDir, a = 2.399963 * d, r = std::sqrt(1 - z * z);
     D[3 * d] = float(r * std::sin(a)); D[3 * d + 1] = float(r * std::cos(a)); D[3 * d + 2] = float(z);
   }
-  double best = -1;
-  uint32_t bestChunk = s.chunkSensors;
-  uint64_t bestRays = s.batchRays;
+  struct Trial { uint32_t chunk; uint64_t rays; double rate; };
+  std::vector<Trial> trials;
   for (uint32_t chunk : {2048u, 8192u, 32768u})
-    for (uint64_t br : {uint64_t(1) << 28, uint64_t(1) << 30}) {
+    for (uint64_t br : {uint64_t(1) << 26, uint64_t(1) << 27, uint64_t(1) << 28}) {
       s.chunkSensors = chunk;
       s.batchRays = br;
       if (!make_pools(s, err)) return false;
@@ -478,32 +699,41 @@ bool autotune(Server& s, std::string& err) {
       r.kind = 0;
       r.d = kgb_daylight_request{0, nSens, nDir, 1, P.data(), N.data(), D.data(), W.data(), 1u, KGB_RAY_TERMINATE_ON_FIRST_HIT | KGB_RAY_DISABLE_ANYHIT, out.data()};
       r.nSensors = nSens;
+      r.raysPerSensor = nDir;
+      r.devBytes = request_bytes(s, &r);
       if (!upload(s, &r, err)) return false;
-      std::vector<Part> parts;
-      uint64_t acc = 0;
-      uint32_t sens = 0;
-      for (uint32_t i = 0; i < nSens && parts.size() < kMaxSegs && acc < br && sens + chunk <= s.maxSensPerBatch; i += chunk) {
-        const uint32_t c = std::min(chunk, nSens - i);
-        parts.push_back(Part{&r, i, c});
-        acc += uint64_t(c) * nDir;
-        sens += c;
+      cudaEventRecord(s.upDone, s.up);
+      double best = 0;
+      for (int rep = 0; rep < 2; ++rep) {   // the first run warms the caches and the graph
+        std::vector<Part> parts;
+        uint64_t acc = 0;
+        uint32_t sens = 0;
+        for (uint32_t i = 0; i < nSens && parts.size() < kMaxSegs && acc < br && sens + chunk <= s.maxSensPerBatch; i += chunk) {
+          const uint32_t c = std::min(chunk, nSens - i);
+          parts.push_back(Part{&r, i, c});
+          acc += uint64_t(c) * nDir;
+          sens += c;
+        }
+        double sec = 0;
+        if (!run_batch_now(s, parts, sec, err)) { cudaFreeAsync(r.dev, s.st); return false; }
+        best = std::max(best, double(acc) / sec);
       }
-      const auto t0 = Clock::now();
-      const bool ok = run_daylight_batch(s, parts, err);
-      const double sec = std::chrono::duration<double>(Clock::now() - t0).count();
-      uint64_t rays = 0;
-      for (const Part& p : parts) rays += uint64_t(p.n) * nDir;
-      cudaFree(r.dev);
-      s.used -= r.devBytes;
-      if (!ok) return false;
-      const double rate = rays / sec;
-      if (rate > best) { best = rate; bestChunk = chunk; bestRays = br; }
+      cudaFreeAsync(r.dev, s.st);
+      trials.push_back(Trial{chunk, br, best});
     }
-  s.chunkSensors = bestChunk;
-  s.batchRays = bestRays;
+  double top = 0;
+  for (const Trial& t : trials) top = std::max(top, t.rate);
+  Trial pick = trials.front();
+  bool have = false;
+  for (const Trial& t : trials)
+    if (t.rate >= 0.95 * top && (!have || t.rays < pick.rays || (t.rays == pick.rays && t.rate > pick.rate))) { pick = t; have = true; }
+  s.chunkSensors = pick.chunk;
+  s.batchRays = pick.rays;
   s.rays = 0;
-  s.batches = 0;
-  return make_pools(s, err);
+  s.items = 0;
+  s.gpuSec[0] = s.gpuSec[1] = s.kindRays[0] = s.kindRays[1] = s.queuedSec = 0;
+  s.cost[1] = 3 * s.cost[0];
+  return make_pools(s, err) && cuok(cudaStreamSynchronize(s.st), err, "autotune");
 }
 
 }  // namespace
@@ -518,18 +748,43 @@ KGB_API kgb_server* kgb_server_create(uint64_t hbmBudgetBytes) {
   std::string err;
   const auto bad = [&](const std::string& m) { set_error(m); kgb_server_destroy(reinterpret_cast<kgb_server*>(s)); return nullptr; };
   int n = 0;
-  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return bad("no CUDA device");
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) { delete s; set_error("no CUDA device"); return nullptr; }
   cudaGetDevice(&s->device);
   cudaDeviceGetAttribute(&s->numSMs, cudaDevAttrMultiProcessorCount, s->device);
   s->gridBits = s->numSMs * 4;
+  s->gridView = s->numSMs * view_blocks_per_sm();
   s->budget = hbmBudgetBytes;
+  cudaMemPoolProps props{};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = s->device;
   if (!cuok(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking), err, "stream") ||
-      !cuok(cudaMallocHost(&s->hSegs, sizeof(Seg) * kMaxSegs), err, "pinned") || !cuok(cudaMallocHost(&s->hHdr, sizeof(BatchHdr)), err, "pinned") ||
-      !cuok(cudaMalloc(&s->dSegs, sizeof(Seg) * kMaxSegs), err, "segments") || !cuok(cudaMalloc(&s->dHdr, sizeof(BatchHdr)), err, "segments") ||
-      !cuok(cudaMalloc(&s->dCtl, 64), err, "control"))
+      !cuok(cudaStreamCreateWithFlags(&s->up, cudaStreamNonBlocking), err, "stream") ||
+      !cuok(cudaEventCreateWithFlags(&s->upDone, cudaEventDisableTiming), err, "event") || !cuok(cudaMemPoolCreate(&s->pool, &props), err, "memory pool"))
     return bad(err);
-  std::memset(s->hSegs, 0, sizeof(Seg) * kMaxSegs);
-  std::memset(s->hHdr, 0, sizeof(BatchHdr));
+  // the pool keeps freed memory for the next requests, and an upload never waits for the work stream to reuse memory
+  uint64_t keep = ~uint64_t(0);
+  int no = 0;
+  if (!cuok(cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep), err, "memory pool") ||
+      !cuok(cudaMemPoolSetAttribute(s->pool, cudaMemPoolReuseAllowInternalDependencies, &no), err, "memory pool"))
+    return bad(err);
+  for (DaySlot& d : s->day)
+    if (!cuok(cudaMallocHost(&d.hSegs, sizeof(Seg) * kMaxSegs), err, "pinned") || !cuok(cudaMallocHost(&d.hHdr, sizeof(BatchHdr)), err, "pinned") ||
+        !cuok(cudaMallocHost(&d.hStatus, 4), err, "pinned") || !cuok(cudaMalloc(&d.dSegs, sizeof(Seg) * kMaxSegs), err, "segments") ||
+        !cuok(cudaMalloc(&d.dHdr, sizeof(BatchHdr)), err, "segments") || !cuok(cudaMalloc(&d.dCtl, 64), err, "control") ||
+        !cuok(cudaEventCreate(&d.ev[0]), err, "event") || !cuok(cudaEventCreate(&d.ev[1]), err, "event")) {
+      return bad(err);
+    } else {
+      std::memset(d.hSegs, 0, sizeof(Seg) * kMaxSegs);
+      std::memset(d.hHdr, 0, sizeof(BatchHdr));
+    }
+  for (ViewSlot& v : s->view)
+    if (!cuok(cudaMalloc(&v.dCtl, 64), err, "control") || !cuok(cudaMallocHost(&v.hStatus, 4), err, "pinned") ||
+        !cuok(cudaMallocHost(&v.hOut, size_t(kMaxViewChunk) * kMaxNA * 8), err, "pinned") || !cuok(cudaEventCreate(&v.ev[0]), err, "event") ||
+        !cuok(cudaEventCreate(&v.ev[1]), err, "event"))
+      return bad(err);
+  if (!cuok(cudaMalloc(&s->dViewOut, size_t(kMaxViewChunk) * kMaxNA * 8), err, "views columns")) return bad(err);
+  s->used += size_t(kMaxViewChunk) * kMaxNA * 8;
   if (!make_pools(*s, err)) return bad(err);
   s->th = std::thread(loop, s);
   return reinterpret_cast<kgb_server*>(s);
@@ -544,14 +799,31 @@ KGB_API void kgb_server_destroy(kgb_server* h) {
   }
   s->cv.notify_all();
   if (s->th.joinable()) s->th.join();
+  if (s->up) cudaStreamSynchronize(s->up);
+  for (auto& kv : s->all) {
+    if (kv.second->dev && s->st) cudaFreeAsync(kv.second->dev, s->st);
+    delete kv.second;
+  }
   if (s->st) cudaStreamSynchronize(s->st);
-  for (auto& kv : s->all) { if (kv.second->dev) cudaFree(kv.second->dev); delete kv.second; }
   for (DScene& d : s->scenes) { cudaFree(d.nodes); cudaFree(d.tris); }
-  if (s->graph) cudaGraphExecDestroy(s->graph);
-  cudaFree(s->dBits); cudaFree(s->dOut); cudaFree(s->dSegs); cudaFree(s->dHdr); cudaFree(s->dCtl);
-  if (s->hOut) cudaFreeHost(s->hOut);
-  if (s->hSegs) cudaFreeHost(s->hSegs);
-  if (s->hHdr) cudaFreeHost(s->hHdr);
+  free_pools(*s);
+  for (DaySlot& d : s->day) {
+    if (d.hSegs) cudaFreeHost(d.hSegs);
+    if (d.hHdr) cudaFreeHost(d.hHdr);
+    if (d.hStatus) cudaFreeHost(d.hStatus);
+    cudaFree(d.dSegs); cudaFree(d.dHdr); cudaFree(d.dCtl);
+    for (cudaEvent_t e : d.ev) if (e) cudaEventDestroy(e);
+  }
+  for (ViewSlot& v : s->view) {
+    cudaFree(v.dCtl);
+    if (v.hStatus) cudaFreeHost(v.hStatus);
+    if (v.hOut) cudaFreeHost(v.hOut);
+    for (cudaEvent_t e : v.ev) if (e) cudaEventDestroy(e);
+  }
+  cudaFree(s->dViewOut);
+  if (s->pool) cudaMemPoolDestroy(s->pool);
+  if (s->upDone) cudaEventDestroy(s->upDone);
+  if (s->up) cudaStreamDestroy(s->up);
   if (s->st) cudaStreamDestroy(s->st);
   delete s;
 }
@@ -559,9 +831,10 @@ KGB_API void kgb_server_destroy(kgb_server* h) {
 KGB_API int kgb_server_add_scene(kgb_server* h, const float* v, size_t nv, const uint32_t* tri, size_t nt, int32_t* sceneId) {
   Server* s = reinterpret_cast<Server*>(h);
   for (size_t k = 0; k < 3 * nt; ++k) if (tri[k] >= nv) { set_error("kgb_server_add_scene: a triangle's vertex index exceeds the vertices"); return 0; }
+  if (nt >= (size_t(1) << 32)) { set_error("kgb_server_add_scene: at most 2^32 - 1 triangles"); return 0; }
   DScene d;
   std::lock_guard<std::mutex> lk(s->m);
-  if (nt) {   // the device builder (bvh_gpu.cu), on the server's stream
+  if (nt) {   // the device builder (bvh_gpu.cu), on the server's work stream
     uint64_t temp = 0;
     const std::string why = build_bvh8_gpu(v, nv, tri, nt, nullptr, nullptr, s->st, &d.nodes, &d.tris, &d.nNodes, &temp);
     if (!why.empty()) {
@@ -588,6 +861,23 @@ KGB_API int kgb_server_autotune(kgb_server* h) {
   return 1;
 }
 
+KGB_API int kgb_server_set_tuning(kgb_server* h, uint32_t chunkSensors, uint64_t batchRays, uint64_t viewRays) {
+  Server* s = reinterpret_cast<Server*>(h);
+  std::unique_lock<std::mutex> lk(s->m);
+  if (!s->active.empty() || !s->pending.empty()) { set_error("kgb_server_set_tuning: only while idle"); return 0; }
+  if ((chunkSensors && (chunkSensors < 32 || chunkSensors > (1u << 20))) || (batchRays && (batchRays < (1u << 16) || batchRays > (uint64_t(1) << 32))) ||
+      (viewRays && (viewRays < (1u << 16) || viewRays > (uint64_t(1) << 31)))) {
+    set_error("kgb_server_set_tuning: chunk 32..2^20 sensors, batch 2^16..2^32 rays, views chunk 2^16..2^31 rays");
+    return 0;
+  }
+  if (chunkSensors) s->chunkSensors = chunkSensors;
+  if (batchRays) s->batchRays = batchRays;
+  if (viewRays) s->viewRays = viewRays;
+  std::string err;
+  if (!make_pools(*s, err) || !cuok(cudaStreamSynchronize(s->st), err, "tuning")) { set_error(err); return 0; }
+  return 1;
+}
+
 KGB_API int kgb_server_submit(kgb_server* h, const kgb_daylight_request* req, uint64_t* ticket) {
   Server* s = reinterpret_cast<Server*>(h);
   if (req->scene < 0 || size_t(req->scene) >= s->scenes.size()) { set_error("kgb_server_submit: unknown scene"); return 0; }
@@ -596,6 +886,7 @@ KGB_API int kgb_server_submit(kgb_server* h, const kgb_daylight_request* req, ui
   r->kind = 0;
   r->d = *req;
   r->nSensors = req->nSensors;
+  r->raysPerSensor = req->nDir;
   r->tSubmit = Clock::now();
   std::lock_guard<std::mutex> lk(s->m);
   r->ticket = s->nextTicket++;
@@ -611,16 +902,18 @@ KGB_API int kgb_server_submit_views(kgb_server* h, const kgb_views_request* req,
   Server* s = reinterpret_cast<Server*>(h);
   if (req->scene < 0 || size_t(req->scene) >= s->scenes.size()) { set_error("kgb_server_submit_views: unknown scene"); return 0; }
   if (req->nClass > KGB_VIEW_CLASSES || req->nReach > 8) { set_error("kgb_server_submit_views: at most 16 groups and 8 reach distances"); return 0; }
+  const uint64_t K = uint64_t(req->view.nAz) * req->view.nEl;
   Request* r = new Request;
   r->kind = 1;
   r->v = *req;
   r->rowSin.assign(req->view.rowSin, req->view.rowSin + 2 * size_t(req->view.nEl));
   r->wRow.assign(req->wRow, req->wRow + req->view.nEl);
   r->nSensors = req->nSensors;
+  r->raysPerSensor = K;
   r->tSubmit = Clock::now();
   std::lock_guard<std::mutex> lk(s->m);
   r->ticket = s->nextTicket++;
-  if (!r->nSensors) finish(*s, r, true, "");
+  if (!r->nSensors || !K) { std::fill(req->out, req->out + size_t(views_NA(*req)) * req->nSensors, 0.0); finish(*s, r, true, ""); }
   else s->pending.push_back(r);
   s->all[r->ticket] = r;
   *ticket = r->ticket;
@@ -639,8 +932,8 @@ KGB_API int kgb_server_wait(kgb_server* h, uint64_t ticket, double timeoutSec) {
   return 1;
 }
 
-// out[0..7]: completed requests, p50, p90, p99, max latency (s), rays, batches, HBM bytes in use; out[8..9]: the tuned
-// chunk sensors and batch rays
+// out[0..7]: completed requests, p50, p90, p99, max latency (s), rays, work items (daylight batches and views chunks),
+// HBM bytes in use; out[8..9]: the tuned chunk sensors and batch rays
 KGB_API void kgb_server_stats(kgb_server* h, double* out) {
   Server* s = reinterpret_cast<Server*>(h);
   std::lock_guard<std::mutex> lk(s->m);
@@ -648,7 +941,15 @@ KGB_API void kgb_server_stats(kgb_server* h, double* out) {
   std::sort(l.begin(), l.end());
   const auto q = [&](double f) { return l.empty() ? 0.0 : l[std::min(l.size() - 1, size_t(f * (l.size() - 1) + 0.5))]; };
   out[0] = double(l.size()); out[1] = q(0.5); out[2] = q(0.9); out[3] = q(0.99); out[4] = l.empty() ? 0.0 : l.back();
-  out[5] = double(s->rays); out[6] = double(s->batches); out[7] = double(s->used); out[8] = s->chunkSensors; out[9] = double(s->batchRays);
+  out[5] = double(s->rays); out[6] = double(s->items); out[7] = double(s->used); out[8] = s->chunkSensors; out[9] = double(s->batchRays);
+}
+
+// out[0..4]: GPU seconds and rays of daylight batches, of views chunks (each item timed by events around it on the
+// work stream), and wall seconds with work queued on that stream
+KGB_API void kgb_server_timing(kgb_server* h, double* out) {
+  Server* s = reinterpret_cast<Server*>(h);
+  std::lock_guard<std::mutex> lk(s->m);
+  out[0] = s->gpuSec[0]; out[1] = s->kindRays[0]; out[2] = s->gpuSec[1]; out[3] = s->kindRays[1]; out[4] = s->queuedSec;
 }
 
 }  // extern "C"

@@ -107,10 +107,12 @@ SIGNATURES = [
     ("kgb_server_destroy", None, [c_void_p]),
     ("kgb_server_add_scene", c_int, [c_void_p, c_void_p, c_size_t, c_void_p, c_size_t, POINTER(c_int32)]),
     ("kgb_server_autotune", c_int, [c_void_p]),
+    ("kgb_server_set_tuning", c_int, [c_void_p, c_uint32, c_uint64, c_uint64]),
     ("kgb_server_submit", c_int, [c_void_p, POINTER(DaylightRequest), POINTER(c_uint64)]),
     ("kgb_server_submit_views", c_int, [c_void_p, POINTER(ViewsRequest), POINTER(c_uint64)]),
     ("kgb_server_wait", c_int, [c_void_p, c_uint64, c_double]),
     ("kgb_server_stats", None, [c_void_p, POINTER(c_double)]),
+    ("kgb_server_timing", None, [c_void_p, POINTER(c_double)]),
     ("kgb_sky", c_int, [_E, c_int32, c_void_p, c_size_t, c_double, c_int32, c_int32, c_int32, c_void_p]),
     ("kgb_sun_noaa", c_int, [_E, c_void_p, c_size_t, c_void_p]),
     ("kgb_set_builder", c_int, [_E, c_int]),
@@ -371,6 +373,11 @@ class Server:
         if not self.d.kgb_server_autotune(self.h):
             raise KgbError(self.lib.err())
 
+    def set_tuning(self, chunk_sensors=0, batch_rays=0, view_rays=0):
+        """Chunk sensors, daylight batch rays and views chunk rays by hand (0 keeps a value)."""
+        if not self.d.kgb_server_set_tuning(self.h, int(chunk_sensors), int(batch_rays), int(view_rays)):
+            raise KgbError(self.lib.err())
+
     def submit(self, scene, P, N, D, W, use_cos, flags=5):
         """Daylight request: W [nQ x nDir]; use_cos per quantity. Returns a ticket; wait() gives out [nQ x nSensors]."""
         P, N, D = _f32(P, (-1, 3)), _f32(N, (-1, 3)), _f32(D, (-1, 3))
@@ -411,8 +418,14 @@ class Server:
     def stats(self):
         out = (c_double * 10)()
         self.d.kgb_server_stats(self.h, out)
-        keys = ["completed", "p50_s", "p90_s", "p99_s", "max_s", "rays", "batches", "hbm_bytes", "chunk_sensors", "batch_rays"]
+        keys = ["completed", "p50_s", "p90_s", "p99_s", "max_s", "rays", "items", "hbm_bytes", "chunk_sensors", "batch_rays"]
         return dict(zip(keys, list(out)))
+
+    def timing(self):
+        """GPU seconds and rays of daylight batches and of views chunks, and wall seconds with work queued."""
+        out = (c_double * 5)()
+        self.d.kgb_server_timing(self.h, out)
+        return dict(zip(["day_gpu_s", "day_rays", "views_gpu_s", "views_rays", "queued_s"], list(out)))
 
 
 def slots_array(slots):

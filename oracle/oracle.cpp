@@ -967,10 +967,12 @@ KGB_API kgb_server* kgb_server_create(uint64_t) { fail("kgb_server_create: not r
 KGB_API void kgb_server_destroy(kgb_server*) {}
 KGB_API int kgb_server_add_scene(kgb_server*, const float*, size_t, const uint32_t*, size_t, int32_t*) { return fail("not restated"); }
 KGB_API int kgb_server_autotune(kgb_server*) { return fail("not restated"); }
+KGB_API int kgb_server_set_tuning(kgb_server*, uint32_t, uint64_t, uint64_t) { return fail("not restated"); }
 KGB_API int kgb_server_submit(kgb_server*, const kgb_daylight_request*, uint64_t*) { return fail("not restated"); }
 KGB_API int kgb_server_submit_views(kgb_server*, const kgb_views_request*, uint64_t*) { return fail("not restated"); }
 KGB_API int kgb_server_wait(kgb_server*, uint64_t, double) { return fail("not restated"); }
 KGB_API void kgb_server_stats(kgb_server*, double* out) { for (int k = 0; k < 10; ++k) out[k] = 0; }
+KGB_API void kgb_server_timing(kgb_server*, double* out) { for (int k = 0; k < 5; ++k) out[k] = 0; }
 KGB_API int kgb_sky(kgb_engine*, int32_t, const kgb_sky_step*, size_t, double, int32_t, int32_t, int32_t, float*) {
   return fail("kgb_sky: the sky's checker is the reference's own code (tests/golden/sky)");
 }

@@ -68,7 +68,91 @@ def test_mixed_requests_equal_alone(engine_lib, kgb, pkg, budget_gb):
         assert np.array_equal(gotv.view(np.uint64), wantv.view(np.uint64))
         st = srv.stats()
         assert st["completed"] == 15 and st["p99_s"] >= st["p50_s"] > 0
-        print("\nserver (budget %.2f GB): %d requests, %d batches, p50 %.1f ms, p99 %.1f ms, chunk %d sensors" %
-              (budget_gb, st["completed"], st["batches"], 1e3 * st["p50_s"], 1e3 * st["p99_s"], st["chunk_sensors"]))
+        print("\nserver (budget %.2f GB): %d requests, %d work items, p50 %.1f ms, p99 %.1f ms, chunk %d sensors" %
+              (budget_gb, st["completed"], st["items"], 1e3 * st["p50_s"], 1e3 * st["p99_s"], st["chunk_sensors"]))
+    finally:
+        srv.close()
+
+
+def _alone_views(kgb, lib, scene, P, N, fov, cell, label):
+    nAz, nEl, rowSin, wRow = _views_grid(fov, cell)
+    world = fov == 360.0
+    e = kgb.Engine(lib)
+    try:
+        e.build(scene["v"], scene["tri"])
+        e.set_labels(label)
+        e.set_scene(P, N, np.zeros((0, 3), np.float32))
+        e.view(0, len(P), lib.bounce_flags(False), nAz, nEl, 0.0 if world else -fov / 2, fov / nAz, rowSin, world=world, cull=world,
+               groundZ=scene["groundZ"])
+        return e.reduce_view(len(P), wRow, 6, 300.0, reach=[6.0, 20.0] if world else [], isoDim=3 if world else 0)
+    finally:
+        e.close()
+
+
+def test_small_items_equal_alone(engine_lib, kgb, pkg):
+    """Work items far smaller than the requests: every daylight request spans several batches and every views request
+    several chunks, daylight and views items interleave on the work stream, and each result still equals its request
+    run alone, bit for bit."""
+    city = pkg.workloads.views_city(seed=3, n_buildings=60, target_tris=6000, n_sensors=1500)
+    srv = kgb.Server(engine_lib, 64e9)
+    try:
+        sid = srv.add_scene(city["v"], city["tri"])
+        srv.set_tuning(chunk_sensors=64, batch_rays=1 << 16, view_rays=1 << 16)
+        rng = np.random.default_rng(11)
+        day, views = [], []
+        for k in range(6):
+            n = int(rng.integers(300, len(city["P"])))
+            first = int(rng.integers(0, len(city["P"]) - n))
+            P, N = city["P"][first:first + n], city["N"][first:first + n]
+            D = pkg.workloads.hemisphere_dirs(int(rng.integers(100, 400)), int(rng.integers(0, 200)), 20 + k)
+            W = rng.uniform(0.0, 2.0, (2, len(D))).astype(np.float32)
+            day.append((P, N, D, W, srv.submit(sid, P, N, D, W, [True, False])))
+            fov = 120.0 if k % 2 else 360.0
+            nAz, nEl, rowSin, wRow = _views_grid(fov, 4.0)
+            world = fov == 360.0
+            m = int(rng.integers(100, 400))
+            Pv, Nv = city["P"][k * 200:k * 200 + m], city["N"][k * 200:k * 200 + m]
+            views.append((Pv, Nv, fov, srv.submit_views(sid, Pv, Nv, nAz, nEl, 0.0 if world else -fov / 2, fov / nAz, rowSin, wRow, 6, 300.0,
+                                                        reach=[6.0, 20.0] if world else [], isoDim=3 if world else 0, label=city["label"],
+                                                        world=world, cull=world, groundZ=city["groundZ"])))
+        for P, N, D, W, t in day:
+            assert np.array_equal(srv.wait(t), _alone_daylight(kgb, engine_lib, city, P, N, D, W, [True, False]))
+        for Pv, Nv, fov, t in views:
+            got = srv.wait(t)
+            want = _alone_views(kgb, engine_lib, city, Pv, Nv, fov, 4.0, city["label"])
+            assert np.array_equal(got.view(np.uint64), want.view(np.uint64))
+        st = srv.stats()
+        assert st["completed"] == 12 and st["items"] > 40
+        print("\nsmall items: %d requests, %d work items, p50 %.1f ms, p99 %.1f ms" % (st["completed"], st["items"], 1e3 * st["p50_s"], 1e3 * st["p99_s"]))
+    finally:
+        srv.close()
+
+
+def test_set_tuning_rejects_out_of_range(engine_lib, kgb):
+    srv = kgb.Server(engine_lib, 1e9)
+    try:
+        with pytest.raises(kgb.KgbError, match="chunk 32"):
+            srv.set_tuning(chunk_sensors=8)
+        with pytest.raises(kgb.KgbError, match="views chunk"):
+            srv.set_tuning(view_rays=1 << 40)
+    finally:
+        srv.close()
+
+
+def test_chunks_cut_to_the_batch(engine_lib, kgb, pkg):
+    """A tuned chunk far larger than a batch's rays and bit pool: each batch takes the part of a chunk that fits, and
+    the request's sums equal its run alone."""
+    s = pkg.workloads.random_city(4, n_boxes=40)
+    srv = kgb.Server(engine_lib, 64e9)
+    try:
+        sid = srv.add_scene(s["v"], s["tri"])
+        srv.set_tuning(chunk_sensors=1 << 20, batch_rays=1 << 22)
+        n = min(4000, len(s["P"]))
+        P, N = s["P"][:n], s["N"][:n]
+        D = pkg.workloads.hemisphere_dirs(5000, 2000, 9)     # 12000 directions: ~350 sensors a batch
+        W = np.random.default_rng(2).uniform(0.0, 2.0, (1, len(D))).astype(np.float32)
+        got = srv.wait(srv.submit(sid, P, N, D, W, [True]))
+        assert np.array_equal(got, _alone_daylight(kgb, engine_lib, s, P, N, D, W, [True]))
+        assert srv.stats()["items"] >= n * len(D) // (1 << 22)
     finally:
         srv.close()
