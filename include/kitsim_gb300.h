@@ -185,8 +185,13 @@ KGB_API int kgb_view(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, con
  * NA = 3 nClass + 1 + nReach + (glazing ? 1 : 0) + (isoDim ? 1 : 0) */
 KGB_API int kgb_reduce_view(kgb_engine* e, size_t nc, const double* wRow, size_t nRow, uint32_t nClass, double farDist,
                             const float* reach, size_t nReach, int glazing, uint32_t isoDim, double* out);
-/* replaces gpu_download_view (src/internal.h:210): [nc x K] each (transposed from the device's [K x nc]) */
+/* replaces gpu_download_view (src/internal.h:210): [nc x K] each (transposed from the device's [K x nc] on the device) */
 KGB_API int kgb_download_view(kgb_engine* e, size_t nc, uint8_t* cls, float* dist, size_t count);
+/* the last trace's visibility as one row per sensor, transposed on the device: [nc x nWords] words (bits) or
+ * [nc x nDir] bytes; they replace gpu_download_bits / gpu_download_bytes plus the host transposes of the reference's
+ * --dump-bits (src/run.cpp:659-671) */
+KGB_API int kgb_download_bits_rows(kgb_engine* e, size_t nc, uint32_t* out, size_t count);
+KGB_API int kgb_download_bytes_rows(kgb_engine* e, size_t nc, uint8_t* out, size_t count);
 
 /* --- misc ------------------------------------------------------------------------------------------------------------ */
 /* replaces gpu_stats (src/internal.h:216) */

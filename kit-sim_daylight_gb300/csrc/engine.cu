@@ -116,6 +116,24 @@ int upload_large(Staging& s, void* dst, const void* src, size_t bytes, cudaStrea
   return 1;
 }
 
+// A direction-major [K x nc] device buffer (elements of 1 or 4 bytes) to host rows [nc x K]: slices of sensors are
+// transposed on the device into one scratch buffer (at most 64 MiB) and downloaded through the staging slices.
+constexpr size_t kRowsSlice = size_t(64) << 20;
+int download_rows_into(Buf& rows, Staging& staging, const void* dev, size_t esize, size_t K, size_t nc, void* host, cudaStream_t st) {
+  if (!K || !nc) return 1;
+  if (K > 0xffffffffu) return fail("download: more than 2^32 - 1 elements per sensor");
+  const size_t per = std::min<size_t>(std::max<size_t>(1, kRowsSlice / (K * esize)), 0xffffffffu);
+  if (!grow(rows, std::min(per, nc) * K * esize)) return 0;
+  for (size_t i0 = 0; i0 < nc; i0 += per) {
+    const size_t m = std::min(per, nc - i0);
+    if (!launch_rows(static_cast<const char*>(dev) + i0 * esize, nc, rows.p, esize, uint32_t(K), uint32_t(m), st))
+      return fail("download: too many elements per sensor for the transpose grid");
+    CU(cudaGetLastError());
+    if (!download_large(staging, static_cast<char*>(host) + i0 * K * esize, rows.p, m * K * esize, st)) return 0;
+  }
+  return 1;
+}
+
 int upload(Buf& b, const void* h, size_t bytes, cudaStream_t st) {
   if (!grow(b, bytes)) return 0;
   if (bytes) CU(cudaMemcpyAsync(b.p, h, bytes, cudaMemcpyHostToDevice, st));
@@ -156,6 +174,7 @@ struct Engine {
   int seriesForm = 0;         // 0 split-BF16 tensor cores, 1 plain FP32
   Buf vop, sop, csr, sunCol;
   Staging staging;   // pinned slices for the series download
+  Buf rows;          // sensor-major rows of one slice of a direction-major buffer (download_rows)
   kgb_stats stats{};
   int gridBits = 0, gridBytes = 0, gridView = 0;
   int builder = 1;            // 1 device LBVH with treelet restructuring (default), 0 host binned SAH (kgb_set_builder)
@@ -165,6 +184,10 @@ namespace {
 
 Engine* E(kgb_engine* e) { return reinterpret_cast<Engine*>(e); }
 const Engine* E(const kgb_engine* e) { return reinterpret_cast<const Engine*>(e); }
+
+int download_rows(Engine& g, const void* dev, size_t esize, size_t K, size_t nc, void* host) {
+  return download_rows_into(g.rows, g.staging, dev, esize, K, nc, host, g.st);
+}
 
 int sync_status(Engine& g) {   // wait for the stream, then read the kernels' status word
   uint32_t status = 0;
@@ -722,21 +745,29 @@ KGB_API int kgb_reduce_view(kgb_engine* e, size_t nc, const double* wRow, size_t
   return 1;
 }
 
+// gpu.cu:720-734 transposes the device's [K x nc] on the host; here the transpose runs on the device (rows.cu), in
+// sensor slices of at most 64 MiB of rows, each downloaded through the pinned staging slices.
 KGB_API int kgb_download_view(kgb_engine* e, size_t nc, uint8_t* cls, float* dist, size_t count) {
   Engine& g = *E(e);
   if (nc != g.viewN) return fail("gpu_download_view: no gpu_view for this chunk");
   const size_t K = g.viewK;
   if (count != nc * K) return fail("gpu_download_view: wrong element count");
-  std::vector<uint8_t> c(count);
-  std::vector<float> t(count);
-  if (count) {
-    CU(cudaMemcpyAsync(c.data(), g.viewCls.p, count, cudaMemcpyDeviceToHost, g.st));
-    CU(cudaMemcpyAsync(t.data(), g.viewDist.p, count * 4, cudaMemcpyDeviceToHost, g.st));
-  }
-  CU(cudaStreamSynchronize(g.st));
-  for (size_t d = 0; d < K; ++d)
-    for (size_t i = 0; i < nc; ++i) { cls[i * K + d] = c[d * nc + i]; dist[i * K + d] = t[d * nc + i]; }
-  return 1;
+  return download_rows(g, g.viewCls.p, 1, K, nc, cls) && download_rows(g, g.viewDist.p, 4, K, nc, dist);
+}
+
+// The last trace's visibility as one row per sensor: [nc x nWords] words or [nc x nDir] bytes (run.cpp:659-671, the
+// --dump-bits rows, transposed on the device instead of the host).
+KGB_API int kgb_download_bits_rows(kgb_engine* e, size_t nc, uint32_t* out, size_t count) {
+  Engine& g = *E(e);
+  if (g.bytes) return fail("gpu_download_bits: the last trace wrote bytes");
+  if (count != g.nWords * nc || nc != g.visN) return fail("gpu_download_bits: wrong element count");
+  return download_rows(g, g.vis.p, 4, g.nWords, nc, out);
+}
+KGB_API int kgb_download_bytes_rows(kgb_engine* e, size_t nc, uint8_t* out, size_t count) {
+  Engine& g = *E(e);
+  if (!g.bytes) return fail("gpu_download_bytes: the last trace wrote bits");
+  if (count != g.nDir * nc || nc != g.visN) return fail("gpu_download_bytes: wrong element count");
+  return download_rows(g, g.vis.p, 1, g.nDir, nc, out);
 }
 
 KGB_API kgb_stats kgb_get_stats(const kgb_engine* e) { return E(e)->stats; }

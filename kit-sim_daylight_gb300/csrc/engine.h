@@ -75,6 +75,8 @@ struct BounceArgs {
 };
 
 void launch_ray_table(const float* D, uint32_t nDir, void* tab, cudaStream_t st);   // 48 bytes per direction
+// rows.cu: out[i K + d] = in[d ld + i] for d < K, i < m, elements of 1 or 4 bytes; false if the grid cannot hold K
+bool launch_rows(const void* in, size_t ld, void* out, size_t esize, uint32_t K, uint32_t m, cudaStream_t st);
 int bytes_blocks_per_sm();
 int view_blocks_per_sm();
 int bits_blocks_per_sm();

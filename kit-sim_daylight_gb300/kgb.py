@@ -95,6 +95,8 @@ SIGNATURES = [
     ("kgb_download_dc", c_int, [_E, c_size_t, c_void_p, c_size_t]),
     ("kgb_download_bits", c_int, [_E, c_size_t, c_void_p, c_size_t]),
     ("kgb_download_bytes", c_int, [_E, c_size_t, c_void_p, c_size_t]),
+    ("kgb_download_bits_rows", c_int, [_E, c_size_t, c_void_p, c_size_t]),
+    ("kgb_download_bytes_rows", c_int, [_E, c_size_t, c_void_p, c_size_t]),
     ("kgb_view", c_int, [_E, c_size_t, c_size_t, c_uint32, POINTER(ViewIn), POINTER(c_size_t)]),
     ("kgb_reduce_view", c_int, [_E, c_size_t, c_void_p, c_size_t, c_uint32, c_double, c_void_p, c_size_t, c_int, c_uint32, c_void_p]),
     ("kgb_download_view", c_int, [_E, c_size_t, c_void_p, c_void_p, c_size_t]),
@@ -281,6 +283,20 @@ class Engine:
         out = np.zeros(n, np.uint8)
         self._ok(self.d.kgb_download_bytes(self.h, nc, _p(out), n))
         return out.reshape(-1, nc) if nc else out
+
+    def download_bits_rows(self, nc):
+        """The last trace's bits as [nc x nWords] rows (transposed on the device)."""
+        nw = self.dims()["nWords"]
+        out = np.zeros(nw * nc, np.uint32)
+        self._ok(self.d.kgb_download_bits_rows(self.h, nc, _p(out), nw * nc))
+        return out.reshape(nc, nw)
+
+    def download_bytes_rows(self, nc):
+        """The last trace's bytes as [nc x nDir] rows (transposed on the device)."""
+        nd = self.dims()["nDir"]
+        out = np.zeros(nd * nc, np.uint8)
+        self._ok(self.d.kgb_download_bytes_rows(self.h, nc, _p(out), nd * nc))
+        return out.reshape(nc, nd)
 
     def series(self, nc, nSky, row, wsky, S, g, G, sun0, sunStep, sunVec, sunW, Sdc=None):
         row = np.ascontiguousarray(row, dtype=np.int32)

@@ -767,6 +767,23 @@ KGB_API int kgb_download_bytes(kgb_engine* e, size_t nc, uint8_t* out, size_t co
   std::copy(g.byt.begin(), g.byt.end(), out);
   return 1;
 }
+// run.cpp:659-671 (--dump-bits): the direction-major buffers as one row per sensor
+KGB_API int kgb_download_bits_rows(kgb_engine* e, size_t nc, uint32_t* out, size_t count) {
+  Engine& g = *reinterpret_cast<Engine*>(e);
+  if (g.bytes) return fail("gpu_download_bits: the last trace wrote bytes");
+  if (count != g.nWords * nc || g.bits.size() != count) return fail("gpu_download_bits: wrong count");
+  for (size_t w = 0; w < g.nWords; ++w)
+    for (size_t i = 0; i < nc; ++i) out[i * g.nWords + w] = g.bits[w * nc + i];
+  return 1;
+}
+KGB_API int kgb_download_bytes_rows(kgb_engine* e, size_t nc, uint8_t* out, size_t count) {
+  Engine& g = *reinterpret_cast<Engine*>(e);
+  if (!g.bytes) return fail("gpu_download_bytes: the last trace wrote bits");
+  if (count != g.nDir * nc || g.byt.size() != count) return fail("gpu_download_bytes: wrong count");
+  for (size_t d = 0; d < g.nDir; ++d)
+    for (size_t i = 0; i < nc; ++i) out[i * g.nDir + d] = g.byt[d * nc + i];
+  return 1;
+}
 
 // trace_dev.cu:167-232 (__raygen__view) + gpu.cu:572-610. The closest-hit walk over the ray's hits ordered by
 // (t, primitive): own planes (own_hit) pass, at most 3, the 4th ends the ray as an obstruction; a triangle labelled
