@@ -11,10 +11,12 @@
 //   5. boxes, triangle counts and SAH costs bottom-up (each leaf walks towards the root, the second arrival at a node
 //      refits it from its children), then three such passes that also restructure each node's treelet of up to 7
 //      leaves to its least-SAH topology (Karras & Aila 2013)
-//   6. collapse to 8-wide nodes level by level: a wide node adopts the children of its largest-area inner child until
-//      it has 8 (the host builder's rule); subtrees of at most 3 triangles become leaves (their triangles gathered by a
-//      walk: restructured subtrees are no longer ranges of the sorted order); a prefix sum over the level
-//      gives each node its block of inner children and of triangle records, so the layout is deterministic
+//   6. SAH-optimal collapse to 8-wide nodes (Ylitie, Karras & Laine 2017): a bottom-up dynamic program gives each
+//      binary node the least SAH cost of its subtree as at most i = 1..8 children of a wide node, and whether one slot
+//      holds it as a leaf (at most 3 triangles) or as a wide node of its own; level by level, each wide node's children
+//      follow those choices (leaf triangles gathered by a walk: restructured subtrees are no longer ranges of the
+//      sorted order), and a prefix sum over the level gives each node its block of inner children and of triangle
+//      records, so the layout is deterministic
 //   7. each node's child boxes quantised outwards to 8 bits against a power-of-two step per axis (double arithmetic,
 //      as the host builder)
 // Conservative exactly as the host builder: any conservative BVH gives the traversal the brute-force hit set, so the
@@ -268,6 +270,68 @@ __global__ void k_bottom_up(Tree2 T, int n, uint32_t* arrivals, int optimize) {
   }
 }
 
+// SAH-optimal collapse. For binary node x and i = 1..8 slots, C(x, i) is the least SAH cost of x's subtree as at
+// most i children of a wide node:
+//   C(x, 1) = min(leaf: A(x) n kPrimCost, only for n <= 3 triangles; wide node: A(x) kNodeCost + D(x, 8)),
+//   C(x, i) = min(C(x, i - 1), D(x, i)),  D(x, i) = min over 0 < k < i of C(left, k) + C(right, i - k),
+// and a triangle costs A kPrimCost in any number of slots. eff[x][i] is the slot count whose choice C(x, i) takes,
+// split[x][j] the left child's share of j slots (at j = 1: of the 8 slots of x's own wide node), leaf[x] the choice
+// at one slot. The costs weigh a wide node's visit (eight box tests) against a triangle test as 1 : 0.3.
+struct Dp {
+  float* cost;      // [ni x 8], C(x, i) at i - 1
+  uint8_t* eff;     // [ni x 8]
+  uint8_t* split;   // [ni x 8]
+  uint8_t* leaf;    // [ni]
+};
+constexpr float kNodeCost = 1.0f, kPrimCost = 0.3f;
+__device__ __forceinline__ float dp_cost(const Tree2& T, const Dp& D, int c, int i) {
+  if (c < 0) return kPrimCost * box_area(T.plo[T.order[~c]], T.phi[T.order[~c]]);
+  return __ldcg(&D.cost[size_t(c) * 8 + i - 1]);
+}
+__device__ void dp_node(const Tree2& T, const Dp& D, int x) {
+  const int L = __ldcg(&T.left[x]), R = __ldcg(&T.right[x]);
+  float cl[9], cr[9], cd[9];
+  uint8_t kb[9];
+  for (int i = 1; i <= 8; ++i) { cl[i] = dp_cost(T, D, L, i); cr[i] = dp_cost(T, D, R, i); }
+  for (int i = 2; i <= 8; ++i) {
+    float best = INFINITY;
+    int bk = 1;
+    for (int k = 1; k < i; ++k) { const float c = cl[k] + cr[i - k]; if (c < best) { best = c; bk = k; } }
+    cd[i] = best;
+    kb[i] = uint8_t(bk);
+  }
+  const float A = box_area(__ldcg(&T.nlo[x]), __ldcg(&T.nhi[x]));
+  const uint32_t n = __ldcg(&T.count[x]);
+  const float cInner = kNodeCost * A + cd[8], cLeaf = n <= kLeafMax ? kPrimCost * A * float(n) : INFINITY;
+  const size_t o = size_t(x) * 8;
+  float c = fminf(cLeaf, cInner);
+  uint8_t eff = 1;
+  __stcg(&D.leaf[x], uint8_t(cLeaf <= cInner ? 1 : 0));
+  __stcg(&D.cost[o], c);
+  __stcg(&D.eff[o], uint8_t(1));
+  __stcg(&D.split[o], kb[8]);
+  for (int i = 2; i <= 8; ++i) {
+    if (cd[i] < c) { c = cd[i]; eff = uint8_t(i); }
+    __stcg(&D.cost[o + i - 1], c);
+    __stcg(&D.eff[o + i - 1], eff);
+    __stcg(&D.split[o + i - 1], kb[i]);
+  }
+}
+// bottom-up as k_bottom_up: the second arrival at a node fills its row from its children's
+__global__ void k_collapse_dp(Tree2 T, Dp D, int n, uint32_t* arrivals) {
+  const int p = int(blockIdx.x * blockDim.x + threadIdx.x);
+  if (p >= n) return;
+  int node = __ldcg(&T.leafParent[p]);
+  while (node >= 0) {
+    __threadfence();
+    if (atomicAdd(&arrivals[node], 1u) == 0) return;
+    __threadfence();
+    dp_node(T, D, node);
+    __threadfence();
+    node = __ldcg(&T.parent[node]);
+  }
+}
+
 struct Tree {
   const uint32_t* order;   // sorted position -> triangle
   const float4 *plo, *phi, *nlo, *nhi;
@@ -275,7 +339,8 @@ struct Tree {
   const uint32_t* count;
 };
 __device__ __forceinline__ uint32_t count_of(const Tree& T, int c) { return c >= 0 ? T.count[c] : 1u; }
-__device__ __forceinline__ bool leaf_of(const Tree& T, int c) { return count_of(T, c) <= kLeafMax; }
+// a child slot holds a leaf: a triangle, or a subtree the collapse's program made one
+__device__ __forceinline__ bool dp_leaf(const Dp& D, int c) { return c < 0 || D.leaf[c] != 0; }
 // the triangles under a subtree of at most kLeafMax triangles, left to right
 __device__ __forceinline__ uint32_t gather(const Tree& T, int c, uint32_t* out) {
   int st[2 * kLeafMax];
@@ -294,37 +359,38 @@ __device__ __forceinline__ uint32_t gather(const Tree& T, int c, uint32_t* out) 
 __device__ __forceinline__ void box_of(const Tree& T, int c, float4& lo, float4& hi) {
   if (c >= 0) { lo = T.nlo[c]; hi = T.nhi[c]; } else { lo = T.plo[T.order[~c]]; hi = T.phi[T.order[~c]]; }
 }
-__device__ __forceinline__ float area_of(const Tree& T, int c) {
-  float4 lo, hi;
-  box_of(T, c, lo, hi);
-  return box_area(lo, hi);
-}
 
-// level pass 1: each wide node's children (the host builder's greedy opening), inner-child and triangle counts
-__global__ void k_collapse_count(Tree T, const int* wideSrc, uint32_t b, uint32_t e, int* kids, uint32_t* nInner, uint32_t* nTri) {
+// level pass 1: each wide node's children as the collapse's program chose them (left to right), inner-child and
+// triangle counts
+__global__ void k_collapse_count(Tree T, Dp D, const int* wideSrc, uint32_t b, uint32_t e, int* kids, uint32_t* nInner, uint32_t* nTri) {
   const uint32_t w = b + blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= e) return;
   const int src = wideSrc[w];
   int ch[8];
   int n = 0;
-  if (leaf_of(T, src)) ch[n++] = src;   // a leaf root: one leaf child
-  else {
-    ch[n++] = T.left[src]; ch[n++] = T.right[src];
-    while (n < 8) {
-      int best = -1;
-      float bestA = -1.f;
-      for (int k = 0; k < n; ++k)
-        if (!leaf_of(T, ch[k])) { const float a = area_of(T, ch[k]); if (a > bestA) { bestA = a; best = k; } }
-      if (best < 0) break;
-      const int c = ch[best];
-      ch[best] = T.left[c];
-      ch[n++] = T.right[c];
+  if (dp_leaf(D, src)) ch[n++] = src;   // a leaf root: one leaf child
+  else {   // the 8 slots split between src's children, each share expanded by its eff / split choices
+    int stN[8], stI[8];
+    int sp = 0;
+    const int k8 = D.split[size_t(src) * 8];
+    stN[sp] = T.right[src]; stI[sp++] = 8 - k8;
+    stN[sp] = T.left[src]; stI[sp++] = k8;
+    while (sp && n < 8) {   // the shares on the stack sum to at most 8 - n, each at least 1
+      --sp;
+      const int c = stN[sp], i = stI[sp];
+      if (c < 0) { ch[n++] = c; continue; }
+      const int j = D.eff[size_t(c) * 8 + i - 1];
+      if (j <= 1) { ch[n++] = c; continue; }
+      const int k = D.split[size_t(c) * 8 + j - 1];
+      if (sp + 2 > 8) break;
+      stN[sp] = T.right[c]; stI[sp++] = j - k;
+      stN[sp] = T.left[c]; stI[sp++] = k;
     }
   }
   uint32_t ni = 0, nt = 0;
   for (int k = 0; k < 8; ++k) {
     kids[size_t(w - b) * 8 + k] = k < n ? ch[k] : INT32_MIN;
-    if (k < n) { if (leaf_of(T, ch[k])) nt += count_of(T, ch[k]); else ++ni; }
+    if (k < n) { if (dp_leaf(D, ch[k])) nt += count_of(T, ch[k]); else ++ni; }
   }
   nInner[w - b] = ni;
   nTri[w - b] = nt;
@@ -345,7 +411,7 @@ __device__ __forceinline__ void quant_axis(float p, float hi, uint32_t& eb, floa
 }
 
 // level pass 2: node records, triangle records, the next level's sources
-__global__ void k_collapse_emit(Tree T, const float* v, const uint32_t* tri, const uint32_t* slot, const uint8_t* translucent, uint32_t b,
+__global__ void k_collapse_emit(Tree T, Dp D, const float* v, const uint32_t* tri, const uint32_t* slot, const uint8_t* translucent, uint32_t b,
                                 uint32_t e, const int* kids, const uint32_t* innerOff, const uint32_t* triOff, uint32_t triBase0,
                                 uint32_t* nodes, float* tris, int* wideSrc) {
   const uint32_t w = b + blockIdx.x * blockDim.x + threadIdx.x;
@@ -376,7 +442,7 @@ __global__ void k_collapse_emit(Tree T, const float* v, const uint32_t* tri, con
       q[a][k] = uint32_t(fmax(0.0, fmin(255.0, ql)));
       q[3 + a][k] = uint32_t(fmax(0.0, fmin(255.0, qh)));
     }
-    if (!leaf_of(T, ch[k])) {
+    if (!dp_leaf(D, ch[k])) {
       imask |= 1u << k;
       wideSrc[childBase + inner++] = ch[k];
     } else {
@@ -427,7 +493,7 @@ std::string build_bvh8_gpu(const float* v, size_t nv, const uint32_t* tri, size_
   if (nt >= (size_t(1) << 31) - 1) return "more than 2^31 triangles";
   const int n = int(nt);
   DevBuf dv, dtri, dslot, dtr, plo, phi, cen, cb, keys, keys2, vals, vals2, left, right, parent, leafParent, range, nlo, nhi, arr, cnt, cost, wideSrc,
-      kids, nInner, nTri, offI, offT, tmp, maxabs;
+      kids, nInner, nTri, offI, offT, tmp, maxabs, dpCost, dpEff, dpSplit, dpLeaf;
   const size_t tiles = (nt + 255) / 256;
   KGB_TRY(cudaMalloc(&dv.p, nv * 12));
   KGB_TRY(cudaMalloc(&dtri.p, nt * 12));
@@ -484,6 +550,14 @@ std::string build_bvh8_gpu(const float* v, size_t nv, const uint32_t* tri, size_
       k_bottom_up<<<unsigned(tiles), 256, 0, st>>>(T2, n, arr.as<uint32_t>(), pass > 0 ? 1 : 0);
     }
   }
+  // 6a. the collapse's program, bottom-up over the final tree
+  KGB_TRY(cudaMalloc(&dpCost.p, ni * 32)); KGB_TRY(cudaMalloc(&dpEff.p, ni * 8)); KGB_TRY(cudaMalloc(&dpSplit.p, ni * 8));
+  KGB_TRY(cudaMalloc(&dpLeaf.p, ni));
+  const Dp D{dpCost.as<float>(), dpEff.as<uint8_t>(), dpSplit.as<uint8_t>(), dpLeaf.as<uint8_t>()};
+  if (n > 1) {
+    KGB_TRY(cudaMemsetAsync(arr.p, 0, ni * 4, st));
+    k_collapse_dp<<<unsigned(tiles), 256, 0, st>>>(T2, D, n, arr.as<uint32_t>());
+  }
   // 6-7. collapse level by level into the output buffers
   void* nodes = nullptr;
   void* tris = nullptr;
@@ -504,7 +578,7 @@ std::string build_bvh8_gpu(const float* v, size_t nv, const uint32_t* tri, size_
   for (int level = 0; b < e; ++level) {
     if (level > 4096) return "bvh collapse: too many levels";
     const uint32_t cnt = e - b, blocks = (cnt + 127) / 128;
-    k_collapse_count<<<blocks, 128, 0, st>>>(T, wideSrc.as<int>(), b, e, kids.as<int>(), nInner.as<uint32_t>(), nTri.as<uint32_t>());
+    k_collapse_count<<<blocks, 128, 0, st>>>(T, D, wideSrc.as<int>(), b, e, kids.as<int>(), nInner.as<uint32_t>(), nTri.as<uint32_t>());
     size_t sb = tmpBytes;
     KGB_TRY(cub::DeviceScan::ExclusiveSum(tmp.p, sb, nInner.as<uint32_t>(), offI.as<uint32_t>(), int(cnt), st));
     KGB_TRY(cub::DeviceScan::ExclusiveSum(tmp.p, sb, nTri.as<uint32_t>(), offT.as<uint32_t>(), int(cnt), st));
@@ -513,7 +587,7 @@ std::string build_bvh8_gpu(const float* v, size_t nv, const uint32_t* tri, size_
     KGB_TRY(cudaMemcpyAsync(&lastI[1], nInner.as<uint32_t>() + cnt - 1, 4, cudaMemcpyDeviceToHost, st));
     KGB_TRY(cudaMemcpyAsync(&lastT[0], offT.as<uint32_t>() + cnt - 1, 4, cudaMemcpyDeviceToHost, st));
     KGB_TRY(cudaMemcpyAsync(&lastT[1], nTri.as<uint32_t>() + cnt - 1, 4, cudaMemcpyDeviceToHost, st));
-    k_collapse_emit<<<blocks, 128, 0, st>>>(T, dv.as<float>(), dtri.as<uint32_t>(), dslot.as<uint32_t>(), dtr.as<uint8_t>(), b, e, kids.as<int>(),
+    k_collapse_emit<<<blocks, 128, 0, st>>>(T, D, dv.as<float>(), dtri.as<uint32_t>(), dslot.as<uint32_t>(), dtr.as<uint8_t>(), b, e, kids.as<int>(),
                                             offI.as<uint32_t>(), offT.as<uint32_t>(), triBase, static_cast<uint32_t*>(nodes), static_cast<float*>(tris),
                                             wideSrc.as<int>());
     KGB_TRY(cudaGetLastError());
@@ -526,7 +600,7 @@ std::string build_bvh8_gpu(const float* v, size_t nv, const uint32_t* tri, size_
   }
   if (triBase != nt) return "bvh collapse: " + std::to_string(triBase) + " triangle records for " + std::to_string(nt) + " triangles";
   *nNodesOut = e;
-  *tempBytes = nt * (12 + 16 * 3 + 8 * 2 + 4 * 2 + 4 * 4 + 8 + 32 + 4 + 8) + maxNodes * (4 + 32 + 16) + tmpBytes;
+  *tempBytes = nt * (12 + 16 * 3 + 8 * 2 + 4 * 2 + 4 * 4 + 8 + 32 + 4 + 8 + 49) + maxNodes * (4 + 32 + 16) + tmpBytes;
   return "";
 }
 
