@@ -9,7 +9,7 @@
 //   3. 63-bit Morton codes of the centroids, radix-sorted with the triangle index (stable: ties keep index order)
 //   4. binary radix tree (Karras 2012): internal node i's range and split from common prefixes of the sorted codes
 //   5. boxes, triangle counts and SAH costs bottom-up (each leaf walks towards the root, the second arrival at a node
-//      refits it from its children), then three such passes that also restructure each node's treelet of up to 7
+//      refits it from its children), then ten such passes that also restructure each node's treelet of up to 7
 //      leaves to its least-SAH topology (Karras & Aila 2013)
 //   6. SAH-optimal collapse to 8-wide nodes (Ylitie, Karras & Laine 2017): a bottom-up dynamic program gives each
 //      binary node the least SAH cost of its subtree as at most i = 1..8 children of a wide node, and whether one slot
@@ -35,7 +35,7 @@ namespace kgb {
 namespace {
 
 constexpr uint32_t kLeafMax = 3;   // triangles per leaf, as the host builder
-constexpr int kTreeletPasses = 3;  // bottom-up passes of treelet restructuring
+constexpr int kTreeletPasses = 10; // bottom-up passes of treelet restructuring (views city: 3 passes 3.2 G rays/s, 10 passes 3.7)
 
 __device__ __forceinline__ uint32_t ord(float f) {   // order-preserving float -> uint
   const uint32_t u = __float_as_uint(f);
