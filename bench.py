@@ -422,6 +422,7 @@ def run_precision(args, pkg):
             "trace_mrays_s": nc_all * len(D) / tt["trace"] / 1e6, "bounce_mpaths_s": paths / tt["bounce"] / 1e6, "sky_build_s": yr["sky_s"],
             "trace_s": tt["trace"], "bounce_s": tt["bounce"], "series_tc_s": tt["tc"], "series_fp32_s_timed": tt["fp32"],
             "pipeline_s": pipeline_s - (tt["fp32"] if not args.full_fp32 else 0.0),
+            "pipeline_solves_s": nc_all * T / (pipeline_s - (tt["fp32"] if not args.full_fp32 else 0.0)),
             "E_bytes": nc_all * T * 4, "note": "series times include the E download to host memory (pageable), as the reference's gpu_series"}
     print(json.dumps(line), flush=True)
     e.close()

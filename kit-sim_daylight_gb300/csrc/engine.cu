@@ -162,6 +162,7 @@ struct Engine {
   bool bytes = false;
   size_t i0 = 0, visN = 0;
   Buf dc, contrib;   // contrib: one (bin, contribution) pair per path of a bounce launch
+  Buf border;        // a bounce launch's samples in tracing order
   size_t nBins = 0, dcN = 0, dcI0 = 0;
   Buf viewCls, viewDist, rowSin;
   size_t viewN = 0, viewK = 0, viewI0 = 0;
@@ -184,6 +185,31 @@ namespace {
 
 Engine* E(kgb_engine* e) { return reinterpret_cast<Engine*>(e); }
 const Engine* E(const kgb_engine* e) { return reinterpret_cast<const Engine*>(e); }
+
+// The samples [s0, s1) of a bounce launch in tracing order: sorted by the 2-D Morton key of their first direction's
+// coordinates before the per-sensor rotation, (s / M, radical inverse of s), so that 32 consecutive samples of a
+// sensor leave it in a narrow cone.
+int bounce_order(Engine& g, uint32_t s0, uint32_t s1, uint32_t M) {
+  const auto spread = [](uint32_t x) {   // 16 bits to the even bit positions
+    x &= 0xffffu;
+    x = (x | (x << 8)) & 0x00ff00ffu; x = (x | (x << 4)) & 0x0f0f0f0fu; x = (x | (x << 2)) & 0x33333333u; x = (x | (x << 1)) & 0x55555555u;
+    return x;
+  };
+  const auto rev = [](uint32_t x) {
+    x = (x >> 16) | (x << 16); x = ((x & 0xff00ff00u) >> 8) | ((x & 0x00ff00ffu) << 8); x = ((x & 0xf0f0f0f0u) >> 4) | ((x & 0x0f0f0f0fu) << 4);
+    x = ((x & 0xccccccccu) >> 2) | ((x & 0x33333333u) << 2); x = ((x & 0xaaaaaaaau) >> 1) | ((x & 0x55555555u) << 1);
+    return x;
+  };
+  std::vector<std::pair<uint32_t, uint32_t>> key(s1 - s0);
+  for (uint32_t smp = s0; smp < s1; ++smp) {
+    const uint32_t u = uint32_t(std::min(65535.0, double(smp) / double(M) * 65536.0)), v = rev(smp) >> 16;
+    key[smp - s0] = {(spread(v) << 1) | spread(u), smp};
+  }
+  std::sort(key.begin(), key.end());
+  std::vector<uint32_t> ord(key.size());
+  for (size_t k = 0; k < key.size(); ++k) ord[k] = key[k].second;
+  return upload(g.border, ord.data(), ord.size() * 4, g.st);
+}
 
 int download_rows(Engine& g, const void* dev, size_t esize, size_t K, size_t nc, void* host) {
   return download_rows_into(g.rows, g.staging, dev, esize, K, nc, host, g.st);
@@ -255,7 +281,7 @@ KGB_API void kgb_destroy(kgb_engine* e) {
   if (g->st) cudaStreamSynchronize(g->st);
   delete g->sc;
   for (Buf* b : {&g->slots, &g->P, &g->N, &g->D, &g->rayTab, &g->vis, &g->dc, &g->contrib, &g->viewCls, &g->viewDist, &g->rowSin, &g->label, &g->scratch, &g->out, &g->ctl,
-                 &g->vop, &g->sop, &g->csr, &g->sunCol}) b->free();
+                 &g->vop, &g->sop, &g->csr, &g->sunCol, &g->rows, &g->border}) b->free();
   g->staging.free();
   for (cudaEvent_t ev : g->ev) if (ev) cudaEventDestroy(ev);
   if (g->st && g->ownStream) cudaStreamDestroy(g->st);
@@ -604,6 +630,8 @@ KGB_API int kgb_bounce(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, c
     if (!grow(g.contrib, n * nc * 8)) return 0;
     a.contrib = static_cast<uint2*>(g.contrib.p);
     a.s0 = uint32_t(done); a.s1 = uint32_t(done + n);
+    if (!bounce_order(g, a.s0, a.s1, b->M)) return 0;
+    a.order = static_cast<const uint32_t*>(g.border.p);
     if (!reset_ctl(g)) return 0;
     CU(cudaEventRecord(g.ev[0], g.st));
     launch_bounce(a, g.st);

@@ -72,6 +72,7 @@ struct BounceArgs {
   float* dc;
   uint2* contrib;     // [(s1 - s0) x n]: each path's sky bin (or none) and contribution
   uint32_t* status;
+  const uint32_t* order;   // [s1 - s0]: the launch's samples in tracing order (sensor-major), or null (sample-major)
 };
 
 void launch_ray_table(const float* D, uint32_t nDir, void* tab, cudaStream_t st);   // 48 bytes per direction

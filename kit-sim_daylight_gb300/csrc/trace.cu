@@ -64,9 +64,10 @@ __device__ __forceinline__ float crossing(const kgb_slot* slots, uint32_t nSlots
 constexpr int kMaxCross = 16;   // translucent crossings a ray keeps in registers before it walks them in order instead
 
 // Own-plane hits pass (at most 3), an opaque hit blocks, translucent crossings multiply in (t, primitive) order.
-__device__ uint8_t trace_byte(const Scene& s, const TraceArgs& a, F3 o, F3 n, F3 dir, bool cull, uint32_t& overflow) {
+// d: the direction's index, whose precomputed ray part (a.rayTab, when set) gives the ray make_ray would.
+__device__ uint8_t trace_byte(const Scene& s, const TraceArgs& a, F3 o, F3 n, uint32_t d, F3 dir, bool cull, uint32_t& overflow) {
   if (!(n.x * dir.x + n.y * dir.y + n.z * dir.z > 0.f)) return 0;
-  const Ray r = make_ray(o, dir);
+  const Ray r = a.rayTab ? ray_from(a.rayTab, d, o) : make_ray(o, dir);
   bool blocked = false, spill = false;
   int own = 0, nx = 0;
   float ct[kMaxCross], cf[kMaxCross];
@@ -132,7 +133,7 @@ __global__ void __launch_bounds__(256) k_bytes(TraceArgs a) {
     for (uint32_t k = 0; k < 32; ++k) {
       const uint32_t d = w * 32 + k;
       if (d >= a.nDir) break;
-      a.bytes[size_t(d) * a.stride + a.out0 + i] = trace_byte(s, a, o, n, ld3(a.D + 3 * d), cull, overflow);
+      a.bytes[size_t(d) * a.stride + a.out0 + i] = trace_byte(s, a, o, n, d, ld3(a.D + 3 * d), cull, overflow);
     }
   }
   if (overflow) atomicOr(a.status, (overflow & 1u ? kStatusStackOverflow : 0u) | (overflow & 2u ? kStatusVisitLimit : 0u));
@@ -240,13 +241,17 @@ __device__ __forceinline__ uint32_t sky_bin(F3 d, uint32_t mf, uint32_t nBins, f
 constexpr uint64_t kBounceLimitNs = 10000000000ull;   // 10 s: past it a path stops and records kStatusTimeout
 constexpr uint32_t kNoBin = 0xffffffffu;
 
-// One path per thread: sensor i = t % n, sample s0 + t / n. A path adds to at most one sky bin (where it escapes after
-// a reflection): it leaves that bin and its contribution (w x pi / M) in contrib[t], and k_bounce_accum adds them to
-// each sensor's rows in sample order, as the reference's per-sensor loop over samples does.
+// One path per thread. With a.order, sensor i = t / S and sample a.order[t % S] (S = s1 - s0): a warp's 32 paths start
+// at one sensor, and the order (the host sorts the launch's samples by their first direction before the per-sensor
+// rotation) keeps their first directions in a narrow cone, so their walks share nodes; without it sensor i = t % n,
+// sample s0 + t / n. A path adds to at most one sky bin (where it escapes after a reflection): it leaves that bin and
+// its contribution (w x pi / M) in contrib[(sample - s0) n + i], and k_bounce_accum adds them to each sensor's rows in
+// sample order, as the reference's per-sensor loop over samples does; the tracing order changes no result.
 __global__ void __launch_bounds__(128) k_bounce_paths(BounceArgs a) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= a.n * (a.s1 - a.s0)) return;
-  const uint32_t i = t % a.n, smp = a.s0 + t / a.n;
+  const uint32_t S = a.s1 - a.s0;
+  if (t >= a.n * S) return;
+  const uint32_t i = a.order ? t / S : t % a.n, smp = a.order ? a.order[t % S] : a.s0 + t / a.n;
   const Scene s{a.nodes, a.tris, a.nNodes};
   const bool cull = (a.rayFlags & KGB_RAY_CULL_BACK_FACING) != 0;
   const uint32_t gi = a.i0 + i;
@@ -304,7 +309,7 @@ __global__ void __launch_bounds__(128) k_bounce_paths(BounceArgs a) {
     }
     o = add(offset_ray(h.p, h.n), h.lift);
   }
-  a.contrib[t] = make_uint2(late ? kNoBin : bin, __float_as_uint(gain));
+  a.contrib[size_t(smp - a.s0) * a.n + i] = make_uint2(late ? kNoBin : bin, __float_as_uint(gain));
   const uint32_t sum = __reduce_add_sync(__activemask(), segments);
   if ((threadIdx.x & 31) == __ffs(__activemask()) - 1) atomicAdd(reinterpret_cast<unsigned long long*>(a.status + 1), (unsigned long long)sum);
   if (overflow || late)
