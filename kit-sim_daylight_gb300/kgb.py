@@ -298,7 +298,9 @@ class Engine:
         self._ok(self.d.kgb_download_bytes_rows(self.h, nc, _p(out), nd * nc))
         return out.reshape(nc, nd)
 
-    def series(self, nc, nSky, row, wsky, S, g, G, sun0, sunStep, sunVec, sunW, Sdc=None):
+    def series(self, nc, nSky, row, wsky, S, g, G, sun0, sunStep, sunVec, sunW, Sdc=None, out=None):
+        """E [nc x T] (float32); out: a C-contiguous float32 buffer of that shape to write into (the reference's caller
+        reuses one E vector across chunks, run.cpp:683-686), else a new array."""
         row = np.ascontiguousarray(row, dtype=np.int32)
         wsky, S, g, G = _f32(wsky), _f32(S), _f32(g), _f32(G)
         P, T = S.shape
@@ -308,7 +310,12 @@ class Engine:
         s = SeriesIn(nSky, _typed(row, c_int32), _typed(wsky, c_float), _typed(S, c_float), P, T, _typed(g, c_float), _typed(G, c_float),
                      sun0, len(sunStep), _typed(sunStep, c_int32), _typed(sunVec, c_float), _typed(sunW, c_float),
                      _typed(Sdc, c_float) if Sdc is not None else None)
-        E = np.zeros((nc, T), np.float32)
+        if out is None:
+            E = np.zeros((nc, T), np.float32)
+        else:
+            E = out
+            if E.dtype != np.float32 or E.shape != (nc, T) or not E.flags.c_contiguous:
+                raise ValueError("series: out must be a C-contiguous float32 [nc x T] array")
         self._ok(self.d.kgb_series(self.h, nc, ctypes.byref(s), _p(E)))
         return E
 
