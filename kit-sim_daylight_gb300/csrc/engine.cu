@@ -149,6 +149,8 @@ struct SceneObj {
 
 }  // namespace
 
+constexpr uint32_t kSeriesBands = 4;   // bands of a chunk's series whose downloads overlap the next band's kernel
+
 struct Engine {
   int device = 0, numSMs = 0;
   cudaStream_t st = nullptr;
@@ -176,6 +178,8 @@ struct Engine {
   Buf vop, sop, csr, sunCol;
   Staging staging;   // pinned slices for the series download
   Buf rows;          // sensor-major rows of one slice of a direction-major buffer (download_rows)
+  cudaStream_t copySt = nullptr;                  // the series' E downloads, beside the next band's kernel
+  cudaEvent_t bandEv[kSeriesBands] = {};
   kgb_stats stats{};
   int gridBits = 0, gridBytes = 0, gridView = 0;
   int builder = 1;            // 1 device LBVH with treelet restructuring (default), 0 host binned SAH (kgb_set_builder)
@@ -284,6 +288,8 @@ KGB_API void kgb_destroy(kgb_engine* e) {
                  &g->vop, &g->sop, &g->csr, &g->sunCol, &g->rows, &g->border}) b->free();
   g->staging.free();
   for (cudaEvent_t ev : g->ev) if (ev) cudaEventDestroy(ev);
+  for (cudaEvent_t ev : g->bandEv) if (ev) cudaEventDestroy(ev);
+  if (g->copySt) { cudaStreamSynchronize(g->copySt); cudaStreamDestroy(g->copySt); }
   if (g->st && g->ownStream) cudaStreamDestroy(g->st);
   delete g;
 }
@@ -569,12 +575,27 @@ KGB_API int kgb_series(kgb_engine* e, size_t nc, const kgb_series_in* in, float*
     if (!reset_ctl(g)) return 0;
     build_series_operands(p, o, g.st);
     CU(cudaGetLastError());
-    if (const char* why = series_tc(p, g.st)) return fail(why);
-    CU(cudaGetLastError());
+    // E in bands of sensor rows: every band's kernel is queued on the engine's stream, and each band's rows go down
+    // on the copy stream once its kernel is done, beside the next band's kernel (the first band's event also orders
+    // the copies after this call's uploads, which used the same staging slices)
+    const uint32_t mAll = uint32_t((nc + 127) / 128), bands = mAll >= 8 * kSeriesBands ? kSeriesBands : 1, per = (mAll + bands - 1) / bands;
+    if (!g.copySt) CU(cudaStreamCreateWithFlags(&g.copySt, cudaStreamNonBlocking));
+    for (uint32_t b = 0; b < bands; ++b) {
+      if (!g.bandEv[b]) CU(cudaEventCreateWithFlags(&g.bandEv[b], cudaEventDisableTiming));
+      if (const char* why = series_tc_rows(p, b * per, std::min(per, mAll - b * per), g.st)) return fail(why);
+      CU(cudaGetLastError());
+      CU(cudaEventRecord(g.bandEv[b], g.st));
+    }
+    for (uint32_t b = 0; b < bands; ++b) {
+      const size_t r0 = size_t(b) * per * 128, r1 = std::min(nc, size_t(b + 1) * per * 128);
+      CU(cudaStreamWaitEvent(g.copySt, g.bandEv[b], 0));
+      if (!download_large(g.staging, Eh + r0 * T, static_cast<const float*>(g.out.p) + r0 * T, (r1 - r0) * T * 4, g.copySt)) return 0;
+    }
     uint32_t status = 0;
     CU(cudaMemcpyAsync(&status, static_cast<uint32_t*>(g.ctl.p) + 1, 4, cudaMemcpyDeviceToHost, g.st));
     CU(cudaStreamSynchronize(g.st));
     if (status & kStatusTimeout) return fail("gpu_series: the tensor-core pipeline timed out waiting (status recorded by the kernel)");
+    return 1;
   }
   return download_large(g.staging, Eh, g.out.p, nc * T * 4, g.st);
 }

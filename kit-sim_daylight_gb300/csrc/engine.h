@@ -159,6 +159,8 @@ struct SeriesOperands {
 };
 void build_series_operands(const SeriesTcPlan& p, const SeriesOperands& o, cudaStream_t st);
 const char* series_tc(const SeriesTcPlan& p, cudaStream_t st);   // null, or what failed
+// the rows of 128-sensor tiles mBase .. mBase + mCount - 1 only (E's rows mBase * 128 .. , the others untouched)
+const char* series_tc_rows(const SeriesTcPlan& p, uint32_t mBase, uint32_t mCount, cudaStream_t st);
 
 // What a reduce of the last trace reads, for the reduce entry points outside engine.cu (reduce_noalloc.cu).
 struct ReduceInputs {

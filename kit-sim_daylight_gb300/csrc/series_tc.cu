@@ -133,6 +133,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 
 struct SeriesTcArgs {
   uint32_t nc, T, Kp, mTiles, nTiles;
+  uint32_t mBase;            // the launch's first row of tiles (a launch covers rows of tiles mBase .. mBase + mTiles - 1)
   // sun term of the epilogue (the reference's k_series tail, gpu.cu:145-148): column t's sun direction, if any
   const int32_t* sunOfCol;   // [T] -> j or -1
   const float* sunVec;       // [nSun x 3]
@@ -202,7 +203,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
       for (uint32_t tile = blockIdx.x; tile < nTilesAll && !abortFlag; tile += gridDim.x) {
         uint32_t tm, tn;
         tile_coords(tile, a.mTiles, a.nTiles, tm, tn);
-        const int m0 = int(tm) * BM, n0 = int(tn) * BN;
+        const int m0 = int(tm + a.mBase) * BM, n0 = int(tn) * BN;
         for (uint32_t kb = 0; kb < kBlocks; ++kb) {
           if (!mbar_wait(&empty[stage], phase ^ 1, a.status)) { abortFlag = 1; break; }
           uint8_t* s = smem + stage * STAGE_BYTES;
@@ -295,7 +296,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
       if (!ok || abortFlag) { abortFlag = 1; break; }
       uint32_t tm, tn;
       tile_coords(tile, a.mTiles, a.nTiles, tm, tn);
-      const uint32_t m0 = tm * BM, n0 = tn * BN;
+      const uint32_t m0 = (tm + a.mBase) * BM, n0 = tn * BN;
       const uint32_t row = m0 + q * 32 + lane;         // this thread's sensor
       float nrm[3] = {0.f, 0.f, 0.f};
       if (row < a.nc) { nrm[0] = a.N[3 * row]; nrm[1] = a.N[3 * row + 1]; nrm[2] = a.N[3 * row + 2]; }
@@ -463,8 +464,11 @@ static bool make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t K
             CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-const char* series_tc(const SeriesTcPlan& p, cudaStream_t st) {
-  if (p.nc == 0 || p.T == 0) return nullptr;
+const char* series_tc(const SeriesTcPlan& p, cudaStream_t st) { return series_tc_rows(p, 0, (p.nc + BM - 1) / BM, st); }
+
+const char* series_tc_rows(const SeriesTcPlan& p, uint32_t mBase, uint32_t mCount, cudaStream_t st) {
+  if (p.nc == 0 || p.T == 0 || mCount == 0) return nullptr;
+  if (uint64_t(mBase) + mCount > (p.nc + BM - 1) / BM) return "series_tc: rows of tiles beyond the chunk";
   if (p.Kp % BK) return "series_tc: K not padded to 64";
   CUtensorMap mV, mS;
   if (!make_map(&mV, p.v, uint64_t(PIECES) * p.nc, p.Kp, BM) || !make_map(&mS, p.s, uint64_t(PIECES) * p.T, p.Kp, BN))
@@ -478,7 +482,7 @@ const char* series_tc(const SeriesTcPlan& p, cudaStream_t st) {
   }
   SeriesTcArgs a{};
   a.nc = p.nc; a.T = p.T; a.Kp = p.Kp;
-  a.mTiles = (p.nc + BM - 1) / BM; a.nTiles = (p.T + BN - 1) / BN;
+  a.mTiles = mCount; a.mBase = mBase; a.nTiles = (p.T + BN - 1) / BN;
   a.sunOfCol = p.sunOfCol; a.sunVec = p.sunVec; a.sunW = p.sunW; a.sun0 = p.sun0;
   a.bits = p.bits; a.bytes = p.bytes; a.N = p.N; a.E = p.E; a.status = p.status;
   const int grid = int(std::min<uint32_t>(uint32_t(p.numSMs), a.mTiles * a.nTiles));

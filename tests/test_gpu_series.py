@@ -108,3 +108,24 @@ def test_series_chunks_equal_whole(engine_lib, kgb, pkg):
         assert np.array_equal(part, whole[200:500])
     finally:
         e.close()
+
+
+def test_series_bands_equal_chunks(engine_lib, kgb, pkg):
+    """A chunk of at least 32 rows of 128-sensor tiles runs in four bands whose downloads overlap the next band's
+    kernel; its rows equal the same sensors' rows from chunks below that size (one band each), bit for bit."""
+    s = pkg.workloads.random_city(8, n_boxes=40)
+    P, T, nSun, nc = 145, 150, 60, 5000
+    assert len(s["P"]) >= nc
+    D = pkg.workloads.hemisphere_dirs(P, nSun, 8)
+    e = _setup(pkg, kgb, engine_lib, s, D, nc)
+    try:
+        args = _inputs(P, T, nc, D, P, nSun, 4)
+        whole = e.series(nc, **args)
+        parts = []
+        for i0, m in ((0, 3000), (3000, 2000)):
+            e.trace(i0, m, engine_lib.ray_flags(False, False))
+            parts.append(e.series(m, **dict(args, G=args["G"][i0:i0 + m])))
+        assert np.array_equal(whole, np.concatenate(parts))
+        assert np.abs(whole).max() > 0
+    finally:
+        e.close()
