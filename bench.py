@@ -236,10 +236,7 @@ def run_ours(args, pkg):
         torch.distributed.barrier()
     ms = float(sum(times) / len(times))
     ms_e2e = float(sum(e2e_t) / len(e2e_t))
-    if world > 1:
-        t = torch.tensor([ms, ms_e2e], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms, ms_e2e = t.tolist()
+    ms, ms_e2e = pkg.shard.max_over_ranks([ms, ms_e2e], device="cuda")   # the slowest rank's times (NCCL when N > 1)
     rays = nc * nDir
     launches = (st1["launches"] - st0["launches"]) // args.steps + len(Wp)
     # roofline of k_bits: algorithmic bytes = nodes x 80 + triangles tested x 48 + bits out + sensor reads per task

@@ -8,7 +8,7 @@ shim/daylight_gpu.cpp. There is no CPU fallback: `load()` raises when the librar
 import os
 import subprocess
 
-from . import kgb, workloads  # noqa: F401
+from . import kgb, shard, workloads  # noqa: F401
 from .kgb import Engine, KgbError, Lib, Slot  # noqa: F401
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
