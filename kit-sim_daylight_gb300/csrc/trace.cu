@@ -47,7 +47,8 @@ __global__ void __launch_bounds__(256) k_bits(TraceArgs a) {
 
 // ---------------------------------------------------------------------------------------------------- bytes
 // A translucent slot's crossing: tau, 1 on a thin solid's exit face, Radiance glass T(cos) (trace_dev.cu:147-165).
-__device__ __forceinline__ float crossing(const kgb_slot* slots, uint32_t nSlots, uint32_t slot, bool front, F3 v0, F3 v1, F3 v2, F3 d) {
+__device__ __forceinline__ float crossing(const kgb_slot* slots, const double* slotLog, uint32_t nSlots, uint32_t slot, bool front, F3 v0, F3 v1,
+                                         F3 v2, F3 d) {
   const kgb_slot sl = slot < nSlots ? slots[slot] : kgb_slot{0.2f, 0.f, 0.f, 0u};
   float T = sl.tau;
   if ((sl.flags & KGB_SLOT_THIN) && front == ((sl.flags & KGB_SLOT_INWARD) != 0)) T = 1.f;
@@ -56,7 +57,7 @@ __device__ __forceinline__ float crossing(const kgb_slot* slots, uint32_t nSlots
     const float bx = v2.x - v0.x, by = v2.y - v0.y, bz = v2.z - v0.z;
     const float nx = ay * bz - az * by, ny = az * bx - ax * bz, nz = ax * by - ay * bx;
     float R;
-    glass_TR(fabsf(nx * d.x + ny * d.y + nz * d.z) * (1.f / sqrtf(nx * nx + ny * ny + nz * nz)), sl.tn, T, R);
+    glass_TR(fabsf(nx * d.x + ny * d.y + nz * d.z) * (1.f / sqrtf(nx * nx + ny * ny + nz * nz)), sl.tn, slotLog[slot], T, R);
   }
   return T;
 }
@@ -75,7 +76,7 @@ __device__ uint8_t trace_byte(const Scene& s, const TraceArgs& a, F3 o, F3 n, ui
   for_hits(s, r, 1e-5f, INFINITY, cull, [&](const Hit& h, F3 v0, F3 v1, F3 v2, uint32_t flags, uint32_t slot) {
     if (own_hit(v0, v1, v2, h, dir, n)) { if (++own <= 3) return false; blocked = true; return true; }
     if (!(flags & kTriTranslucent)) { blocked = true; return true; }
-    if (nx < kMaxCross) { ct[nx] = h.t; cp[nx] = h.prim; cf[nx] = crossing(a.slots, a.nSlots, slot, h.front, v0, v1, v2, dir); ++nx; }
+    if (nx < kMaxCross) { ct[nx] = h.t; cp[nx] = h.prim; cf[nx] = crossing(a.slots, a.slotLog, a.nSlots, slot, h.front, v0, v1, v2, dir); ++nx; }
     else spill = true;
     return false;
   }, overflow);
@@ -107,7 +108,7 @@ __device__ uint8_t trace_byte(const Scene& s, const TraceArgs& a, F3 o, F3 n, ui
       if (h.t < lastT || (h.t == lastT && h.prim <= lastP)) return false;
       if (!found || h.t < bt || (h.t == bt && h.prim < bp)) {
         found = true; bt = h.t; bp = h.prim;
-        bf = crossing(a.slots, a.nSlots, slot, h.front, v0, v1, v2, dir);
+        bf = crossing(a.slots, a.slotLog, a.nSlots, slot, h.front, v0, v1, v2, dir);
       }
       return false;
     }, overflow);
@@ -292,7 +293,7 @@ __global__ void __launch_bounds__(128) k_bounce_paths(BounceArgs a) {
     if ((sl.flags & (KGB_SLOT_THIN | KGB_SLOT_TWIN)) == KGB_SLOT_THIN && h.front == ((sl.flags & KGB_SLOT_INWARD) != 0)) { o = through(h); continue; }
     const bool mirror = (sl.flags & KGB_SLOT_GLASS) != 0;
     float T = sl.tau, R = sl.rho;
-    if (mirror) { glass_TR(fabsf(dot(d, h.n)), sl.tn, T, R); if (!(sl.tau > 0.f)) T = 0.f; }
+    if (mirror) { glass_TR(fabsf(dot(d, h.n)), sl.tn, a.slotLog[c.slot], T, R); if (!(sl.tau > 0.f)) T = 0.f; }
     else if (diffuse == a.nBounce) R = 0.f;
     if (!(T + R > 0.f)) break;
     const U3 rr = pcg3d(gi, smp, k++);
@@ -356,6 +357,15 @@ void launch_bits(const TraceArgs& a, int grid, cudaStream_t st, bool count) {
 }
 void launch_bytes(const TraceArgs& a, int grid, cudaStream_t st) { k_bytes<<<grid, 256, 0, st>>>(a); }
 void launch_view(const ViewArgs& a, int grid, cudaStream_t st) { k_view<<<grid, 256, 0, st>>>(a); }
+// kgb_log_d(tn) of each slot (glass_TR's per-hit logarithm, once per slot; this file's flags, as the per-hit code's)
+__global__ void k_slot_logs(const kgb_slot* slots, uint32_t n, double* out) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) out[s] = slots[s].tn > 0.f ? kgb_log_d((double)slots[s].tn) : 0.0;
+}
+void launch_slot_logs(const kgb_slot* slots, uint32_t n, double* out, cudaStream_t st) {
+  if (n) k_slot_logs<<<(n + 127) / 128, 128, 0, st>>>(slots, n, out);
+}
+
 void launch_bounce(const BounceArgs& a, cudaStream_t st) {
   const size_t paths = size_t(a.n) * (a.s1 - a.s0);
   k_bounce_paths<<<unsigned((paths + 127) / 128), 128, 0, st>>>(a);
