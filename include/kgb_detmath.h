@@ -93,15 +93,16 @@ KGB_HD double kgb_log_d(double x) {
   return (double)e * 0.69314718055994530942 + 2.0 * s * p;
 }
 
-/* exp(x) in double for |x| < 700: x = k ln2 + r, |r| <= ln2 / 2, Taylor series of e^r to r^16, times 2^k. */
+/* exp(x) in double for |x| < 700: x = k ln2 + r, |r| <= ln2 / 2, Taylor series of e^r to r^16 by Horner's rule, times
+ * 2^k. Every multiply-add is an explicit fma (one rounding, the same on both sides): 18 fused operations. */
 KGB_HD double kgb_exp_d(double x) {
   const double k = rint(x * 1.44269504088896340736);
-  const double r = (x - k * 0.693147180369123816490) - k * 1.90821492927058770002e-10; /* ln 2 = hi + lo */
+  const double r = fma(-k, 1.90821492927058770002e-10, fma(-k, 0.693147180369123816490, x)); /* x - k ln 2, ln 2 = hi + lo */
   double p = 1.0 / 20922789888000.0; /* 1/16! */
   const double inv[16] = {1.0, 1.0, 1.0 / 2, 1.0 / 6, 1.0 / 24, 1.0 / 120, 1.0 / 720, 1.0 / 5040, 1.0 / 40320,
                           1.0 / 362880, 1.0 / 3628800, 1.0 / 39916800, 1.0 / 479001600, 1.0 / 6227020800.0,
                           1.0 / 87178291200.0, 1.0 / 1307674368000.0};
-  for (int j = 15; j >= 0; --j) p = inv[j] + r * p;
+  for (int j = 15; j >= 0; --j) p = fma(r, p, inv[j]);
   return ldexp(p, (int)k);
 }
 
