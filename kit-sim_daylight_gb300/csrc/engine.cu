@@ -165,6 +165,8 @@ struct Engine {
   size_t i0 = 0, visN = 0;
   Buf dc, contrib;   // contrib: one (bin, contribution) pair per path of a bounce launch
   Buf border;        // a bounce launch's samples in tracing order
+  Buf bq;            // a bounce launch's two queues of paths that go on
+  int gridStep = 0;
   Buf slotLog;       // kgb_log_d(tn) per slot (glass transmission)
   size_t nBins = 0, dcN = 0, dcI0 = 0;
   Buf viewCls, viewDist, rowSin;
@@ -286,7 +288,7 @@ KGB_API void kgb_destroy(kgb_engine* e) {
   if (g->st) cudaStreamSynchronize(g->st);
   delete g->sc;
   for (Buf* b : {&g->slots, &g->P, &g->N, &g->D, &g->rayTab, &g->vis, &g->dc, &g->contrib, &g->viewCls, &g->viewDist, &g->rowSin, &g->label, &g->scratch, &g->out, &g->ctl,
-                 &g->vop, &g->sop, &g->csr, &g->sunCol, &g->rows, &g->border, &g->slotLog}) b->free();
+                 &g->vop, &g->sop, &g->csr, &g->sunCol, &g->rows, &g->border, &g->slotLog, &g->bq}) b->free();
   g->staging.free();
   for (cudaEvent_t ev : g->ev) if (ev) cudaEventDestroy(ev);
   for (cudaEvent_t ev : g->bandEv) if (ev) cudaEventDestroy(ev);
@@ -646,20 +648,22 @@ KGB_API int kgb_bounce(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, c
   a.rayFlags = rayFlags; a.slots = static_cast<const kgb_slot*>(g.slots.p); a.nSlots = g.nSlots;
   a.slotLog = static_cast<const double*>(g.slotLog.p);
   a.dc = static_cast<float*>(g.dc.p); a.status = static_cast<uint32_t*>(g.ctl.p) + 1;
-  const size_t nCap = std::max<size_t>(1, (size_t(256) << 20) / (8 * nc));   // per-path results of a launch: at most 256 MiB
+  // paths of a launch: at most 2^23 (their results 64 MiB, the two queues of paths that go on 768 MiB)
+  const size_t nCap = std::max<size_t>(1, (size_t(1) << 23) / nc);
+  if (!g.gridStep) g.gridStep = g.numSMs * bounce_step_blocks_per_sm();
   // the reference starts at 2^13 / nc samples (1..64); here also at least ~4 paths per resident thread (a path a thread)
   const size_t fill = (size_t(4) * size_t(g.numSMs) * 2048 + nc - 1) / nc;
   for (size_t done = 0, n = std::max(std::clamp<size_t>((size_t(1) << 13) / nc, 1, 64), fill); done < b->M;) {
     if (b->cancel && b->cancel(b->cancelCtx)) return fail("cancelled");
     n = std::min({n, size_t(b->M) - done, nCap});
-    if (!grow(g.contrib, n * nc * 8)) return 0;
+    if (!grow(g.contrib, n * nc * 8) || !grow(g.bq, 2 * n * nc * bounce_state_bytes())) return 0;
     a.contrib = static_cast<uint2*>(g.contrib.p);
     a.s0 = uint32_t(done); a.s1 = uint32_t(done + n);
     if (!bounce_order(g, a.s0, a.s1, b->M)) return 0;
     a.order = static_cast<const uint32_t*>(g.border.p);
     if (!reset_ctl(g)) return 0;
     CU(cudaEventRecord(g.ev[0], g.st));
-    launch_bounce(a, g.st);
+    launch_bounce(a, static_cast<PathState*>(g.bq.p), static_cast<uint32_t*>(g.ctl.p) + 28, g.gridStep, g.st);
     CU(cudaEventRecord(g.ev[1], g.st));
     uint32_t ctl[32] = {};
     CU(cudaMemcpyAsync(ctl, g.ctl.p, 128, cudaMemcpyDeviceToHost, g.st));

@@ -58,6 +58,7 @@ struct ViewArgs {
   uint32_t* status;
 };
 
+struct PathState;   // a path between segments (trace.cu)
 struct BounceArgs {
   const Node8* nodes;
   const TriRec* tris;
@@ -75,6 +76,10 @@ struct BounceArgs {
   uint32_t* status;
   const uint32_t* order;   // [s1 - s0]: the launch's samples in tracing order (sensor-major), or null (sample-major)
   const double* slotLog;   // [nSlots]: kgb_log_d(tn) per slot (k_slot_logs)
+  const PathState* qIn;    // the paths a step continues, and their count
+  const uint32_t* qInCount;
+  PathState* qOut;         // the paths that go on after it, appended
+  uint32_t* qOutCount;
 };
 
 void launch_ray_table(const float* D, uint32_t nDir, void* tab, cudaStream_t st);   // 48 bytes per direction
@@ -87,7 +92,9 @@ int bits_blocks_per_sm();
 void launch_bits(const TraceArgs& a, int grid, cudaStream_t st, bool count = false);
 void launch_bytes(const TraceArgs& a, int grid, cudaStream_t st);
 void launch_view(const ViewArgs& a, int grid, cudaStream_t st);
-void launch_bounce(const BounceArgs& a, cudaStream_t st);
+void launch_bounce(const BounceArgs& a, PathState* queues, uint32_t* qCount, int stepGrid, cudaStream_t st);
+size_t bounce_state_bytes();   // one queued path
+int bounce_step_blocks_per_sm();
 
 // reductions (reduce.cu)
 void launch_reduce_bits(const uint32_t* bits, uint32_t nc, uint32_t nWords, uint32_t nDir, const float* N, const float* D, const float* W,

@@ -2,7 +2,9 @@
 //  k_bits   visibility bits, any-hit (replaces the reference's __raygen__bits, trace_dev.cu:91-108)
 //  k_bytes  transmittance bytes (replaces __raygen__bytes + __anyhit__tr, trace_dev.cu:115-165)
 //  k_view   class + distance of the closest hit per view cell (replaces __raygen__view, trace_dev.cu:177-232)
-//  k_bounce reflected-light paths binned by sky patch (replaces __raygen__bounce, trace_dev.cu:260-311)
+//  k_bounce_paths, k_bounce_step, k_bounce_accum
+//           reflected-light paths binned by sky patch (replaces __raygen__bounce, trace_dev.cu:260-311), as a wavefront
+//           of segments: first segments, then steps over a compacted queue of the paths that go on
 // The visibility kernels are persistent: each warp takes tasks of 32 consecutive sensors x one 32-direction word
 // from a global counter, so a warp traces one direction for 32 neighbouring sensors at a time (coherent rays).
 #include "engine.h"
@@ -239,15 +241,92 @@ __device__ __forceinline__ uint32_t sky_bin(F3 d, uint32_t mf, uint32_t nBins, f
   return b + uint32_t(az * (float(n) / 6.28318531f) + .5f) % n;
 }
 
-constexpr uint64_t kBounceLimitNs = 10000000000ull;   // 10 s: past it a path stops and records kStatusTimeout
 constexpr uint32_t kNoBin = 0xffffffffu;
 
-// One path per thread. With a.order, sensor i = t / S and sample a.order[t % S] (S = s1 - s0): a warp's 32 paths start
-// at one sensor, and the order (the host sorts the launch's samples by their first direction before the per-sensor
-// rotation) keeps their first directions in a narrow cone, so their walks share nodes; without it sensor i = t % n,
-// sample s0 + t / n. A path adds to at most one sky bin (where it escapes after a reflection): it leaves that bin and
-// its contribution (w x pi / M) in contrib[(sample - s0) n + i], and k_bounce_accum adds them to each sensor's rows in
-// sample order, as the reference's per-sensor loop over samples does; the tracing order changes no result.
+// A path between segments (48 bytes): where it is, where it goes, its weight and counters.
+struct __align__(16) PathState {
+  float ox, oy, oz;
+  uint32_t gi;       // global sensor index
+  float dx, dy, dz;
+  uint32_t smp;      // sample
+  float w;
+  uint32_t k;        // random-number counter
+  uint32_t bits;     // diffuse reflections (bits 0-7), reflected (bit 8), segments done (bits 16-31)
+  uint32_t at;       // its result's index: contrib[(sample - s0) n + i]
+};
+
+// One segment of a path: the body of the reference's per-sample loop (trace_dev.cu:260-311). Returns true when the path
+// goes on (o, d, w, k, diffuse, reflected updated), false when it has ended (bin and gain set if it escaped after a
+// reflection). nn: the sensor's normal, read on the first segment only.
+__device__ __forceinline__ bool bounce_segment(const BounceArgs& a, const Scene& s, bool cull, uint32_t seg, F3 nn, uint32_t gi, uint32_t smp, F3& o,
+                                               F3& d, float& w, uint32_t& k, uint32_t& diffuse, bool& reflected, uint32_t& bin, float& gain,
+                                               uint32_t& overflow) {
+  ClosestOut c;
+  const bool found = closest(s, make_ray(o, d), 1e-5f, FLT_MAX, cull, c, overflow);
+  if (overflow & 2u) {   // the walk gave up: the first such path leaves its ray for the error message
+    uint32_t* diag = a.status + 15;   // ctl words 16..
+    if (atomicCAS(diag, 0u, 1u) == 0u) {
+      diag[1] = gi; diag[2] = smp; diag[3] = seg;
+      diag[4] = __float_as_uint(o.x); diag[5] = __float_as_uint(o.y); diag[6] = __float_as_uint(o.z);
+      diag[7] = __float_as_uint(d.x); diag[8] = __float_as_uint(d.y); diag[9] = __float_as_uint(d.z);
+    }
+    return false;
+  }
+  if (!found) {
+    if (reflected) { bin = sky_bin(d, a.mf, a.nBins, a.alpha, a.cosN, a.sinN); gain = w * (3.14159265f / float(a.M)); }
+    return false;
+  }
+  const kgb_slot sl = c.slot < a.nSlots ? a.slots[c.slot] : kgb_slot{0.2f, 0.f, 0.f, 0u};
+  TriHit h;
+  if (!tri_geom(c.v0, c.v1, c.v2, c.h, h)) return false;
+  if (seg == 0 && own_plane(h, c.h.t, d, nn)) { o = through(h); return true; }
+  if ((sl.flags & (KGB_SLOT_THIN | KGB_SLOT_TWIN)) == KGB_SLOT_THIN && h.front == ((sl.flags & KGB_SLOT_INWARD) != 0)) { o = through(h); return true; }
+  const bool mirror = (sl.flags & KGB_SLOT_GLASS) != 0;
+  float T = sl.tau, R = sl.rho;
+  if (mirror) { glass_TR(fabsf(dot(d, h.n)), sl.tn, a.slotLog[c.slot], T, R); if (!(sl.tau > 0.f)) T = 0.f; }
+  else if (diffuse == a.nBounce) R = 0.f;
+  if (!(T + R > 0.f)) return false;
+  const U3 rr = pcg3d(gi, smp, k++);
+  w *= T + R;
+  if (u01(rr.x) * (T + R) < T) { o = through(h); return true; }
+  reflected = true;
+  if (mirror) d = sub(d, mul(2.f * dot(d, h.n), h.n));
+  else {
+    d = cosine_dir(h.n, u01(rr.y), u01(rr.z));
+    if (++diffuse >= 2) {
+      if (u01(pcg3d(gi, smp, k++).x) >= w) return false;
+      w = 1.f;
+    }
+  }
+  o = add(offset_ray(h.p, h.n), h.lift);
+  return true;
+}
+
+// The warp's paths that go on, appended to the queue in lane order with one atomic per warp.
+__device__ __forceinline__ void enqueue(bool go, const PathState& st, PathState* q, uint32_t* count) {
+  const uint32_t lane = threadIdx.x & 31, act = __activemask(), m = __ballot_sync(act, go);
+  if (!m) return;
+  const uint32_t leader = __ffs(act) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(count, __popc(m));
+  base = __shfl_sync(act, base, leader);
+  if (go) q[base + __popc(m & ((1u << lane) - 1u))] = st;
+}
+
+__device__ __forceinline__ void add_segments(const BounceArgs& a, uint32_t segments) {
+  const uint32_t sum = __reduce_add_sync(__activemask(), segments);
+  if ((threadIdx.x & 31) == __ffs(__activemask()) - 1) atomicAdd(reinterpret_cast<unsigned long long*>(a.status + 1), (unsigned long long)sum);
+}
+
+// Paths as a wavefront: k_bounce_paths traces every path's first segment, one thread a path; with a.order, sensor
+// i = t / S and sample a.order[t % S] (S = s1 - s0): a warp's 32 paths start at one sensor and the order (the host sorts
+// the launch's samples by their first direction before the per-sensor rotation) keeps their first directions in a
+// narrow cone, so their walks share nodes; without it sensor i = t % n, sample s0 + t / n. The paths that go on are
+// compacted into a queue, and k_bounce_step runs one more segment of each queued path, at most nBounce + 15 times, so
+// a warp's lanes stay busy whatever the lengths of its paths. A path's segments are the reference's loop body in order
+// with its own counters, so where and when it runs changes no result. A path that ends leaves its sky bin (where it
+// escaped after a reflection, or none) and contribution (w x pi / M) in contrib[(sample - s0) n + i]; k_bounce_accum
+// adds them to each sensor's rows in sample order, as the reference's per-sensor loop over samples does.
 __global__ void __launch_bounds__(128) k_bounce_paths(BounceArgs a) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t S = a.s1 - a.s0;
@@ -256,65 +335,61 @@ __global__ void __launch_bounds__(128) k_bounce_paths(BounceArgs a) {
   const Scene s{a.nodes, a.tris, a.nNodes};
   const bool cull = (a.rayFlags & KGB_RAY_CULL_BACK_FACING) != 0;
   const uint32_t gi = a.i0 + i;
-  const F3 nn = ld3(a.N + 3 * gi), o0 = offset_ray(ld3(a.P + 3 * gi), nn);
+  const F3 nn = ld3(a.N + 3 * gi);
+  F3 o = offset_ray(ld3(a.P + 3 * gi), nn);
   const U3 rot = pcg3d(gi, ~0u, ~0u);
-  const float r0 = u01(rot.x), r1 = u01(rot.y), weight = 3.14159265f / float(a.M);
-  uint32_t overflow = 0, segments = 0, bin = kNoBin;
-  float gain = 0.f;
-  const uint64_t start = clock_ns();
-  bool late = false;
+  const float r0 = u01(rot.x), r1 = u01(rot.y);
   const float u = float(smp) / float(a.M) + r0, v = u01(__brev(smp)) + r1;
-  F3 o = o0, d = cosine_dir(nn, u - floorf(u), v - floorf(v));
-  float w = 1.f;
-  uint32_t diffuse = 0, k = 0;
+  F3 d = cosine_dir(nn, u - floorf(u), v - floorf(v));
+  float w = 1.f, gain = 0.f;
+  uint32_t k = 0, diffuse = 0, bin = kNoBin, overflow = 0;
   bool reflected = false;
-  for (uint32_t seg = 0; seg < a.nBounce + 16; ++seg) {
-    if (clock_ns() - start > kBounceLimitNs) { late = true; break; }
-    ++segments;
-    ClosestOut c;
-    const bool found = closest(s, make_ray(o, d), 1e-5f, FLT_MAX, cull, c, overflow);
-    if (overflow & 2u) {   // the walk gave up: the first such path leaves its ray for the error message
-      uint32_t* diag = a.status + 15;   // ctl words 16..
-      if (atomicCAS(diag, 0u, 1u) == 0u) {
-        diag[1] = gi; diag[2] = smp; diag[3] = seg;
-        diag[4] = __float_as_uint(o.x); diag[5] = __float_as_uint(o.y); diag[6] = __float_as_uint(o.z);
-        diag[7] = __float_as_uint(d.x); diag[8] = __float_as_uint(d.y); diag[9] = __float_as_uint(d.z);
-      }
-      break;
-    }
-    if (!found) {
-      if (reflected) { bin = sky_bin(d, a.mf, a.nBins, a.alpha, a.cosN, a.sinN); gain = w * weight; }
-      break;
-    }
-    const kgb_slot sl = c.slot < a.nSlots ? a.slots[c.slot] : kgb_slot{0.2f, 0.f, 0.f, 0u};
-    TriHit h;
-    if (!tri_geom(c.v0, c.v1, c.v2, c.h, h)) break;
-    if (seg == 0 && own_plane(h, c.h.t, d, nn)) { o = through(h); continue; }
-    if ((sl.flags & (KGB_SLOT_THIN | KGB_SLOT_TWIN)) == KGB_SLOT_THIN && h.front == ((sl.flags & KGB_SLOT_INWARD) != 0)) { o = through(h); continue; }
-    const bool mirror = (sl.flags & KGB_SLOT_GLASS) != 0;
-    float T = sl.tau, R = sl.rho;
-    if (mirror) { glass_TR(fabsf(dot(d, h.n)), sl.tn, a.slotLog[c.slot], T, R); if (!(sl.tau > 0.f)) T = 0.f; }
-    else if (diffuse == a.nBounce) R = 0.f;
-    if (!(T + R > 0.f)) break;
-    const U3 rr = pcg3d(gi, smp, k++);
-    w *= T + R;
-    if (u01(rr.x) * (T + R) < T) { o = through(h); continue; }
-    reflected = true;
-    if (mirror) d = sub(d, mul(2.f * dot(d, h.n), h.n));
-    else {
-      d = cosine_dir(h.n, u01(rr.y), u01(rr.z));
-      if (++diffuse >= 2) {
-        if (u01(pcg3d(gi, smp, k++).x) >= w) break;
-        w = 1.f;
-      }
-    }
-    o = add(offset_ray(h.p, h.n), h.lift);
+  const uint32_t at = (smp - a.s0) * a.n + i;
+  const bool go = bounce_segment(a, s, cull, 0, nn, gi, smp, o, d, w, k, diffuse, reflected, bin, gain, overflow) && a.nBounce + 16 > 1;
+  PathState st;
+  if (go) {
+    st.ox = o.x; st.oy = o.y; st.oz = o.z; st.gi = gi; st.dx = d.x; st.dy = d.y; st.dz = d.z; st.smp = smp;
+    st.w = w; st.k = k; st.bits = diffuse | (reflected ? 0x100u : 0u) | (1u << 16); st.at = at;
+  } else {
+    a.contrib[at] = make_uint2(bin, __float_as_uint(gain));
   }
-  a.contrib[size_t(smp - a.s0) * a.n + i] = make_uint2(late ? kNoBin : bin, __float_as_uint(gain));
-  const uint32_t sum = __reduce_add_sync(__activemask(), segments);
-  if ((threadIdx.x & 31) == __ffs(__activemask()) - 1) atomicAdd(reinterpret_cast<unsigned long long*>(a.status + 1), (unsigned long long)sum);
-  if (overflow || late)
-    atomicOr(a.status, (overflow & 1u ? kStatusStackOverflow : 0u) | (overflow & 2u ? kStatusVisitLimit : 0u) | (late ? kStatusTimeout : 0u));
+  enqueue(go, st, a.qOut, a.qOutCount);
+  add_segments(a, 1u);
+  if (overflow) atomicOr(a.status, (overflow & 1u ? kStatusStackOverflow : 0u) | (overflow & 2u ? kStatusVisitLimit : 0u));
+}
+
+// One more segment of each path in the queue (grid-stride); the ones that go on into the next queue.
+__global__ void __launch_bounds__(128) k_bounce_step(BounceArgs a) {
+  const Scene s{a.nodes, a.tris, a.nNodes};
+  const bool cull = (a.rayFlags & KGB_RAY_CULL_BACK_FACING) != 0;
+  const uint32_t count = *a.qInCount, stride = gridDim.x * blockDim.x;
+  uint32_t overflow = 0, segments = 0;
+  for (uint32_t q0 = blockIdx.x * blockDim.x; q0 < count; q0 += stride) {   // whole warps in step: enqueue is warp-wide
+    const uint32_t qi = q0 + threadIdx.x;
+    const bool mine = qi < count;
+    PathState st{};
+    bool go = false;
+    if (mine) {
+      st = a.qIn[qi];
+      F3 o = f3(st.ox, st.oy, st.oz), d = f3(st.dx, st.dy, st.dz);
+      float w = st.w, gain = 0.f;
+      uint32_t k = st.k, diffuse = st.bits & 0xffu, bin = kNoBin;
+      bool reflected = (st.bits & 0x100u) != 0;
+      const uint32_t seg = st.bits >> 16;
+      go = bounce_segment(a, s, cull, seg, f3(0.f, 0.f, 0.f), st.gi, st.smp, o, d, w, k, diffuse, reflected, bin, gain, overflow) &&
+           seg + 1 < a.nBounce + 16;
+      ++segments;
+      if (go) {
+        st.ox = o.x; st.oy = o.y; st.oz = o.z; st.dx = d.x; st.dy = d.y; st.dz = d.z; st.w = w; st.k = k;
+        st.bits = diffuse | (reflected ? 0x100u : 0u) | ((seg + 1) << 16);
+      } else {
+        a.contrib[st.at] = make_uint2(bin, __float_as_uint(gain));
+      }
+    }
+    enqueue(go, st, a.qOut, a.qOutCount);
+  }
+  add_segments(a, segments);
+  if (overflow) atomicOr(a.status, (overflow & 1u ? kStatusStackOverflow : 0u) | (overflow & 2u ? kStatusVisitLimit : 0u));
 }
 
 // Per sensor, the launch's samples in order: row[bin] = row[bin] + contribution (the reference's float additions).
@@ -366,10 +441,28 @@ void launch_slot_logs(const kgb_slot* slots, uint32_t n, double* out, cudaStream
   if (n) k_slot_logs<<<(n + 127) / 128, 128, 0, st>>>(slots, n, out);
 }
 
-void launch_bounce(const BounceArgs& a, cudaStream_t st) {
+// The first segments, then up to nBounce + 15 steps over the queue of paths that go on (two queues in turn; a step
+// over an empty queue does nothing), then the accumulation. qCount: two counters; queues: two of n (s1 - s0) paths.
+void launch_bounce(const BounceArgs& args, PathState* queues, uint32_t* qCount, int stepGrid, cudaStream_t st) {
+  BounceArgs a = args;
   const size_t paths = size_t(a.n) * (a.s1 - a.s0);
+  a.qOut = queues; a.qOutCount = qCount;
+  cudaMemsetAsync(qCount, 0, 8, st);
   k_bounce_paths<<<unsigned((paths + 127) / 128), 128, 0, st>>>(a);
+  for (uint32_t step = 1; step < a.nBounce + 16; ++step) {
+    const int in = int((step + 1) & 1);   // the queue the previous launch filled
+    a.qIn = queues + size_t(in) * paths; a.qInCount = qCount + in;
+    a.qOut = queues + size_t(in ^ 1) * paths; a.qOutCount = qCount + (in ^ 1);
+    cudaMemsetAsync(a.qOutCount, 0, 4, st);
+    k_bounce_step<<<stepGrid, 128, 0, st>>>(a);
+  }
   k_bounce_accum<<<(a.n + 255) / 256, 256, 0, st>>>(a);
+}
+size_t bounce_state_bytes() { return sizeof(PathState); }
+int bounce_step_blocks_per_sm() {   // resident blocks of k_bounce_step per SM (its grid-stride grid fills the GPU once)
+  int b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_bounce_step, 128, 0) != cudaSuccess || b < 1) b = 1;
+  return b;
 }
 
 }  // namespace kgb
