@@ -242,6 +242,7 @@ __device__ __forceinline__ uint32_t sky_bin(F3 d, uint32_t mf, uint32_t nBins, f
 }
 
 constexpr uint32_t kNoBin = 0xffffffffu;
+constexpr uint64_t kBounceLimitNs = 10000000000ull;   // 10 s: past it a step ends its remaining paths, kStatusTimeout
 
 // A path between segments (48 bytes): where it is, where it goes, its weight and counters.
 struct __align__(16) PathState {
@@ -364,12 +365,17 @@ __global__ void __launch_bounds__(128) k_bounce_step(BounceArgs a) {
   const bool cull = (a.rayFlags & KGB_RAY_CULL_BACK_FACING) != 0;
   const uint32_t count = *a.qInCount, stride = gridDim.x * blockDim.x;
   uint32_t overflow = 0, segments = 0;
+  const uint64_t start = clock_ns();
+  bool late = false;
   for (uint32_t q0 = blockIdx.x * blockDim.x; q0 < count; q0 += stride) {   // whole warps in step: enqueue is warp-wide
     const uint32_t qi = q0 + threadIdx.x;
     const bool mine = qi < count;
     PathState st{};
     bool go = false;
-    if (mine) {
+    if (mine && !late && clock_ns() - start > kBounceLimitNs) late = true;
+    if (mine && late) {   // past the limit: the path ends with no contribution, and the call fails
+      a.contrib[a.qIn[qi].at] = make_uint2(kNoBin, 0u);
+    } else if (mine) {
       st = a.qIn[qi];
       F3 o = f3(st.ox, st.oy, st.oz), d = f3(st.dx, st.dy, st.dz);
       float w = st.w, gain = 0.f;
@@ -389,7 +395,8 @@ __global__ void __launch_bounds__(128) k_bounce_step(BounceArgs a) {
     enqueue(go, st, a.qOut, a.qOutCount);
   }
   add_segments(a, segments);
-  if (overflow) atomicOr(a.status, (overflow & 1u ? kStatusStackOverflow : 0u) | (overflow & 2u ? kStatusVisitLimit : 0u));
+  if (overflow || late)
+    atomicOr(a.status, (overflow & 1u ? kStatusStackOverflow : 0u) | (overflow & 2u ? kStatusVisitLimit : 0u) | (late ? kStatusTimeout : 0u));
 }
 
 // Per sensor, the launch's samples in order: row[bin] = row[bin] + contribution (the reference's float additions).
