@@ -99,15 +99,23 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
+// One warp per sensor. A lane's per-class sums sit in shared memory as [class][lane] (a warp's lanes touch 32
+// different banks whatever their classes), so a ray costs its own class's three updates, not a select over every
+// class: GB300's FP64 pipe is narrow, and predicated double operations still take its slots. Classes at or past nClass
+// are never reported and are not kept; the reach sums likewise hold nReach slots.
+constexpr uint32_t kViewWarps = 8;   // warps (sensors) per block
 __global__ void __launch_bounds__(256) k_view_reduce(ViewReduceArgs a) {
-  const uint32_t i = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x & 31;
+  extern __shared__ double vsm[];
+  const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x & 31, i = blockIdx.x * kViewWarps + warp;
+  const uint32_t C = a.nClass, R = a.nReach;
+  double* sw = vsm + size_t(warp) * (2 * C + R) * 32;   // w [C][32], wl [C][32], reach [R][32]
+  double* swl = sw + C * 32;
+  double* src = swl + C * 32;
+  float* smn = reinterpret_cast<float*>(vsm + size_t(kViewWarps) * (2 * C + R) * 32) + size_t(warp) * C * 32;   // mn [C][32]
+  for (uint32_t c = 0; c < C; ++c) { sw[c * 32 + lane] = 0; swl[c * 32 + lane] = 0; smn[c * 32 + lane] = __int_as_float(0x7f800000); }
+  for (uint32_t r = 0; r < R; ++r) src[r * 32 + lane] = 0;
   if (i >= a.nc) return;   // whole warps
-  double w[KGB_VIEW_CLASSES], wl[KGB_VIEW_CLASSES], rc[8], own = 0, gz = 0;
-  float mn[KGB_VIEW_CLASSES];
-#pragma unroll
-  for (uint32_t c = 0; c < KGB_VIEW_CLASSES; ++c) { w[c] = 0; wl[c] = 0; mn[c] = __int_as_float(0x7f800000); }
-#pragma unroll
-  for (uint32_t r = 0; r < 8; ++r) rc[r] = 0;
+  double own = 0, gz = 0;
   for (uint32_t d = lane; d < a.K; d += 32) {
     uint32_t c = a.cls[size_t(d) * a.nc + i];
     const float t = a.dist[size_t(d) * a.nc + i];
@@ -116,29 +124,30 @@ __global__ void __launch_bounds__(256) k_view_reduce(ViewReduceArgs a) {
     if (c & KGB_VIEW_GLAZED) { gz += wd; c &= ~uint32_t(KGB_VIEW_GLAZED); }
     const float dd = fminf(fmaxf(t, 0.1f), a.farDist);
     const double ln = dd == a.farDist ? a.lnFar : dd == 0.1f ? -2.302585092994045684 : (double)kgb_logf(dd);
-    // class-indexed accumulators stay in registers: a select per class instead of an indexed store
-#pragma unroll
-    for (uint32_t q = 0; q < KGB_VIEW_CLASSES; ++q)
-      if (q == c) { w[q] += wd; wl[q] += wd * ln; mn[q] = fminf(mn[q], dd); }
-#pragma unroll
-    for (uint32_t r = 0; r < 8; ++r) if (r < a.nReach && t >= a.reach[r]) rc[r] += wd;
+    if (c < C) {
+      const uint32_t at = c * 32 + lane;
+      sw[at] += wd;
+      swl[at] += wd * ln;
+      smn[at] = fminf(smn[at], dd);
+    }
+    for (uint32_t r = 0; r < R; ++r) if (t >= a.reach[r]) src[r * 32 + lane] += wd;
   }
   double* o = a.out + size_t(i) * a.NA;
-  for (uint32_t c = 0; c < a.nClass; ++c) {
-    float m = mn[c];
+  for (uint32_t c = 0; c < C; ++c) {
+    float m = smn[c * 32 + lane];
     for (uint32_t s = 16; s; s >>= 1) m = fminf(m, __shfl_down_sync(~0u, m, s));
-    const double x = warp_sum(w[c]), y = warp_sum(wl[c]);
+    const double x = warp_sum(sw[c * 32 + lane]), y = warp_sum(swl[c * 32 + lane]);
     if (!lane) { o[3 * c] = x; o[3 * c + 1] = y; o[3 * c + 2] = m; }
   }
   const double ow = warp_sum(own);
-  if (!lane) o[3 * a.nClass] = ow;
-  for (uint32_t r = 0; r < a.nReach; ++r) {
-    const double x = warp_sum(rc[r]);
-    if (!lane) o[3 * a.nClass + 1 + r] = x;
+  if (!lane) o[3 * C] = ow;
+  for (uint32_t r = 0; r < R; ++r) {
+    const double x = warp_sum(src[r * 32 + lane]);
+    if (!lane) o[3 * C + 1 + r] = x;
   }
   if (a.glazing) {
     const double x = warp_sum(gz);
-    if (!lane) o[3 * a.nClass + 1 + a.nReach] = x;
+    if (!lane) o[3 * C + 1 + R] = x;
   }
 }
 
@@ -215,7 +224,15 @@ void launch_reduce_dc(const float* dc, uint32_t nc, uint32_t nBins, const float*
   k_reduce_dc<<<(nc + 255) / 256, 256, 0, st>>>(dc, nc, nBins, W, out);
 }
 void launch_reduce_view(const ViewReduceArgs& a, cudaStream_t st) {
-  k_view_reduce<<<(a.nc + 7) / 8, 256, 0, st>>>(a);
+  // shared memory: per warp 2 C + R doubles and C floats per lane (at most 19 classes and 8 reach distances: 111 KB)
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_view_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(kViewWarps * 32 * ((2 * KGB_VIEW_CLASSES + 8) * 8 + KGB_VIEW_CLASSES * 4)));
+    attr = true;
+  }
+  const size_t smem = size_t(kViewWarps) * 32 * ((2 * a.nClass + a.nReach) * 8 + a.nClass * 4);
+  k_view_reduce<<<(a.nc + kViewWarps - 1) / kViewWarps, kViewWarps * 32, smem, st>>>(a);
   if (a.isoDim) k_iso<<<(a.nc + 7) / 8, 256, 0, st>>>(a);
 }
 
