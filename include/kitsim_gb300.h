@@ -223,7 +223,8 @@ KGB_API int kgb_sun_noaa(kgb_engine* e, const double* in, size_t T, double* out)
 /* --- serving (no reference counterpart: the reference runs one request at a time, src/run.cpp:35) ---------------- */
 /* A server keeps scenes resident and runs daylight and views requests of any size with continuous batching: requests
  * are admitted as the HBM budget allows and cut into work items that run back to back on one stream, two queued at a
- * time, picked by a priority (remaining work over age plus 0.3 s): daylight batches packing chunks of any number of
+ * time, picked by a priority (requests waiting over 1.2 s first, in arrival order; the others by remaining work over
+ * age plus 0.3 s): daylight batches packing chunks of any number of
  * requests (one persistent any-hit launch + one multi-quantity reduce, a CUDA graph) and views chunks (the view
  * kernels on a range of one request's sensors). Results equal the single-request entry points' bit for bit. A
  * request's host arrays must stay valid until kgb_server_wait returns for it. */

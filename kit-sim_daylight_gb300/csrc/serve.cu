@@ -9,10 +9,11 @@
 //    pipeline (segment table up, counter reset, the two kernels, the sums and the status down into pinned memory) is a
 //    CUDA graph built once per slot and replayed per batch, its copy sizes and the reduce's grid set per batch;
 //  - a views chunk: the view kernels (k_view, k_view_reduce, k_iso) on a range of one request's sensors, sized by rays.
-// The scheduler picks the next item by a priority over every request with sensors not yet issued: its remaining work
-// (rays times a running estimate of seconds per ray of its kind, measured from the items' own GPU time) divided by its
-// age plus 0.3 s. Short requests overtake long ones, and a long one's priority grows as it waits, which keeps the p50
-// near one item's time while bounding the p99. A daylight batch is packed in that order, a chunk at a time.
+// The scheduler picks the next item by a priority over every request with sensors not yet issued: a request that has
+// waited more than 1.2 s goes first, in arrival order; the others by their remaining work (rays times a running
+// estimate of seconds per ray of its kind, measured from the items' own GPU time) divided by their age plus 0.3 s.
+// Short requests overtake long ones, which keeps the p50 near one item's time, and no request waits behind younger
+// ones for long, which keeps the p99 at arrival order's. A daylight batch is packed in that order, a chunk at a time.
 // Admitted requests' inputs go up on a separate upload stream into stream-ordered allocations from the server's own
 // memory pool, so neither uploads nor frees wait for the work stream. A request completes when its last item has; its
 // results are bit-identical to the request run alone through the single-request entry points (same kernels, same
@@ -126,6 +127,7 @@ constexpr size_t kDepth = 2;                    // work items queued on the work
 constexpr uint32_t kMaxViewChunk = 65536;       // sensors in one views chunk
 constexpr uint32_t kMaxNA = 3 * KGB_VIEW_CLASSES + 1 + 8 + 1 + 1;   // views columns
 constexpr double kAgeSeconds = 0.3;             // the priority's age offset
+constexpr double kOldSeconds = 1.2;             // past this wait a request goes first, in arrival order
 
 struct DScene {
   void* nodes = nullptr;
@@ -401,8 +403,10 @@ bool order_after_uploads(Server& s, std::string& err) {
 }
 
 double priority(const Server& s, const Request* r, Clock::time_point now) {
+  const double age = std::chrono::duration<double>(now - r->tSubmit).count();
+  if (age > kOldSeconds) return -1e9 - age;   // the oldest first, before every younger request
   const double rem = double(r->nSensors - r->nextSensor) * double(r->raysPerSensor) * s.cost[r->kind];
-  return rem / (std::chrono::duration<double>(now - r->tSubmit).count() + kAgeSeconds);
+  return rem / (age + kAgeSeconds);
 }
 
 // a daylight batch of the given parts into slot k, launched on the work stream
