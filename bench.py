@@ -360,10 +360,21 @@ def run_precision(args, pkg):
     chunk = max(1, (256 << 20) // len(D))   # the reference's 256 MiB cap on the per-chunk visibility
     sargs = dict(nSky=nSky, row=np.arange(nSky), wsky=omega, S=yr["S"], g=yr["g"], sun0=sun0, sunStep=yr["sunStep"], sunVec=yr["sunVec"],
                  sunW=yr["sunW"], Sdc=yr["Sdc"])
-    tt = {"trace": 0.0, "bounce": 0.0, "tc": 0.0, "fp32": 0.0, "copy": 0.0}
+    tt = {"trace": 0.0, "bounce": 0.0, "tc": 0.0, "fp32": 0.0, "copy": 0.0, "fwrite": 0.0, "direct": 0.0}
     first = fp32_first = None
     Ebuf = np.empty((min(chunk, nc_all), T), np.float32)   # one E for every chunk, written with zeros first (run.cpp:683-686)
     Ebuf.fill(0.0)
+    # the --timeseries file, two ways: the reference's (gpu_series into E, then fwrite) and kgb_series_file (the rows
+    # written from the engine's pinned staging); both files under a 128-byte header, compared byte for byte after
+    import shutil
+    import tempfile
+    E_bytes = nc_all * T * 4
+    tmpdir = tempfile.mkdtemp(prefix="kgb_series_")
+    files = shutil.disk_usage(tmpdir).free > 2 * E_bytes + (2 << 30)
+    if files:
+        f_ref = open(os.path.join(tmpdir, "ref.npy"), "wb")
+        f_ref.write(b"\0" * 128)
+        fd_dir = os.open(os.path.join(tmpdir, "direct.npy"), os.O_CREAT | os.O_RDWR | os.O_TRUNC, 0o644)
     t_all = time.perf_counter()
     for i0 in range(0, nc_all, chunk):
         nc = min(chunk, nc_all - i0)
@@ -382,6 +393,17 @@ def run_precision(args, pkg):
             t0 = time.perf_counter()
             E = e.series(nc, G=G, out=Ebuf[:nc], **sargs)
             tt[key] += time.perf_counter() - t0
+            if key == "tc" and files:   # untimed by the pipeline: the file output of the same chunk, both ways
+                t1 = time.perf_counter()
+                E.tofile(f_ref)
+                f_ref.flush()
+                d1 = time.perf_counter() - t1
+                t1 = time.perf_counter()
+                e.series_file(nc, fd_dir, 128 + i0 * T * 4, G=G, **sargs)
+                d2 = time.perf_counter() - t1
+                tt["fwrite"] += d1
+                tt["direct"] += d2
+                tt["copy"] += d1 + d2
             if i0 == 0:   # kept for the accuracy check; the copy is not part of the pipeline
                 t0 = time.perf_counter()
                 if form == 0:
@@ -391,6 +413,23 @@ def run_precision(args, pkg):
                 tt["copy"] += time.perf_counter() - t0
     e.set_series_form(0)
     pipeline_s = time.perf_counter() - t_all - tt["copy"]
+    series_file = {"skipped": "less than twice the file's size free in %s" % tmpdir}
+    if files:
+        f_ref.close()
+        os.close(fd_dir)
+        same = True
+        with open(os.path.join(tmpdir, "ref.npy"), "rb") as a, open(os.path.join(tmpdir, "direct.npy"), "rb") as b:
+            while True:
+                x, y = a.read(1 << 28), b.read(1 << 28)
+                if x != y:
+                    same = False
+                    break
+                if not x:
+                    break
+        series_file = {"bytes": E_bytes, "reference_way_s": tt["tc"] + tt["fwrite"], "fwrite_s": tt["fwrite"], "direct_s": tt["direct"],
+                       "direct_gb_s": E_bytes / tt["direct"] / 1e9, "files_identical": same,
+                       "note": "reference way: gpu_series into one reused E, then fwrite per chunk; direct: kgb_series_file per chunk"}
+    shutil.rmtree(tmpdir, ignore_errors=True)
     # accuracy: a contiguous 64-sensor range of the first chunk, traced and bounced by the oracle at the same global
     # indices, its series in FP64 from the same FP32 inputs
     s0 = int(np.random.default_rng(9).integers(0, min(chunk, nc_all) - 64))
@@ -424,7 +463,7 @@ def run_precision(args, pkg):
             "trace_s": tt["trace"], "bounce_s": tt["bounce"], "series_tc_s": tt["tc"], "series_fp32_s_timed": tt["fp32"],
             "pipeline_s": pipeline_s - (tt["fp32"] if not args.full_fp32 else 0.0),
             "pipeline_solves_s": nc_all * T / (pipeline_s - (tt["fp32"] if not args.full_fp32 else 0.0)),
-            "E_bytes": nc_all * T * 4, "note": "series times include the E download to host memory (pageable, one buffer reused across chunks), as the reference's gpu_series"}
+            "E_bytes": nc_all * T * 4, "series_file": series_file, "note": "series times include the E download to host memory (pageable, one buffer reused across chunks), as the reference's gpu_series"}
     print(json.dumps(line), flush=True)
     e.close()
 

@@ -169,6 +169,10 @@ KGB_API int kgb_reduce(kgb_engine* e, size_t nc, const float* W, int useCos, dou
 KGB_API int kgb_reduce_noalloc(kgb_engine* e, size_t nc, const float* W, int useCos, double* out);
 /* replaces gpu_series (src/internal.h:171): E[i*T + t] (host, nc x T floats) */
 KGB_API int kgb_series(kgb_engine* e, size_t nc, const kgb_series_in* in, float* E);
+/* gpu_series followed by the reference's fwrite of E into the --timeseries .npy (src/run.cpp:683-686), in one call:
+ * the same rows written to the open file fd at byte offset (its header's length + i0 x T x 4 for the chunk that starts
+ * at sensor i0), straight from the engine's pinned staging, while the next rows come down */
+KGB_API int kgb_series_file(kgb_engine* e, size_t nc, const kgb_series_in* in, int fd, uint64_t offset);
 /* replaces gpu_bounce (src/internal.h:179) */
 KGB_API int kgb_bounce(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, const kgb_bounce_in* b);
 /* replaces gpu_reduce_dc (src/internal.h:180): out[i] = sum_b dc(b, i) * W[b] (double) */

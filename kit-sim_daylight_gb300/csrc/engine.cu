@@ -9,7 +9,10 @@
 #include "engine.h"
 #include "rt.cuh"
 
+#include <unistd.h>
+
 #include <algorithm>
+#include <cerrno>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -67,12 +70,33 @@ void host_copy(void* dst, const void* src, size_t bytes) {
   }
   for (auto& x : th) x.join();
 }
-int download_large(Staging& s, void* dst, const void* src, size_t bytes, cudaStream_t st) {
-  if (bytes < 2 * Staging::kSlice) {   // small results: one plain copy
-    CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
+// Where a download goes: pageable host memory (dst), or a file (fd >= 0) at a byte offset, written with pwrite.
+struct Sink {
+  void* dst = nullptr;
+  int fd = -1;
+  uint64_t offset = 0;
+};
+// len bytes of pinned src to the sink at byte pos: a few threads copy (memory), or pwrite calls (file: writes to one
+// file take its lock in turn, so one writer is as fast as several)
+int sink_put(const Sink& k, size_t pos, const void* src, size_t len) {
+  if (k.fd < 0) { host_copy(static_cast<char*>(k.dst) + pos, src, len); return 1; }
+  for (size_t a = 0; a < len;) {
+    const ssize_t n = pwrite(k.fd, static_cast<const char*>(src) + a, len - a, off_t(k.offset + pos + a));
+    if (n < 0 && errno == EINTR) continue;
+    if (n <= 0) return fail(std::string("gpu_series: writing the series file failed: ") + std::strerror(n < 0 ? errno : EIO));
+    a += size_t(n);
+  }
+  return 1;
+}
+// Device -> sink copy of bytes at byte pos of the sink, through the staging slices (memory results under two slices:
+// one plain copy)
+int download_to(Staging& s, const Sink& sk, size_t pos, const void* src, size_t bytes, cudaStream_t st) {
+  if (sk.fd < 0 && bytes < 2 * Staging::kSlice) {
+    CU(cudaMemcpyAsync(static_cast<char*>(sk.dst) + pos, src, bytes, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
     return 1;
   }
+  if (!bytes) return 1;
   for (int k = 0; k < 2; ++k) {
     if (!s.h[k]) CU(cudaMallocHost(&s.h[k], Staging::kSlice));
     if (!s.ev[k]) CU(cudaEventCreateWithFlags(&s.ev[k], cudaEventDisableTiming));
@@ -88,9 +112,14 @@ int download_large(Staging& s, void* dst, const void* src, size_t bytes, cudaStr
       CU(cudaEventRecord(s.ev[b ^ 1], st));
     }
     CU(cudaEventSynchronize(s.ev[b]));
-    host_copy(static_cast<char*>(dst) + k * Staging::kSlice, s.h[b], slice(k));
+    if (!sink_put(sk, pos + k * Staging::kSlice, s.h[b], slice(k))) return 0;
   }
   return 1;
+}
+int download_large(Staging& s, void* dst, const void* src, size_t bytes, cudaStream_t st) {
+  Sink k;
+  k.dst = dst;
+  return download_to(s, k, 0, src, bytes, st);
 }
 
 // Host -> device copy of a large input through the same staging slices (the host fills slice k while slice k - 1
@@ -508,8 +537,9 @@ KGB_API int kgb_reduce(kgb_engine* e, size_t nc, const float* W, int useCos, dou
   return 1;
 }
 
-KGB_API int kgb_series(kgb_engine* e, size_t nc, const kgb_series_in* in, float* Eh) {
-  Engine& g = *E(e);
+namespace kgb {
+// gpu_series's body; E's rows go to the sink (the caller's memory, or a file at an offset)
+static int series_impl(Engine& g, size_t nc, const kgb_series_in* in, const Sink& out) {
   if (nc == 0 || in->T <= 0) return 1;
   if (in->Sdc && nc != g.dcN) return fail("gpu_series: no gpu_bounce rows for this chunk");
   if (nc != g.visN) return fail("gpu_series: no trace of this chunk");
@@ -594,7 +624,7 @@ KGB_API int kgb_series(kgb_engine* e, size_t nc, const kgb_series_in* in, float*
     for (uint32_t b = 0; b < bands; ++b) {
       const size_t r0 = size_t(b) * per * 128, r1 = std::min(nc, size_t(b + 1) * per * 128);
       CU(cudaStreamWaitEvent(g.copySt, g.bandEv[b], 0));
-      if (!download_large(g.staging, Eh + r0 * T, static_cast<const float*>(g.out.p) + r0 * T, (r1 - r0) * T * 4, g.copySt)) return 0;
+      if (!download_to(g.staging, out, r0 * T * 4, static_cast<const float*>(g.out.p) + r0 * T, (r1 - r0) * T * 4, g.copySt)) return 0;
     }
     uint32_t status = 0;
     CU(cudaMemcpyAsync(&status, static_cast<uint32_t*>(g.ctl.p) + 1, 4, cudaMemcpyDeviceToHost, g.st));
@@ -602,7 +632,25 @@ KGB_API int kgb_series(kgb_engine* e, size_t nc, const kgb_series_in* in, float*
     if (status & kStatusTimeout) return fail("gpu_series: the tensor-core pipeline timed out waiting (status recorded by the kernel)");
     return 1;
   }
-  return download_large(g.staging, Eh, g.out.p, nc * T * 4, g.st);
+  return download_to(g.staging, out, 0, g.out.p, nc * T * 4, g.st);
+}
+}  // namespace kgb
+
+KGB_API int kgb_series(kgb_engine* e, size_t nc, const kgb_series_in* in, float* Eh) {
+  Sink k;
+  k.dst = Eh;
+  return series_impl(*E(e), nc, in, k);
+}
+
+// gpu_series + the reference's fwrite of E (run.cpp:683-686) in one call: the rows go from the pinned staging slices
+// into the file at byte offset (the .npy header's length plus i0 x T x 4 for a chunk starting at sensor i0), written
+// by a few threads while the next slice comes down
+KGB_API int kgb_series_file(kgb_engine* e, size_t nc, const kgb_series_in* in, int fd, uint64_t offset) {
+  if (fd < 0) return fail("gpu_series: no file");
+  Sink k;
+  k.fd = fd;
+  k.offset = offset;
+  return series_impl(*E(e), nc, in, k);
 }
 
 KGB_API int kgb_sky(kgb_engine* e, int32_t mf, const kgb_sky_step* steps, size_t T, double grefl, int32_t sun, int32_t sky,

@@ -96,6 +96,7 @@ SIGNATURES = [
     ("kgb_download_bits", c_int, [_E, c_size_t, c_void_p, c_size_t]),
     ("kgb_download_bytes", c_int, [_E, c_size_t, c_void_p, c_size_t]),
     ("kgb_download_bits_rows", c_int, [_E, c_size_t, c_void_p, c_size_t]),
+    ("kgb_series_file", c_int, [_E, c_size_t, c_void_p, c_int, c_uint64]),
     ("kgb_download_bytes_rows", c_int, [_E, c_size_t, c_void_p, c_size_t]),
     ("kgb_view", c_int, [_E, c_size_t, c_size_t, c_uint32, POINTER(ViewIn), POINTER(c_size_t)]),
     ("kgb_reduce_view", c_int, [_E, c_size_t, c_void_p, c_size_t, c_uint32, c_double, c_void_p, c_size_t, c_int, c_uint32, c_void_p]),
@@ -318,6 +319,19 @@ class Engine:
                 raise ValueError("series: out must be a C-contiguous float32 [nc x T] array")
         self._ok(self.d.kgb_series(self.h, nc, ctypes.byref(s), _p(E)))
         return E
+
+    def series_file(self, nc, fd, offset, nSky, row, wsky, S, g, G, sun0, sunStep, sunVec, sunW, Sdc=None):
+        """The series' rows [nc x T] float32 written to the open file descriptor fd at byte offset."""
+        row = np.ascontiguousarray(row, dtype=np.int32)
+        wsky, S, g, G = _f32(wsky), _f32(S), _f32(g), _f32(G)
+        P, T = S.shape
+        sunStep = np.ascontiguousarray(sunStep, dtype=np.int32)
+        sunVec, sunW = _f32(sunVec, (-1, 3)), _f32(sunW)
+        Sdc = None if Sdc is None else _f32(Sdc)
+        s = SeriesIn(nSky, _typed(row, c_int32), _typed(wsky, c_float), _typed(S, c_float), P, T, _typed(g, c_float), _typed(G, c_float),
+                     sun0, len(sunStep), _typed(sunStep, c_int32), _typed(sunVec, c_float), _typed(sunW, c_float),
+                     _typed(Sdc, c_float) if Sdc is not None else None)
+        self._ok(self.d.kgb_series_file(self.h, nc, ctypes.byref(s), int(fd), int(offset)))
 
     def bounce(self, i0, nc, flags, N=1, M=1024, mf=1, north=0.0, cancel=None):
         cb = CANCEL_FN(lambda _ctx: int(bool(cancel()))) if cancel else CANCEL_FN()

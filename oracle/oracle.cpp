@@ -19,6 +19,9 @@
 #include "kitsim_gb300.h"
 #include "kgb_detmath.h"
 
+#include <unistd.h>
+#include <cerrno>
+
 #include <algorithm>
 #include <cfloat>
 #include <atomic>
@@ -658,6 +661,23 @@ KGB_API int kgb_series(kgb_engine* e, size_t nc, const kgb_series_in* in, float*
       }
     for (size_t t = 0; t < T; ++t) E[i * T + t] = float(acc[t]);
   });
+  return 1;
+}
+
+// gpu_series + the caller's fwrite of E (run.cpp:683-686): the same rows written to fd at offset
+KGB_API int kgb_series_file(kgb_engine* e, size_t nc, const kgb_series_in* in, int fd, uint64_t offset) {
+  if (fd < 0) return fail("gpu_series: no file");
+  std::vector<float> E(nc * size_t(in->T > 0 ? in->T : 0));
+  if (!kgb_series(e, nc, in, E.data())) return 0;
+  const char* p = reinterpret_cast<const char*>(E.data());
+  size_t left = E.size() * 4, at = 0;
+  while (left) {
+    const ssize_t n = pwrite(fd, p + at, left, off_t(offset + at));
+    if (n < 0 && errno == EINTR) continue;
+    if (n <= 0) return fail("gpu_series: writing the series file failed");
+    at += size_t(n);
+    left -= size_t(n);
+  }
   return 1;
 }
 

@@ -129,3 +129,29 @@ def test_series_bands_equal_chunks(engine_lib, kgb, pkg):
         assert np.abs(whole).max() > 0
     finally:
         e.close()
+
+
+def test_series_file_matches_series(engine_lib, kgb, pkg, tmp_path):
+    """kgb_series_file writes the rows kgb_series returns, bit for bit, at the caller's offsets: chunks of 5000 sensors
+    (four bands, each more than a staging slice of rows) appended after a header, as the reference's --timeseries
+    file."""
+    import os
+    s = pkg.workloads.random_city(8, n_boxes=40)
+    P, T, nSun, nc = 145, 4000, 600, 5000
+    D = pkg.workloads.hemisphere_dirs(P, nSun, 8)
+    e = _setup(pkg, kgb, engine_lib, s, D, nc)
+    try:
+        args = _inputs(P, T, nc, D, P, nSun, 6)
+        want = e.series(nc, **args)
+        header = 128
+        path = str(tmp_path / "series.npy")
+        fd = os.open(path, os.O_CREAT | os.O_RDWR | os.O_TRUNC, 0o644)
+        try:
+            os.pwrite(fd, b"H" * header, 0)
+            e.series_file(nc, fd, header, **args)
+        finally:
+            os.close(fd)
+        got = np.fromfile(path, np.float32, offset=header).reshape(nc, T)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    finally:
+        e.close()
