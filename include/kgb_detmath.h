@@ -9,7 +9,7 @@
  * compile them without floating-point contraction (nvcc -fmad=false; gcc -ffp-contract=off). Division and square root
  * are the correctly rounded IEEE operations on both sides (nvcc -prec-div=true -prec-sqrt=true, its default).
  *
- * Accuracy: a few ulps in float, ~1e-15 relative for the double exp/log used by kgb_powf.
+ * Accuracy: a few ulps in float; ~1e-15 relative for the double logarithm (kgb_log_d) that kgb_powf's ln x comes from.
  */
 #ifndef KGB_DETMATH_H
 #define KGB_DETMATH_H
@@ -93,23 +93,46 @@ KGB_HD double kgb_log_d(double x) {
   return (double)e * 0.69314718055994530942 + 2.0 * s * p;
 }
 
-/* exp(x) in double for |x| < 700: x = k ln2 + r, |r| <= ln2 / 2, Taylor series of e^r to r^16 by Horner's rule, times
- * 2^k. Every multiply-add is an explicit fma (one rounding, the same on both sides): 18 fused operations. */
-KGB_HD double kgb_exp_d(double x) {
-  const double k = rint(x * 1.44269504088896340736);
-  const double r = fma(-k, 1.90821492927058770002e-10, fma(-k, 0.693147180369123816490, x)); /* x - k ln 2, ln 2 = hi + lo */
-  double p = 1.0 / 20922789888000.0; /* 1/16! */
-  const double inv[16] = {1.0, 1.0, 1.0 / 2, 1.0 / 6, 1.0 / 24, 1.0 / 120, 1.0 / 720, 1.0 / 5040, 1.0 / 40320,
-                          1.0 / 362880, 1.0 / 3628800, 1.0 / 39916800, 1.0 / 479001600, 1.0 / 6227020800.0,
-                          1.0 / 87178291200.0, 1.0 / 1307674368000.0};
-  for (int j = 15; j >= 0; --j) p = fma(r, p, inv[j]);
-  return ldexp(p, (int)k);
+/* e^(th + tl) in float, th + tl a float pair with |th| < 87: k = round(th log2 e), r = th - k ln 2 + tl with
+ * ln 2 = hi + lo (hi has 15 significant bits, so k hi is exact), the Taylor series of e^r to r^8 (|r| <= 0.35: the
+ * first term left out is below 2^-32) by fused Horner steps, times 2^k. A few float ulps; every multiply-add is an
+ * explicit fmaf, so every machine gets the same bits. */
+KGB_HD float kgb_expf_pair(float th, float tl) {
+  const float k = rintf(th * 1.44269504f);
+  float r = fmaf(-k, 0.693145751953125f, th);
+  r = fmaf(-k, 1.42860677e-06f, r) + tl;
+  float p = 1.0f / 40320.0f;
+  p = fmaf(p, r, 1.0f / 5040.0f);
+  p = fmaf(p, r, 1.0f / 720.0f);
+  p = fmaf(p, r, 1.0f / 120.0f);
+  p = fmaf(p, r, 1.0f / 24.0f);
+  p = fmaf(p, r, 1.0f / 6.0f);
+  p = fmaf(p, r, 0.5f);
+  p = fmaf(p, r, 1.0f);
+  p = fmaf(p, r, 1.0f);
+  return ldexpf(p, (int)k);
 }
 
-/* x^y for x > 0 (0 -> 0), as float(exp(y ln x)) in double. */
+/* ln x as a float pair (hi = float(ln x), lo = float(ln x - hi)) from the double logarithm, x > 0. */
+KGB_HD void kgb_ln_pair(float x, float* hi, float* lo) {
+  const double l = kgb_log_d((double)x);
+  *hi = (float)l;
+  *lo = (float)(l - (double)*hi);
+}
+
+/* x^y = e^(y ln x) for x > 0 given ln x as a float pair: y ln x formed exactly as a pair (fmaf), then kgb_expf_pair. */
+KGB_HD float kgb_pow_ln(float lnh, float lnl, float y) {
+  const float th = y * lnh;
+  const float tl = fmaf(y, lnh, -th) + y * lnl;
+  return kgb_expf_pair(th, tl);
+}
+
+/* x^y for x > 0 (0 -> 0): kgb_pow_ln with ln x from kgb_ln_pair. */
 KGB_HD float kgb_powf(float x, float y) {
   if (!(x > 0.0f)) return 0.0f;
-  return (float)kgb_exp_d((double)y * kgb_log_d((double)x));
+  float h, l;
+  kgb_ln_pair(x, &h, &l);
+  return kgb_pow_ln(h, l, y);
 }
 
 #endif /* KGB_DETMATH_H */

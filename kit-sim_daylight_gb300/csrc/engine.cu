@@ -196,7 +196,7 @@ struct Engine {
   Buf border;        // a bounce launch's samples in tracing order
   Buf bq;            // a bounce launch's two queues of paths that go on
   int gridStep = 0;
-  Buf slotLog;       // kgb_log_d(tn) per slot (glass transmission)
+  Buf slotLog;       // ln tn per slot as a float pair (glass transmission)
   size_t nBins = 0, dcN = 0, dcI0 = 0;
   Buf viewCls, viewDist, rowSin;
   size_t viewN = 0, viewK = 0, viewI0 = 0;
@@ -401,7 +401,7 @@ KGB_API int kgb_set_slots(kgb_engine* e, const kgb_slot* slots, size_t n) {
   const kgb_slot one{0.2f, 0.f, 0.f, 0u};
   if (!n) { slots = &one; n = 1; }
   if (!upload(g.slots, slots, n * sizeof(kgb_slot), g.st) || !grow(g.slotLog, n * 8)) return 0;
-  launch_slot_logs(static_cast<const kgb_slot*>(g.slots.p), uint32_t(n), static_cast<double*>(g.slotLog.p), g.st);
+  launch_slot_logs(static_cast<const kgb_slot*>(g.slots.p), uint32_t(n), static_cast<float2*>(g.slotLog.p), g.st);
   CU(cudaGetLastError());
   g.nSlots = uint32_t(n);
   CU(cudaStreamSynchronize(g.st));
@@ -475,7 +475,7 @@ static int trace_impl(Engine& g, size_t i0, size_t nc, uint32_t rayFlags, uint64
   a.stride = uint32_t(nc); a.nDir = uint32_t(g.nDir); a.nWords = uint32_t(g.nWords); a.rayFlags = rayFlags;
   a.bits = any ? nullptr : static_cast<uint32_t*>(g.vis.p);
   a.bytes = any ? static_cast<uint8_t*>(g.vis.p) : nullptr;
-  a.slots = static_cast<const kgb_slot*>(g.slots.p); a.nSlots = g.nSlots; a.slotLog = static_cast<const double*>(g.slotLog.p);
+  a.slots = static_cast<const kgb_slot*>(g.slots.p); a.nSlots = g.nSlots; a.slotLog = static_cast<const float2*>(g.slotLog.p);
   a.counter = static_cast<uint32_t*>(g.ctl.p); a.status = static_cast<uint32_t*>(g.ctl.p) + 1;
   a.rayTab = static_cast<const RayDir*>(g.rayTab.p);
   while (done < nc) {
@@ -694,7 +694,7 @@ KGB_API int kgb_bounce(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, c
   a.M = b->M; a.nBounce = b->N; a.mf = mf; a.nBins = uint32_t(g.nBins);
   a.alpha = float((KGB_PI_D / 2.) / (7 * mf + .5)); a.cosN = float(std::cos(rad)); a.sinN = float(std::sin(rad));
   a.rayFlags = rayFlags; a.slots = static_cast<const kgb_slot*>(g.slots.p); a.nSlots = g.nSlots;
-  a.slotLog = static_cast<const double*>(g.slotLog.p);
+  a.slotLog = static_cast<const float2*>(g.slotLog.p);
   a.dc = static_cast<float*>(g.dc.p); a.status = static_cast<uint32_t*>(g.ctl.p) + 1;
   // paths of a launch: at most 2^23 (their results 64 MiB, the two queues of paths that go on 768 MiB)
   const size_t nCap = std::max<size_t>(1, (size_t(1) << 23) / nc);

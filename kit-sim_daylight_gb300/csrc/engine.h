@@ -37,7 +37,7 @@ struct TraceArgs {
   uint32_t* counter;
   uint32_t* status;
   const RayDir* rayTab;   // the directions' precomputed ray parts (k_bits), or null
-  const double* slotLog;  // [nSlots]: kgb_log_d(tn) per slot (k_slot_logs)
+  const float2* slotLog;  // [nSlots]: ln tn per slot as a float pair (k_slot_logs)
 };
 
 struct ViewArgs {
@@ -75,7 +75,7 @@ struct BounceArgs {
   uint2* contrib;     // [(s1 - s0) x n]: each path's sky bin (or none) and contribution
   uint32_t* status;
   const uint32_t* order;   // [s1 - s0]: the launch's samples in tracing order (sensor-major), or null (sample-major)
-  const double* slotLog;   // [nSlots]: kgb_log_d(tn) per slot (k_slot_logs)
+  const float2* slotLog;   // [nSlots]: ln tn per slot as a float pair (k_slot_logs)
   const PathState* qIn;    // the paths a step continues, and their count
   const uint32_t* qInCount;
   PathState* qOut;         // the paths that go on after it, appended
@@ -83,7 +83,7 @@ struct BounceArgs {
 };
 
 void launch_ray_table(const float* D, uint32_t nDir, void* tab, cudaStream_t st);   // 48 bytes per direction
-void launch_slot_logs(const kgb_slot* slots, uint32_t n, double* out, cudaStream_t st);   // kgb_log_d(tn) per slot
+void launch_slot_logs(const kgb_slot* slots, uint32_t n, float2* out, cudaStream_t st);   // ln tn per slot, a float pair
 // rows.cu: out[i K + d] = in[d ld + i] for d < K, i < m, elements of 1 or 4 bytes; false if the grid cannot hold K
 bool launch_rows(const void* in, size_t ld, void* out, size_t esize, uint32_t K, uint32_t m, cudaStream_t st);
 int bytes_blocks_per_sm();

@@ -59,13 +59,13 @@ __device__ __forceinline__ U3 pcg3d(uint32_t x, uint32_t y, uint32_t z) {
 }
 __device__ __forceinline__ float u01(uint32_t v) { return float(v >> 8) * (1.f / 16777216.f); }
 
-// Radiance glass (the reference's glass_TR, glass.h:17-25; rad5R4 m_glass.c), powf as kgb_powf. logTn: the slot's
-// kgb_log_d(tn), computed once per slot by k_slot_logs with the same code, so tn^(1 / c2) = float(exp(y logTn)) is
-// kgb_powf's value bit for bit with half its double-precision work per hit.
-__device__ __forceinline__ void glass_TR(float c, float tn, double logTn, float& T, float& R) {
+// Radiance glass (the reference's glass_TR, glass.h:17-25; rad5R4 m_glass.c), powf as kgb_powf. lnTn: the slot's ln tn
+// as a float pair (kgb_ln_pair, computed once per slot by k_slot_logs), so tn^(1 / c2) = kgb_pow_ln(lnTn, 1 / c2) is
+// kgb_powf's value bit for bit, in float arithmetic only.
+__device__ __forceinline__ void glass_TR(float c, float tn, float2 lnTn, float& T, float& R) {
   const float n = 1.52f;
   const float c2 = sqrtf((1.f - 1.f / (n * n)) + c * c / (n * n));
-  const float d = tn > 0.f ? (float)kgb_exp_d((double)(1.f / c2) * logTn) : 0.f, d2 = d * d;
+  const float d = tn > 0.f ? kgb_pow_ln(lnTn.x, lnTn.y, 1.f / c2) : 0.f, d2 = d * d;
   float rs = (c - n * c2) / (c + n * c2), rp = (c2 - n * c) / (c2 + n * c);
   rs *= rs; rp *= rp;
   T = .5f * (1.f - rs) * (1.f - rs) * d / (1.f - rs * rs * d2) + .5f * (1.f - rp) * (1.f - rp) * d / (1.f - rp * rp * d2);

@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(256) k_bits(TraceArgs a) {
 
 // ---------------------------------------------------------------------------------------------------- bytes
 // A translucent slot's crossing: tau, 1 on a thin solid's exit face, Radiance glass T(cos) (trace_dev.cu:147-165).
-__device__ __forceinline__ float crossing(const kgb_slot* slots, const double* slotLog, uint32_t nSlots, uint32_t slot, bool front, F3 v0, F3 v1,
+__device__ __forceinline__ float crossing(const kgb_slot* slots, const float2* slotLog, uint32_t nSlots, uint32_t slot, bool front, F3 v0, F3 v1,
                                          F3 v2, F3 d) {
   const kgb_slot sl = slot < nSlots ? slots[slot] : kgb_slot{0.2f, 0.f, 0.f, 0u};
   float T = sl.tau;
@@ -439,12 +439,15 @@ void launch_bits(const TraceArgs& a, int grid, cudaStream_t st, bool count) {
 }
 void launch_bytes(const TraceArgs& a, int grid, cudaStream_t st) { k_bytes<<<grid, 256, 0, st>>>(a); }
 void launch_view(const ViewArgs& a, int grid, cudaStream_t st) { k_view<<<grid, 256, 0, st>>>(a); }
-// kgb_log_d(tn) of each slot (glass_TR's per-hit logarithm, once per slot; this file's flags, as the per-hit code's)
-__global__ void k_slot_logs(const kgb_slot* slots, uint32_t n, double* out) {
+// ln tn of each slot as a float pair (glass_TR's logarithm, once per slot; kgb_ln_pair, as kgb_powf takes it)
+__global__ void k_slot_logs(const kgb_slot* slots, uint32_t n, float2* out) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < n) out[s] = slots[s].tn > 0.f ? kgb_log_d((double)slots[s].tn) : 0.0;
+  if (s >= n) return;
+  float h = 0.f, l = 0.f;
+  if (slots[s].tn > 0.f) kgb_ln_pair(slots[s].tn, &h, &l);
+  out[s] = make_float2(h, l);
 }
-void launch_slot_logs(const kgb_slot* slots, uint32_t n, double* out, cudaStream_t st) {
+void launch_slot_logs(const kgb_slot* slots, uint32_t n, float2* out, cudaStream_t st) {
   if (n) k_slot_logs<<<(n + 127) / 128, 128, 0, st>>>(slots, n, out);
 }
 
