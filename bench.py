@@ -505,13 +505,22 @@ def run_views(args, pkg):
         K = nAz * nEl
         res[name] = {"rays": nc * K, "trace_s": best[0], "reduce_s": best[1], "mrays_s": nc * K / best[0] / 1e6,
                      "shares_sum_check": float(np.abs(out[:, 0] + out[:, 3] + out[:, 6] + out[:, 9] + out[:, 12] + out[:, 15] + out[:, 18] - 1).max())}
-        if world:   # the per-ray rows (gpu_download_view: classes + distances, [nc x K]), transposed on the device
+        if world:   # the per-ray rows (gpu_download_view: classes + distances, [nc x K]), transposed on the device, into
+            # buffers already written (the reference's caller resizes its vectors first, gpu.cu:730-731)
+            cls, dist = np.zeros((nc, K), np.uint8), np.zeros((nc, K), np.float32)
+            cls.fill(0)
+            dist.fill(0.0)
             t0 = time.perf_counter()
-            cls, dist = e.download_view(nc)
+            e.download_view(nc, out=(cls, dist))
             t1 = time.perf_counter()
-            back = (np.ascontiguousarray(cls.T), np.ascontiguousarray(dist.T))   # the same transpose on the host, one thread
+            back_c, back_d = np.zeros((K, nc), np.uint8), np.zeros((K, nc), np.float32)   # the same transpose on the host,
+            back_c.fill(0)                                                              # one thread, into written buffers
+            back_d.fill(0.0)
+            t1 = time.perf_counter()
+            np.copyto(back_c, cls.T)
+            np.copyto(back_d, dist.T)
             t2 = time.perf_counter()
-            del back
+            del back_c, back_d
             res[name]["download_rows"] = {"bytes": nc * K * 5, "s": t1 - t0, "gb_s": nc * K * 5 / (t1 - t0) / 1e9, "host_transpose_s": t2 - t1}
             del cls, dist
     # the host binned-SAH builder on the same city: build time, and the fov 120 trace on its tree (same results)

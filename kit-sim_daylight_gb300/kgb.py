@@ -369,12 +369,19 @@ class Engine:
         self._ok(self.d.kgb_reduce_view(self.h, nc, _p(wRow), wRow.size, nClass, farDist, _p(reach), reach.size, int(glazing), isoDim, _p(out)))
         return out
 
-    def download_view(self, nc):
+    def download_view(self, nc, out=None):
+        """Classes [nc x K] uint8 and distances [nc x K] float32; out: a (cls, dist) pair of C-contiguous arrays of
+        those shapes to write into (the reference's caller resizes its vectors before gpu_download_view), else new ones."""
         K = self.dims()["K"]
-        cls = np.zeros(nc * K, np.uint8)
-        dist = np.zeros(nc * K, np.float32)
+        if out is None:
+            cls, dist = np.zeros((nc, K), np.uint8), np.zeros((nc, K), np.float32)
+        else:
+            cls, dist = out
+            if cls.shape != (nc, K) or dist.shape != (nc, K) or cls.dtype != np.uint8 or dist.dtype != np.float32 or \
+                    not (cls.flags.c_contiguous and dist.flags.c_contiguous):
+                raise ValueError("download_view: out must be C-contiguous uint8 and float32 [nc x K] arrays")
         self._ok(self.d.kgb_download_view(self.h, nc, _p(cls), _p(dist), nc * K))
-        return cls.reshape(nc, K), dist.reshape(nc, K)
+        return cls, dist
 
 
 class Server:
