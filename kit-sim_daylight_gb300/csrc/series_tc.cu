@@ -11,9 +11,12 @@
 //    products run per K step: hi.hi, then the corrections hi.mid + mid.hi + hi.lo + mid.mid + lo.hi (the dropped
 //    mid.lo, lo.mid, lo.lo are 2^-24 of the product and below);
 //  - the tensor core's FP32 accumulation truncates, so a long accumulation chain drifts low by about a quarter ulp per
-//    instruction (1e-5 over 2305 patches). Every accumulation chain is therefore short: per 64-wide K block (a chunk)
-//    hi.hi goes into one TMEM accumulator and the five corrections into another, both from zero (4 and 20 MMAs), and
-//    the epilogue adds both chunk sums into FP32 registers with Kahan compensation;
+//    instruction (1e-5 over 2305 patches). The hi.hi chains are therefore short: each 64 of K goes into a TMEM
+//    accumulator from zero (4 MMAs), and per 128 of K (a chunk: two such sums) the epilogue adds the chunk's sum into
+//    FP32 registers with Kahan compensation. (One chain of 8 MMAs a chunk doubled the drift: the column error went
+//    from 4e-7 to 7e-7 of the column's maximum.) The five corrections are 2^-8 of the result or less: their chain runs over the whole tile in a
+//    second accumulator (its drift, about 1e-7 of the result at K 4672, stays well inside the 1e-6 bound), which the
+//    epilogue reads once per tile;
 //  - the sun term (one direction per step, exact in the reference's float arithmetic) is added in the epilogue, where
 //    each output is finished in registers and stored with 16-byte row stores.
 //
@@ -21,12 +24,18 @@
 // (tile_coords), so that the CTAs running at once share a few V panels and the band's S panels in L2:
 //   warp 0      TMA producer: per 64-wide K block, the three pieces of V (128 x 64) and of S (64 x 64), bf16,
 //               128-byte swizzled, into a 3-stage shared-memory ring (72 KB a stage)
-//   warp 1      MMA issuer (one thread): 24 tcgen05.mma (M 128, N 64, K 16) per stage: hi.hi into H[chunk % 2], the
-//               corrections into C[chunk % 2] (TMEM: H0 H1 C0 C1, 64 columns each); tcgen05.commit frees the stage
-//               and hands a finished chunk to the epilogue
+//   warp 1      MMA issuer (one thread): 24 tcgen05.mma (M 128, N 64, K 16) per stage: hi.hi into H[chunk % 3] (two
+//               accumulators, one per K block of the chunk), the corrections into C[tile % 2] (TMEM: 3 x 2 + 2
+//               accumulators of 64 columns, the whole 512); tcgen05.commit frees the stage,
+//               hands a finished chunk's hi.hi and a finished tile's corrections to the epilogue
 //   warps 2-5   epilogue, one per TMEM lane quarter (warp w reads lanes 32 (w % 4) ..), a thread per output row: per
-//               chunk, tcgen05.ld of H and C added into the row's 64 Kahan-compensated FP32 sums (128 registers); per
-//               tile, the sun term, and the row of E stored 16 bytes at a time
+//               chunk, tcgen05.ld of H added into the row's 64 Kahan-compensated FP32 sums (128 registers); per tile,
+//               the corrections, the sun term, and the row of E stored 16 bytes at a time
+// (The corrections were first summed per chunk beside hi.hi: the epilogue then spent more time per chunk, 8 TMEM loads
+// and 128 compensated adds a thread, than the chunk's 24 MMAs, and the tensor pipe waited on it. Chunks of 64 of K with
+// two hi.hi accumulators took 12 % longer than chunks of 128 with four buffers: each chunk is a round trip MMA ->
+// epilogue -> MMA. The MMA itself bounds the rest: an M 128 N 64 K 16 instruction takes about 71 cycles, some 29 of them the A
+// operand's read, so the tensor pipe stays near half busy at this tile width.)
 // The 64-column tile keeps the Kahan sums in registers: six warps per CTA leave a scheduler at most two warps, so a
 // thread may hold up to 255 registers (the register file is split between the SM's four schedulers).
 // Every wait on an mbarrier is bounded: past the limit the kernel records kStatusTimeout and leaves its loops (the
@@ -42,14 +51,18 @@
 namespace kgb {
 
 constexpr int BM = 128, BN = 64, BK = 64, STAGES = 3, PIECES = 3;
-constexpr int CHUNK_BLOCKS = 1;                      // K blocks (of BK) per accumulation chunk: 4 hi.hi + 20 correction MMAs
+constexpr int CHUNK_BLOCKS = 2;                      // K blocks (of BK) per accumulation chunk, each block's 4 hi.hi MMAs
+                                                     // in an accumulator of its own
+constexpr uint32_t NH = 3;                           // chunk buffers: the MMA issuer runs up to 2 chunks ahead
 constexpr int V_TILE = BM * BK * 2;                  // 16 KB: one bf16 V tile (128 rows x 128 B)
 constexpr int S_TILE = BN * BK * 2;                  // 8 KB: one bf16 S^T tile (64 rows x 128 B)
 constexpr int STAGE_BYTES = PIECES * (V_TILE + S_TILE); // V hi mid lo, S hi mid lo
 constexpr int EPI_WARPS = 4;                        // one per TMEM lane quarter, the tile's 64 columns each
 constexpr int THREADS = 32 * (2 + EPI_WARPS);
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /* align */ + 256 /* barriers */;
-constexpr uint32_t TMEM_COLS = 4 * BN;               // H0 H1 (hi.hi of a chunk), C0 C1 (its corrections)
+static_assert((2 * STAGES + 2 * NH + 4) * 8 + 4 <= 256, "the barriers and the TMEM slot fit their 256 bytes");
+constexpr uint32_t TMEM_COLS = NH * CHUNK_BLOCKS * BN + 2 * BN;   // H0..H2 (a chunk's two hi.hi blocks each), C0 C1
+static_assert(TMEM_COLS == 512, "a power of two of TMEM columns");
 constexpr uint64_t kWaitLimitNs = 4000000000ull;   // 4 s: no wait of a healthy run comes near it
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
@@ -171,21 +184,22 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
   uint64_t* full = bars;                 // [STAGES] TMA -> MMA
   uint64_t* empty = bars + STAGES;       // [STAGES] MMA -> TMA
-  uint64_t* hFull = bars + 2 * STAGES;   // [2] MMA -> epilogue: a chunk's two sums (hi.hi, corrections) are complete
-  uint64_t* hEmpty = hFull + 2;          // [2] epilogue -> MMA
-  uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(hFull + 4);
+  uint64_t* hFull = bars + 2 * STAGES;   // [NH] MMA -> epilogue: a chunk's hi.hi sum is complete
+  uint64_t* hEmpty = hFull + NH;         // [NH] epilogue -> MMA
+  uint64_t* cFull = hEmpty + NH;         // [2] MMA -> epilogue: a tile's corrections are complete
+  uint64_t* cEmpty = cFull + 2;          // [2] epilogue -> MMA
+  uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(cEmpty + 2);
   __shared__ volatile uint32_t abortFlag;
 
   const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
-    for (int b = 0; b < 2; ++b) {
-      mbar_init(&hFull[b], 1); mbar_init(&hEmpty[b], EPI_WARPS * 32);
-    }
+    for (uint32_t b = 0; b < NH; ++b) { mbar_init(&hFull[b], 1); mbar_init(&hEmpty[b], EPI_WARPS * 32); }
+    for (int b = 0; b < 2; ++b) { mbar_init(&cFull[b], 1); mbar_init(&cEmpty[b], EPI_WARPS * 32); }
     abortFlag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 1) {   // TMEM: four accumulators of BN fp32 columns x 128 lanes
+  if (warp == 1) {   // TMEM: NH x CHUNK_BLOCKS + 2 accumulators of BN fp32 columns x 128 lanes
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmemSlot)), "r"(TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
@@ -221,19 +235,23 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
     __syncwarp();
   } else if (warp == 1) {
     if (lane == 0) {   // ---------------- MMA issuer
-      uint32_t stage = 0, phase = 0, chunk = 0;
-      for (uint32_t tile = blockIdx.x; tile < nTilesAll && !abortFlag; tile += gridDim.x) {
-        uint32_t hT = tmemBase, cT = tmemBase + 2 * BN, hbuf = 0;
+      uint32_t stage = 0, phase = 0, chunk = 0, nt = 0;
+      for (uint32_t tile = blockIdx.x; tile < nTilesAll && !abortFlag; tile += gridDim.x, ++nt) {
+        // the tile's corrections into C[nt % 2], from zero at its first K step, over all its chunks
+        const uint32_t cbuf = nt & 1;
+        if (!mbar_wait(&cEmpty[cbuf], ((nt >> 1) & 1) ^ 1, a.status)) { abortFlag = 1; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t cT = tmemBase + (NH * CHUNK_BLOCKS + cbuf) * BN;
+        uint32_t hT = tmemBase, hbuf = 0;
         bool ok = true;
         for (uint32_t kb = 0; kb < kBlocks && ok; ++kb) {
           const uint32_t kc = kb % CHUNK_BLOCKS;
-          if (kc == 0) {   // a new chunk: hi.hi into H[buf], the corrections into C[buf], both from zero
-            hbuf = chunk & 1;
-            if (!mbar_wait(&hEmpty[hbuf], ((chunk >> 1) & 1) ^ 1, a.status)) { ok = false; break; }
+          if (kc == 0) {   // a new chunk: its hi.hi into H[buf]
+            hbuf = chunk % NH;
+            if (!mbar_wait(&hEmpty[hbuf], ((chunk / NH) & 1) ^ 1, a.status)) { ok = false; break; }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            hT = tmemBase + hbuf * BN;
-            cT = tmemBase + (2 + hbuf) * BN;
           }
+          hT = tmemBase + (hbuf * CHUNK_BLOCKS + kc) * BN;   // the block's own accumulator, from zero
           if (!mbar_wait(&full[stage], phase, a.status)) { ok = false; break; }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint8_t* s = smem + stage * STAGE_BYTES;
@@ -243,9 +261,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
 #pragma unroll
           for (int k = 0; k < BK / 16; ++k) {   // 16 bf16 = 32 bytes along K: +2 in the descriptor's address field
             const uint64_t off = uint64_t(2 * k);
-            const uint32_t acc = (kc | uint32_t(k)) != 0;
-            mma_bf16(hT, v0 + off, s0 + off, acc);
-            mma_bf16(cT, v0 + off, s1 + off, acc);
+            mma_bf16(hT, v0 + off, s0 + off, k != 0);
+            mma_bf16(cT, v0 + off, s1 + off, (kb | uint32_t(k)) != 0);
             mma_bf16(cT, v1 + off, s0 + off, 1);
             mma_bf16(cT, v0 + off, s2 + off, 1);
             mma_bf16(cT, v1 + off, s1 + off, 1);
@@ -256,44 +273,53 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
           if (kc == CHUNK_BLOCKS - 1 || kb == kBlocks - 1) { mma_commit(&hFull[hbuf]); ++chunk; }
         }
         if (!ok) { abortFlag = 1; break; }
+        mma_commit(&cFull[cbuf]);
       }
     }
     __syncwarp();
   } else {   // ---------------- epilogue: warps 2..5
     const uint32_t q = warp & 3;                       // the TMEM lane quarter this warp may read
     const uint32_t laneBase = (q * 32u) << 16;
-    uint32_t chunk = 0;
-    for (uint32_t tile = blockIdx.x; tile < nTilesAll; tile += gridDim.x) {
-      // the chunks' sums (hi.hi and corrections), added with Kahan compensation (acc - cmp is the running sum)
+    uint32_t chunk = 0, nt = 0;
+    for (uint32_t tile = blockIdx.x; tile < nTilesAll; tile += gridDim.x, ++nt) {
+      // the chunks' hi.hi sums, added with Kahan compensation (acc - cmp is the running sum)
       float acc[BN], cmp[BN];
 #pragma unroll
       for (int c = 0; c < BN; ++c) { acc[c] = 0.f; cmp[c] = 0.f; }
       bool ok = true;
       for (uint32_t ch = 0; ch < nChunks; ++ch, ++chunk) {
-        const uint32_t hbuf = chunk & 1;
-        ok = __all_sync(~0u, mbar_wait(&hFull[hbuf], (chunk >> 1) & 1, a.status));
+        const uint32_t hbuf = chunk % NH;
+        ok = __all_sync(~0u, mbar_wait(&hFull[hbuf], (chunk / NH) & 1, a.status));
         if (!ok || abortFlag) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const bool two = ch * CHUNK_BLOCKS + 1 < kBlocks;   // the last chunk may hold one block
+        const uint32_t hAt = tmemBase + laneBase + hbuf * CHUNK_BLOCKS * BN;
 #pragma unroll
-        for (int part = 0; part < 2; ++part) {   // the chunk's hi.hi sum, then its corrections
+        for (int g = 0; g < BN / 16; ++g) {
+          float v[16];
+          tmem_ld16(hAt + g * 16, v);
+          if (two) {   // the chunk's two block sums first (half an ulp of a chunk sum), then the compensated sum
+            float w[16];
+            tmem_ld16(hAt + BN + g * 16, w);
 #pragma unroll
-          for (int g = 0; g < BN / 16; ++g) {
-            float v[16];
-            tmem_ld16(tmemBase + laneBase + (2 * part + hbuf) * BN + g * 16, v);
+            for (int c = 0; c < 16; ++c) v[c] = __fadd_rn(v[c], w[c]);
+          }
 #pragma unroll
-            for (int c = 0; c < 16; ++c) {
-              const int j = g * 16 + c;
-              const float y = __fsub_rn(v[c], cmp[j]);
-              const float t = __fadd_rn(acc[j], y);
-              cmp[j] = __fsub_rn(__fsub_rn(t, acc[j]), y);
-              acc[j] = t;
-            }
+          for (int c = 0; c < 16; ++c) {
+            const int j = g * 16 + c;
+            const float y = __fsub_rn(v[c], cmp[j]);
+            const float t = __fadd_rn(acc[j], y);
+            cmp[j] = __fsub_rn(__fsub_rn(t, acc[j]), y);
+            acc[j] = t;
           }
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         mbar_arrive(&hEmpty[hbuf]);
       }
       if (!ok || abortFlag) { abortFlag = 1; break; }
+      const uint32_t cbuf = nt & 1;   // the tile's corrections, summed in TMEM over all its chunks
+      if (!__all_sync(~0u, mbar_wait(&cFull[cbuf], (nt >> 1) & 1, a.status)) || abortFlag) { abortFlag = 1; break; }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       uint32_t tm, tn;
       tile_coords(tile, a.mTiles, a.nTiles, tm, tn);
       const uint32_t m0 = (tm + a.mBase) * BM, n0 = tn * BN;
@@ -304,10 +330,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
       const bool vec = (a.T & 3u) == 0;                  // 16-byte row stores when rows are 16-byte aligned
 #pragma unroll
       for (int g = 0; g < BN / 16; ++g) {
-        float v[16];
+        float v[16], corr[16];
+        tmem_ld16(tmemBase + laneBase + (NH * CHUNK_BLOCKS + cbuf) * BN + g * 16, corr);
 #pragma unroll
         for (int c = 0; c < 16; ++c) {
-          float x = __fsub_rn(acc[g * 16 + c], cmp[g * 16 + c]);
+          float x = __fadd_rn(__fsub_rn(acc[g * 16 + c], cmp[g * 16 + c]), corr[c]);
           const uint32_t t = n0 + g * 16 + c;
           if (t < a.T && row < a.nc) {
             const int j = __ldg(a.sunOfCol + t);
@@ -332,6 +359,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
           }
         }
       }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      mbar_arrive(&cEmpty[cbuf]);   // the tile's corrections are read: C[cbuf] is free for the tile after next
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
