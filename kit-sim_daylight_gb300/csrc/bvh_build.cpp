@@ -1,11 +1,11 @@
 // Host builder of the engine's acceleration structure: a binned-SAH binary BVH (32 bins on the widest centroid axis,
 // leaves of at most 3 triangles) collapsed to 8-wide nodes (each inner node adopts the children of its largest-area
-// inner child until it has 8) with child boxes quantised to 8 bits against a power-of-two step per axis (the compressed
-// wide BVH of Ylitie, Karras, Laine 2017), stored as the 80-byte node / 48-byte triangle records rt.cuh reads.
+// inner child until it has 8) with float child boxes, stored as the 208-byte node / 48-byte triangle records rt.cuh
+// reads.
 //
 // Conservative by construction: every triangle box is expanded by 2^-16 x the scene's largest coordinate (256 ulps at
-// that magnitude) before anything is built, and quantisation rounds outwards, so a box test never drops a triangle the
-// watertight test would report; the traversal then equals the brute-force hit set on any input.
+// that magnitude) before anything is built, so a box test never drops a triangle the watertight test would report;
+// the traversal then equals the brute-force hit set on any input.
 #include "engine.h"
 
 #include <algorithm>
@@ -87,20 +87,6 @@ struct Builder {
   }
 };
 
-// One quantised axis: the step s = 2^(eb - 127) with p + 255 s covering the node's extent.
-void quant_axis(float p, float hi, uint32_t& eb, float& s) {
-  const double ext = std::max(double(hi) - double(p), 1e-30);
-  int e = 0;
-  std::frexp(ext / 255.0, &e);   // ext / 255 < 2^e
-  e = std::max(-126, std::min(127, e));
-  for (;;) {
-    s = std::ldexp(1.f, e);
-    if (double(p) + 255.0 * double(s) >= double(hi) || e >= 127) break;
-    ++e;
-  }
-  eb = uint32_t(e + 127);
-}
-
 }  // namespace
 
 void build_bvh8(const float* v, size_t nv, const uint32_t* tri, size_t nt, const uint32_t* slot, const uint8_t* translucent, BvhOut& out) {
@@ -153,26 +139,16 @@ void build_bvh8(const float* v, size_t nv, const uint32_t* tri, size_t nt, const
   for (size_t w = 0; w < wideSrc.size(); ++w) {
     int ch[8];
     const int n = children(wideSrc[w], ch);
-    Box box;
-    for (int k = 0; k < n; ++k) box.grow(B.nodes[size_t(ch[k])].box);
-    uint32_t rec[20] = {};
-    float p[3];
-    uint32_t eb[3];
-    float s[3];
-    for (int a = 0; a < 3; ++a) { p[a] = box.lo[a]; quant_axis(p[a], box.hi[a], eb[a], s[a]); }
+    uint32_t rec[kNodeWords] = {};
     uint32_t imask = 0, meta[8] = {};
     const uint32_t childBase = uint32_t(wideSrc.size()), triBase = uint32_t(tris.size() / 12);
     uint32_t triOff = 0;
-    uint8_t q[6][8];
-    std::memset(q, 0, sizeof q);
+    float plane[6][8];   // lo.x hi.x lo.y hi.y lo.z hi.z of each child; empty slots +inf / -inf
+    for (int k = 0; k < 8; ++k)
+      for (int a = 0; a < 3; ++a) { plane[2 * a][k] = INFINITY; plane[2 * a + 1][k] = -INFINITY; }
     for (int k = 0; k < n; ++k) {
       const Node2& c = B.nodes[size_t(ch[k])];
-      for (int a = 0; a < 3; ++a) {
-        const double lo = std::floor((double(c.box.lo[a]) - double(p[a])) / double(s[a]));
-        const double hi = std::ceil((double(c.box.hi[a]) - double(p[a])) / double(s[a]));
-        q[a][k] = uint8_t(std::max(0.0, std::min(255.0, lo)));
-        q[3 + a][k] = uint8_t(std::max(0.0, std::min(255.0, hi)));
-      }
+      for (int a = 0; a < 3; ++a) { plane[2 * a][k] = c.box.lo[a]; plane[2 * a + 1][k] = c.box.hi[a]; }
       if (!c.count) {
         imask |= 1u << k;
         wideSrc.push_back(ch[k]);
@@ -190,20 +166,12 @@ void build_bvh8(const float* v, size_t nv, const uint32_t* tri, size_t nt, const
         triOff += c.count;
       }
     }
-    std::memcpy(&rec[0], &p[0], 4); std::memcpy(&rec[1], &p[1], 4); std::memcpy(&rec[2], &p[2], 4);
-    rec[3] = eb[0] | (eb[1] << 8) | (eb[2] << 16) | (imask << 24);
-    rec[4] = childBase;
-    rec[5] = triBase;
-    rec[6] = meta[0] | (meta[1] << 8) | (meta[2] << 16) | (meta[3] << 24);
-    rec[7] = meta[4] | (meta[5] << 8) | (meta[6] << 16) | (meta[7] << 24);
-    // n2: qlo.x[8] qlo.y[8]; n3: qlo.z[8] qhi.x[8]; n4: qhi.y[8] qhi.z[8]
-    const int order[6] = {0, 1, 2, 3, 4, 5};
-    for (int f = 0; f < 6; ++f) {
-      const int src = order[f];
-      rec[8 + 2 * f] = uint32_t(q[src][0]) | (uint32_t(q[src][1]) << 8) | (uint32_t(q[src][2]) << 16) | (uint32_t(q[src][3]) << 24);
-      rec[9 + 2 * f] = uint32_t(q[src][4]) | (uint32_t(q[src][5]) << 8) | (uint32_t(q[src][6]) << 16) | (uint32_t(q[src][7]) << 24);
-    }
-    nodes.insert(nodes.end(), rec, rec + 20);
+    rec[0] = childBase | (imask << 24);   // fewer than 2^24 nodes: the engine checks the triangle count first
+    rec[1] = triBase;
+    rec[2] = meta[0] | (meta[1] << 8) | (meta[2] << 16) | (meta[3] << 24);
+    rec[3] = meta[4] | (meta[5] << 8) | (meta[6] << 16) | (meta[7] << 24);
+    std::memcpy(&rec[4], plane, sizeof plane);   // n1 n2 lo.x, n3 n4 hi.x, n5 n6 lo.y, ...
+    nodes.insert(nodes.end(), rec, rec + kNodeWords);
   }
   out.nNodes = uint32_t(wideSrc.size());
 }

@@ -1,8 +1,8 @@
 // Device builder of the engine's acceleration structure (the reference's gpu_build, gpu.cu:386-457, builds an OptiX
 // GAS on the device; this is the GB300 counterpart): a linear BVH over Morton codes (Karras 2012), refined by treelet
 // restructuring, collapsed to the
-// 8-wide quantised nodes and 48-byte triangle records that rt.cuh reads, the same layout as the host builder
-// (bvh_build.cpp) makes.
+// 8-wide nodes with float child boxes and the 48-byte triangle records that rt.cuh reads, the same layout as the host
+// builder (bvh_build.cpp) makes.
 //
 //   1. |coordinates| maximum -> eps = max(1, M) / 65536 (the host builder's expansion)
 //   2. per triangle: box (expanded by eps), centroid; centroid bounds
@@ -17,8 +17,7 @@
 //      follow those choices (leaf triangles gathered by a walk: restructured subtrees are no longer ranges of the
 //      sorted order), and a prefix sum over the level gives each node its block of inner children and of triangle
 //      records, so the layout is deterministic
-//   7. each node's child boxes quantised outwards to 8 bits against a power-of-two step per axis (double arithmetic,
-//      as the host builder)
+//   7. each node's child boxes written as floats (the expanded boxes of step 2, merged), empty slots +inf / -inf
 // Conservative exactly as the host builder: any conservative BVH gives the traversal the brute-force hit set, so the
 // results do not depend on which builder made the scene.
 #include "engine.h"
@@ -396,20 +395,6 @@ __global__ void k_collapse_count(Tree T, Dp D, const int* wideSrc, uint32_t b, u
   nTri[w - b] = nt;
 }
 
-// the host builder's quant_axis: step s = 2^(eb - 127) with p + 255 s covering the extent
-__device__ __forceinline__ void quant_axis(float p, float hi, uint32_t& eb, float& s) {
-  const double ext = fmax(double(hi) - double(p), 1e-30);
-  int e = 0;
-  frexp(ext / 255.0, &e);
-  e = max(-126, min(127, e));
-  for (int it = 0; it < 300; ++it) {   // e rises to 127 at most
-    s = ldexpf(1.f, e);
-    if (double(p) + 255.0 * double(s) >= double(hi) || e >= 127) break;
-    ++e;
-  }
-  eb = uint32_t(e + 127);
-}
-
 // level pass 2: node records, triangle records, the next level's sources
 __global__ void k_collapse_emit(Tree T, Dp D, const float* v, const uint32_t* tri, const uint32_t* slot, const uint8_t* translucent, uint32_t b,
                                 uint32_t e, const int* kids, const uint32_t* innerOff, const uint32_t* triOff, uint32_t triBase0,
@@ -419,29 +404,17 @@ __global__ void k_collapse_emit(Tree T, Dp D, const float* v, const uint32_t* tr
   int ch[8];
   int n = 0;
   for (int k = 0; k < 8; ++k) { ch[k] = kids[size_t(w - b) * 8 + k]; if (ch[k] != INT32_MIN) n = k + 1; }
-  float4 blo = make_float4(INFINITY, INFINITY, INFINITY, 0.f), bhi = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
-  for (int k = 0; k < n; ++k) {
-    float4 lo, hi;
-    box_of(T, ch[k], lo, hi);
-    blo = make_float4(fminf(blo.x, lo.x), fminf(blo.y, lo.y), fminf(blo.z, lo.z), 0.f);
-    bhi = make_float4(fmaxf(bhi.x, hi.x), fmaxf(bhi.y, hi.y), fmaxf(bhi.z, hi.z), 0.f);
-  }
-  const float p[3] = {blo.x, blo.y, blo.z}, ph[3] = {bhi.x, bhi.y, bhi.z};
-  uint32_t eb[3];
-  float s[3];
-  for (int a = 0; a < 3; ++a) quant_axis(p[a], ph[a], eb[a], s[a]);
   const uint32_t childBase = e + innerOff[w - b], triBase = triBase0 + triOff[w - b];
-  uint32_t imask = 0, meta[8] = {}, q[6][8] = {}, inner = 0, tOff = 0;
+  uint32_t* rec = nodes + size_t(w) * kNodeWords;
+  uint32_t imask = 0, meta[8] = {}, inner = 0, tOff = 0;
+  for (int k = 0; k < 8; ++k) {   // lo.x hi.x lo.y hi.y lo.z hi.z of each child at word 4 + 8 plane + k; empty slots +inf / -inf
+    float4 lo = make_float4(INFINITY, INFINITY, INFINITY, 0.f), hi = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
+    if (k < n) box_of(T, ch[k], lo, hi);
+    rec[4 + 0 * 8 + k] = __float_as_uint(lo.x); rec[4 + 1 * 8 + k] = __float_as_uint(hi.x);
+    rec[4 + 2 * 8 + k] = __float_as_uint(lo.y); rec[4 + 3 * 8 + k] = __float_as_uint(hi.y);
+    rec[4 + 4 * 8 + k] = __float_as_uint(lo.z); rec[4 + 5 * 8 + k] = __float_as_uint(hi.z);
+  }
   for (int k = 0; k < n; ++k) {
-    float4 lo, hi;
-    box_of(T, ch[k], lo, hi);
-    const float cl[3] = {lo.x, lo.y, lo.z}, chh[3] = {hi.x, hi.y, hi.z};
-    for (int a = 0; a < 3; ++a) {
-      const double ql = floor((double(cl[a]) - double(p[a])) / double(s[a]));
-      const double qh = ceil((double(chh[a]) - double(p[a])) / double(s[a]));
-      q[a][k] = uint32_t(fmax(0.0, fmin(255.0, ql)));
-      q[3 + a][k] = uint32_t(fmax(0.0, fmin(255.0, qh)));
-    }
     if (!dp_leaf(D, ch[k])) {
       imask |= 1u << k;
       wideSrc[childBase + inner++] = ch[k];
@@ -461,17 +434,10 @@ __global__ void k_collapse_emit(Tree T, Dp D, const float* v, const uint32_t* tr
       tOff += cnt;
     }
   }
-  uint32_t* rec = nodes + size_t(w) * 20;
-  rec[0] = __float_as_uint(p[0]); rec[1] = __float_as_uint(p[1]); rec[2] = __float_as_uint(p[2]);
-  rec[3] = eb[0] | (eb[1] << 8) | (eb[2] << 16) | (imask << 24);
-  rec[4] = childBase;
-  rec[5] = triBase;
-  rec[6] = meta[0] | (meta[1] << 8) | (meta[2] << 16) | (meta[3] << 24);
-  rec[7] = meta[4] | (meta[5] << 8) | (meta[6] << 16) | (meta[7] << 24);
-  for (int f = 0; f < 6; ++f) {
-    rec[8 + 2 * f] = q[f][0] | (q[f][1] << 8) | (q[f][2] << 16) | (q[f][3] << 24);
-    rec[9 + 2 * f] = q[f][4] | (q[f][5] << 8) | (q[f][6] << 16) | (q[f][7] << 24);
-  }
+  rec[0] = childBase | (imask << 24);   // fewer than 2^24 nodes: the engine checks the triangle count first
+  rec[1] = triBase;
+  rec[2] = meta[0] | (meta[1] << 8) | (meta[2] << 16) | (meta[3] << 24);
+  rec[3] = meta[4] | (meta[5] << 8) | (meta[6] << 16) | (meta[7] << 24);
 }
 
 struct DevBuf {
@@ -562,7 +528,7 @@ std::string build_bvh8_gpu(const float* v, size_t nv, const uint32_t* tri, size_
   void* nodes = nullptr;
   void* tris = nullptr;
   const size_t maxNodes = std::max<size_t>(1, nt);   // a wide node has at least two children but the root
-  KGB_TRY(cudaMalloc(&nodes, maxNodes * 80));
+  KGB_TRY(cudaMalloc(&nodes, maxNodes * kNodeBytes));
   if (cudaMalloc(&tris, nt * 48) != cudaSuccess) { cudaFree(nodes); return "cudaMalloc(tris) failed"; }
   *nodesOut = nodes;
   *trisOut = tris;

@@ -370,12 +370,12 @@ KGB_API void kgb_destroy(kgb_engine* e) {
 }
 
 // Device bytes a build of nt triangles over nv vertices peaks at: inputs stay on the host (the builder runs there),
-// the device holds the triangle records (48 B each) and at most nt/2 + 2 nodes of 80 B; counted twice (the new scene
-// and a parked one may coexist during a swap).
+// the device holds the triangle records (48 B each) and at most nt/2 + 2 nodes of kNodeBytes; counted twice (the new
+// scene and a parked one may coexist during a swap).
 KGB_API uint64_t kgb_build_bytes(kgb_engine*, size_t nv, size_t nt, int slotted) {
   if (!nt) return 0;
   const uint64_t inputs = uint64_t(nv) * 12 + uint64_t(nt) * (12 + (slotted ? 4 : 0));
-  const uint64_t out = uint64_t(nt) * 64 + (uint64_t(nt) / 2 + 2) * 80 + 4096;
+  const uint64_t out = uint64_t(nt) * 64 + (uint64_t(nt) / 2 + 2) * kNodeBytes + 4096;
   return inputs + 2 * out;
 }
 
@@ -407,11 +407,11 @@ KGB_API int kgb_build(kgb_engine* e, const float* v, size_t nv, const uint32_t* 
     uint64_t temp = 0;
     const std::string why = build_bvh8_gpu(v, nv, tri, nt, slotted ? slot : nullptr, slotted ? translucent.data() : nullptr, g.st, &nodes, &tris,
                                            &nNodes, &temp);
-    s.nodes.p = nodes; s.nodes.cap = std::max<size_t>(1, nt) * 80;
+    s.nodes.p = nodes; s.nodes.cap = std::max<size_t>(1, nt) * kNodeBytes;
     s.tris.p = tris; s.tris.cap = nt * 48;
     if (!why.empty()) return fail("gpu_build: " + why);
     s.nNodes = nNodes;
-    s.bytes = uint64_t(nNodes) * 80 + uint64_t(nt) * 48;
+    s.bytes = uint64_t(nNodes) * kNodeBytes + uint64_t(nt) * 48;
     g.stats.buildTempBytes = temp;
   } else {   // on the host (binned SAH)
     BvhOut b;
@@ -421,6 +421,7 @@ KGB_API int kgb_build(kgb_engine* e, const float* v, size_t nv, const uint32_t* 
     s.bytes = b.nodes.size() * 4 + b.tris.size() * 4;
     g.stats.buildTempBytes = uint64_t(nt) * 64;
   }
+  if (s.nNodes >= kMaxNodes) return fail("gpu_build: 2^24 nodes or more (the node records' child index has 24 bits)");
   s.nTris = uint32_t(nt);
   CU(cudaEventRecord(g.ev[1], g.st));
   CU(cudaStreamSynchronize(g.st));

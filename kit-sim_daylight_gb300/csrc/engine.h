@@ -10,6 +10,12 @@
 
 namespace kgb {
 
+// BVH8 node record (rt.cuh): 52 words = 208 bytes; a node's childBase field holds 24 bits, so a tree has fewer than
+// 2^24 nodes (a scene of nt triangles has at most nt / 2 + 2).
+constexpr uint32_t kNodeWords = 52;
+constexpr uint32_t kNodeBytes = 4 * kNodeWords;
+constexpr uint32_t kMaxNodes = 1u << 24;
+
 struct Node8;
 struct TriRec;
 struct RayDir;
@@ -189,9 +195,9 @@ void engine_reduce_inputs(kgb_engine* e, ReduceInputs& in);
 const char* sky_steps(int mf, const kgb_sky_step* steps, size_t T, double grefl, int sun, int sky, int visible, float* out, cudaStream_t st);
 const char* sun_steps(const double* in, size_t T, double* out, cudaStream_t st);
 
-// host BVH builder (bvh_build.cpp): binned-SAH binary BVH, collapsed to the 8-wide quantised layout of rt.cuh
+// host BVH builder (bvh_build.cpp): binned-SAH binary BVH, collapsed to the 8-wide float-plane layout of rt.cuh
 struct BvhOut {
-  std::vector<uint32_t> nodes;   // 20 words per node
+  std::vector<uint32_t> nodes;   // kNodeWords words per node
   std::vector<float> tris;       // 12 words per triangle record
   uint32_t nNodes = 0;
 };

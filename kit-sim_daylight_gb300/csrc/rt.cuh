@@ -1,4 +1,4 @@
-// Device-side ray casting of the engine: the watertight ray/triangle test, the compressed 8-wide BVH traversal
+// Device-side ray casting of the engine: the watertight ray/triangle test, the 8-wide BVH traversal
 // (any-hit and closest-hit), and the reference's per-hit rules (own planes, glass, offsets, hashes).
 //
 // Numerics contract: the code deciding a result (hit or miss, t, own plane, transmittance byte, direction cell, sky
@@ -11,19 +11,26 @@
 #include <cstdint>
 #include "kgb_detmath.h"
 #include "kitsim_gb300.h"
+#include "engine.h"
 
 namespace kgb {
 
 // ------------------------------------------------------------------------------------------------ data layout (HBM)
-// BVH8 node, 80 bytes = 5 x 16 B, read with five 128-bit loads:
-//   n0: p.x p.y p.z (float, the node box origin), e.x e.y e.z (biased float exponents of the child quantisation
-//       steps, byte 12..14), imask (byte 15: bit k = child k is an inner node)
-//   n1: childBase (index of the node's first inner child; its inner children are consecutive in slot order),
-//       triBase (index of the node's first triangle record), meta[8] (leaf child k: count << 5 | offset of its
-//       triangles from triBase; 0: empty slot)
-//   n2..n4: qlo.x[8] qlo.y[8] | qlo.z[8] qhi.x[8] | qhi.y[8] qhi.z[8] (child boxes: p + 2^(e-127) q)
+// BVH8 node, 208 bytes = 13 x 16 B:
+//   n0: childBase | imask << 24 (childBase: index of the node's first inner child, below 2^24; its inner children are
+//       consecutive in slot order; imask bit k: child k is an inner node), triBase (index of the node's first
+//       triangle record), meta[8] (leaf child k: count << 5 | offset of its triangles from triBase; 0: empty slot)
+//   n1 n2: lo.x of children 0..3, 4..7 (float)   n3 n4: hi.x
+//   n5 n6: lo.y                                  n7 n8: hi.y
+//   n9 n10: lo.z                                 n11 n12: hi.z
+//   (an empty slot holds lo = +inf, hi = -inf, which no ray enters)
+// The child boxes are plain floats: the box test reads a ray's near and far planes straight from the two vectors its
+// octant picks (Ray::nearX..: n1 or n3 for x; the far one is the index ^ 2), with no decoding. (The 80-byte form
+// with 8-bit child boxes of Ylitie, Karras and Laine 2017 spent most of the box test's instructions decoding bytes:
+// the test is 87 % of the any-hit walk's instructions.)
 // Triangle record, 48 bytes = 3 x 16 B: v0.xyz + primitive index | v1.xyz + flags | v2.xyz + slot.
-struct __align__(16) Node8 { uint4 n[5]; };
+struct __align__(16) Node8 { uint4 n[kNodeWords / 4]; };
+static_assert(sizeof(Node8) == 4 * kNodeWords, "node record size");
 struct __align__(16) TriRec { float4 a, b, c; };
 enum : uint32_t { kTriTranslucent = 1u };   // TriRec.b.w flag bits: the slot transmitted at build (any-hit)
 
@@ -87,7 +94,13 @@ struct Ray {
   F3 inv;     // box test: 1 / d with zero components replaced by +-2^-80
   F3 oinv;    // o * inv
   uint32_t oct;   // sign bits of d (closest-hit child order)
+  uint32_t nearX, nearY, nearZ;   // node vectors of the near planes per axis (lo if inv >= 0, else hi); far: ^ 2
 };
+__device__ __forceinline__ void near_planes(Ray& r) {
+  r.nearX = r.inv.x < 0.f ? 3u : 1u;
+  r.nearY = r.inv.y < 0.f ? 7u : 5u;
+  r.nearZ = r.inv.z < 0.f ? 11u : 9u;
+}
 __device__ __forceinline__ Ray make_ray(F3 o, F3 d) {
   Ray r;
   r.o = o; r.d = d;
@@ -105,6 +118,7 @@ __device__ __forceinline__ Ray make_ray(F3 o, F3 d) {
   r.inv = f3(1.f / dx, 1.f / dy, 1.f / dzz);
   r.oinv = f3(o.x * r.inv.x, o.y * r.inv.y, o.z * r.inv.z);
   r.oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
+  near_planes(r);
   return r;
 }
 
@@ -129,6 +143,7 @@ __device__ __forceinline__ Ray ray_from(const RayDir* tab, uint32_t d, F3 o) {
   r.Sx = a.w; r.Sy = b.w; r.Sz = c.x;
   r.inv = f3(b.x, b.y, b.z);
   r.oinv = f3(o.x * r.inv.x, o.y * r.inv.y, o.z * r.inv.z);
+  near_planes(r);
   return r;
 }
 
@@ -194,11 +209,6 @@ __device__ __forceinline__ F3 through(const TriHit& h) { return sub(offset_ray(h
 // ------------------------------------------------------------------------------------------------ BVH8 traversal
 __device__ __forceinline__ uint32_t byte_of(uint32_t w, int k) { return (w >> (8 * k)) & 0xffu; }
 
-// Byte b of w as a float, exactly: the bit pattern 0x4B0000qq is 2^23 + q, and the subtraction of 2^23 is exact.
-// One byte permute and one add instead of a bit-field extract and an integer-to-float conversion.
-__device__ __forceinline__ float qf(uint32_t w, int b) {
-  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | uint32_t(b))) - 8388608.f;
-}
 // The helpers below hold inline PTX; their host branches (plain C++, the same values) let tests and tools compile
 // this header for the CPU.
 __device__ __forceinline__ float max3f(float a, float b, float c) {
@@ -238,17 +248,6 @@ __device__ __forceinline__ void up2(unsigned long long r, float& a, float& b) {
   a = __uint_as_float(uint32_t(r)); b = __uint_as_float(uint32_t(r >> 32));
 #endif
 }
-__device__ __forceinline__ unsigned long long add2(unsigned long long a, unsigned long long b) {
-#if defined(__CUDA_ARCH__)
-  unsigned long long r;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-#else
-  float a0, a1, b0, b1;
-  up2(a, a0, a1); up2(b, b0, b1);
-  return pk2(a0 + b0, a1 + b1);
-#endif
-}
 __device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b, unsigned long long c) {
 #if defined(__CUDA_ARCH__)
   unsigned long long r;
@@ -271,65 +270,63 @@ __device__ __forceinline__ unsigned long long mul2(unsigned long long a, unsigne
   return pk2(a0 * b0, a1 * b1);
 #endif
 }
-// Bytes b and b + 1 of w as the bit patterns 2^23 + q (see qf), packed.
-__device__ __forceinline__ unsigned long long qf2raw(uint32_t w, int b) {
-  return pk2(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | uint32_t(b))), __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | uint32_t(b + 1))));
+// Two words as one packed pair (the low word first).
+__device__ __forceinline__ unsigned long long pku(uint32_t a, uint32_t b) {
+#if defined(__CUDA_ARCH__)
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "r"(a), "r"(b));
+  return r;
+#else
+  return (unsigned long long)a | ((unsigned long long)b << 32);
+#endif
 }
 
-// Child boxes of a node against the ray in [tmin, tmax] (tmin >= 0): returns the mask of hit children (bit k), their
-// entry distances in tn[8]. Conservative: the boxes were expanded at build; the exit distance is widened by 2^-20.
-// Per axis the near plane is the low one when the ray's inverse direction is non-negative (the slab distance
-// fma(q, adj, o) is then non-decreasing in q), else the high one: the words of near and far planes are picked once
-// per node. Children go in pairs through the packed instructions: per pair and plane two byte permutes, one packed
-// add (the exact byte value) and one packed fma; per child one 3-input max and one 3-input min. Empty child slots need
-// no test: a leaf slot without triangles that the box test lets through tests nothing.
+// Child boxes of the node at p against the ray in [tmin, tmax] (tmin >= 0): returns the mask of hit children (bit k),
+// their entry distances in tn[8]. Per axis the slab distance of a plane is fma(plane, inv, -o inv); the near planes
+// are the low ones when inv >= 0, else the high ones, and the ray's nearX.. index picks their vector (the far one is
+// the other). Children go in pairs through the packed fma: per pair one fma.f32x2 per plane, per child one 3-input max
+// and one 3-input min. Conservative: the triangle boxes were expanded at build by 2^-16 of the scene's largest
+// coordinate, far beyond the rounding of these distances, and the exit distance is widened by 2^-20 besides. Empty
+// child slots (lo +inf, hi -inf) fail the test; a leaf slot without triangles that passes tests nothing.
 // CLIP: the exit is also clipped at tmax (closest hit, where tmax shrinks to the best hit). Without it boxes beyond
 // tmax pass as well, which is conservative: the triangle test applies tmax (the any-hit walks run to infinity).
 template <bool CLIP = true>
-__device__ __forceinline__ uint32_t node_hits(const uint4* n, const Ray& r, float tmin, float tmax, float* tn) {
-  const float px = __uint_as_float(n[0].x), py = __uint_as_float(n[0].y), pz = __uint_as_float(n[0].z);
-  const uint32_t ew = n[0].w;
-  const float sx = __uint_as_float((ew & 0xffu) << 23), sy = __uint_as_float(((ew >> 8) & 0xffu) << 23), sz = __uint_as_float(((ew >> 16) & 0xffu) << 23);
-  const float adjx = sx * r.inv.x, adjy = sy * r.inv.y, adjz = sz * r.inv.z;
-  const float ox = __fmaf_rn(px, r.inv.x, -r.oinv.x), oy = __fmaf_rn(py, r.inv.y, -r.oinv.y), oz = __fmaf_rn(pz, r.inv.z, -r.oinv.z);
-  const unsigned long long AX = pk2(adjx, adjx), AY = pk2(adjy, adjy), AZ = pk2(adjz, adjz);
-  const unsigned long long OX = pk2(ox, ox), OY = pk2(oy, oy), OZ = pk2(oz, oz);
-  const unsigned long long MAGIC = pk2(-8388608.f, -8388608.f), WIDEN = pk2(1.00000095367431640625f, 1.00000095367431640625f);
-  // quantised bounds: qlo.x = n2.x,n2.y  qlo.y = n2.z,n2.w  qlo.z = n3.x,n3.y  qhi.x = n3.z,n3.w  qhi.y = n4.x,n4.y  qhi.z = n4.z,n4.w
-  const bool nx = r.inv.x < 0.f, ny = r.inv.y < 0.f, nz = r.inv.z < 0.f;
-  const uint32_t nearX[2] = {nx ? n[3].z : n[2].x, nx ? n[3].w : n[2].y}, farX[2] = {nx ? n[2].x : n[3].z, nx ? n[2].y : n[3].w};
-  const uint32_t nearY[2] = {ny ? n[4].x : n[2].z, ny ? n[4].y : n[2].w}, farY[2] = {ny ? n[2].z : n[4].x, ny ? n[2].w : n[4].y};
-  const uint32_t nearZ[2] = {nz ? n[4].z : n[3].x, nz ? n[4].w : n[3].y}, farZ[2] = {nz ? n[3].x : n[4].z, nz ? n[3].y : n[4].w};
+__device__ __forceinline__ uint32_t node_hits(const uint4* p, const Ray& r, float tmin, float tmax, float* tn) {
+  const unsigned long long IX = pk2(r.inv.x, r.inv.x), IY = pk2(r.inv.y, r.inv.y), IZ = pk2(r.inv.z, r.inv.z);
+  const unsigned long long OX = pk2(-r.oinv.x, -r.oinv.x), OY = pk2(-r.oinv.y, -r.oinv.y), OZ = pk2(-r.oinv.z, -r.oinv.z);
+  const unsigned long long WIDEN = pk2(1.00000095367431640625f, 1.00000095367431640625f);
+  const uint32_t fX = r.nearX ^ 2u, fY = r.nearY ^ 2u, fZ = r.nearZ ^ 2u;
   uint32_t mask = 0;
 #pragma unroll
-  for (int k = 0; k < 8; k += 2) {
-    const int h = k >> 2, b = k & 3;
-    float tnx[2], tny[2], tnz[2], tfx[2], tfy[2], tfz[2];
-    up2(fma2(add2(qf2raw(nearX[h], b), MAGIC), AX, OX), tnx[0], tnx[1]);
-    up2(fma2(add2(qf2raw(farX[h], b), MAGIC), AX, OX), tfx[0], tfx[1]);
-    up2(fma2(add2(qf2raw(nearY[h], b), MAGIC), AY, OY), tny[0], tny[1]);
-    up2(fma2(add2(qf2raw(farY[h], b), MAGIC), AY, OY), tfy[0], tfy[1]);
-    up2(fma2(add2(qf2raw(nearZ[h], b), MAGIC), AZ, OZ), tnz[0], tnz[1]);
-    up2(fma2(add2(qf2raw(farZ[h], b), MAGIC), AZ, OZ), tfz[0], tfz[1]);
-    // exit widened to tfar (1 + 2^-20): for tfar >= 0 the value fma(|tfar|, 2^-20, tfar), and a negative tfar fails
-    // against tnear >= tmin >= 0 either way
-    float tf[2];
-    up2(mul2(pk2(min3f(tfx[0], tfy[0], tfz[0]), min3f(tfx[1], tfy[1], tfz[1])), WIDEN), tf[0], tf[1]);
+  for (int h = 0; h < 2; ++h) {   // children 4h .. 4h + 3: the second vector of each plane set
+    const uint4 nx = __ldg(p + r.nearX + h), fx = __ldg(p + fX + h);
+    const uint4 ny = __ldg(p + r.nearY + h), fy = __ldg(p + fY + h);
+    const uint4 nz = __ldg(p + r.nearZ + h), fz = __ldg(p + fZ + h);
 #pragma unroll
-    for (int e = 0; e < 2; ++e) {
-      const float tnear = max3f(tnx[e], tny[e], fmaxf(tnz[e], tmin));
-      const float tfar = CLIP ? fminf(tf[e], tmax) : tf[e];
-      if (tnear <= tfar) { mask |= 1u << (k + e); tn[k + e] = tnear; }
+    for (int j = 0; j < 2; ++j) {   // the pair 4h + 2j, 4h + 2j + 1
+      const int k = 4 * h + 2 * j;
+      float tnx[2], tny[2], tnz[2], tfx[2], tfy[2], tfz[2];
+      up2(fma2(j ? pku(nx.z, nx.w) : pku(nx.x, nx.y), IX, OX), tnx[0], tnx[1]);
+      up2(fma2(j ? pku(fx.z, fx.w) : pku(fx.x, fx.y), IX, OX), tfx[0], tfx[1]);
+      up2(fma2(j ? pku(ny.z, ny.w) : pku(ny.x, ny.y), IY, OY), tny[0], tny[1]);
+      up2(fma2(j ? pku(fy.z, fy.w) : pku(fy.x, fy.y), IY, OY), tfy[0], tfy[1]);
+      up2(fma2(j ? pku(nz.z, nz.w) : pku(nz.x, nz.y), IZ, OZ), tnz[0], tnz[1]);
+      up2(fma2(j ? pku(fz.z, fz.w) : pku(fz.x, fz.y), IZ, OZ), tfz[0], tfz[1]);
+      // exit widened to tfar (1 + 2^-20): for tfar >= 0 the value fma(|tfar|, 2^-20, tfar), and a negative tfar fails
+      // against tnear >= tmin >= 0 either way
+      float tf[2];
+      up2(mul2(pk2(min3f(tfx[0], tfy[0], tfz[0]), min3f(tfx[1], tfy[1], tfz[1])), WIDEN), tf[0], tf[1]);
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const float tnear = max3f(tnx[e], tny[e], fmaxf(tnz[e], tmin));
+        const float tfar = CLIP ? fminf(tf[e], tmax) : tf[e];
+        if (tnear <= tfar) { mask |= 1u << (k + e); tn[k + e] = tnear; }
+      }
     }
   }
   return mask;
 }
 
-__device__ __forceinline__ void load_node(const Node8* nodes, uint32_t idx, uint4* n) {
-  const uint4* p = reinterpret_cast<const uint4*>(nodes + idx);
-#pragma unroll
-  for (int q = 0; q < 5; ++q) n[q] = __ldg(p + q);
-}
 __device__ __forceinline__ void load_tri(const TriRec* tris, uint32_t j, F3& v0, F3& v1, F3& v2, uint32_t& prim, uint32_t& flags, uint32_t& slot) {
   const float4* p = reinterpret_cast<const float4*>(tris + j);
   const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
@@ -376,18 +373,18 @@ __device__ __forceinline__ void for_hits(const Scene& s, const Ray& r, float tmi
   const uint32_t cap = visit_cap(s);
   for (uint32_t visits = 0;; ++visits) {
     if (visits >= cap || cur >= s.nNodes) { overflow |= 2u; return; }
-    uint4 n[5];
-    load_node(s.nodes, cur, n);
+    const uint4* np = reinterpret_cast<const uint4*>(s.nodes + cur);
+    const uint4 hd = __ldg(np);
     if (COUNT) ctr->nodes++;
     float tn[8];
-    const uint32_t hit = node_hits<false>(n, r, tmin, tmax, tn);
-    const uint32_t imask = n[0].w >> 24;
+    const uint32_t hit = node_hits<false>(np, r, tmin, tmax, tn);
+    const uint32_t imask = hd.x >> 24, childBase = hd.x & 0xffffffu;
     uint32_t leaves = hit & ~imask;
     while (leaves) {
       const int k = __ffs(leaves) - 1;
       leaves &= leaves - 1;
-      const uint32_t meta = byte_of(k < 4 ? n[1].z : n[1].w, k & 3);
-      const uint32_t first = n[1].y + (meta & 31u), cnt = meta >> 5;
+      const uint32_t meta = byte_of(k < 4 ? hd.z : hd.w, k & 3);
+      const uint32_t first = hd.y + (meta & 31u), cnt = meta >> 5;
       for (uint32_t j = first; j < first + cnt; ++j) {
         F3 v0, v1, v2;
         uint32_t prim, flags, slot;
@@ -405,10 +402,10 @@ __device__ __forceinline__ void for_hits(const Scene& s, const Ray& r, float tmi
       const int k = __ffs(inner) - 1;
       const uint32_t rest = inner & (inner - 1);
       if (rest) {
-        if (sp < kStack) stack[sp++] = make_uint2(n[1].x, (imask << 8) | rest);
+        if (sp < kStack) stack[sp++] = make_uint2(childBase, (imask << 8) | rest);
         else overflow = 1;
       }
-      cur = n[1].x + __popc(imask & ((1u << k) - 1u));
+      cur = childBase + __popc(imask & ((1u << k) - 1u));
       continue;
     }
     if (!sp) return;
@@ -436,17 +433,17 @@ __device__ __forceinline__ bool closest(const Scene& s, const Ray& r, float tmin
   const uint32_t cap = visit_cap(s);
   for (;;) {
     if (++visits > cap || cur >= s.nNodes) { overflow |= 2u; return any; }
-    uint4 n[5];
-    load_node(s.nodes, cur, n);
+    const uint4* np = reinterpret_cast<const uint4*>(s.nodes + cur);
+    const uint4 hd = __ldg(np);
     float tn[8];
-    const uint32_t hit = node_hits<true>(n, r, tmin, best, tn);
-    const uint32_t imask = n[0].w >> 24;
+    const uint32_t hit = node_hits<true>(np, r, tmin, best, tn);
+    const uint32_t imask = hd.x >> 24, childBase = hd.x & 0xffffffu;
     uint32_t leaves = hit & ~imask;
     while (leaves) {
       const int k = __ffs(leaves) - 1;
       leaves &= leaves - 1;
-      const uint32_t meta = byte_of(k < 4 ? n[1].z : n[1].w, k & 3);
-      const uint32_t first = n[1].y + (meta & 31u), cnt = meta >> 5;
+      const uint32_t meta = byte_of(k < 4 ? hd.z : hd.w, k & 3);
+      const uint32_t first = hd.y + (meta & 31u), cnt = meta >> 5;
       for (uint32_t j = first; j < first + cnt; ++j) {
         F3 v0, v1, v2;
         uint32_t prim, flags, slot;
@@ -470,7 +467,7 @@ __device__ __forceinline__ bool closest(const Scene& s, const Ray& r, float tmin
       const int k = __ffs(inner) - 1;
       inner &= inner - 1;
       if (tn[k] > best) continue;
-      const Entry x{n[1].x + __popc(imask & ((1u << k) - 1u)), tn[k]};
+      const Entry x{childBase + __popc(imask & ((1u << k) - 1u)), tn[k]};
       int b = m - 1;
       while (b >= 0 && ch[b].t < x.t) { ch[b + 1] = ch[b]; --b; }
       ch[b + 1] = x;

@@ -679,11 +679,13 @@ bool autotune(Server& s, std::string& err) {
   const uint32_t nDir = 1024, nSens = 65536;
   std::vector<float> P(3 * nSens), N(3 * nSens), D(3 * nDir), W(nDir, 1.f);
   std::vector<double> out(nSens);
-  // sensors on a horizontal grid over the middle of the scene's first node box, looking up; directions over the sky
-  float p0[3];
-  std::vector<uint32_t> node(20);
-  if (!cuok(cudaMemcpy(node.data(), sc.nodes, 80, cudaMemcpyDeviceToHost), err, "autotune")) return false;
-  std::memcpy(p0, node.data(), 12);
+  // sensors on a horizontal grid over the middle of the scene's root box (its children's lowest x and y), looking up;
+  // directions over the sky
+  float p0[2] = {INFINITY, INFINITY};
+  std::vector<float> node(kNodeWords);
+  if (!cuok(cudaMemcpy(node.data(), sc.nodes, kNodeBytes, cudaMemcpyDeviceToHost), err, "autotune")) return false;
+  for (int k = 0; k < 8; ++k) { p0[0] = std::min(p0[0], node[4 + k]); p0[1] = std::min(p0[1], node[4 + 16 + k]); }
+  if (!std::isfinite(p0[0]) || !std::isfinite(p0[1])) p0[0] = p0[1] = 0.f;
   for (uint32_t i = 0; i < nSens; ++i) {
     P[3 * i] = p0[0] * 0.5f + float(i % 256); P[3 * i + 1] = p0[1] * 0.5f + float(i / 256); P[3 * i + 2] = 1.f;
     N[3 * i] = 0; N[3 * i + 1] = 0; N[3 * i + 2] = 1;
@@ -848,8 +850,14 @@ KGB_API int kgb_server_add_scene(kgb_server* h, const float* v, size_t nv, const
       return 0;
     }
   }
+  if (d.nNodes >= kMaxNodes) {
+    cudaFree(d.nodes);
+    cudaFree(d.tris);
+    set_error("kgb_server_add_scene: 2^24 nodes or more (the node records' child index has 24 bits)");
+    return 0;
+  }
   d.nTris = uint32_t(nt);
-  d.bytes = uint64_t(d.nNodes) * 80 + uint64_t(nt) * 48;
+  d.bytes = uint64_t(d.nNodes) * kNodeBytes + uint64_t(nt) * 48;
   s->used += d.bytes;
   s->scenes.push_back(d);
   *sceneId = int32_t(s->scenes.size() - 1);

@@ -2,7 +2,7 @@
 // kernels walk, on the CPU, decoding the records exactly as kit-sim_daylight_gb300/csrc/rt.cuh does.
 //  - every inner child index < nNodes and every node but the root is some node's child exactly once;
 //  - every leaf's triangle range lies within the records, every triangle record appears exactly once;
-//  - every child box (p + 2^(e-127) q, evaluated in double) contains its subtree's triangles;
+//  - every child box (float planes) contains its subtree's triangles, and every empty slot holds the empty box;
 //  - the depth fits the traversal stacks (48 node groups any-hit, 192 entries closest-hit).
 #include <cmath>
 #include <cstdio>
@@ -19,7 +19,8 @@ extern "C" int bvh_check(const float* v, size_t nv, const uint32_t* tri, size_t 
   const auto bad = [&](const char* what, long a, long c) { std::snprintf(msg, msgLen, "%s (%ld, %ld)", what, a, c); return 1; };
   if (!nt) return b.nNodes == 0 ? 0 : bad("empty scene with nodes", b.nNodes, 0);
   const uint32_t N = b.nNodes, T = uint32_t(b.tris.size() / 12);
-  if (b.nodes.size() != size_t(N) * 20) return bad("node words", long(b.nodes.size()), N);
+  if (b.nodes.size() != size_t(N) * kNodeWords) return bad("node words", long(b.nodes.size()), N);
+  if (N >= kMaxNodes) return bad("node count beyond the 24-bit child index", long(N), 0);
   if (T != nt) return bad("triangle records", T, long(nt));
   std::vector<int> parentSeen(N, 0), triSeen(T, 0), primSeen(nt, 0);
   std::vector<uint32_t> depth(N, 0);
@@ -28,18 +29,20 @@ extern "C" int bvh_check(const float* v, size_t nv, const uint32_t* tri, size_t 
   std::vector<std::vector<uint32_t>> subtreeTris(N);
   // breadth-first order: children have larger indices, so walk from the last node to the first
   for (int64_t w = int64_t(N) - 1; w >= 0; --w) {
-    const uint32_t* r = &b.nodes[size_t(w) * 20];
-    float p[3];
-    std::memcpy(p, r, 12);
-    const uint32_t imask = r[3] >> 24, childBase = r[4], triBase = r[5];
-    double s[3];
-    for (int a = 0; a < 3; ++a) s[a] = std::ldexp(1.0, int((r[3] >> (8 * a)) & 0xffu) - 127);
+    const uint32_t* r = &b.nodes[size_t(w) * kNodeWords];
+    const uint32_t imask = r[0] >> 24, childBase = r[0] & 0xffffffu, triBase = r[1];
     uint32_t innerRank = 0;
     for (int k = 0; k < 8; ++k) {
-      const uint32_t meta = ((k < 4 ? r[6] : r[7]) >> (8 * (k & 3))) & 0xffu;
-      const auto q = [&](int f) { return double((r[8 + 2 * f + (k >> 2)] >> (8 * (k & 3))) & 0xffu); };
+      const uint32_t meta = ((k < 4 ? r[2] : r[3]) >> (8 * (k & 3))) & 0xffu;
+      const auto plane = [&](int f) { float x; std::memcpy(&x, &r[4 + 8 * f + k], 4); return double(x); };   // lo.x hi.x lo.y ..
       double lo[3], hi[3];
-      for (int a = 0; a < 3; ++a) { lo[a] = p[a] + s[a] * q(a); hi[a] = p[a] + s[a] * q(3 + a); }
+      for (int a = 0; a < 3; ++a) { lo[a] = plane(2 * a); hi[a] = plane(2 * a + 1); }
+      const bool empty = !((imask >> k) & 1u) && !meta;
+      if (empty) {
+        for (int a = 0; a < 3; ++a)
+          if (!(std::isinf(lo[a]) && lo[a] > 0 && std::isinf(hi[a]) && hi[a] < 0)) return bad("empty slot with a box", long(w), k);
+        continue;
+      }
       std::vector<uint32_t> under;
       if ((imask >> k) & 1u) {
         const uint32_t c = childBase + innerRank++;
@@ -71,10 +74,10 @@ extern "C" int bvh_check(const float* v, size_t nv, const uint32_t* tri, size_t 
   for (uint32_t c = 1; c < N; ++c) if (parentSeen[c] != 1) return bad("orphan node", long(c), parentSeen[c]);
   for (uint32_t j = 0; j < T; ++j) if (triSeen[j] != 1) return bad("unreferenced triangle record", long(j), 0);
   for (uint32_t w = 0; w < N; ++w) {   // depth, top-down
-    const uint32_t* r = &b.nodes[size_t(w) * 20];
-    const uint32_t imask = r[3] >> 24;
+    const uint32_t* r = &b.nodes[size_t(w) * kNodeWords];
+    const uint32_t imask = r[0] >> 24;
     uint32_t k = 0;
-    for (int c = 0; c < 8; ++c) if ((imask >> c) & 1u) depth[r[4] + k++] = depth[w] + 1;
+    for (int c = 0; c < 8; ++c) if ((imask >> c) & 1u) depth[(r[0] & 0xffffffu) + k++] = depth[w] + 1;
     maxDepth = std::max(maxDepth, depth[w]);
   }
   *depthOut = maxDepth;
