@@ -110,6 +110,16 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def measured_peak(key):
+    """(value, kind) of a MEASURED_PEAKS.json entry, else the fallback figure (bf16 dense burst 1900 TFLOP/s)."""
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        m = json.load(open(p))
+        if key in m:
+            return float(m[key]), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}[key], "fallback"
+
+
 def profiled_traffic():
     """Per-launch DRAM bytes of k_bits from the committed ncu summary (profiles/k_bits_urban.md), if there is one."""
     p = os.path.join(REPO, "profiles", "k_bits_urban.md")
@@ -381,6 +391,7 @@ def run_precision(args, pkg):
         f_ref = open(os.path.join(tmpdir, "ref.npy"), "wb")
         f_ref.write(b"\0" * 128)
         fd_dir = os.open(os.path.join(tmpdir, "direct.npy"), os.O_CREAT | os.O_RDWR | os.O_TRUNC, 0o644)
+    st0 = e.stats()
     t_all = time.perf_counter()
     for i0 in range(0, nc_all, chunk):
         nc = min(chunk, nc_all - i0)
@@ -419,6 +430,13 @@ def run_precision(args, pkg):
                 tt["copy"] += time.perf_counter() - t0
     e.set_series_form(0)
     pipeline_s = time.perf_counter() - t_all - tt["copy"]
+    st1 = e.stats()
+    # roofline of k_series_tc: 6 bf16 products x 2 x Kp flop per output, over the kernels' CUDA-event time (every
+    # tensor-core series call of the run, the file-writing ones included)
+    Kp = (P + 1 + (P + 1) + 63) // 64 * 64
+    series_ms = st1["seriesMs"] - st0["seriesMs"]
+    series_flop = (st1["seriesOutputs"] - st0["seriesOutputs"]) * 12 * Kp
+    tc_peak = measured_peak("bf16_tflops")
     series_file = {"skipped": "less than twice the file's size free in %s" % tmpdir}
     if files:
         f_ref.close()
@@ -461,7 +479,11 @@ def run_precision(args, pkg):
             "config": {"workload": "precision: urban block, %d sensors, %d patches + ground, %d directions, %d series columns (non-night hours), "
                                    "20%% glass tau 0.64 (byte mode), 1 bounce x %d paths (%d reflected-light bins in K), chunks of %d sensors"
                                    % (nc_all, P, len(D), T, M, P + 1, chunk)},
-            "dtype": "split-bf16 (3 pieces, 6 products) on tcgen05, fp32 accumulate per 64-K chunk, chunks Kahan-summed; sun term fp32",
+            "dtype": "split-bf16 (3 pieces, 6 products) on tcgen05, fp32 accumulate in chains of 64 of K, added per 128 of K with Kahan compensation; sun term fp32",
+            "roofline": {"bound": "tensor", "kernel": "k_series_tc", "achieved": series_flop / (series_ms / 1000) / 1e12 if series_ms else None,
+                         "peak": tc_peak[0], "unit": "TFLOP/s", "peak_kind": tc_peak[1] + " bf16 burst",
+                         "frac": series_flop / (series_ms / 1000) / 1e12 / tc_peak[0] if series_ms else None, "traffic": None,
+                         "flop_per_output": 12 * Kp, "kernel_ms": series_ms},
             "column_error_vs_fp64": {"max": float(ce.max()), "p99": float(np.percentile(ce, 99)), "median": float(np.median(ce)),
                                      "columns_over_1e-6": int((ce > 1e-6).sum()), "columns": int(ce.size), "sample_sensors": len(sub)},
             "fp32_column_error_vs_fp64": {"max": float(ce32.max()), "median": float(np.median(ce32))},

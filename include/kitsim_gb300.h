@@ -74,6 +74,8 @@ typedef struct kgb_stats {
   double buildMs, traceMs, bounceMs;
   uint64_t rays, gasBytes, launches, paths, bounceLaunches;
   uint64_t buildTempBytes, buildOutputBytes;
+  double seriesMs;          /* device time of the tensor-core series kernels (CUDA events), summed over calls */
+  uint64_t seriesOutputs;   /* outputs those kernels wrote (sensors x steps), summed */
 } kgb_stats;
 
 /* Cancel hook: returns non-zero once the run should stop (the reference's const std::atomic<bool>*). */

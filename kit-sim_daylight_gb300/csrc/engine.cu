@@ -659,12 +659,14 @@ static int series_impl(Engine& g, size_t nc, const kgb_series_in* in, const Sink
     // the copies after this call's uploads, which used the same staging slices)
     const uint32_t mAll = uint32_t((nc + 127) / 128), bands = mAll >= 8 * kSeriesBands ? kSeriesBands : 1, per = (mAll + bands - 1) / bands;
     if (!g.copySt) CU(cudaStreamCreateWithFlags(&g.copySt, cudaStreamNonBlocking));
+    CU(cudaEventRecord(g.ev[0], g.st));
     for (uint32_t b = 0; b < bands; ++b) {
       if (!g.bandEv[b]) CU(cudaEventCreateWithFlags(&g.bandEv[b], cudaEventDisableTiming));
       if (const char* why = series_tc_rows(p, b * per, std::min(per, mAll - b * per), g.st)) return fail(why);
       CU(cudaGetLastError());
       CU(cudaEventRecord(g.bandEv[b], g.st));
     }
+    CU(cudaEventRecord(g.ev[1], g.st));
     // E straight into the caller's rows where they can be page-locked (registered while the first band runs)
     HostLock lock(out.fd < 0 ? out.dst : nullptr, nc * T * 4, false, g.copySt, g.st);
     Sink sink = out;
@@ -678,6 +680,8 @@ static int series_impl(Engine& g, size_t nc, const kgb_series_in* in, const Sink
     CU(cudaMemcpyAsync(&status, static_cast<uint32_t*>(g.ctl.p) + 1, 4, cudaMemcpyDeviceToHost, g.st));
     CU(cudaStreamSynchronize(g.st));
     if (status & kStatusTimeout) return fail("gpu_series: the tensor-core pipeline timed out waiting (status recorded by the kernel)");
+    g.stats.seriesMs += elapsed(g);
+    g.stats.seriesOutputs += uint64_t(nc) * T;
     return 1;
   }
   HostLock lock(out.fd < 0 ? out.dst : nullptr, nc * T * 4, false, g.st);

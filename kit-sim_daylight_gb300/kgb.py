@@ -26,7 +26,7 @@ class SceneHandle(ctypes.Structure):
 class Stats(ctypes.Structure):
     _fields_ = [("buildMs", c_double), ("traceMs", c_double), ("bounceMs", c_double), ("rays", c_uint64), ("gasBytes", c_uint64),
                 ("launches", c_uint64), ("paths", c_uint64), ("bounceLaunches", c_uint64), ("buildTempBytes", c_uint64),
-                ("buildOutputBytes", c_uint64)]
+                ("buildOutputBytes", c_uint64), ("seriesMs", c_double), ("seriesOutputs", c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
