@@ -117,7 +117,7 @@ def measured_peak(key):
         m = json.load(open(p))
         if key in m:
             return float(m[key]), "measured"
-    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}[key], "fallback"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}[key], "fallback"
 
 
 def profiled_traffic():
@@ -436,7 +436,7 @@ def run_precision(args, pkg):
     Kp = (P + 1 + (P + 1) + 63) // 64 * 64
     series_ms = st1["seriesMs"] - st0["seriesMs"]
     series_flop = (st1["seriesOutputs"] - st0["seriesOutputs"]) * 12 * Kp
-    tc_peak = measured_peak("bf16_tflops")
+    tc_peak = measured_peak("bf16_tflops_sustained")   # the kernels run inside a pipeline of seconds
     series_file = {"skipped": "less than twice the file's size free in %s" % tmpdir}
     if files:
         f_ref.close()
@@ -481,7 +481,7 @@ def run_precision(args, pkg):
                                    % (nc_all, P, len(D), T, M, P + 1, chunk)},
             "dtype": "split-bf16 (3 pieces, 6 products) on tcgen05, fp32 accumulate in chains of 64 of K, added per 128 of K with Kahan compensation; sun term fp32",
             "roofline": {"bound": "tensor", "kernel": "k_series_tc", "achieved": series_flop / (series_ms / 1000) / 1e12 if series_ms else None,
-                         "peak": tc_peak[0], "unit": "TFLOP/s", "peak_kind": tc_peak[1] + " bf16 burst",
+                         "peak": tc_peak[0], "unit": "TFLOP/s", "peak_kind": tc_peak[1] + " bf16 sustained",
                          "frac": series_flop / (series_ms / 1000) / 1e12 / tc_peak[0] if series_ms else None, "traffic": None,
                          "flop_per_output": 12 * Kp, "kernel_ms": series_ms},
             "column_error_vs_fp64": {"max": float(ce.max()), "p99": float(np.percentile(ce, 99)), "median": float(np.median(ce)),
