@@ -10,32 +10,33 @@
 //  - each FP32 operand is split x = hi + mid + lo exactly into three bf16 pieces (24 significant bits), and six
 //    products run per K step: hi.hi, then the corrections hi.mid + mid.hi + hi.lo + mid.mid + lo.hi (the dropped
 //    mid.lo, lo.mid, lo.lo are 2^-24 of the product and below);
-//  - the tensor core's FP32 accumulation truncates, so a long accumulation chain drifts low by about a quarter ulp per
-//    instruction (1e-5 over 2305 patches). The hi.hi chains are therefore short: each 64 of K goes into a TMEM
-//    accumulator from zero (4 MMAs), and per 128 of K (a chunk: two such sums) the epilogue adds the chunk's sum into
-//    FP32 registers with Kahan compensation. (One chain of 8 MMAs a chunk doubled the drift: the column error went
-//    from 4e-7 to 7e-7 of the column's maximum.) The five corrections are 2^-8 of the result or less: their chain runs over the whole tile in a
-//    second accumulator (its drift, about 1e-7 of the result at K 4672, stays well inside the 1e-6 bound), which the
-//    epilogue reads once per tile;
+//  - the tensor core's FP32 accumulation truncates, so a long accumulation chain drifts low by about half an ulp of
+//    the chain's magnitude per instruction (1e-5 over 2305 patches as one chain). The chains are therefore short: each
+//    64 of K (a chunk) accumulates from zero in TMEM (4 K steps), and the epilogue adds the chunk's sum into FP32
+//    registers with Kahan compensation (chains of 8 K steps doubled the column error, 4e-7 to 7e-7 of the column's
+//    maximum);
 //  - the sun term (one direction per step, exact in the reference's float arithmetic) is added in the epilogue, where
 //    each output is finished in registers and stored with 16-byte row stores.
+//
+// The six products take three MMAs per K step: the three S pieces are consecutive tiles in shared memory, so one B
+// operand of N 192 is [S hi | S mid | S lo], and a chunk's accumulator [H | C1 | C2] (3 x 64 columns) receives
+//    hi  x [hi | mid | lo]   (N 192, into H C1 C2)
+//    mid x [hi | mid]        (N 128, into C1 C2)
+//    lo  x [hi]              (N 64, into C2)
+// so H = hi.hi, C1 = hi.mid + mid.hi, C2 = hi.lo + mid.mid + lo.hi, and the epilogue adds H + (C1 + C2) per chunk.
+// An M 128 K 16 MMA costs about 29 cycles (its A operand's read from shared memory) plus 0.66 a column: six of N 64
+// take some 426 cycles a K step, these three 340 (7.6 to 6.85 ms a 29,609-sensor chunk).
 //
 // Kernel k_series_tc, one CTA per SM, persistent over 128 x 64 output tiles (sensors x steps) in bands of 16 step-tiles
 // (tile_coords), so that the CTAs running at once share a few V panels and the band's S panels in L2:
 //   warp 0      TMA producer: per 64-wide K block, the three pieces of V (128 x 64) and of S (64 x 64), bf16,
 //               128-byte swizzled, into a 3-stage shared-memory ring (72 KB a stage)
-//   warp 1      MMA issuer (one thread): 24 tcgen05.mma (M 128, N 64, K 16) per stage: hi.hi into H[chunk % 3] (two
-//               accumulators, one per K block of the chunk), the corrections into C[tile % 2] (TMEM: 3 x 2 + 2
-//               accumulators of 64 columns, the whole 512); tcgen05.commit frees the stage,
-//               hands a finished chunk's hi.hi and a finished tile's corrections to the epilogue
+//   warp 1      MMA issuer (one thread): 12 tcgen05.mma per stage (M 128, K 16; N 192, 128, 64) into the chunk's
+//               accumulator [H | C1 | C2] (two of them, at TMEM columns 0 and 256); tcgen05.commit frees the stage and
+//               hands the finished chunk to the epilogue
 //   warps 2-5   epilogue, one per TMEM lane quarter (warp w reads lanes 32 (w % 4) ..), a thread per output row: per
-//               chunk, tcgen05.ld of H added into the row's 64 Kahan-compensated FP32 sums (128 registers); per tile,
-//               the corrections, the sun term, and the row of E stored 16 bytes at a time
-// (The corrections were first summed per chunk beside hi.hi: the epilogue then spent more time per chunk, 8 TMEM loads
-// and 128 compensated adds a thread, than the chunk's 24 MMAs, and the tensor pipe waited on it. Chunks of 64 of K with
-// two hi.hi accumulators took 12 % longer than chunks of 128 with four buffers: each chunk is a round trip MMA ->
-// epilogue -> MMA. The MMA itself bounds the rest: an M 128 N 64 K 16 instruction takes about 71 cycles, some 29 of them the A
-// operand's read, so the tensor pipe stays near half busy at this tile width.)
+//               chunk, tcgen05.ld of H, C1, C2 (one wait), H + (C1 + C2) added into the row's 64 Kahan-compensated FP32
+//               sums (128 registers); per tile, the sun term and the row of E stored 16 bytes at a time
 // The 64-column tile keeps the Kahan sums in registers: six warps per CTA leave a scheduler at most two warps, so a
 // thread may hold up to 255 registers (the register file is split between the SM's four schedulers).
 // Every wait on an mbarrier is bounded: past the limit the kernel records kStatusTimeout and leaves its loops (the
@@ -51,18 +52,17 @@
 namespace kgb {
 
 constexpr int BM = 128, BN = 64, BK = 64, STAGES = 3, PIECES = 3;
-constexpr int CHUNK_BLOCKS = 2;                      // K blocks (of BK) per accumulation chunk, each block's 4 hi.hi MMAs
-                                                     // in an accumulator of its own
-constexpr uint32_t NH = 3;                           // chunk buffers: the MMA issuer runs up to 2 chunks ahead
+constexpr uint32_t NH = 2;                           // chunk accumulators [H | C1 | C2]: the MMA issuer runs a chunk ahead
 constexpr int V_TILE = BM * BK * 2;                  // 16 KB: one bf16 V tile (128 rows x 128 B)
 constexpr int S_TILE = BN * BK * 2;                  // 8 KB: one bf16 S^T tile (64 rows x 128 B)
 constexpr int STAGE_BYTES = PIECES * (V_TILE + S_TILE); // V hi mid lo, S hi mid lo
 constexpr int EPI_WARPS = 4;                        // one per TMEM lane quarter, the tile's 64 columns each
 constexpr int THREADS = 32 * (2 + EPI_WARPS);
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /* align */ + 256 /* barriers */;
-static_assert((2 * STAGES + 2 * NH + 4) * 8 + 4 <= 256, "the barriers and the TMEM slot fit their 256 bytes");
-constexpr uint32_t TMEM_COLS = NH * CHUNK_BLOCKS * BN + 2 * BN;   // H0..H2 (a chunk's two hi.hi blocks each), C0 C1
-static_assert(TMEM_COLS == 512, "a power of two of TMEM columns");
+static_assert((2 * STAGES + 2 * NH) * 8 + 4 <= 256, "the barriers and the TMEM slot fit their 256 bytes");
+constexpr uint32_t TMEM_COLS = 512;
+constexpr uint32_t kChunkCols = 256;                 // chunk accumulator b at column 256 b: [H | C1 | C2] in 3 x BN of them
+static_assert(3 * BN <= kChunkCols && NH * kChunkCols <= TMEM_COLS, "the chunk accumulators fit TMEM");
 constexpr uint64_t kWaitLimitNs = 4000000000ull;   // 4 s: no wait of a healthy run comes near it
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
@@ -107,41 +107,36 @@ __device__ __forceinline__ uint64_t smem_desc(const void* tile) {
   const uint64_t a = smem_u32(tile);
   return ((a >> 4) & 0x3FFFull) | (uint64_t(1024 >> 4) << 32) | (uint64_t(1) << 46) | (uint64_t(2) << 61);
 }
-// kind::f16 instruction descriptor: D f32, A and B bf16, both K-major, N = BN, M = BM.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(BN >> 3) << 17) | (uint32_t(BM >> 4) << 24);
+// kind::f16 instruction descriptor: D f32, A and B bf16, both K-major, M = BM, N as given.
+constexpr uint32_t idesc(uint32_t n) { return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | (uint32_t(BM >> 4) << 24); }
 
+template <uint32_t N>
 __device__ __forceinline__ void mma_bf16(uint32_t dTmem, uint64_t aDesc, uint64_t bDesc, uint32_t accumulate) {
+  static_assert(N % 16 == 0 && N >= 16 && N <= 256, "M 128 takes N in 16 .. 256, a multiple of 16");
   asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-               ::"r"(dTmem), "l"(aDesc), "l"(bDesc), "r"(kIdesc), "r"(accumulate));
+               ::"r"(dTmem), "l"(aDesc), "l"(bDesc), "r"(idesc(N)), "r"(accumulate));
 }
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
-  uint32_t r[32];
+// Columns [c, c + 16) of three accumulators (TMEM addresses h, c1, c2) for this warp's 32 lanes, one wait for all.
+__device__ __forceinline__ void tmem_ld16x3(uint32_t h, uint32_t c1, uint32_t c2, float* vh, float* v1, float* v2) {
+  uint32_t a[16], b[16], c[16];
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,"
-      "%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]),
-        "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
-        "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
-        "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%48];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%49];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47}, [%50];\n"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(a[0]), "=r"(a[1]), "=r"(a[2]), "=r"(a[3]), "=r"(a[4]), "=r"(a[5]), "=r"(a[6]), "=r"(a[7]), "=r"(a[8]), "=r"(a[9]), "=r"(a[10]),
+        "=r"(a[11]), "=r"(a[12]), "=r"(a[13]), "=r"(a[14]), "=r"(a[15]),
+        "=r"(b[0]), "=r"(b[1]), "=r"(b[2]), "=r"(b[3]), "=r"(b[4]), "=r"(b[5]), "=r"(b[6]), "=r"(b[7]), "=r"(b[8]), "=r"(b[9]), "=r"(b[10]),
+        "=r"(b[11]), "=r"(b[12]), "=r"(b[13]), "=r"(b[14]), "=r"(b[15]),
+        "=r"(c[0]), "=r"(c[1]), "=r"(c[2]), "=r"(c[3]), "=r"(c[4]), "=r"(c[5]), "=r"(c[6]), "=r"(c[7]), "=r"(c[8]), "=r"(c[9]), "=r"(c[10]),
+        "=r"(c[11]), "=r"(c[12]), "=r"(c[13]), "=r"(c[14]), "=r"(c[15])
+      : "r"(h), "r"(c1), "r"(c2)
+      : "memory");
 #pragma unroll
-  for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
-}
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]),
-        "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+  for (int k = 0; k < 16; ++k) { vh[k] = __uint_as_float(a[k]); v1[k] = __uint_as_float(b[k]); v2[k] = __uint_as_float(c[k]); }
 }
 
 struct SeriesTcArgs {
@@ -184,22 +179,19 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
   uint64_t* full = bars;                 // [STAGES] TMA -> MMA
   uint64_t* empty = bars + STAGES;       // [STAGES] MMA -> TMA
-  uint64_t* hFull = bars + 2 * STAGES;   // [NH] MMA -> epilogue: a chunk's hi.hi sum is complete
+  uint64_t* hFull = bars + 2 * STAGES;   // [NH] MMA -> epilogue: a chunk's sums are complete
   uint64_t* hEmpty = hFull + NH;         // [NH] epilogue -> MMA
-  uint64_t* cFull = hEmpty + NH;         // [2] MMA -> epilogue: a tile's corrections are complete
-  uint64_t* cEmpty = cFull + 2;          // [2] epilogue -> MMA
-  uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(cEmpty + 2);
+  uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(hEmpty + NH);
   __shared__ volatile uint32_t abortFlag;
 
   const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
     for (uint32_t b = 0; b < NH; ++b) { mbar_init(&hFull[b], 1); mbar_init(&hEmpty[b], EPI_WARPS * 32); }
-    for (int b = 0; b < 2; ++b) { mbar_init(&cFull[b], 1); mbar_init(&cEmpty[b], EPI_WARPS * 32); }
     abortFlag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 1) {   // TMEM: NH x CHUNK_BLOCKS + 2 accumulators of BN fp32 columns x 128 lanes
+  if (warp == 1) {   // TMEM: NH chunk accumulators of 3 x BN fp32 columns x 128 lanes
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmemSlot)), "r"(TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
@@ -208,7 +200,6 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmemBase = *tmemSlot;
   const uint32_t kBlocks = a.Kp / BK;
-  const uint32_t nChunks = (kBlocks + CHUNK_BLOCKS - 1) / CHUNK_BLOCKS;
   const uint32_t nTilesAll = a.mTiles * a.nTiles;
 
   if (warp == 0) {
@@ -235,79 +226,58 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
     __syncwarp();
   } else if (warp == 1) {
     if (lane == 0) {   // ---------------- MMA issuer
-      uint32_t stage = 0, phase = 0, chunk = 0, nt = 0;
-      for (uint32_t tile = blockIdx.x; tile < nTilesAll && !abortFlag; tile += gridDim.x, ++nt) {
-        // the tile's corrections into C[nt % 2], from zero at its first K step, over all its chunks
-        const uint32_t cbuf = nt & 1;
-        if (!mbar_wait(&cEmpty[cbuf], ((nt >> 1) & 1) ^ 1, a.status)) { abortFlag = 1; break; }
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t cT = tmemBase + (NH * CHUNK_BLOCKS + cbuf) * BN;
-        uint32_t hT = tmemBase, hbuf = 0;
+      uint32_t stage = 0, phase = 0, chunk = 0;
+      for (uint32_t tile = blockIdx.x; tile < nTilesAll && !abortFlag; tile += gridDim.x) {
         bool ok = true;
-        for (uint32_t kb = 0; kb < kBlocks && ok; ++kb) {
-          const uint32_t kc = kb % CHUNK_BLOCKS;
-          if (kc == 0) {   // a new chunk: its hi.hi into H[buf]
-            hbuf = chunk % NH;
-            if (!mbar_wait(&hEmpty[hbuf], ((chunk / NH) & 1) ^ 1, a.status)) { ok = false; break; }
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          }
-          hT = tmemBase + (hbuf * CHUNK_BLOCKS + kc) * BN;   // the block's own accumulator, from zero
+        for (uint32_t kb = 0; kb < kBlocks; ++kb, ++chunk) {   // a chunk: one K block, its sums from zero in [H | C1 | C2]
+          const uint32_t hbuf = chunk % NH;
+          if (!mbar_wait(&hEmpty[hbuf], ((chunk / NH) & 1) ^ 1, a.status)) { ok = false; break; }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t hT = tmemBase + hbuf * kChunkCols;
           if (!mbar_wait(&full[stage], phase, a.status)) { ok = false; break; }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint8_t* s = smem + stage * STAGE_BYTES;
           const uint64_t v0 = smem_desc(s), v1 = smem_desc(s + V_TILE), v2 = smem_desc(s + 2 * V_TILE);
-          const uint8_t* st = s + PIECES * V_TILE;
-          const uint64_t s0 = smem_desc(st), s1 = smem_desc(st + S_TILE), s2 = smem_desc(st + 2 * S_TILE);
+          const uint64_t sAll = smem_desc(s + PIECES * V_TILE);   // S hi, mid, lo: consecutive tiles, one operand of N 192
 #pragma unroll
           for (int k = 0; k < BK / 16; ++k) {   // 16 bf16 = 32 bytes along K: +2 in the descriptor's address field
             const uint64_t off = uint64_t(2 * k);
-            mma_bf16(hT, v0 + off, s0 + off, k != 0);
-            mma_bf16(cT, v0 + off, s1 + off, (kb | uint32_t(k)) != 0);
-            mma_bf16(cT, v1 + off, s0 + off, 1);
-            mma_bf16(cT, v0 + off, s2 + off, 1);
-            mma_bf16(cT, v1 + off, s1 + off, 1);
-            mma_bf16(cT, v2 + off, s0 + off, 1);
+            mma_bf16<3 * BN>(hT, v0 + off, sAll + off, k != 0);   // hi.hi | hi.mid | hi.lo
+            mma_bf16<2 * BN>(hT + BN, v1 + off, sAll + off, 1);   //         mid.hi | mid.mid
+            mma_bf16<BN>(hT + 2 * BN, v2 + off, sAll + off, 1);   //                  lo.hi
           }
           mma_commit(&empty[stage]);   // the stage is free once these MMAs have read it
+          mma_commit(&hFull[hbuf]);
           if (++stage == STAGES) { stage = 0; phase ^= 1; }
-          if (kc == CHUNK_BLOCKS - 1 || kb == kBlocks - 1) { mma_commit(&hFull[hbuf]); ++chunk; }
         }
         if (!ok) { abortFlag = 1; break; }
-        mma_commit(&cFull[cbuf]);
       }
     }
     __syncwarp();
   } else {   // ---------------- epilogue: warps 2..5
     const uint32_t q = warp & 3;                       // the TMEM lane quarter this warp may read
     const uint32_t laneBase = (q * 32u) << 16;
-    uint32_t chunk = 0, nt = 0;
-    for (uint32_t tile = blockIdx.x; tile < nTilesAll; tile += gridDim.x, ++nt) {
-      // the chunks' hi.hi sums, added with Kahan compensation (acc - cmp is the running sum)
+    uint32_t chunk = 0;
+    for (uint32_t tile = blockIdx.x; tile < nTilesAll; tile += gridDim.x) {
+      // each chunk's H + (C1 + C2), added with Kahan compensation (acc - cmp is the running sum)
       float acc[BN], cmp[BN];
 #pragma unroll
       for (int c = 0; c < BN; ++c) { acc[c] = 0.f; cmp[c] = 0.f; }
       bool ok = true;
-      for (uint32_t ch = 0; ch < nChunks; ++ch, ++chunk) {
+      for (uint32_t ch = 0; ch < kBlocks; ++ch, ++chunk) {
         const uint32_t hbuf = chunk % NH;
         ok = __all_sync(~0u, mbar_wait(&hFull[hbuf], (chunk / NH) & 1, a.status));
         if (!ok || abortFlag) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const bool two = ch * CHUNK_BLOCKS + 1 < kBlocks;   // the last chunk may hold one block
-        const uint32_t hAt = tmemBase + laneBase + hbuf * CHUNK_BLOCKS * BN;
+        const uint32_t hAt = tmemBase + laneBase + hbuf * kChunkCols;
 #pragma unroll
         for (int g = 0; g < BN / 16; ++g) {
-          float v[16];
-          tmem_ld16(hAt + g * 16, v);
-          if (two) {   // the chunk's two block sums first (half an ulp of a chunk sum), then the compensated sum
-            float w[16];
-            tmem_ld16(hAt + BN + g * 16, w);
-#pragma unroll
-            for (int c = 0; c < 16; ++c) v[c] = __fadd_rn(v[c], w[c]);
-          }
+          float v[16], c1[16], c2[16];
+          tmem_ld16x3(hAt + g * 16, hAt + BN + g * 16, hAt + 2 * BN + g * 16, v, c1, c2);
 #pragma unroll
           for (int c = 0; c < 16; ++c) {
             const int j = g * 16 + c;
-            const float y = __fsub_rn(v[c], cmp[j]);
+            const float y = __fsub_rn(__fadd_rn(v[c], __fadd_rn(c1[c], c2[c])), cmp[j]);
             const float t = __fadd_rn(acc[j], y);
             cmp[j] = __fsub_rn(__fsub_rn(t, acc[j]), y);
             acc[j] = t;
@@ -317,9 +287,6 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
         mbar_arrive(&hEmpty[hbuf]);
       }
       if (!ok || abortFlag) { abortFlag = 1; break; }
-      const uint32_t cbuf = nt & 1;   // the tile's corrections, summed in TMEM over all its chunks
-      if (!__all_sync(~0u, mbar_wait(&cFull[cbuf], (nt >> 1) & 1, a.status)) || abortFlag) { abortFlag = 1; break; }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       uint32_t tm, tn;
       tile_coords(tile, a.mTiles, a.nTiles, tm, tn);
       const uint32_t m0 = (tm + a.mBase) * BM, n0 = tn * BN;
@@ -330,11 +297,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
       const bool vec = (a.T & 3u) == 0;                  // 16-byte row stores when rows are 16-byte aligned
 #pragma unroll
       for (int g = 0; g < BN / 16; ++g) {
-        float v[16], corr[16];
-        tmem_ld16(tmemBase + laneBase + (NH * CHUNK_BLOCKS + cbuf) * BN + g * 16, corr);
+        float v[16];
 #pragma unroll
         for (int c = 0; c < 16; ++c) {
-          float x = __fadd_rn(__fsub_rn(acc[g * 16 + c], cmp[g * 16 + c]), corr[c]);
+          float x = __fsub_rn(acc[g * 16 + c], cmp[g * 16 + c]);
           const uint32_t t = n0 + g * 16 + c;
           if (t < a.T && row < a.nc) {
             const int j = __ldg(a.sunOfCol + t);
@@ -359,8 +325,6 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
           }
         }
       }
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      mbar_arrive(&cEmpty[cbuf]);   // the tile's corrections are read: C[cbuf] is free for the tile after next
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
