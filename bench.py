@@ -489,6 +489,8 @@ def run_precision(args, pkg):
             "fp32_column_error_vs_fp64": {"max": float(ce32.max()), "median": float(np.median(ce32))},
             "trace_mrays_s": nc_all * len(D) / tt["trace"] / 1e6, "bounce_mpaths_s": paths / tt["bounce"] / 1e6, "sky_build_s": yr["sky_s"],
             "trace_s": tt["trace"], "bounce_s": tt["bounce"], "series_tc_s": tt["tc"], "series_fp32_s_timed": tt["fp32"],
+            "device_s": {"trace": (st1["traceMs"] - st0["traceMs"]) / 1000, "bounce": (st1["bounceMs"] - st0["bounceMs"]) / 1000,
+                         "series_tc": series_ms / 1000, "bounce_launches": int(st1["bounceLaunches"] - st0["bounceLaunches"])},
             "pipeline_s": pipeline_s - (tt["fp32"] if not args.full_fp32 else 0.0),
             "pipeline_solves_s": nc_all * T / (pipeline_s - (tt["fp32"] if not args.full_fp32 else 0.0)),
             "E_bytes": nc_all * T * 4, "series_file": series_file, "note": "series times include the E download to host memory (pageable, one buffer reused across chunks), as the reference's gpu_series"}

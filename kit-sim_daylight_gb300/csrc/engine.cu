@@ -16,6 +16,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -61,35 +63,72 @@ struct Staging {
 };
 // A caller's host range page-locked for one call (cudaHostRegister), so that its copies run straight between the range
 // and the device: the copy engines move about 190 GB/s over NVLink-C2C to and from page-locked memory, and registering
-// costs about 2 us per MB on a Grace host. Memory the caller page-locked already is used as it is. Where the range
-// cannot be registered (a read-only mapping, a range partly registered already) `direct` stays false and the staged
-// path runs. Before it unregisters the range, the destructor waits for the streams whose copies use it.
+// costs about 2 us per MB on a Grace host. Before it unregisters the range, the destructor waits for the streams whose
+// copies use it. The ranges this library registers are counted in one registry for the process, so that two calls
+// copying the same range at once (two engines reading one input array) share one registration, which ends with the
+// last of them. Memory the caller page-locked (cudaMallocHost, cudaHostRegister) is used as it is. Where the range
+// cannot be registered (a read-only mapping) or overlaps a registration of this library's without matching it,
+// `direct` stays false and the staged path runs.
 constexpr size_t kLockMin = size_t(16) << 20;   // below this a plain copy is as fast as registering first
 static bool page_locked(const void* p) {
   cudaPointerAttributes a{};
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
   return a.type == cudaMemoryTypeHost;
 }
+struct LockRegistry {
+  struct Range { size_t bytes; int refs; };
+  std::mutex m;
+  std::map<const char*, Range> ranges;   // by start address
+  // the registered range overlapping [p, p + n), if any
+  std::map<const char*, Range>::iterator overlap(const char* p, size_t n) {
+    auto it = ranges.upper_bound(p);
+    if (it != ranges.begin()) {
+      auto prev = std::prev(it);
+      if (prev->first + prev->second.bytes > p) return prev;
+    }
+    if (it != ranges.end() && it->first < p + n) return it;
+    return ranges.end();
+  }
+};
+static LockRegistry& lock_registry() {
+  static LockRegistry* r = new LockRegistry;   // never destroyed: engines may outlive static destruction order
+  return *r;
+}
 struct HostLock {
-  void* p = nullptr;
-  bool direct = false, owned = false;
+  const char* p = nullptr;
+  bool direct = false, counted = false;
   cudaStream_t st[2] = {nullptr, nullptr};
-  HostLock(const void* ptr, size_t bytes, bool readOnly, cudaStream_t s0, cudaStream_t s1 = nullptr) : p(const_cast<void*>(ptr)), st{s0, s1} {
+  HostLock(const void* ptr, size_t bytes, bool readOnly, cudaStream_t s0, cudaStream_t s1 = nullptr)
+      : p(static_cast<const char*>(ptr)), st{s0, s1} {
     if (!ptr || bytes < kLockMin) return;
     static const unsigned roFlag = [] {
       int dev = 0, ok = 0;
       return cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&ok, cudaDevAttrHostRegisterReadOnlySupported, dev) == cudaSuccess && ok
                  ? unsigned(cudaHostRegisterReadOnly) : 0u;
     }();
-    const cudaError_t e = cudaHostRegister(p, bytes, readOnly ? roFlag : unsigned(cudaHostRegisterDefault));
-    if (e == cudaSuccess) { direct = owned = true; return; }
+    LockRegistry& R = lock_registry();
+    std::lock_guard<std::mutex> g(R.m);
+    const auto it = R.overlap(p, bytes);
+    if (it != R.ranges.end()) {   // registered by another call of this library: share it if it covers this range
+      if (it->first <= p && p + bytes <= it->first + it->second.bytes) { it->second.refs++; direct = counted = true; }
+      p = counted ? it->first : nullptr;
+      return;
+    }
+    const cudaError_t e = cudaHostRegister(const_cast<char*>(p), bytes, readOnly ? roFlag : unsigned(cudaHostRegisterDefault));
+    if (e == cudaSuccess) { R.ranges[p] = {bytes, 1}; direct = counted = true; return; }
     cudaGetLastError();   // a refused registration leaves no error behind for the next call
-    direct = e == cudaErrorHostMemoryAlreadyRegistered && page_locked(p) && page_locked(static_cast<const char*>(p) + bytes - 1);
+    direct = e == cudaErrorHostMemoryAlreadyRegistered && page_locked(p) && page_locked(p + bytes - 1);   // the caller's
   }
   ~HostLock() {
-    if (!owned) return;
+    if (!counted) return;
     for (cudaStream_t s : st) if (s) cudaStreamSynchronize(s);
-    cudaHostUnregister(p);
+    LockRegistry& R = lock_registry();
+    std::lock_guard<std::mutex> g(R.m);
+    auto it = R.ranges.find(p);
+    if (it != R.ranges.end() && --it->second.refs == 0) {
+      cudaHostUnregister(const_cast<char*>(p));
+      R.ranges.erase(it);
+    }
   }
   HostLock(const HostLock&) = delete;
   HostLock& operator=(const HostLock&) = delete;

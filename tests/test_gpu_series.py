@@ -155,3 +155,57 @@ def test_series_file_matches_series(engine_lib, kgb, pkg, tmp_path):
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
     finally:
         e.close()
+
+
+def test_series_two_engines_share_inputs(engine_lib, kgb, pkg):
+    """Two engines on two threads compute series from the same host arrays at once. The inputs (S of 20 MB) and the
+    outputs (E of 18 MB) are page-locked for each call; the two calls share the registration of S, which ends with
+    the later of them. Each engine's rows equal the rows it computes alone, bit for bit."""
+    import threading
+    s = pkg.workloads.random_city(8, n_boxes=40)
+    P, T, nSun, nc = 2305, 2200, 300, 2000
+    D = pkg.workloads.hemisphere_dirs(P, nSun, 8)
+    engs = [_setup(pkg, kgb, engine_lib, s, D, nc) for _ in range(2)]
+    try:
+        args = _inputs(P, T, nc, D, P, nSun, 6)
+        assert args["S"].nbytes >= 16 << 20 and nc * T * 4 >= 16 << 20
+        alone = [x.series(nc, **args) for x in engs]
+        assert np.array_equal(alone[0], alone[1]) and np.abs(alone[0]).max() > 0
+        out = [np.full((nc, T), np.nan, np.float32) for _ in engs]
+        errs = []
+
+        def work(k):
+            try:
+                for _ in range(3):
+                    engs[k].series(nc, out=out[k], **args)
+            except Exception as ex:   # reported below: an assertion in a thread would not fail the test
+                errs.append(ex)
+        th = [threading.Thread(target=work, args=(k,)) for k in range(2)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        assert not errs, errs
+        for k in range(2):
+            assert np.array_equal(out[k], alone[0])
+    finally:
+        for x in engs:
+            x.close()
+
+
+def test_series_into_caller_pinned_memory(engine_lib, kgb, pkg):
+    """E written into memory the caller page-locked (torch's pinned allocator) is used as it is: the same rows as
+    into pageable memory."""
+    import torch
+    s = pkg.workloads.random_city(8, n_boxes=40)
+    P, T, nSun, nc = 2305, 2200, 300, 2000
+    D = pkg.workloads.hemisphere_dirs(P, nSun, 8)
+    e = _setup(pkg, kgb, engine_lib, s, D, nc)
+    try:
+        args = _inputs(P, T, nc, D, P, nSun, 6)
+        ref = e.series(nc, **args)
+        pinned = torch.empty((nc, T), dtype=torch.float32).pin_memory().numpy()
+        got = e.series(nc, out=pinned, **args)
+        assert np.array_equal(got, ref) and np.array_equal(pinned, ref)
+    finally:
+        e.close()
