@@ -26,6 +26,10 @@
 // so H = hi.hi, C1 = hi.mid + mid.hi, C2 = hi.lo + mid.mid + lo.hi, and the epilogue adds H + (C1 + C2) per chunk.
 // An M 128 K 16 MMA costs about 29 cycles (its A operand's read from shared memory) plus 0.66 a column: six of N 64
 // take some 426 cycles a K step, these three 340 (7.6 to 6.85 ms a 29,609-sensor chunk).
+// With two chunk accumulators the MMA issuer runs one chunk ahead of the epilogue, so the epilogue's work per chunk
+// bounds the kernel once it outlasts the chunk's MMAs: its compensated sums run on packed pairs of columns
+// (add / sub .f32x2, the same roundings as the scalar form), which took a chunk from 6.85 to 5.59 ms (5.31 ms with no
+// per-chunk epilogue work at all).
 //
 // Kernel k_series_tc, one CTA per SM, persistent over 128 x 64 output tiles (sensors x steps) in bands of 16 step-tiles
 // (tile_coords), so that the CTAs running at once share a few V panels and the band's S panels in L2:
@@ -36,7 +40,8 @@
 //               hands the finished chunk to the epilogue
 //   warps 2-5   epilogue, one per TMEM lane quarter (warp w reads lanes 32 (w % 4) ..), a thread per output row: per
 //               chunk, tcgen05.ld of H, C1, C2 (one wait), H + (C1 + C2) added into the row's 64 Kahan-compensated FP32
-//               sums (128 registers); per tile, the sun term and the row of E stored 16 bytes at a time
+//               sums (32 packed pairs each of sum and compensation); per tile, the sun term and the row of E stored 16
+//               bytes at a time
 // The 64-column tile keeps the Kahan sums in registers: six warps per CTA leave a scheduler at most two warps, so a
 // thread may hold up to 255 registers (the register file is split between the SM's four schedulers).
 // Every wait on an mbarrier is bounded: past the limit the kernel records kStatusTimeout and leaves its loops (the
@@ -120,8 +125,7 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 // Columns [c, c + 16) of three accumulators (TMEM addresses h, c1, c2) for this warp's 32 lanes, one wait for all.
-__device__ __forceinline__ void tmem_ld16x3(uint32_t h, uint32_t c1, uint32_t c2, float* vh, float* v1, float* v2) {
-  uint32_t a[16], b[16], c[16];
+__device__ __forceinline__ void tmem_ld16x3(uint32_t h, uint32_t c1, uint32_t c2, uint32_t* a, uint32_t* b, uint32_t* c) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%48];\n"
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%49];\n"
@@ -135,8 +139,24 @@ __device__ __forceinline__ void tmem_ld16x3(uint32_t h, uint32_t c1, uint32_t c2
         "=r"(c[11]), "=r"(c[12]), "=r"(c[13]), "=r"(c[14]), "=r"(c[15])
       : "r"(h), "r"(c1), "r"(c2)
       : "memory");
-#pragma unroll
-  for (int k = 0; k < 16; ++k) { vh[k] = __uint_as_float(a[k]); v1[k] = __uint_as_float(b[k]); v2[k] = __uint_as_float(c[k]); }
+}
+
+// Packed pairs of floats (add / sub .f32x2, sm_100 and later): each half is rounded exactly as the scalar add.rn /
+// sub.rn rounds it, so the compensated sums below equal their scalar form bit for bit, in half the instructions.
+__device__ __forceinline__ unsigned long long f2(uint32_t lo, uint32_t hi) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "r"(lo), "r"(hi));
+  return r;
+}
+__device__ __forceinline__ unsigned long long add2(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ unsigned long long sub2(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
 }
 
 struct SeriesTcArgs {
@@ -259,10 +279,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
     const uint32_t laneBase = (q * 32u) << 16;
     uint32_t chunk = 0;
     for (uint32_t tile = blockIdx.x; tile < nTilesAll; tile += gridDim.x) {
-      // each chunk's H + (C1 + C2), added with Kahan compensation (acc - cmp is the running sum)
-      float acc[BN], cmp[BN];
+      // each chunk's H + (C1 + C2), added with Kahan compensation (acc - cmp is the running sum); columns 2p and 2p + 1
+      // share the packed pair p of acc and cmp
+      unsigned long long acc[BN / 2], cmp[BN / 2];
 #pragma unroll
-      for (int c = 0; c < BN; ++c) { acc[c] = 0.f; cmp[c] = 0.f; }
+      for (int c = 0; c < BN / 2; ++c) { acc[c] = 0ull; cmp[c] = 0ull; }
       bool ok = true;
       for (uint32_t ch = 0; ch < kBlocks; ++ch, ++chunk) {
         const uint32_t hbuf = chunk % NH;
@@ -272,14 +293,14 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
         const uint32_t hAt = tmemBase + laneBase + hbuf * kChunkCols;
 #pragma unroll
         for (int g = 0; g < BN / 16; ++g) {
-          float v[16], c1[16], c2[16];
+          uint32_t v[16], c1[16], c2[16];
           tmem_ld16x3(hAt + g * 16, hAt + BN + g * 16, hAt + 2 * BN + g * 16, v, c1, c2);
 #pragma unroll
-          for (int c = 0; c < 16; ++c) {
-            const int j = g * 16 + c;
-            const float y = __fsub_rn(__fadd_rn(v[c], __fadd_rn(c1[c], c2[c])), cmp[j]);
-            const float t = __fadd_rn(acc[j], y);
-            cmp[j] = __fsub_rn(__fsub_rn(t, acc[j]), y);
+          for (int c = 0; c < 16; c += 2) {
+            const int j = (g * 16 + c) / 2;
+            const unsigned long long y = sub2(add2(f2(v[c], v[c + 1]), add2(f2(c1[c], c1[c + 1]), f2(c2[c], c2[c + 1]))), cmp[j]);
+            const unsigned long long t = add2(acc[j], y);
+            cmp[j] = sub2(sub2(t, acc[j]), y);
             acc[j] = t;
           }
         }
@@ -299,8 +320,13 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
       for (int g = 0; g < BN / 16; ++g) {
         float v[16];
 #pragma unroll
+        for (int c = 0; c < 16; c += 2) {
+          const unsigned long long d = sub2(acc[(g * 16 + c) / 2], cmp[(g * 16 + c) / 2]);
+          v[c] = __uint_as_float(uint32_t(d)); v[c + 1] = __uint_as_float(uint32_t(d >> 32));
+        }
+#pragma unroll
         for (int c = 0; c < 16; ++c) {
-          float x = __fsub_rn(acc[g * 16 + c], cmp[g * 16 + c]);
+          float x = v[c];
           const uint32_t t = n0 + g * 16 + c;
           if (t < a.T && row < a.nc) {
             const int j = __ldg(a.sunOfCol + t);
