@@ -121,6 +121,8 @@ def test_series_bands_equal_chunks(engine_lib, kgb, pkg):
     try:
         args = _inputs(P, T, nc, D, P, nSun, 4)
         whole = e.series(nc, **args)
+        st = e.stats()   # the tensor-core kernels' event time and outputs (the bench's roofline reads them)
+        assert st["seriesMs"] > 0 and st["seriesOutputs"] == nc * T
         parts = []
         for i0, m in ((0, 3000), (3000, 2000)):
             e.trace(i0, m, engine_lib.ray_flags(False, False))
