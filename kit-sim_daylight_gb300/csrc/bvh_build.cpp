@@ -168,6 +168,7 @@ void build_bvh8(const float* v, size_t nv, const uint32_t* tri, size_t nt, const
     }
     rec[0] = childBase | (imask << 24);   // fewer than 2^24 nodes: the engine checks the triangle count first
     rec[1] = triBase;
+    for (int b = 0; b < 3; ++b) meta[b] |= ((uint32_t(n - 1) >> b) & 1u) << 7;   // the slot count (n >= 1), on slots in use
     rec[2] = meta[0] | (meta[1] << 8) | (meta[2] << 16) | (meta[3] << 24);
     rec[3] = meta[4] | (meta[5] << 8) | (meta[6] << 16) | (meta[7] << 24);
     std::memcpy(&rec[4], plane, sizeof plane);   // n1 n2 lo.x, n3 n4 hi.x, n5 n6 lo.y, ...

@@ -436,6 +436,7 @@ __global__ void k_collapse_emit(Tree T, Dp D, const float* v, const uint32_t* tr
   }
   rec[0] = childBase | (imask << 24);   // fewer than 2^24 nodes: the engine checks the triangle count first
   rec[1] = triBase;
+  for (int b = 0; b < 3; ++b) meta[b] |= ((uint32_t(n - 1) >> b) & 1u) << 7;   // slots up to the last child (n >= 1), on slots in use
   rec[2] = meta[0] | (meta[1] << 8) | (meta[2] << 16) | (meta[3] << 24);
   rec[3] = meta[4] | (meta[5] << 8) | (meta[6] << 16) | (meta[7] << 24);
 }

@@ -19,7 +19,9 @@ namespace kgb {
 // BVH8 node, 208 bytes = 13 x 16 B:
 //   n0: childBase | imask << 24 (childBase: index of the node's first inner child, below 2^24; its inner children are
 //       consecutive in slot order; imask bit k: child k is an inner node), triBase (index of the node's first
-//       triangle record), meta[8] (leaf child k: count << 5 | offset of its triangles from triBase; 0: empty slot)
+//       triangle record), meta[8] (leaf child k: count << 5 | offset of its triangles from triBase, below 128; 0: empty
+//       slot); bit 7 of meta[0], meta[1], meta[2] holds bit 0, 1, 2 of slots - 1 (slots: 1 + the last slot in use, so
+//       these bits fall on slots in use only)
 //   n1 n2: lo.x of children 0..3, 4..7 (float)   n3 n4: hi.x
 //   n5 n6: lo.y                                  n7 n8: hi.y
 //   n9 n10: lo.z                                 n11 n12: hi.z
@@ -290,8 +292,17 @@ __device__ __forceinline__ unsigned long long pku(uint32_t a, uint32_t b) {
 // child slots (lo +inf, hi -inf) fail the test; a leaf slot without triangles that passes tests nothing.
 // CLIP: the exit is also clipped at tmax (closest hit, where tmax shrinks to the best hit). Without it boxes beyond
 // tmax pass as well, which is conservative: the triangle test applies tmax (the any-hit walks run to infinity).
-template <bool CLIP = true>
-__device__ __forceinline__ uint32_t node_hits(const uint4* p, const Ray& r, float tmin, float tmax, float* tn) {
+// 1 + the node's last slot in use, from bit 7 of its first three meta bytes (the word of meta[0..3]).
+__device__ __forceinline__ uint32_t node_slots(uint32_t meta03) {
+  return 1u + (((meta03 >> 7) & 1u) | ((meta03 >> 14) & 2u) | ((meta03 >> 21) & 4u));
+}
+
+// SKIP: slots past the node's last child (empty boxes, which fail the test anyway) are neither read nor tested. The
+// byte-mode trace and the bounce's walks run faster with it (10.5 against 9.8 G rays/s, 1283 against 1200 M paths/s);
+// the visibility bits' walk and the views' closest hits run slower (the extra branches cost more than the tests they
+// save: 64.9 against 61.0 ms for the urban trace), so those test every slot.
+template <bool CLIP = true, bool SKIP = false>
+__device__ __forceinline__ uint32_t node_hits(const uint4* p, const Ray& r, float tmin, float tmax, uint32_t slots, float* tn) {
   const unsigned long long IX = pk2(r.inv.x, r.inv.x), IY = pk2(r.inv.y, r.inv.y), IZ = pk2(r.inv.z, r.inv.z);
   const unsigned long long OX = pk2(-r.oinv.x, -r.oinv.x), OY = pk2(-r.oinv.y, -r.oinv.y), OZ = pk2(-r.oinv.z, -r.oinv.z);
   const unsigned long long WIDEN = pk2(1.00000095367431640625f, 1.00000095367431640625f);
@@ -299,12 +310,14 @@ __device__ __forceinline__ uint32_t node_hits(const uint4* p, const Ray& r, floa
   uint32_t mask = 0;
 #pragma unroll
   for (int h = 0; h < 2; ++h) {   // children 4h .. 4h + 3: the second vector of each plane set
+    if (SKIP && 4 * h >= int(slots)) break;
     const uint4 nx = __ldg(p + r.nearX + h), fx = __ldg(p + fX + h);
     const uint4 ny = __ldg(p + r.nearY + h), fy = __ldg(p + fY + h);
     const uint4 nz = __ldg(p + r.nearZ + h), fz = __ldg(p + fZ + h);
 #pragma unroll
     for (int j = 0; j < 2; ++j) {   // the pair 4h + 2j, 4h + 2j + 1
       const int k = 4 * h + 2 * j;
+      if (SKIP && k >= int(slots)) break;
       float tnx[2], tny[2], tnz[2], tfx[2], tfy[2], tfz[2];
       up2(fma2(j ? pku(nx.z, nx.w) : pku(nx.x, nx.y), IX, OX), tnx[0], tnx[1]);
       up2(fma2(j ? pku(fx.z, fx.w) : pku(fx.x, fx.y), IX, OX), tfx[0], tfx[1]);
@@ -363,7 +376,7 @@ struct Count {
 };
 
 // Visit every triangle hit in [tmin, tmax] (any order); f(hit, v0, v1, v2, flags, slot) returns true to stop.
-template <bool COUNT = false, class Fn>
+template <bool COUNT = false, bool SKIP = false, class Fn>
 __device__ __forceinline__ void for_hits(const Scene& s, const Ray& r, float tmin, float tmax, bool cull, Fn&& f, uint32_t& overflow,
                                          Count* ctr = nullptr) {
   if (!s.nNodes) return;
@@ -377,14 +390,14 @@ __device__ __forceinline__ void for_hits(const Scene& s, const Ray& r, float tmi
     const uint4 hd = __ldg(np);
     if (COUNT) ctr->nodes++;
     float tn[8];
-    const uint32_t hit = node_hits<false>(np, r, tmin, tmax, tn);
+    const uint32_t hit = node_hits<false, SKIP>(np, r, tmin, tmax, SKIP ? node_slots(hd.z) : 8u, tn);
     const uint32_t imask = hd.x >> 24, childBase = hd.x & 0xffffffu;
     uint32_t leaves = hit & ~imask;
     while (leaves) {
       const int k = __ffs(leaves) - 1;
       leaves &= leaves - 1;
       const uint32_t meta = byte_of(k < 4 ? hd.z : hd.w, k & 3);
-      const uint32_t first = hd.y + (meta & 31u), cnt = meta >> 5;
+      const uint32_t first = hd.y + (meta & 31u), cnt = (meta >> 5) & 3u;
       for (uint32_t j = first; j < first + cnt; ++j) {
         F3 v0, v1, v2;
         uint32_t prim, flags, slot;
@@ -422,6 +435,7 @@ __device__ __forceinline__ void for_hits(const Scene& s, const Ray& r, float tmi
 // nearest inner child next, the others pushed far to near; a node whose entry lies beyond the best hit so far is
 // skipped. The visiting order changes nothing but the work: the result is the closest hit of the whole hit set.
 struct ClosestOut { Hit h; F3 v0, v1, v2; uint32_t flags, slot; };
+template <bool SKIP = false>
 __device__ __forceinline__ bool closest(const Scene& s, const Ray& r, float tmin, float tmax, bool cull, ClosestOut& out, uint32_t& overflow) {
   if (!s.nNodes) return false;
   struct Entry { uint32_t node; float t; };
@@ -436,14 +450,14 @@ __device__ __forceinline__ bool closest(const Scene& s, const Ray& r, float tmin
     const uint4* np = reinterpret_cast<const uint4*>(s.nodes + cur);
     const uint4 hd = __ldg(np);
     float tn[8];
-    const uint32_t hit = node_hits<true>(np, r, tmin, best, tn);
+    const uint32_t hit = node_hits<true, SKIP>(np, r, tmin, best, SKIP ? node_slots(hd.z) : 8u, tn);
     const uint32_t imask = hd.x >> 24, childBase = hd.x & 0xffffffu;
     uint32_t leaves = hit & ~imask;
     while (leaves) {
       const int k = __ffs(leaves) - 1;
       leaves &= leaves - 1;
       const uint32_t meta = byte_of(k < 4 ? hd.z : hd.w, k & 3);
-      const uint32_t first = hd.y + (meta & 31u), cnt = meta >> 5;
+      const uint32_t first = hd.y + (meta & 31u), cnt = (meta >> 5) & 3u;
       for (uint32_t j = first; j < first + cnt; ++j) {
         F3 v0, v1, v2;
         uint32_t prim, flags, slot;

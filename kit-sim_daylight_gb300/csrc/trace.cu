@@ -75,7 +75,7 @@ __device__ uint8_t trace_byte(const Scene& s, const TraceArgs& a, F3 o, F3 n, ui
   int own = 0, nx = 0;
   float ct[kMaxCross], cf[kMaxCross];
   uint32_t cp[kMaxCross];
-  for_hits(s, r, 1e-5f, INFINITY, cull, [&](const Hit& h, F3 v0, F3 v1, F3 v2, uint32_t flags, uint32_t slot) {
+  for_hits<false, true>(s, r, 1e-5f, INFINITY, cull, [&](const Hit& h, F3 v0, F3 v1, F3 v2, uint32_t flags, uint32_t slot) {
     if (own_hit(v0, v1, v2, h, dir, n)) { if (++own <= 3) return false; blocked = true; return true; }
     if (!(flags & kTriTranslucent)) { blocked = true; return true; }
     if (nx < kMaxCross) { ct[nx] = h.t; cp[nx] = h.prim; cf[nx] = crossing(a.slots, a.slotLog, a.nSlots, slot, h.front, v0, v1, v2, dir); ++nx; }
@@ -105,7 +105,7 @@ __device__ uint8_t trace_byte(const Scene& s, const TraceArgs& a, F3 o, F3 n, ui
     bool found = false;
     float bt = 0.f, bf = 0.f;
     uint32_t bp = 0;
-    for_hits(s, r, 1e-5f, INFINITY, cull, [&](const Hit& h, F3 v0, F3 v1, F3 v2, uint32_t flags, uint32_t slot) {
+    for_hits<false, true>(s, r, 1e-5f, INFINITY, cull, [&](const Hit& h, F3 v0, F3 v1, F3 v2, uint32_t flags, uint32_t slot) {
       if (!(flags & kTriTranslucent) || own_hit(v0, v1, v2, h, dir, n)) return false;
       if (h.t < lastT || (h.t == lastT && h.prim <= lastP)) return false;
       if (!found || h.t < bt || (h.t == bt && h.prim < bp)) {
@@ -263,7 +263,7 @@ __device__ __forceinline__ bool bounce_segment(const BounceArgs& a, const Scene&
                                                F3& d, float& w, uint32_t& k, uint32_t& diffuse, bool& reflected, uint32_t& bin, float& gain,
                                                uint32_t& overflow) {
   ClosestOut c;
-  const bool found = closest(s, make_ray(o, d), 1e-5f, FLT_MAX, cull, c, overflow);
+  const bool found = closest<true>(s, make_ray(o, d), 1e-5f, FLT_MAX, cull, c, overflow);
   if (overflow & 2u) {   // the walk gave up: the first such path leaves its ray for the error message
     uint32_t* diag = a.status + 15;   // ctl words 16..
     if (atomicCAS(diag, 0u, 1u) == 0u) {

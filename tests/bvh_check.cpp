@@ -31,13 +31,15 @@ extern "C" int bvh_check(const float* v, size_t nv, const uint32_t* tri, size_t 
   for (int64_t w = int64_t(N) - 1; w >= 0; --w) {
     const uint32_t* r = &b.nodes[size_t(w) * kNodeWords];
     const uint32_t imask = r[0] >> 24, childBase = r[0] & 0xffffffu, triBase = r[1];
+    const uint32_t slots = 1 + (((r[2] >> 7) & 1u) | ((r[2] >> 14) & 2u) | ((r[2] >> 21) & 4u));
     uint32_t innerRank = 0;
     for (int k = 0; k < 8; ++k) {
-      const uint32_t meta = ((k < 4 ? r[2] : r[3]) >> (8 * (k & 3))) & 0xffu;
+      const uint32_t meta = ((k < 4 ? r[2] : r[3]) >> (8 * (k & 3))) & 0x7fu;   // bit 7: the slot count's
       const auto plane = [&](int f) { float x; std::memcpy(&x, &r[4 + 8 * f + k], 4); return double(x); };   // lo.x hi.x lo.y ..
       double lo[3], hi[3];
       for (int a = 0; a < 3; ++a) { lo[a] = plane(2 * a); hi[a] = plane(2 * a + 1); }
       const bool empty = !((imask >> k) & 1u) && !meta;
+      if (!empty && uint32_t(k) >= slots) return bad("a child past the node's slot count", long(w), k);
       if (empty) {
         for (int a = 0; a < 3; ++a)
           if (!(std::isinf(lo[a]) && lo[a] > 0 && std::isinf(hi[a]) && hi[a] < 0)) return bad("empty slot with a box", long(w), k);
