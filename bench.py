@@ -120,12 +120,14 @@ def measured_peak(key):
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}[key], "fallback"
 
 
-def profiled_traffic():
-    """Per-launch DRAM bytes of k_bits from the committed ncu summary (profiles/k_bits_urban.md), if there is one."""
+def profiled(key):
+    """A figure of the committed ncu summary of k_bits on the urban block (profiles/k_bits_urban.md: lines `key: value`),
+    or None: traffic_per_full_trace_bytes (DRAM read + write of one trace), inst_per_full_trace (warp instructions of
+    one trace), thread_inst_per_full_trace (the same counted per active thread)."""
     p = os.path.join(REPO, "profiles", "k_bits_urban.md")
     if os.path.exists(p):
         for line in open(p):
-            if line.startswith("traffic_per_full_trace_bytes:"):
+            if line.startswith(key + ":"):
                 return float(line.split(":")[1])
     return None
 
@@ -146,6 +148,34 @@ def cpu_baseline(pkg, scene, D, Ws, sample, seed=0):
     dt = time.perf_counter() - t0
     o.close()
     return sample * len(D) / dt / 1e6, dt
+
+
+def exact_geometry(pkg, scene, D, sensors=1024, seed=11):
+    """The checker (the oracle, untimed): how many rays of a seeded sample of the block the shared float decision takes
+    differently from every test and rule evaluated in double (oracle kgbo_recheck_bits; categories as in
+    tests/test_grazing.py)."""
+    import ctypes
+    lib = pkg.kgb.Lib(os.path.join(REPO, "oracle", "_build", "liboracle.so"))
+    f = lib.dll.kgbo_recheck_bits
+    f.restype, f.argtypes = ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_uint32, ctypes.c_double, ctypes.c_void_p]
+    o = pkg.kgb.Engine(lib)
+    o.build(scene["v"], scene["tri"])
+    o.set_scene(scene["P"], scene["N"], D)
+    tot = np.zeros(24)
+    t0 = time.perf_counter()
+    for i0 in np.random.default_rng(seed).choice(len(scene["P"]) // 128, sensors // 128, replace=False) * 128:
+        out = np.zeros(24)
+        if not f(o.h, int(i0), 128, lib.ray_flags(False, False), 2.0 ** -16, out.ctypes.data_as(ctypes.c_void_p)):
+            o.close()
+            return {"error": lib.err()}
+        tot[:17] += out[:17]
+        tot[[17, 18]] = np.maximum(tot[[17, 18]], out[[17, 18]])
+    o.close()
+    keys = ["rays", "decided_differently", "edge", "grazing", "threshold", "tie", "rounding", "other"]
+    r = {k: int(x) for k, x in zip(keys, tot[:8])}
+    r.update(edge_band="2^-16 x (|o|max + t)", max_edge_distance_m=float(tot[17]), sample="%d seeded sensors x %d directions" % (sensors, len(D)),
+             seconds=time.perf_counter() - t0)
+    return r
 
 
 def run_reference(args, pkg):
@@ -256,8 +286,10 @@ def run_ours(args, pkg):
     alg = cnt["nodes"] * NODE_BYTES + cnt["tris"] * 48 + nc * ((nDir + 31) // 32) * 4 + tasks * 32 * 24
     ms_trace = float(np.median(ttrace))
     peak, kind = peaks()
-    achieved = alg / (ms_trace / 1000) / 1e9
-    traffic = profiled_traffic()
+    traffic, inst, tinst = profiled("traffic_per_full_trace_bytes"), profiled("inst_per_full_trace"), profiled("thread_inst_per_full_trace")
+    sm_mhz = clk.summary()["sm_mhz"] or 2070.0
+    num_sms = torch.cuda.get_device_properties(local).multi_processor_count
+    issue_peak = 4.0 * num_sms * sm_mhz * 1e6   # four schedulers per SM, one warp instruction each per cycle
     if rank == 0:
         line = {"metric": "Mrays/s", "value": world * rays / (ms / 1000) / 1e6, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -272,78 +304,47 @@ def run_ours(args, pkg):
                         "h2d_bytes_per_step": int(P.nbytes + N.nbytes + Dp.nbytes + sum(W.nbytes for W, _ in Wp)),
                         "d2h_bytes_per_step": int(8 * nc * len(Wp))},
                 "gpu_launches": int(launches),
-                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                             "traffic": traffic, "peak_kind": kind, "kernel": "k_bits",
-                             "algorithmic_bytes_per_trace": alg, "nodes_visited": cnt["nodes"], "tris_tested": cnt["tris"],
-                             "rays_traced": cnt["rays"], "trace_ms": ms_trace, "bvh_bytes": cnt["bvh_bytes"],
-                             "note": "the node and triangle records a ray reads come from L1 / L2 (the tree is %d MB; DRAM moves "
-                                     "`traffic` bytes a trace), so the algorithmic bytes exceed what HBM could deliver: the kernel is "
-                                     "bound by instruction issue, not by HBM" % (cnt["bvh_bytes"] >> 20)},
+                "roofline": {"bound": "issue", "kernel": "k_bits",
+                             "achieved": inst / (ms_trace / 1000) if inst else None, "peak": issue_peak, "unit": "warp-inst/s",
+                             "frac": inst / (ms_trace / 1000) / issue_peak if inst else None,
+                             "peak_kind": "4 issue slots per SM per cycle x %d SMs at the sampled median SM clock (%.0f MHz)" % (num_sms, sm_mhz),
+                             "lanes_active_of_32": tinst / inst if (inst and tinst) else None,
+                             "traffic": traffic, "trace_ms": ms_trace,
+                             "hbm": {"achieved": traffic / (ms_trace / 1000) / 1e9 if traffic else None, "peak": peak, "unit": "GB/s",
+                                     "frac": traffic / (ms_trace / 1000) / 1e9 / peak if traffic else None, "peak_kind": kind,
+                                     "bytes": "traffic: dram__bytes_read.sum + dram__bytes_write.sum of one full trace"},
+                             "cache_bytes": {"per_trace": alg, "per_s": alg / (ms_trace / 1000),
+                                             "what": "node records x 208 B + triangle records x 48 B read by the rays (L1 93 %, L2), "
+                                                     "+ bits out + sensor reads, from the instrumented traversal on the same inputs"},
+                             "nodes_visited": cnt["nodes"], "tris_tested": cnt["tris"], "rays_traced": cnt["rays"], "bvh_bytes": cnt["bvh_bytes"],
+                             "inst_per_trace": inst, "note": "the traversal is bound by instruction issue: its 27 MB tree stays in L2 and "
+                                                             "93 % of its loads hit L1, so HBM is nearly idle (hbm.frac); achieved = warp "
+                                                             "instructions of one trace (ncu, profiles/k_bits_urban.md) / the trace's "
+                                                             "CUDA-event time"},
                 "step_ms": {"device": [float(x) for x in times], "e2e": [float(x) for x in e2e_t]},
                 "clocks": clk.summary()}
         if not args.no_cpu_baseline:
             v, dt = cpu_baseline(pkg, scene, D, Ws, args.cpu_sample)
             line["cpu_baseline"] = {"value": v, "unit": "Mrays/s", "cores": os.cpu_count(), "kind": "port",
                                     "sample": "%d seeded sensors of the block x %d directions + the 4 reduces (%.1f s)" % (args.cpu_sample, nDir, dt)}
-        print(json.dumps(line), flush=True)
+            line["exact_geometry"] = exact_geometry(pkg, scene, D)
     e.close()
+    if rank == 0 and world == 1 and not args.no_extras and not args.sensors:
+        # the other measured configurations, after the timed region: each keeps its own metric and config
+        for key, fn in (("precision", run_precision), ("views", run_views), ("serving", run_serving)):
+            t0 = time.perf_counter()
+            try:
+                line[key] = fn(args, pkg)
+            except Exception as ex:   # the headline stands without them
+                line[key] = {"error": "%s: %s" % (type(ex).__name__, ex)}
+            line[key]["wall_s"] = time.perf_counter() - t0
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
 
 
 # ---------------------------------------------------------------------------------------------- config 3: precision
-KRF, KGF, KBF = 0.265074126, 0.670114631, 0.064811243   # Radiance CIE_rf / gf / bf (bright())
-
-
-def patch_dirs(mf):
-    """Reinhart / Tregenza patch centres (gendaymtx order), float as the reference's make_patches + dir_from_altaz."""
-    tnaz = [30, 30, 24, 24, 18, 12, 6]
-    alpha = (np.pi / 2) / (7 * mf + .5)
-    alt, azi, om = [], [], []
-    for i in range(7 * mf):
-        n = tnaz[i // mf] * mf
-        for j in range(n):
-            alt.append(np.float32(alpha * (i + .5)))
-            azi.append(np.float32(2 * np.pi * j / n))
-            om.append(np.float32(2 * np.pi * (np.sin(alpha * (i + 1)) - np.sin(alpha * i)) / n))
-    alt.append(np.float32(np.pi / 2)); azi.append(np.float32(0)); om.append(np.float32(2 * np.pi * (1 - np.cos(alpha * .5))))
-    a, z = np.array(alt, np.float64), np.array(azi, np.float64)
-    D = np.stack([np.cos(a) * np.sin(z), np.cos(a) * np.cos(z), np.sin(a)], axis=1).astype(np.float32)
-    return D, np.array(om, np.float32)
-
-
-def urban_year_sky(e, mf):
-    """The urban weather year's series operands on the GPU: NOAA sun per hour (kgb_sun_noaa) and the Perez sky per
-    hour and patch (kgb_sky, FP64), as the reference's run.cpp builds them on the host (physical mode, radiometric)."""
-    w = np.load(os.path.join(GOLDEN, "urban_sky", "weather.npy")).astype(np.float64)   # [2, 8760] DNI, DHI
-    dim = [31, 28, 31, 30, 31, 30, 31, 31, 30, 31, 30, 31]
-    month = np.repeat(np.arange(1, 13), [24 * d for d in dim])
-    day = np.concatenate([np.repeat(np.arange(1, d + 1), 24) for d in dim])
-    hour = np.tile(np.arange(24) + 0.5, 365)
-    jd = np.repeat(np.arange(1, 366), 24)
-    rows = np.stack([np.full(8760, 52.52), np.full(8760, 13.41), np.full(8760, 1.0), month, day, hour, np.zeros(8760)], axis=1)
-    t0 = time.perf_counter()
-    sun = e.sun_noaa(rows)
-    steps = np.stack([jd, np.radians(sun[:, 0]), np.radians(sun[:, 1]), w[0], w[1]], axis=1)
-    sky = e.sky(mf, steps, grefl=0.2, sun=False, sky=True, visible=False)
-    sunbin = e.sky(mf, steps, grefl=0.2, sun=True, sky=False, visible=False)   # the sun as gendaymtx bins it (AddDirect)
-    sky_s = time.perf_counter() - t0
-    bright = KRF * sky[:, :, 0] + KGF * sky[:, :, 1] + KBF * sky[:, :, 2]
-    bright_sun = KRF * sunbin[:, :, 0] + KGF * sunbin[:, :, 1] + KBF * sunbin[:, :, 2]
-    col = (w[0] + w[1]) > 1e-4
-    colOf = np.cumsum(col) - 1
-    S = np.ascontiguousarray(bright[col, 1:].T, np.float32)
-    g = np.ascontiguousarray(bright[col, 0], np.float32)
-    # reflected light (run.cpp:411-419): bin 0 the ground, bin 1 + p the patch radiance plus the binned sun
-    Sdc = np.concatenate([g[None, :], (S.astype(np.float64) + bright_sun[col, 1:].T).astype(np.float32)]).astype(np.float32)
-    up = sun[:, 2] > 0
-    sunVec = sun[up, 3:6].astype(np.float32)
-    ups = np.nonzero(up)[0]
-    sunStep = np.where(col[ups], colOf[ups], 0).astype(np.int32)
-    sunW = np.where(col[ups], w[0][ups], 0).astype(np.float32)
-    return dict(S=S, g=g, Sdc=Sdc, sunVec=sunVec, sunStep=sunStep, sunW=sunW, sky_s=sky_s, T=int(col.sum()))
-
-
 def run_precision(args, pkg):
     """Config 3: the urban block at 2305 patches, 20 % glass (byte mode), one diffuse bounce of 1024 paths per sensor,
     and the hourly series of the non-night hours with reflected light, chunk by chunk as the reference's run() does
@@ -356,9 +357,9 @@ def run_precision(args, pkg):
     lib = pkg.load()
     e = pkg.engine()
     mf, M = 4, 1024
-    Dsky, omega = patch_dirs(mf)
+    Dsky, omega = pkg.workloads.patch_dirs(mf)
     P = len(Dsky)
-    yr = urban_year_sky(e, mf)
+    yr = pkg.workloads.urban_year_sky(e, mf, np.load(os.path.join(GOLDEN, "urban_sky", "weather.npy")))
     D = np.concatenate([Dsky, -Dsky, yr["sunVec"]]).astype(np.float32)
     nSky, sun0 = P, 2 * P
     scene = pkg.workloads.urban_block(glass_share=0.2)
@@ -454,23 +455,31 @@ def run_precision(args, pkg):
                        "direct_gb_s": E_bytes / tt["direct"] / 1e9, "files_identical": same,
                        "note": "reference way: gpu_series into one reused E, then fwrite per chunk; direct: kgb_series_file per chunk"}
     shutil.rmtree(tmpdir, ignore_errors=True)
-    # accuracy: a contiguous 64-sensor range of the first chunk, traced and bounced by the oracle at the same global
-    # indices, its series in FP64 from the same FP32 inputs
-    s0 = int(np.random.default_rng(9).integers(0, min(chunk, nc_all) - 64))
-    sub = np.arange(s0, s0 + 64)
+    # accuracy (the checker, untimed): a contiguous range of the first chunk's sensors, traced and bounced by the oracle
+    # at the same global indices, its series in FP64 from the same FP32 inputs; the error per output column
+    # (max_i |E - E64| / max_i |E64|) and per output (|E - E64| / E64 for outputs at or above 1e-6 of their column's
+    # maximum: every term of the contraction is non-negative, so no output is a cancellation)
+    ns = min(args.accuracy_sensors, min(chunk, nc_all))
+    s0 = int(np.random.default_rng(9).integers(0, min(chunk, nc_all) - ns + 1))
+    sub = np.arange(s0, s0 + ns)
     subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle"), "all"])
     o = kgb.Engine(kgb.Lib(os.path.join(REPO, "oracle", "_build", "liboracle.so")))
     o.build(scene["v"], scene["tri"], scene["slot"], slots, per_slot=True)
     o.set_slots(slots)
     o.set_scene(scene["P"], scene["N"], D)
-    o.trace(s0, 64, flags)
-    o.bounce(s0, 64, bflags, N=1, M=M, mf=mf, north=0.0)
-    E64 = o.series(64, G=first[1][sub], **sargs)
+    o.trace(s0, ns, flags)
+    o.bounce(s0, ns, bflags, N=1, M=M, mf=mf, north=0.0)
+    E64 = o.series(ns, G=first[1][sub], **sargs).astype(np.float64)
     o.close()
+    cmax = np.abs(E64).max(axis=0)
+    live = cmax > 0
+    mask = (E64 > 0) & (E64 >= 1e-6 * cmax[None, :])
     def colerr(E):
-        cmax = np.abs(E64).max(axis=0)
-        live = cmax > 0
         return np.abs(E[sub] - E64).max(axis=0)[live] / cmax[live]
+    def elemerr(E):
+        rel = np.abs(E[sub].astype(np.float64) - E64)[mask] / E64[mask]
+        return {"max": float(rel.max()), "p99": float(np.percentile(rel, 99)), "median": float(np.median(rel)), "outputs": int(mask.sum()),
+                "floor": "E64 >= 1e-6 x its column's maximum"}
     ce, ce32 = colerr(first[0]), colerr(fp32_first)
     n_fp32 = nc_all if args.full_fp32 else min(chunk, nc_all)
     paths = nc_all * M
@@ -486,7 +495,9 @@ def run_precision(args, pkg):
                          "flop_per_output": 12 * Kp, "kernel_ms": series_ms},
             "column_error_vs_fp64": {"max": float(ce.max()), "p99": float(np.percentile(ce, 99)), "median": float(np.median(ce)),
                                      "columns_over_1e-6": int((ce > 1e-6).sum()), "columns": int(ce.size), "sample_sensors": len(sub)},
+            "element_error_vs_fp64": elemerr(first[0]),
             "fp32_column_error_vs_fp64": {"max": float(ce32.max()), "median": float(np.median(ce32))},
+            "fp32_element_error_vs_fp64": elemerr(fp32_first),
             "trace_mrays_s": nc_all * len(D) / tt["trace"] / 1e6, "bounce_mpaths_s": paths / tt["bounce"] / 1e6, "sky_build_s": yr["sky_s"],
             "trace_s": tt["trace"], "bounce_s": tt["bounce"], "series_tc_s": tt["tc"], "series_fp32_s_timed": tt["fp32"],
             "device_s": {"trace": (st1["traceMs"] - st0["traceMs"]) / 1000, "bounce": (st1["bounceMs"] - st0["bounceMs"]) / 1000,
@@ -494,8 +505,8 @@ def run_precision(args, pkg):
             "pipeline_s": pipeline_s - (tt["fp32"] if not args.full_fp32 else 0.0),
             "pipeline_solves_s": nc_all * T / (pipeline_s - (tt["fp32"] if not args.full_fp32 else 0.0)),
             "E_bytes": nc_all * T * 4, "series_file": series_file, "note": "series times include the E download to host memory (pageable, one buffer reused across chunks), as the reference's gpu_series"}
-    print(json.dumps(line), flush=True)
     e.close()
+    return line
 
 
 # ---------------------------------------------------------------------------------------------- config 4: views
@@ -575,8 +586,8 @@ def run_views(args, pkg):
                                    "(10800 rays, isovist volume, reach 6/20/50), jitter on" % (nc, len(city["tri"]))},
             "fov120": res["fov120"], "fov360": res["fov360"], "bvh_build_s": build_s, "bvh": "device LBVH + treelet restructuring",
             "host_sah_tree": host_tree}
-    print(json.dumps(line), flush=True)
     e.close()
+    return line
 
 
 # ---------------------------------------------------------------------------------------------- config 5: serving
@@ -586,7 +597,7 @@ def serving_requests(pkg, scenes, rate, window, seed=5):
     or 360 at 2 degree cells, sensors log-uniform 1k..50k); scenes uniform over the resident four."""
     rng = np.random.default_rng(seed)
     t, out = 0.0, []
-    dirs = {mf: patch_dirs(mf) for mf in (1, 2, 4)}
+    dirs = {mf: pkg.workloads.patch_dirs(mf) for mf in (1, 2, 4)}
     while True:
         t += rng.exponential(1.0 / rate)
         if t > window:
@@ -692,7 +703,7 @@ def run_serving(args, pkg):
             "server": {k: st[k] for k in ("completed", "items", "rays", "chunk_sensors", "batch_rays")}, "wall_s": wall,
             "gpu": {"daylight_s": tm["day_gpu_s"], "daylight_mrays_s": tm["day_rays"] / max(tm["day_gpu_s"], 1e-9) / 1e6, "views_s": tm["views_gpu_s"],
                     "views_mrays_s": tm["views_rays"] / max(tm["views_gpu_s"], 1e-9) / 1e6, "queued_s": tm["queued_s"]}}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def main():
@@ -710,14 +721,16 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--window", type=float, default=2.0)
     ap.add_argument("--full-fp32", action="store_true")
+    ap.add_argument("--accuracy-sensors", type=int, default=1024, help="precision: sensors of the FP64 accuracy check")
+    ap.add_argument("--no-extras", action="store_true", help="urban: leave out the precision, views and serving keys")
     args = ap.parse_args()
     pkg = package()
     if args.config == "precision":
-        run_precision(args, pkg)
+        print(json.dumps(run_precision(args, pkg)), flush=True)
     elif args.config == "views":
-        run_views(args, pkg)
+        print(json.dumps(run_views(args, pkg)), flush=True)
     elif args.config == "serving":
-        run_serving(args, pkg)
+        print(json.dumps(run_serving(args, pkg)), flush=True)
     elif args.impl == "reference":
         run_reference(args, pkg)
     else:

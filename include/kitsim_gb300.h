@@ -162,7 +162,7 @@ KGB_API int kgb_reduce(kgb_engine* e, size_t nc, const float* W, int useCos, dou
  * kernels and results as kgb_reduce, bit for bit; the weights and the sums are staged in one fixed 1 MiB array of
  * device memory that belongs to the library (every GPU that loads the library holds it until the process exits)
  * instead of in engine buffers that kgb_reduce may have to grow. Limit: nDir weights (4 bytes each, rounded up to
- * 256 bytes) plus nc sums (8 bytes each) must fit in 1 MiB, e.g. at most 128,260 sensors per call with 5610
+ * 256 bytes) plus nc sums (8 bytes each) must fit in 1 MiB, e.g. at most 128,256 sensors per call with 5610
  * directions; a larger call fails with a message giving the limit. The first call on a device looks the array's
  * address up (cudaGetSymbolAddress): make that first call before any stream capture. Every call uses the same
  * array, so calls whose work overlaps on the GPU (other threads, other engines on the device) race; each call waits
@@ -297,6 +297,14 @@ KGB_API int kgb_set_series_form(kgb_engine* e, int form);
  * Every result is the same either way (both trees are conservative); the device builder is 15x faster on 2 M
  * triangles and its tree traces about as fast. */
 KGB_API int kgb_set_builder(kgb_engine* e, int which);
+/* No counterpart in the reference: lowers the bounded-execution limits of the following calls, so that tests can drive
+ * them to their error returns. nodeLimit: the traversals of kgb_trace, kgb_view and kgb_bounce see only the BVH's first
+ * nodeLimit nodes, and so at most nodeLimit + 8 node visits per query; a query that needs more gives up and the call
+ * fails ("traversal gave up ...", the message of a walk past its visit cap; 0: every node, the cap then the node count
+ * + 8, at most 2^20). bounceLimitNs: how long one bounce step kernel may run before it ends its remaining paths and
+ * kgb_bounce fails ("... passed its ... limit ..."; 0: the default, 10 s; larger values are clamped to it). The engine
+ * stays usable after such a failure. */
+KGB_API int kgb_set_limits(kgb_engine* e, uint32_t nodeLimit, uint64_t bounceLimitNs);
 /* Instrumentation for the traversal roofline: traces sensors [i0, i0+nc) exactly as kgb_trace does (same bits / bytes
  * left on the device) with counting kernels, out[0] = BVH nodes visited, out[1] = triangles tested, out[2] = rays
  * traced past the hemisphere cull, out[3] = BVH bytes (nodes + triangle records). */

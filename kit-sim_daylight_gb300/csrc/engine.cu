@@ -297,11 +297,16 @@ struct Engine {
   kgb_stats stats{};
   int gridBits = 0, gridBytes = 0, gridView = 0;
   int builder = 1;            // 1 device LBVH with treelet restructuring (default), 0 host binned SAH (kgb_set_builder)
+  uint32_t nodeLimit = 0;     // kgb_set_limits: the walks see only this many of the BVH's nodes (0: all)
+  uint64_t bounceLimitNs = kBounceLimitNs;   // kgb_set_limits: a bounce step kernel's time limit
 };
 
 namespace {
 
 Engine* E(kgb_engine* e) { return reinterpret_cast<Engine*>(e); }
+// The nodes a walk may use: all of the scene's, or the first nodeLimit (kgb_set_limits). A walk that reaches a node
+// index beyond them gives up as one past its visit cap does (rt.cuh), so a small limit drives that error path.
+uint32_t walk_nodes(const Engine& g) { return g.nodeLimit && g.nodeLimit < g.sc->nNodes ? g.nodeLimit : g.sc->nNodes; }
 const Engine* E(const kgb_engine* e) { return reinterpret_cast<const Engine*>(e); }
 
 // The samples [s0, s1) of a bounce launch in tracing order: sorted by the 2-D Morton key of their first direction's
@@ -339,7 +344,8 @@ int sync_status(Engine& g) {   // wait for the stream, then read the kernels' st
   CU(cudaStreamSynchronize(g.st));
   CU(cudaGetLastError());
   if (status & kStatusStackOverflow) return fail("traversal stack overflow (BVH deeper than the kernel's stack)");
-  if (status & kStatusVisitLimit) return fail("traversal gave up: a query passed 2^20 node visits or met a node index beyond the BVH");
+  if (status & kStatusVisitLimit)
+    return fail("traversal gave up: a query passed its node-visit limit (the BVH's node count + 8, at most 2^20) or met a node index beyond the BVH");
   return 1;
 }
 int reset_ctl(Engine& g) {
@@ -553,7 +559,7 @@ static int trace_impl(Engine& g, size_t i0, size_t nc, uint32_t rayFlags, uint64
   const size_t nMax = std::max<size_t>(32, size_t(0xffffffffu) / g.nWords * 32);   // warp tasks are counted in 32 bits
   size_t done = 0, n = std::min(counters ? nc : std::min(any ? nMin : size_t(4096), nc), nMax);
   TraceArgs a{};
-  a.nodes = static_cast<const Node8*>(g.sc->nodes.p); a.tris = static_cast<const TriRec*>(g.sc->tris.p); a.nNodes = g.sc->nNodes;
+  a.nodes = static_cast<const Node8*>(g.sc->nodes.p); a.tris = static_cast<const TriRec*>(g.sc->tris.p); a.nNodes = walk_nodes(g);
   a.P = static_cast<const float*>(g.P.p); a.N = static_cast<const float*>(g.N.p); a.D = static_cast<const float*>(g.D.p);
   a.stride = uint32_t(nc); a.nDir = uint32_t(g.nDir); a.nWords = uint32_t(g.nWords); a.rayFlags = rayFlags;
   a.bits = any ? nullptr : static_cast<uint32_t*>(g.vis.p);
@@ -763,6 +769,13 @@ KGB_API int kgb_set_builder(kgb_engine* e, int which) {
   return 1;
 }
 
+KGB_API int kgb_set_limits(kgb_engine* e, uint32_t nodeLimit, uint64_t bounceLimitNs) {
+  Engine& g = *E(e);
+  g.nodeLimit = nodeLimit;
+  g.bounceLimitNs = bounceLimitNs ? std::min(bounceLimitNs, kBounceLimitNs) : kBounceLimitNs;
+  return 1;
+}
+
 KGB_API int kgb_set_series_form(kgb_engine* e, int form) {
   if (form != 0 && form != 1) return fail("kgb_set_series_form: 0 (tensor cores) or 1 (plain FP32)");
   E(e)->seriesForm = form;
@@ -782,7 +795,7 @@ KGB_API int kgb_bounce(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, c
   CU(cudaMemsetAsync(g.dc.p, 0, g.nBins * nc * 4, g.st));
   const double rad = b->north * KGB_PI_D / 180;
   BounceArgs a{};
-  a.nodes = static_cast<const Node8*>(g.sc->nodes.p); a.tris = static_cast<const TriRec*>(g.sc->tris.p); a.nNodes = g.sc->nNodes;
+  a.nodes = static_cast<const Node8*>(g.sc->nodes.p); a.tris = static_cast<const TriRec*>(g.sc->tris.p); a.nNodes = walk_nodes(g);
   a.P = static_cast<const float*>(g.P.p); a.N = static_cast<const float*>(g.N.p);
   a.i0 = uint32_t(i0); a.n = uint32_t(nc); a.nc = uint32_t(nc);
   a.M = b->M; a.nBounce = b->N; a.mf = mf; a.nBins = uint32_t(g.nBins);
@@ -790,6 +803,7 @@ KGB_API int kgb_bounce(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, c
   a.rayFlags = rayFlags; a.slots = static_cast<const kgb_slot*>(g.slots.p); a.nSlots = g.nSlots;
   a.slotLog = static_cast<const float2*>(g.slotLog.p);
   a.dc = static_cast<float*>(g.dc.p); a.status = static_cast<uint32_t*>(g.ctl.p) + 1;
+  a.limitNs = g.bounceLimitNs;
   // paths of a launch: at most 2^23 (their results 64 MiB, the two queues of paths that go on 768 MiB)
   const size_t nCap = std::max<size_t>(1, (size_t(1) << 23) / nc);
   if (!g.gridStep) g.gridStep = g.numSMs * bounce_step_blocks_per_sm();
@@ -819,11 +833,14 @@ KGB_API int kgb_bounce(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, c
               std::to_string(ctl[19]) + ", origin (" + f(20) + ", " + f(21) + ", " + f(22) + "), direction (" + f(23) + ", " + f(24) + ", " +
               f(25) + ")";
     }
-    if (ctl[1] & kStatusTimeout)
-      return fail("gpu_bounce: a launch of " + std::to_string(n) + " samples x " + std::to_string(nc) + " sensors passed its 10 s limit after " +
-                  std::to_string(segments) + " path segments" + where);
+    if (ctl[1] & kStatusTimeout) {
+      char lim[32];
+      std::snprintf(lim, sizeof lim, "%.9g s", double(g.bounceLimitNs) * 1e-9);
+      return fail("gpu_bounce: a launch of " + std::to_string(n) + " samples x " + std::to_string(nc) + " sensors passed its " + lim +
+                  " limit after " + std::to_string(segments) + " path segments" + where);
+    }
     if (ctl[1] & kStatusVisitLimit)
-      return fail("gpu_bounce: traversal gave up (more node visits than the BVH has nodes, or a node index beyond it)" + where);
+      return fail("gpu_bounce: traversal gave up (a walk passed its node-visit limit, or met a node index beyond the BVH)" + where);
     if (!sync_status(g)) return 0;
     const double ms = elapsed(g);
     g.stats.bounceMs += ms; g.stats.paths += n * nc; g.stats.bounceLaunches++;
@@ -884,7 +901,7 @@ KGB_API int kgb_view(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, con
   if (!g.gridView) g.gridView = g.numSMs * view_blocks_per_sm();
   const double rad = v->north * KGB_PI_D / 180;
   ViewArgs a{};
-  a.nodes = static_cast<const Node8*>(g.sc->nodes.p); a.tris = static_cast<const TriRec*>(g.sc->tris.p); a.nNodes = g.sc->nNodes;
+  a.nodes = static_cast<const Node8*>(g.sc->nodes.p); a.tris = static_cast<const TriRec*>(g.sc->tris.p); a.nNodes = walk_nodes(g);
   a.P = static_cast<const float*>(g.P.p); a.N = static_cast<const float*>(g.N.p);
   a.stride = uint32_t(nc); a.i0 = uint32_t(i0); a.K = uint32_t(K); a.nWords = uint32_t(nWords); a.nAz = v->nAz; a.nEl = v->nEl;
   a.rayFlags = rayFlags; a.rowSin = static_cast<const float*>(g.rowSin.p); a.az0 = v->az0; a.dAz = v->dAz; a.groundZ = v->groundZ;

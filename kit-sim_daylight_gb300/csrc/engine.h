@@ -64,6 +64,9 @@ struct ViewArgs {
   uint32_t* status;
 };
 
+// The bounce's step kernels end their remaining paths and fail the call once a step has run this long.
+constexpr uint64_t kBounceLimitNs = 10000000000ull;   // 10 s
+
 struct PathState;   // a path between segments (trace.cu)
 struct BounceArgs {
   const Node8* nodes;
@@ -86,6 +89,7 @@ struct BounceArgs {
   const uint32_t* qInCount;
   PathState* qOut;         // the paths that go on after it, appended
   uint32_t* qOutCount;
+  uint64_t limitNs;        // a step kernel's time limit (kBounceLimitNs unless lowered by kgb_set_limits)
 };
 
 void launch_ray_table(const float* D, uint32_t nDir, void* tab, cudaStream_t st);   // 48 bytes per direction

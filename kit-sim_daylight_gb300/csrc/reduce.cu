@@ -165,34 +165,57 @@ __device__ __forceinline__ float det3(F3 a, F3 b, F3 c) {
   return a.x * (u.y * w.z - u.z * w.y) + a.y * (u.z * w.x - u.x * w.z) + a.z * (u.x * w.y - u.y * w.x);
 }
 
+// Isovist of a sensor, one warp per sensor. A ray's end point is its clipped length (0 on the sensor's own surface, at
+// most farDist) along its cell's direction in the field's own frame. isoDim 2: the area of the polygon through row 0's
+// end points, one triangle (eye, column c, column c + 1) per column. isoDim 3: the volume enclosed by the end points,
+// as the signed volumes of two tetrahedra with the eye per cell quad between rows r - 1 and r and columns c and c + 1.
+// Column c + 1 of the last column is column 0 for a full circle; a narrower fan has no piece after its last column.
+// Lane l owns the columns l, l + 32, ... Each piece is evaluated in float and added to the lane's double sum in row
+// order; the lanes' sums are then combined by warp_sum's fixed tree. Those two orders and the float expressions of the
+// pieces decide the resulting double, so they are kept equal to the reference's k_iso (gpu.cu:197-236).
+struct IsoEnds { float here, next; };   // end lengths of a lane's column and of the column after it, in one row
+
+__device__ __forceinline__ float iso_len(const ViewReduceArgs& a, uint32_t i, uint32_t k) {
+  const size_t at = size_t(k) * a.nc + i;
+  return a.cls[at] == 254 ? 0.f : fminf(a.dist[at], a.farDist);
+}
+// The next column's length comes from lane + 1 by shuffle, except where lane + 1 does not hold it (lane 31, or the wrap
+// to column 0), which reads it itself. Every lane calls this in every group of columns, so the shuffle has the whole warp.
+__device__ __forceinline__ IsoEnds iso_ends(const ViewReduceArgs& a, uint32_t i, uint32_t row, uint32_t col, uint32_t nxt, bool readsNext) {
+  IsoEnds e;
+  e.here = iso_len(a, i, row * a.nAz + col);
+  const float fromNeighbour = __shfl_down_sync(~0u, e.here, 1);
+  e.next = readsNext ? iso_len(a, i, row * a.nAz + nxt) : fromNeighbour;
+  return e;
+}
+
 __global__ void __launch_bounds__(256) k_iso(ViewReduceArgs a) {
   const uint32_t i = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x & 31;
-  if (i >= a.nc) return;
+  if (i >= a.nc) return;   // the whole warp leaves together
   const uint32_t gi = a.i0 + i, element = gi / a.nS, side = a.nS == 2 ? gi % 2 : a.back;
-  const auto len = [&](uint32_t k) {
-    const size_t at = size_t(k) * a.nc + i;
-    return a.cls[at] == 254 ? 0.f : fminf(a.dist[at], a.farDist);
-  };
+  const bool jit = a.jitter != 0;
   double sum = 0;
-  for (uint32_t base = 0; base < a.nAz; base += 32) {   // every lane runs every round: the shuffles need them all
-    const uint32_t col = min(base + lane, a.nAz - 1), c1 = col + 1 == a.nAz ? 0 : col + 1;
-    const bool on = base + lane < a.nAz && (a.world || col + 1 < a.nAz);
-    const bool alone = lane == 31 || c1 == 0;
-    const auto pair = [&](uint32_t row) {
-      const float l = len(row * a.nAz + col), nb = __shfl_down_sync(~0u, l, 1);
-      return make_float2(l, alone ? len(row * a.nAz + c1) : nb);
-    };
-    F3 p = iso_cell(col, col, a.rowSin[0], a.rowSin[1], a.az0, a.dAz, a.jitter != 0, element, side);
-    F3 q = iso_cell(c1, c1, a.rowSin[0], a.rowSin[1], a.az0, a.dAz, a.jitter != 0, element, side);
-    float2 l0 = pair(0);
-    if (a.isoDim == 2) { if (on) sum += double(0.5f * l0.x * l0.y * (p.y * q.x - p.x * q.y)); continue; }
+  for (uint32_t base = 0; base < a.nAz; base += 32) {
+    // lanes past the last column repeat it and add nothing, but still take part in the shuffles
+    const uint32_t col = min(base + lane, a.nAz - 1);
+    const uint32_t nxt = col + 1 == a.nAz ? 0 : col + 1;
+    const bool adds = base + lane < a.nAz && (a.world || col + 1 < a.nAz);
+    const bool readsNext = lane == 31 || nxt == 0;
+    F3 up0 = iso_cell(col, col, a.rowSin[0], a.rowSin[1], a.az0, a.dAz, jit, element, side);   // row 0, columns col, nxt
+    F3 up1 = iso_cell(nxt, nxt, a.rowSin[0], a.rowSin[1], a.az0, a.dAz, jit, element, side);
+    IsoEnds top = iso_ends(a, i, 0, col, nxt, readsNext);
+    if (a.isoDim == 2) {   // the triangle's area: half the two lengths times the sine of the clockwise turn
+      if (adds) sum += double(0.5f * top.here * top.next * (up0.y * up1.x - up0.x * up1.y));
+      continue;
+    }
     for (uint32_t r = 1; r < a.nEl; ++r) {
       const uint32_t d = r * a.nAz + col;
-      const float2 l1 = pair(r);
-      const F3 c = iso_cell(d, col, a.rowSin[2 * r], a.rowSin[2 * r + 1], a.az0, a.dAz, a.jitter != 0, element, side);
-      const F3 e = iso_cell(d - col + c1, c1, a.rowSin[2 * r], a.rowSin[2 * r + 1], a.az0, a.dAz, a.jitter != 0, element, side);
-      if (on) sum += double(l0.x * l0.y * l1.x * det3(p, q, c) + l0.y * l1.y * l1.x * det3(q, e, c));
-      p = c; q = e; l0 = l1;
+      const IsoEnds low = iso_ends(a, i, r, col, nxt, readsNext);
+      const F3 lo0 = iso_cell(d, col, a.rowSin[2 * r], a.rowSin[2 * r + 1], a.az0, a.dAz, jit, element, side);
+      const F3 lo1 = iso_cell(d - col + nxt, nxt, a.rowSin[2 * r], a.rowSin[2 * r + 1], a.az0, a.dAz, jit, element, side);
+      // six times the volumes of (eye, up0, up1, lo0) and (eye, up1, lo1, lo0), each determinant scaled by its lengths
+      if (adds) sum += double(top.here * top.next * low.here * det3(up0, up1, lo0) + top.next * low.next * low.here * det3(up1, lo1, lo0));
+      up0 = lo0; up1 = lo1; top = low;
     }
   }
   const double v = warp_sum(a.isoDim == 2 ? sum : sum / 6);

@@ -11,7 +11,7 @@
 // Limits and sharing:
 //  - the array is kNoAllocScratchBytes (1 MiB) on each device, held by every GPU that loads the library until the
 //    process exits. The nDir weights (4 bytes each, rounded up to 256 bytes) plus the nc sums (8 bytes each) must
-//    fit: with 5610 directions that is up to 128,260 sensors per call. A larger call fails with a message that gives
+//    fit: with 5610 directions that is up to 128,256 sensors per call. A larger call fails with a message that gives
 //    the limit;
 //  - every call on a device uses the same array, so calls whose work overlaps on the GPU (from other threads, or
 //    other engines on the same device) race. Each call waits for its own work before it returns, so calls made one
@@ -60,7 +60,7 @@ extern "C" KGB_API int kgb_reduce_noalloc(kgb_engine* e, size_t nc, const float*
   ReduceInputs in{};
   engine_reduce_inputs(e, in);
   if (nc == 0) return 1;
-  if (nc != in.visN) return set_error("gpu_reduce: no trace of this chunk");
+  if (nc != in.visN) return set_error("kgb_reduce_noalloc: no trace of this chunk");
   const size_t wBytes = (in.nDir * 4 + 255) & ~size_t(255);
   if (wBytes + nc * 8 > kNoAllocScratchBytes) {
     const size_t most = wBytes < kNoAllocScratchBytes ? (kNoAllocScratchBytes - wBytes) / 8 : 0;

@@ -44,8 +44,11 @@
 //               bytes at a time
 // The 64-column tile keeps the Kahan sums in registers: six warps per CTA leave a scheduler at most two warps, so a
 // thread may hold up to 255 registers (the register file is split between the SM's four schedulers).
-// Every wait on an mbarrier is bounded: past the limit the kernel records kStatusTimeout and leaves its loops (the
-// TMEM it holds is released on the way out).
+// Every wait on an mbarrier is bounded: past the limit the kernel records kStatusTimeout and leaves its loops. Before the
+// CTA releases its TMEM and exits, the producer waits for the last fill it issued into each stage (so no bulk copy still
+// writes shared memory) and the MMA issuer commits to a drain barrier and waits for it (so no MMA still runs); both
+// waits have their own 4 s limit. In a run that did not time out both return at once: every fill and every MMA has
+// been consumed by then.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -64,7 +67,7 @@ constexpr int STAGE_BYTES = PIECES * (V_TILE + S_TILE); // V hi mid lo, S hi mid
 constexpr int EPI_WARPS = 4;                        // one per TMEM lane quarter, the tile's 64 columns each
 constexpr int THREADS = 32 * (2 + EPI_WARPS);
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /* align */ + 256 /* barriers */;
-static_assert((2 * STAGES + 2 * NH) * 8 + 4 <= 256, "the barriers and the TMEM slot fit their 256 bytes");
+static_assert((2 * STAGES + 2 * NH + 1) * 8 + 4 <= 256, "the barriers and the TMEM slot fit their 256 bytes");
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t kChunkCols = 256;                 // chunk accumulator b at column 256 b: [H | C1 | C2] in 3 x BN of them
 static_assert(3 * BN <= kChunkCols && NH * kChunkCols <= TMEM_COLS, "the chunk accumulators fit TMEM");
@@ -86,8 +89,8 @@ __device__ __forceinline__ uint64_t globaltimer() {
   asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
   return t;
 }
-// Bounded wait for the phase of the given parity; false (and the status bit) once kWaitLimitNs have passed.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t* status) {
+// Bounded wait for the phase of the given parity; false (and the status bit) once limitNs have passed.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t* status, uint64_t limitNs) {
   uint64_t t0 = 0;
   for (uint32_t k = 0;; ++k) {
     uint32_t ok;
@@ -97,7 +100,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
     if ((k & 255) == 0) {
       const uint64_t t = globaltimer();
       if (!t0) t0 = t;
-      else if (t - t0 > kWaitLimitNs) { atomicOr(status, kStatusTimeout); return false; }
+      else if (t - t0 > limitNs) { atomicOr(status, kStatusTimeout); return false; }
     }
   }
 }
@@ -172,6 +175,7 @@ struct SeriesTcArgs {
   const float* N;            // chunk normals
   float* E;                  // [nc x T]
   uint32_t* status;
+  uint64_t waitLimitNs;      // the pipeline's mbarrier waits give up past this (kWaitLimitNs)
 };
 
 // Tile order: bands of kBand step-tiles; within a band every row of tiles, steps fastest. The CTAs running at once share
@@ -201,13 +205,15 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
   uint64_t* empty = bars + STAGES;       // [STAGES] MMA -> TMA
   uint64_t* hFull = bars + 2 * STAGES;   // [NH] MMA -> epilogue: a chunk's sums are complete
   uint64_t* hEmpty = hFull + NH;         // [NH] epilogue -> MMA
-  uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(hEmpty + NH);
+  uint64_t* drain = hEmpty + NH;         // the MMA issuer's last commit: every MMA it issued has completed
+  uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(drain + 1);
   __shared__ volatile uint32_t abortFlag;
 
   const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
     for (uint32_t b = 0; b < NH; ++b) { mbar_init(&hFull[b], 1); mbar_init(&hEmpty[b], EPI_WARPS * 32); }
+    mbar_init(drain, 1);
     abortFlag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -225,12 +231,13 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
   if (warp == 0) {
     if (lane == 0) {   // ---------------- TMA producer
       uint32_t stage = 0, phase = 0;
+      uint32_t filled = 0, fillParity = 0;   // bit s: stage s received a fill; the phase parity of its last one
       for (uint32_t tile = blockIdx.x; tile < nTilesAll && !abortFlag; tile += gridDim.x) {
         uint32_t tm, tn;
         tile_coords(tile, a.mTiles, a.nTiles, tm, tn);
         const int m0 = int(tm + a.mBase) * BM, n0 = int(tn) * BN;
         for (uint32_t kb = 0; kb < kBlocks; ++kb) {
-          if (!mbar_wait(&empty[stage], phase ^ 1, a.status)) { abortFlag = 1; break; }
+          if (!mbar_wait(&empty[stage], phase ^ 1, a.status, a.waitLimitNs)) { abortFlag = 1; break; }
           uint8_t* s = smem + stage * STAGE_BYTES;
           mbar_expect_tx(&full[stage], STAGE_BYTES);
           const int k0 = int(kb) * BK;
@@ -239,9 +246,15 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
             tma_load_2d(s + p * V_TILE, &mapV, k0, m0 + p * int(a.nc), &full[stage]);
             tma_load_2d(s + PIECES * V_TILE + p * S_TILE, &mapS, k0, n0 + p * int(a.T), &full[stage]);
           }
+          filled |= 1u << stage;
+          fillParity = (fillParity & ~(1u << stage)) | (phase << stage);
           if (++stage == STAGES) { stage = 0; phase ^= 1; }
         }
       }
+      // A stage's fill is issued only after the previous one was consumed, so only the last fill of each stage can be
+      // in flight here: wait until it has landed.
+      for (uint32_t st = 0; st < uint32_t(STAGES); ++st)
+        if ((filled >> st) & 1u) mbar_wait(&full[st], (fillParity >> st) & 1u, a.status, kWaitLimitNs);
     }
     __syncwarp();
   } else if (warp == 1) {
@@ -251,10 +264,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
         bool ok = true;
         for (uint32_t kb = 0; kb < kBlocks; ++kb, ++chunk) {   // a chunk: one K block, its sums from zero in [H | C1 | C2]
           const uint32_t hbuf = chunk % NH;
-          if (!mbar_wait(&hEmpty[hbuf], ((chunk / NH) & 1) ^ 1, a.status)) { ok = false; break; }
+          if (!mbar_wait(&hEmpty[hbuf], ((chunk / NH) & 1) ^ 1, a.status, a.waitLimitNs)) { ok = false; break; }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t hT = tmemBase + hbuf * kChunkCols;
-          if (!mbar_wait(&full[stage], phase, a.status)) { ok = false; break; }
+          if (!mbar_wait(&full[stage], phase, a.status, a.waitLimitNs)) { ok = false; break; }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint8_t* s = smem + stage * STAGE_BYTES;
           const uint64_t v0 = smem_desc(s), v1 = smem_desc(s + V_TILE), v2 = smem_desc(s + 2 * V_TILE);
@@ -272,6 +285,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
         }
         if (!ok) { abortFlag = 1; break; }
       }
+      // tcgen05.commit tracks every MMA this thread issued before it: once the drain barrier completes, none runs
+      mma_commit(drain);
+      mbar_wait(drain, 0, a.status, kWaitLimitNs);
     }
     __syncwarp();
   } else {   // ---------------- epilogue: warps 2..5
@@ -287,7 +303,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
       bool ok = true;
       for (uint32_t ch = 0; ch < kBlocks; ++ch, ++chunk) {
         const uint32_t hbuf = chunk % NH;
-        ok = __all_sync(~0u, mbar_wait(&hFull[hbuf], (chunk / NH) & 1, a.status));
+        ok = __all_sync(~0u, mbar_wait(&hFull[hbuf], (chunk / NH) & 1, a.status, a.waitLimitNs));
         if (!ok || abortFlag) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t hAt = tmemBase + laneBase + hbuf * kChunkCols;
@@ -504,6 +520,7 @@ const char* series_tc_rows(const SeriesTcPlan& p, uint32_t mBase, uint32_t mCoun
   a.mTiles = mCount; a.mBase = mBase; a.nTiles = (p.T + BN - 1) / BN;
   a.sunOfCol = p.sunOfCol; a.sunVec = p.sunVec; a.sunW = p.sunW; a.sun0 = p.sun0;
   a.bits = p.bits; a.bytes = p.bytes; a.N = p.N; a.E = p.E; a.status = p.status;
+  a.waitLimitNs = kWaitLimitNs;
   const int grid = int(std::min<uint32_t>(uint32_t(p.numSMs), a.mTiles * a.nTiles));
   k_series_tc<<<grid, THREADS, SMEM_BYTES, st>>>(mV, mS, a);
   return nullptr;

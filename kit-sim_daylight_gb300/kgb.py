@@ -121,6 +121,7 @@ SIGNATURES = [
     ("kgb_set_builder", c_int, [_E, c_int]),
     ("kgb_set_series_form", c_int, [_E, c_int]),
     ("kgb_trace_counters", c_int, [_E, c_size_t, c_size_t, c_uint32, POINTER(c_uint64)]),
+    ("kgb_set_limits", c_int, [_E, c_uint32, c_uint64]),
 ]
 
 
@@ -256,6 +257,11 @@ class Engine:
     def set_series_form(self, form):
         """0: split-BF16 on the tensor cores (default); 1: the plain FP32 form."""
         self._ok(self.d.kgb_set_series_form(self.h, form))
+
+    def set_limits(self, node_limit=0, bounce_limit_ns=0):
+        """Lowers the traversal's node limit (the walks see only the BVH's first node_limit nodes) and the bounce step's
+        time limit; 0 restores a default."""
+        self._ok(self.d.kgb_set_limits(self.h, int(node_limit), int(bounce_limit_ns)))
 
     def trace_counters(self, i0, nc, flags):
         """The instrumented trace: dict(nodes, tris, rays, bvh_bytes) for the roofline (results as trace())."""

@@ -274,3 +274,60 @@ def views_grid(fov, cell, lo=-70.0, hi=50.0):
         wRow[k] = np.radians(dAz) * (1 if flat else top - bot)
     wRow /= wRow.sum() * nAz
     return nAz, nEl, float(dAz), rowSin, wRow
+
+
+# ---------------------------------------------------------------------------------------------- sky of the urban year
+KRF, KGF, KBF = 0.265074126, 0.670114631, 0.064811243   # Radiance CIE_rf / gf / bf (bright())
+
+
+def patch_dirs(mf):
+    """Reinhart / Tregenza patch centres (gendaymtx order, src/sky.cpp:240-270) and their solid angles, float as the
+    reference's make_patches + dir_from_altaz."""
+    tnaz = [30, 30, 24, 24, 18, 12, 6]
+    alpha = (np.pi / 2) / (7 * mf + .5)
+    alt, azi, om = [], [], []
+    for i in range(7 * mf):
+        n = tnaz[i // mf] * mf
+        for j in range(n):
+            alt.append(np.float32(alpha * (i + .5)))
+            azi.append(np.float32(2 * np.pi * j / n))
+            om.append(np.float32(2 * np.pi * (np.sin(alpha * (i + 1)) - np.sin(alpha * i)) / n))
+    alt.append(np.float32(np.pi / 2)); azi.append(np.float32(0)); om.append(np.float32(2 * np.pi * (1 - np.cos(alpha * .5))))
+    a, z = np.array(alt, np.float64), np.array(azi, np.float64)
+    D = np.stack([np.cos(a) * np.sin(z), np.cos(a) * np.cos(z), np.sin(a)], axis=1).astype(np.float32)
+    return D, np.array(om, np.float32)
+
+
+def urban_year_sky(e, mf, weather):
+    """The urban weather year's series operands built on the GPU: NOAA sun per hour (kgb_sun_noaa) and the Perez sky per
+    hour and patch (kgb_sky, FP64), as the reference's run.cpp builds them on the host (src/run.cpp:350-419, physical
+    mode, radiometric). weather: [2 x 8760] DNI and DHI of the year (Berlin, UTC+1). Returns the series inputs of the
+    non-night hours: S [P x T], g [T], Sdc [(P + 1) x T] (bin 0 the ground, bin 1 + p the patch radiance plus the binned
+    sun), the sun-up hours' directions, columns and DNI, and the build's wall time."""
+    import time
+    w = np.asarray(weather, np.float64)
+    dim = [31, 28, 31, 30, 31, 30, 31, 31, 30, 31, 30, 31]
+    month = np.repeat(np.arange(1, 13), [24 * d for d in dim])
+    day = np.concatenate([np.repeat(np.arange(1, d + 1), 24) for d in dim])
+    hour = np.tile(np.arange(24) + 0.5, 365)
+    jd = np.repeat(np.arange(1, 366), 24)
+    rows = np.stack([np.full(8760, 52.52), np.full(8760, 13.41), np.full(8760, 1.0), month, day, hour, np.zeros(8760)], axis=1)
+    t0 = time.perf_counter()
+    sun = e.sun_noaa(rows)
+    steps = np.stack([jd, np.radians(sun[:, 0]), np.radians(sun[:, 1]), w[0], w[1]], axis=1)
+    sky = e.sky(mf, steps, grefl=0.2, sun=False, sky=True, visible=False)
+    sunbin = e.sky(mf, steps, grefl=0.2, sun=True, sky=False, visible=False)   # the sun as gendaymtx bins it (AddDirect)
+    sky_s = time.perf_counter() - t0
+    bright = KRF * sky[:, :, 0] + KGF * sky[:, :, 1] + KBF * sky[:, :, 2]
+    bright_sun = KRF * sunbin[:, :, 0] + KGF * sunbin[:, :, 1] + KBF * sunbin[:, :, 2]
+    col = (w[0] + w[1]) > 1e-4
+    colOf = np.cumsum(col) - 1
+    S = np.ascontiguousarray(bright[col, 1:].T, np.float32)
+    g = np.ascontiguousarray(bright[col, 0], np.float32)
+    Sdc = np.concatenate([g[None, :], (S.astype(np.float64) + bright_sun[col, 1:].T).astype(np.float32)]).astype(np.float32)
+    up = sun[:, 2] > 0
+    sunVec = sun[up, 3:6].astype(np.float32)
+    ups = np.nonzero(up)[0]
+    sunStep = np.where(col[ups], colOf[ups], 0).astype(np.int32)
+    sunW = np.where(col[ups], w[0][ups], 0).astype(np.float32)
+    return dict(S=S, g=g, Sdc=Sdc, sunVec=sunVec, sunStep=sunStep, sunW=sunW, sky_s=sky_s, T=int(col.sum()))

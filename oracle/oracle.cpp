@@ -457,6 +457,75 @@ unsigned sky_bin(F3 d, unsigned mf, unsigned nBins, float alpha, float cosN, flo
   return b + unsigned(az * (float(n) / 6.28318531f) + .5f) % n;
 }
 
+// The reported distance of the hit that decided a view ray. The watertight test's t = T / det rounds with the vertices'
+// coordinates relative to the origin, so a triangle whose vertices lie far beyond the hit (a kilometre-long ground quad
+// seen from 100 m) gives t off by up to 1e-3 relative. Where a vertex lies more than 4 t from the origin along an axis
+// (in float), t is recomputed from the triangle's plane in double: float(dot(v0 - o, ng)) / float(dot(d, ng)) with
+// ng = (v1 - v0) x (v2 - v0), whose differences and products of float coordinates are exact or within 2^-52 in double;
+// the result lies within 2 ulps of the exact distance. Measured against a double-precision walk on the 2 M-triangle views
+// city: 9 % of the hits are recomputed, and every distance lies within 3.2e-6 of the double one (7e-4 without). The walk
+// itself (which hits, their order, the own-plane rules) keeps the float t.
+bool g_refine = true;   // kgbo_set_refine: a test switches the refinement off to plant the error it removes
+float refine_t(F3 o, F3 d, F3 v0, F3 v1, F3 v2, float t) {
+  if (!g_refine) return t;
+  const float reach = std::max({std::fabs(v0.x - o.x), std::fabs(v0.y - o.y), std::fabs(v0.z - o.z), std::fabs(v1.x - o.x), std::fabs(v1.y - o.y),
+                                std::fabs(v1.z - o.z), std::fabs(v2.x - o.x), std::fabs(v2.y - o.y), std::fabs(v2.z - o.z)});
+  if (!(reach > 4.f * t)) return t;
+  const double ex = double(v1.x) - double(v0.x), ey = double(v1.y) - double(v0.y), ez = double(v1.z) - double(v0.z);
+  const double fx = double(v2.x) - double(v0.x), fy = double(v2.y) - double(v0.y), fz = double(v2.z) - double(v0.z);
+  const double nx = ey * fz - ez * fy, ny = ez * fx - ex * fz, nz = ex * fy - ey * fx;
+  const double num = ((double(v0.x) - double(o.x)) * nx + (double(v0.y) - double(o.y)) * ny) + (double(v0.z) - double(o.z)) * nz;
+  const double den = (double(d.x) * nx + double(d.y) * ny) + double(d.z) * nz;
+  const float r = float(num) / float(den);
+  return r > 0.f && r < INFINITY ? r : t;
+}
+
+// trace_dev.cu:200-232 (__raygen__view's walk) for one ray: its class and distance. Own-plane hits are stepped over
+// (at most 3; the 4th ends the ray as an obstruction at its distance), panes labelled KGB_LABEL_PASS are passed (at most
+// 16) and set the glazed bit; a downward ray ends 1 cm below the virtual ground, whose plane it reports on a miss. The
+// distance of the hit that ends the walk is refine_t's.
+void view_ray(const Engine& g, F3 o, F3 nn, F3 dir, bool none, bool cull, const kgb_view_in& v, uint8_t& cl, float& t) {
+  const float inf = INFINITY;
+  cl = 2;
+  t = inf;
+  if (none || (v.cull && dot(nn, dir) <= 0.f)) { cl = 254; return; }
+  if (v.vground && dir.z < 0.f && !(o.z > v.groundZ)) { cl = 1; t = 0.1f; return; }
+  const bool plane = v.vground && dir.z < 0.f;
+  const float tg = plane ? (o.z - v.groundZ) / -dir.z : inf;
+  const float tmax = plane ? (o.z - v.groundZ + 0.01f) / -dir.z : FLT_MAX;
+  float tmin = 1e-5f;
+  unsigned own = 0, panes = 0;
+  const Ray ray = make_ray(o, dir);
+  Hit hh;
+  bool byHit = false;   // the walk ended on a hit (not past the last one)
+  for (;;) {
+    if (!closest(*g.sc, ray, tmin, tmax, cull, hh)) { cl = dir.z >= 0.f ? 0 : 1; t = tg; break; }
+    t = hh.t;
+    if (own_hit(*g.sc, hh, dir, nn)) { if (++own == 4) { byHit = true; break; } }
+    else {
+      const uint8_t lb = g.label.empty() ? 2 : g.label[hh.prim];
+      if (lb != KGB_LABEL_PASS) { cl = lb; byHit = true; break; }
+      if (++panes > KGB_MAX_PANES) { byHit = true; break; }
+    }
+    tmin = next_up(t);
+  }
+  if (byHit) t = refine_t(o, dir, g.sc->v[g.sc->tri[3 * hh.prim]], g.sc->v[g.sc->tri[3 * hh.prim + 1]], g.sc->v[g.sc->tri[3 * hh.prim + 2]], t);
+  if (panes) cl |= KGB_VIEW_GLAZED;
+}
+
+// The frame of a sensor's view field (trace_dev.cu:186-197): world-fixed (360 mode, turned by north) or the normal's.
+void view_frame(F3 nn, bool world, float cosN, float sinN, F3& f, F3& r, F3& u) {
+  if (world) { f = f3(-sinN, cosN, 0.f); r = f3(cosN, sinN, 0.f); u = f3(0.f, 0.f, 1.f); return; }
+  const float l = std::sqrt(nn.x * nn.x + nn.y * nn.y);
+  f = nn;
+  if (l > 1e-3f) r = f3(nn.y / l, -nn.x / l, 0.f);
+  else {
+    r = f3(cosN, sinN, 0.f);
+    if (l > 0.f) { r = sub(r, mul(dot(r, nn), nn)); r = mul(1.f / std::sqrt(dot(r, r)), r); }
+  }
+  u = f3(r.y * f.z - r.z * f.y, r.z * f.x - r.x * f.z, r.x * f.y - r.y * f.x);
+}
+
 // params.h:77-89 (view_cell / view_local), sincospif as kgb_sincospi
 F3 view_cell(unsigned d, unsigned col, float rsx, float rsy, float az0, float dAz, bool jitter, unsigned element, unsigned side) {
   float a = 0.5f, s = 0.5f * (rsx + rsy);
@@ -820,7 +889,6 @@ KGB_API int kgb_view(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, con
   const bool cull = (rayFlags & KGB_RAY_CULL_BACK_FACING) != 0;
   const double rad = v->north * KGB_PI_D / 180;
   const float cosN = float(std::cos(rad)), sinN = float(std::sin(rad));
-  const float inf = INFINITY;
   const size_t nMin = std::max<size_t>(1, (size_t(1) << 13) / nWords);
   size_t n = std::max(*launch, nMin);
   for (size_t done = 0; done < nc;) {
@@ -833,46 +901,14 @@ KGB_API int kgb_view(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, con
       const F3 nn = g.N[i0 + i], o = offset_ray(g.P[i0 + i], nn);
       const bool none = !(dot(nn, nn) > 0.f);
       F3 f, r, u;
-      if (v->world) { f = f3(-sinN, cosN, 0.f); r = f3(cosN, sinN, 0.f); u = f3(0.f, 0.f, 1.f); }
-      else {
-        const float l = std::sqrt(nn.x * nn.x + nn.y * nn.y);
-        f = nn;
-        if (l > 1e-3f) r = f3(nn.y / l, -nn.x / l, 0.f);
-        else {
-          r = f3(cosN, sinN, 0.f);
-          if (l > 0.f) { r = sub(r, mul(dot(r, nn), nn)); r = mul(1.f / std::sqrt(dot(r, r)), r); }
-        }
-        u = f3(r.y * f.z - r.z * f.y, r.z * f.x - r.x * f.z, r.x * f.y - r.y * f.x);
-      }
+      view_frame(nn, v->world != 0, cosN, sinN, f, r, u);
       for (size_t d = 0; d < K; ++d) {
         const unsigned col = unsigned(d % v->nAz), row = unsigned(d / v->nAz);
         const F3 l = view_cell(unsigned(d), col, g.rowSin[2 * row], g.rowSin[2 * row + 1], v->az0, v->dAz, v->jitter != 0, element, side);
         const F3 dir = add(add(mul(l.x, r), mul(l.y, f)), mul(l.z, u));
-        uint8_t cl = 2;
-        float t = inf;
-        if (none || (v->cull && dot(nn, dir) <= 0.f)) cl = 254;
-        else if (v->vground && dir.z < 0.f && !(o.z > v->groundZ)) { cl = 1; t = 0.1f; }
-        else {
-          const bool plane = v->vground && dir.z < 0.f;
-          const float tg = plane ? (o.z - v->groundZ) / -dir.z : inf;
-          const float tmax = plane ? (o.z - v->groundZ + 0.01f) / -dir.z : FLT_MAX;
-          float tmin = 1e-5f;
-          unsigned own = 0, panes = 0;
-          const Ray ray = make_ray(o, dir);
-          for (;;) {
-            Hit hh;
-            if (!closest(*g.sc, ray, tmin, tmax, cull, hh)) { cl = dir.z >= 0.f ? 0 : 1; t = tg; break; }
-            t = hh.t;
-            if (own_hit(*g.sc, hh, dir, nn)) { if (++own == 4) break; }
-            else {
-              const uint8_t lb = g.label.empty() ? 2 : g.label[hh.prim];
-              if (lb != KGB_LABEL_PASS) { cl = lb; break; }
-              if (++panes > KGB_MAX_PANES) break;
-            }
-            tmin = next_up(t);
-          }
-          if (panes) cl |= KGB_VIEW_GLAZED;
-        }
+        uint8_t cl;
+        float t;
+        view_ray(g, o, nn, dir, none, cull, *v, cl, t);
         g.cls[d * nc + i] = cl;
         g.dist[d * nc + i] = t;
       }
@@ -1018,6 +1054,9 @@ KGB_API int kgb_sun_noaa(kgb_engine*, const double*, size_t, double*) {
 }
 // The restatement has one builder (its binary SAH tree): every builder choice gives the same results.
 KGB_API int kgb_set_builder(kgb_engine*, int which) { return which == 0 || which == 1 ? 1 : fail("kgb_set_builder: 0 or 1"); }
+// The engine's bounded-execution limits guard its device walks; the oracle's host recursion needs none, so there is
+// nothing to lower here.
+KGB_API int kgb_set_limits(kgb_engine*, uint32_t, uint64_t) { return 1; }
 KGB_API int kgb_set_series_form(kgb_engine*, int form) { return form == 0 || form == 1 ? 1 : fail("kgb_set_series_form: 0 or 1"); }
 KGB_API int kgb_trace_counters(kgb_engine*, size_t, size_t, uint32_t, uint64_t out[4]) {
   out[0] = out[1] = out[2] = out[3] = 0;
@@ -1032,4 +1071,374 @@ KGB_API void kgb_dims(const kgb_engine* e, uint64_t out[6]) {
   out[0] = g.nSensors; out[1] = g.nDir; out[2] = g.nWords; out[3] = g.nBins; out[4] = g.viewK; out[5] = g.bytes ? 1 : 0;
 }
 
+}  // extern "C"
+
+// ============================================================================================ FP64 re-decision
+// TEST INFRASTRUCTURE ONLY, like the rest of this file. The engine and this oracle decide every hit with one watertight
+// float test (hit_tri), so they agree bit for bit; the functions below measure how far that shared decision lies from
+// exact geometry. Each ray of a sample is decided twice: by the float code above (the engine's decision), and with every
+// ray/triangle test and every per-hit rule (hemisphere cull, own plane, the 1/32 m and tmin bounds, the virtual ground's
+// ray end) evaluated in double from the same float inputs (vertices, origin after offset_ray, direction, normal). Double
+// rounding is 2^-29 of float's, so where the two differ the float decision is the one off exact geometry. A ray whose
+// decisions differ is attributed to
+//   edge       a triangle that the two tests hit differently, where the ray passes within edgeRel x (|o|max + t) of the
+//              triangle's nearest edge (the ray's point on the triangle's plane, to the nearest point of its boundary);
+//              the float test's rounding scales with the coordinates relative to the origin;
+//   grazing    such a triangle met at |cos| < 0.05 (the reference's exclusion of grazing hits, validate/README.md:189);
+//   threshold  no triangle hit differently, but a sign or threshold test of the rules decided differently (the reference
+//              excludes rays within 1e-6 of a sign test and hits within 1 mm of the downward ray's end);
+//   tie        (views) the same triangles hit in both, but the two nearest lie within 1e-5 of each other's distance, so
+//              their order differs;
+//   rounding   (views) the same triangle decides in both with the same class, but the float distance differs from the
+//              double one by more than the reference's distance check (1e-5 t + 1e-4 m);
+//   other      none of these (the tests require none).
+namespace {
+
+struct D3 { double x, y, z; };
+inline D3 d3(F3 a) { return D3{a.x, a.y, a.z}; }
+inline D3 dsub(D3 a, D3 b) { return D3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline D3 dadd(D3 a, D3 b) { return D3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline D3 dmul(double s, D3 a) { return D3{s * a.x, s * a.y, s * a.z}; }
+inline double ddot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline D3 dcross(D3 a, D3 b) { return D3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline double dcomp(D3 a, int k) { return k == 0 ? a.x : k == 1 ? a.y : a.z; }
+inline double dlen(D3 a) { return std::sqrt(ddot(a, a)); }
+
+struct HitD { double t = 0, u = 0, v = 0; uint32_t prim = 0; bool front = false; };
+// hit_tri's test in double: the same dominant axis and shear, edge functions, tie rule on exact zeros and t range
+bool hit_tri_d(const Ray& rf, D3 o, D3 d, D3 v0, D3 v1, D3 v2, double tmin, double tmax, bool cullBack, HitD& h) {
+  const int kx = rf.kx, ky = rf.ky, kz = rf.kz;
+  const double dz = dcomp(d, kz), Sx = dcomp(d, kx) / dz, Sy = dcomp(d, ky) / dz, Sz = 1.0 / dz;
+  const D3 A = dsub(v0, o), B = dsub(v1, o), C = dsub(v2, o);
+  const double Ax = dcomp(A, kx) - Sx * dcomp(A, kz), Ay = dcomp(A, ky) - Sy * dcomp(A, kz);
+  const double Bx = dcomp(B, kx) - Sx * dcomp(B, kz), By = dcomp(B, ky) - Sy * dcomp(B, kz);
+  const double Cx = dcomp(C, kx) - Sx * dcomp(C, kz), Cy = dcomp(C, ky) - Sy * dcomp(C, kz);
+  const double U = Cx * By - Cy * Bx, V = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
+  if ((U < 0 || V < 0 || W < 0) && (U > 0 || V > 0 || W > 0)) return false;
+  const double det = U + V + W;
+  if (det == 0) return false;
+  if (cullBack && det < 0) return false;
+  if (U == 0 || V == 0 || W == 0) {
+    const double s = det > 0 ? 1 : -1;
+    const auto owns = [](double ex, double ey) { return ey > 0 || (ey == 0 && ex > 0); };
+    if (U == 0 && !owns(s * (Cx - Bx), s * (Cy - By))) return false;
+    if (V == 0 && !owns(s * (Ax - Cx), s * (Ay - Cy))) return false;
+    if (W == 0 && !owns(s * (Bx - Ax), s * (By - Ay))) return false;
+  }
+  const double t = (U * (Sz * dcomp(A, kz)) + V * (Sz * dcomp(B, kz)) + W * (Sz * dcomp(C, kz))) / det;
+  if (!(t >= tmin && t <= tmax)) return false;
+  h.t = t; h.u = V / det; h.v = W / det; h.front = det > 0;
+  return true;
+}
+// own_hit's rules in double (trace_dev.cu:60-72): t (n.d) under 1/32 m, the hit within ext 2^-22 of the sensor's plane
+// along the ray and the triangle's normal on the ray's side facing away from the sensor's
+bool own_hit_d(D3 v0, D3 v1, D3 v2, const HitD& h, D3 d, D3 n, double* margin) {
+  const D3 e1 = dsub(v1, v0), e2 = dsub(v2, v0), ng = dcross(e1, e2);
+  const double l2 = ddot(ng, ng);
+  const double a = h.t * ddot(n, d), lim1 = 1.0 / 32;
+  double m = std::fabs(a - lim1) / lim1;
+  bool ok = a < lim1 && l2 > 0;
+  if (l2 > 0) {
+    const D3 hn = dmul((h.front ? 1 : -1) / std::sqrt(l2), ng);
+    const double ext = std::max({std::fabs(e1.x), std::fabs(e1.y), std::fabs(e1.z), std::fabs(e2.x), std::fabs(e2.y), std::fabs(e2.z)});
+    const double lhs = h.t * std::fabs(ddot(d, hn)), rhs = ext * double(2.3841858e-7f), nh = ddot(n, hn);
+    ok = ok && lhs < rhs && nh <= 0;
+    m = std::min({m, std::fabs(lhs - rhs) / std::max(rhs, 1e-300), std::fabs(nh)});
+  }
+  if (margin) *margin = m;
+  return ok;
+}
+// The ray's point on the triangle's plane, its distance to the triangle's boundary, and |cos| with the plane's normal.
+void edge_metrics(D3 o, D3 d, D3 v0, D3 v1, D3 v2, double& dist, double& cosA, double& tPlane) {
+  const D3 ng = dcross(dsub(v1, v0), dsub(v2, v0));
+  const double ln = dlen(ng), dn = ddot(d, ng);
+  cosA = ln > 0 ? std::fabs(dn) / (ln * dlen(d)) : 0;
+  dist = 0; tPlane = 0;
+  if (!(ln > 0) || dn == 0) return;
+  tPlane = ddot(dsub(v0, o), ng) / dn;
+  const D3 X = dadd(o, dmul(tPlane, d));
+  const auto seg = [&](D3 a, D3 b) {
+    const D3 ab = dsub(b, a);
+    const double L = ddot(ab, ab), s = L > 0 ? std::clamp(ddot(dsub(X, a), ab) / L, 0.0, 1.0) : 0.0;
+    return dlen(dsub(X, dadd(a, dmul(s, ab))));
+  };
+  dist = std::min({seg(v0, v1), seg(v1, v2), seg(v2, v0)});
+}
+// The triangles whose boxes the ray passes (every triangle the ray meets at t >= 0 is among them: the boxes are
+// conservative, expanded by 2^-16 of the scene's largest coordinate).
+template <class Fn>
+void for_candidates(const Scene& s, const Ray& r, Fn&& f) {
+  if (s.nodes.empty()) return;
+  uint32_t stack[128];
+  int sp = 0;
+  stack[sp++] = 0;
+  while (sp) {
+    const Node& nd = s.nodes[stack[--sp]];
+    if (!box_hit(nd, r, 0.f, INFINITY)) continue;
+    if (nd.count) for (uint32_t j = nd.first; j < nd.first + nd.count; ++j) f(s.order[j]);
+    else { stack[sp++] = nd.left; stack[sp++] = nd.right; }
+  }
+}
+
+enum { kAgree = 0, kEdge = 1, kGrazing = 2, kThreshold = 3, kTie = 4, kRounding = 5, kOther = 6 };
+struct Tally {   // what one sensor's rays add to the report (kgbo_recheck_*'s out[])
+  double v[24] = {};
+  void flip_metrics(double dist, double rel, double cosA) {
+    const double edges[5] = {1e-7, 1e-6, 1e-5, 1e-4, 1e-3};
+    int b = 0;
+    while (b < 5 && dist >= edges[b]) ++b;
+    v[8 + b] += 1;
+    v[14 + (cosA < 0.05 ? 0 : cosA < 0.2 ? 1 : 2)] += 1;
+    v[17] = std::max(v[17], dist);
+    v[18] = std::max(v[18], rel);
+  }
+};
+struct Tri3 { D3 a, b, c; };
+Tri3 tri_d(const Scene& s, uint32_t k) { return Tri3{d3(s.v[s.tri[3 * k]]), d3(s.v[s.tri[3 * k + 1]]), d3(s.v[s.tri[3 * k + 2]])}; }
+double omax(F3 o) { return std::max({std::fabs(o.x), std::fabs(o.y), std::fabs(o.z)}); }
+
+// One visibility bit decided in float (visible_bit) and in double; the category of a difference.
+int recheck_bit(const Engine& g, F3 o, F3 n, F3 dir, bool cull, double edgeRel, Tally& T) {
+  const bool f = visible_bit(g, o, n, dir, cull);
+  const D3 od = d3(o), dd = d3(dir), nd = d3(n);
+  const double cd = ddot(nd, dd);
+  const bool cullF = n.x * dir.x + n.y * dir.y + n.z * dir.z > 0.f;
+  const Ray r = make_ray(o, dir);
+  const double tmin = double(1e-5f);
+  bool dvis = cd > 0;
+  std::vector<uint32_t> cand;
+  if (cullF || dvis) for_candidates(*g.sc, r, [&](uint32_t k) { cand.push_back(k); });
+  if (dvis) {
+    int own = 0;
+    for (uint32_t k : cand) {
+      const Tri3 t = tri_d(*g.sc, k);
+      HitD h;
+      if (!hit_tri_d(r, od, dd, t.a, t.b, t.c, tmin, INFINITY, cull, h)) continue;
+      if (own_hit_d(t.a, t.b, t.c, h, dd, nd, nullptr) && ++own <= 3) continue;
+      dvis = false;
+      break;
+    }
+  }
+  if (cullF) T.v[0] += 1;
+  if (f == dvis) return kAgree;
+  T.v[1] += 1;
+  if ((cd > 0) != cullF) return kThreshold;   // the hemisphere's sign test
+  // the triangles the two tests hit differently, and hits whose own-plane status differs
+  double best = INFINITY, bestRel = INFINITY, bestCos = 1;
+  bool member = false, thresh = false;
+  for (uint32_t k : cand) {
+    const Tri3 t = tri_d(*g.sc, k);
+    const F3 a = g.sc->v[g.sc->tri[3 * k]], b = g.sc->v[g.sc->tri[3 * k + 1]], c = g.sc->v[g.sc->tri[3 * k + 2]];
+    Hit hf;
+    HitD hd;
+    const bool fh = hit_tri(r, a, b, c, 1e-5f, INFINITY, cull, hf), dh = hit_tri_d(r, od, dd, t.a, t.b, t.c, tmin, INFINITY, cull, hd);
+    if (fh != dh) {
+      Hit x;
+      HitD y;
+      const bool fe = hit_tri(r, a, b, c, -INFINITY, INFINITY, cull, x), de = hit_tri_d(r, od, dd, t.a, t.b, t.c, -INFINITY, INFINITY, cull, y);
+      if (fe == de) { thresh = true; continue; }   // the same edge decision: the t range's bound decided
+      double dist, cosA, tp;
+      edge_metrics(od, dd, t.a, t.b, t.c, dist, cosA, tp);
+      const double rel = dist / (omax(o) + std::fabs(tp) + 1e-30);
+      if (!member || rel < bestRel) { best = dist; bestRel = rel; bestCos = cosA; }
+      member = true;
+    } else if (fh) {
+      hf.prim = k;
+      const bool of = own_hit(*g.sc, hf, dir, n), od2 = own_hit_d(t.a, t.b, t.c, hd, dd, nd, nullptr);
+      if (of != od2) thresh = true;
+    }
+  }
+  if (member) {
+    T.flip_metrics(best, bestRel, bestCos);
+    if (bestCos < 0.05) return kGrazing;
+    return bestRel <= edgeRel ? kEdge : kOther;
+  }
+  return thresh ? kThreshold : kOther;
+}
+
+// One view ray decided in float (view_ray) and in double: classes and distances; the category of a difference.
+// out flags: bit 0 class differs, bit 1 distance differs (beyond 1e-5 t + 1e-4 m, the reference's distance check).
+int recheck_view(const Engine& g, F3 o, F3 nn, F3 dir, bool none, bool cull, const kgb_view_in& v, double edgeRel, Tally& T) {
+  uint8_t clF;
+  float tF;
+  view_ray(g, o, nn, dir, none, cull, v, clF, tF);
+  if (clF == 254 || none) { T.v[0] += 1; return kAgree; }
+  const D3 od = d3(o), dd = d3(dir), nd = d3(nn);
+  T.v[0] += 1;
+  if (v.cull && ((ddot(nd, dd) <= 0) != (dot(nn, dir) <= 0.f))) { T.v[1] += 1; T.v[19] += 1; return kThreshold; }
+  if (v.vground && dir.z < 0.f && !(o.z > v.groundZ)) return kAgree;   // exact comparisons: the same in double
+  const bool plane = v.vground && dir.z < 0.f;
+  const double gz = v.groundZ;
+  const double tg = plane ? (od.z - gz) / -dd.z : INFINITY;
+  const double tmax = plane ? (od.z - gz + double(0.01f)) / -dd.z : double(FLT_MAX);
+  const double tmin = double(1e-5f);
+  const Ray r = make_ray(o, dir);
+  std::vector<HitD> hits;
+  std::vector<uint32_t> cand;
+  for_candidates(*g.sc, r, [&](uint32_t k) { cand.push_back(k); });
+  for (uint32_t k : cand) {
+    const Tri3 t = tri_d(*g.sc, k);
+    HitD h;
+    if (hit_tri_d(r, od, dd, t.a, t.b, t.c, tmin, tmax, cull, h)) { h.prim = k; hits.push_back(h); }
+  }
+  std::sort(hits.begin(), hits.end(), [](const HitD& a, const HitD& b) { return a.t < b.t || (a.t == b.t && a.prim < b.prim); });
+  uint8_t clD = 2;
+  double tD = INFINITY;
+  unsigned own = 0, panes = 0;
+  double last = -INFINITY;
+  uint32_t decider = ~0u;
+  bool ended = false;
+  for (const HitD& h : hits) {
+    if (!(h.t > last)) continue;   // the float walk resumes past the hit's distance
+    const Tri3 t = tri_d(*g.sc, h.prim);
+    tD = h.t;
+    last = h.t;
+    decider = h.prim;
+    if (own_hit_d(t.a, t.b, t.c, h, dd, nd, nullptr)) { if (++own == 4) { ended = true; break; } continue; }
+    const uint8_t lb = g.label.empty() ? 2 : g.label[h.prim];
+    if (lb != KGB_LABEL_PASS) { clD = lb; ended = true; break; }
+    if (++panes > KGB_MAX_PANES) { ended = true; break; }
+  }
+  if (!ended) { clD = dir.z >= 0.f ? 0 : 1; tD = tg; decider = ~0u; }
+  if (panes) clD |= KGB_VIEW_GLAZED;
+  const bool clsDiff = clD != clF;
+  if (!clsDiff && ended && tD > 0) T.v[21] = std::max(T.v[21], std::fabs(double(tF) - tD) / tD);
+  const bool distDiff = !clsDiff && std::isfinite(tD) && std::fabs(double(tF) - tD) > 1e-5 * tD + 1e-4;
+  if (!clsDiff && !distDiff) return kAgree;
+  T.v[1] += 1;
+  T.v[clsDiff ? 19 : 20] += 1;
+  // the float walk's deciding hit
+  uint32_t fDecider = ~0u;
+  double tFd = 0;
+  {
+    float tmn = 1e-5f;
+    unsigned ow = 0, pn = 0;
+    const float tmaxF = plane ? (o.z - v.groundZ + 0.01f) / -dir.z : FLT_MAX;
+    for (;;) {
+      Hit hh;
+      if (!closest(*g.sc, r, tmn, tmaxF, cull, hh)) break;
+      fDecider = hh.prim; tFd = hh.t;
+      if (own_hit(*g.sc, hh, dir, nn)) { if (++ow == 4) break; }
+      else {
+        const uint8_t lb = g.label.empty() ? 2 : g.label[hh.prim];
+        if (lb != KGB_LABEL_PASS) break;
+        if (++pn > KGB_MAX_PANES) break;
+      }
+      tmn = next_up(hh.t);
+      fDecider = ~0u;
+    }
+  }
+  // a deciding hit at the downward ray's end (1 cm below the ground plane): the reference's 1 mm exclusion
+  const double tEnd = tmax;
+  if (plane && ((decider != ~0u && std::fabs(tD - tEnd) * -dd.z < 1e-3) || (fDecider != ~0u && std::fabs(tFd - tEnd) * -dd.z < 1e-3)))
+    return kThreshold;
+  // the triangles that decided: did the two tests hit them differently?
+  double best = INFINITY, bestRel = INFINITY, bestCos = 1;
+  bool member = false;
+  for (uint32_t k : {decider, fDecider}) {
+    if (k == ~0u) continue;
+    const Tri3 t = tri_d(*g.sc, k);
+    const F3 a = g.sc->v[g.sc->tri[3 * k]], b = g.sc->v[g.sc->tri[3 * k + 1]], c = g.sc->v[g.sc->tri[3 * k + 2]];
+    Hit hf;
+    HitD hd;
+    const bool fh = hit_tri(r, a, b, c, 1e-5f, plane ? (o.z - v.groundZ + 0.01f) / -dir.z : FLT_MAX, cull, hf);
+    const bool dh = hit_tri_d(r, od, dd, t.a, t.b, t.c, tmin, tmax, cull, hd);
+    if (fh == dh) continue;
+    double dist, cosA, tp;
+    edge_metrics(od, dd, t.a, t.b, t.c, dist, cosA, tp);
+    const double rel = dist / (omax(o) + std::fabs(tp) + 1e-30);
+    if (!member || rel < bestRel) { best = dist; bestRel = rel; bestCos = cosA; }
+    member = true;
+  }
+  if (member) {
+    T.flip_metrics(best, bestRel, bestCos);
+    if (bestCos < 0.05) return kGrazing;
+    return bestRel <= edgeRel ? kEdge : kOther;
+  }
+  // both deciding triangles hit in both precisions: the same triangle (the float distance's rounding), the order of
+  // two close hits, or an own-plane rule decided differently
+  if (decider == fDecider && !clsDiff) return decider != ~0u ? kRounding : kOther;
+  if (decider != ~0u && fDecider != ~0u && decider != fDecider && std::fabs(tD - tFd) <= 1e-5 * std::max(tD, tFd)) return kTie;
+  for (uint32_t k : {decider, fDecider}) {   // a deciding hit whose own-plane status differs
+    if (k == ~0u) continue;
+    const Tri3 t = tri_d(*g.sc, k);
+    const F3 a = g.sc->v[g.sc->tri[3 * k]], b = g.sc->v[g.sc->tri[3 * k + 1]], c = g.sc->v[g.sc->tri[3 * k + 2]];
+    Hit hf;
+    HitD hd;
+    if (hit_tri(r, a, b, c, 1e-5f, INFINITY, cull, hf) && hit_tri_d(r, od, dd, t.a, t.b, t.c, tmin, INFINITY, cull, hd)) {
+      hf.prim = k;
+      if (own_hit(*g.sc, hf, dir, nn) != own_hit_d(t.a, t.b, t.c, hd, dd, nd, nullptr)) return kThreshold;
+    }
+  }
+  return kOther;
+}
+
+void tally_out(const std::vector<Tally>& per, const std::vector<int64_t>& firstOther, size_t i0, double* out) {
+  for (int k = 0; k < 24; ++k) out[k] = 0;
+  out[22] = out[23] = -1;
+  for (size_t i = 0; i < per.size(); ++i) {
+    for (int k = 0; k < 22; ++k) out[k] = (k == 17 || k == 18 || k == 21) ? std::max(out[k], per[i].v[k]) : out[k] + per[i].v[k];
+    if (firstOther[i] >= 0 && out[22] < 0) { out[22] = double(i0 + i); out[23] = double(firstOther[i]); }
+  }
+}
+}  // namespace
+
+extern "C" {
+// out[24] (doubles, summed over the chunk's rays): [0] rays traced (bits: past the hemisphere cull), [1] rays decided
+// differently in double, of which [2] edge, [3] grazing, [4] threshold, [5] tie, [6] rounding, [7] other; [8..13] the
+// nearest-edge distance of the differences with a triangle hit differently, bins < 1e-7, 1e-6, 1e-5, 1e-4, 1e-3,
+// >= 1e-3 m; [14..16] their |cos|: < 0.05, < 0.2, >= 0.2; [17] the largest such distance (m), [18] the largest relative
+// to |o|max + t; [19] class differences, [20] distance-only differences (views); [21] the largest relative difference
+// between the float and the double distance over the rays whose class agrees and that end on a hit (views); [22], [23]
+// sensor and direction of the first ray of category other (-1: none).
+// Test-only: 0 switches refine_t off (the float walk's own distances), 1 back on; a test plants that error and checks
+// that the FP64 re-decision catches it.
+KGB_API void kgbo_set_refine(int on) { g_refine = on != 0; }
+
+KGB_API int kgbo_recheck_bits(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, double edgeRel, double* out) {
+  Engine& g = *reinterpret_cast<Engine*>(e);
+  if (i0 + nc > g.nSensors) return fail("kgbo_recheck_bits: sensor range exceeds the scene");
+  const bool cull = (rayFlags & KGB_RAY_CULL_BACK_FACING) != 0;
+  std::vector<Tally> per(nc);
+  std::vector<int64_t> firstOther(nc, -1);
+  par_for(nc, [&](size_t i) {
+    const F3 n = g.N[i0 + i], o = offset_ray(g.P[i0 + i], n);
+    for (size_t d = 0; d < g.nDir; ++d) {
+      const int c = recheck_bit(g, o, n, g.D[d], cull, edgeRel, per[i]);
+      if (c) per[i].v[1 + c] += 1;
+      if (c == kOther && firstOther[i] < 0) firstOther[i] = int64_t(d);
+    }
+  });
+  tally_out(per, firstOther, i0, out);
+  return 1;
+}
+
+KGB_API int kgbo_recheck_view(kgb_engine* e, size_t i0, size_t nc, uint32_t rayFlags, const kgb_view_in* v, double edgeRel, double* out) {
+  Engine& g = *reinterpret_cast<Engine*>(e);
+  if (i0 + nc > g.nSensors) return fail("kgbo_recheck_view: sensor range exceeds the scene");
+  const size_t K = size_t(v->nAz) * v->nEl;
+  const bool cull = (rayFlags & KGB_RAY_CULL_BACK_FACING) != 0;
+  const double rad = v->north * KGB_PI_D / 180;
+  const float cosN = float(std::cos(rad)), sinN = float(std::sin(rad));
+  std::vector<float> rs(v->rowSin, v->rowSin + 2 * size_t(v->nEl));
+  std::vector<Tally> per(nc);
+  std::vector<int64_t> firstOther(nc, -1);
+  par_for(nc, [&](size_t i) {
+    const unsigned gi = unsigned(i0 + i), element = gi / v->nS, side = v->nS == 2 ? gi % 2 : unsigned(v->back != 0);
+    const F3 nn = g.N[i0 + i], o = offset_ray(g.P[i0 + i], nn);
+    const bool none = !(dot(nn, nn) > 0.f);
+    F3 f, r, u;
+    view_frame(nn, v->world != 0, cosN, sinN, f, r, u);
+    for (size_t d = 0; d < K; ++d) {
+      const unsigned col = unsigned(d % v->nAz), row = unsigned(d / v->nAz);
+      const F3 l = view_cell(unsigned(d), col, rs[2 * row], rs[2 * row + 1], v->az0, v->dAz, v->jitter != 0, element, side);
+      const F3 dir = add(add(mul(l.x, r), mul(l.y, f)), mul(l.z, u));
+      const int c = recheck_view(g, o, nn, dir, none, cull, *v, edgeRel, per[i]);
+      if (c) per[i].v[1 + c] += 1;
+      if (c == kOther && firstOther[i] < 0) firstOther[i] = int64_t(d);
+    }
+  });
+  tally_out(per, firstOther, i0, out);
+  return 1;
+}
 }  // extern "C"

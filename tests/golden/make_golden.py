@@ -9,7 +9,7 @@ written with its inputs and results to tests/golden/<case>/. The tests replay th
 It also extracts the reference's published outputs for tests/box.obj from its docs (docs/daylight.md, docs/views.md:
 the example blocks) into published.json, and checks the recorded runs against them.
 
-usage: python tests/golden/make_golden.py [--ref /root/reference]
+usage: python tests/golden/make_golden.py [--ref REFERENCE_CHECKOUT]  (default: $KITSIM_REFERENCE, else ../reference beside the repo)
 """
 import argparse
 import ctypes
@@ -221,7 +221,7 @@ def sky_goldens(ref):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("KITSIM_REFERENCE") or os.path.join(os.path.dirname(REPO), "reference"))
     ap.add_argument("--case")
     a = ap.parse_args()
     if a.case:

@@ -30,6 +30,16 @@ def load_calls(case):
     return calls, arr
 
 
+def urban_sky():
+    """The urban block's direction table D [nDir x 3] and its per-quantity weights [(W, useCos)] as the reference's host
+    code made them (the last gpu_set_scene of the urban_sky recording and the gpu_reduce calls after it)."""
+    calls, arr = load_calls("urban_sky")
+    last = max(i for i, c in enumerate(calls) if c["call"] == "gpu_set_scene")
+    D = arr(calls[last], "D").reshape(-1, 3)
+    Ws = [(arr(c, "W"), bool(c["useCos"])) for c in calls[last:] if c["call"] == "gpu_reduce"]
+    return D, Ws
+
+
 def _slots(raw, kgb):
     n = raw.size // 16
     return (kgb.Slot * max(n, 1)).from_buffer_copy(raw.tobytes() if n else bytes(16))

@@ -9,7 +9,7 @@ import pytest
 
 from conftest import REPO
 
-REF = os.environ.get("KGB_REFERENCE", "/root/reference")
+REF = os.environ.get("KITSIM_REFERENCE") or os.path.join(os.path.dirname(REPO), "reference")
 pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src")), reason="reference tree not present (GPU box)")
 
 
