@@ -331,7 +331,7 @@ def run_ours(args, pkg):
     e.close()
     if rank == 0 and world == 1 and not args.no_extras and not args.sensors:
         # the other measured configurations, after the timed region: each keeps its own metric and config
-        for key, fn in (("precision", run_precision), ("views", run_views), ("serving", run_serving)):
+        for key, fn in (("precision", run_precision), ("views", run_views), ("serving", run_serving), ("serving_series", run_serving_series)):
             t0 = time.perf_counter()
             try:
                 line[key] = fn(args, pkg)
@@ -706,6 +706,91 @@ def run_serving(args, pkg):
     return line
 
 
+# ---------------------------------------------------------------------------------------------- serving: time series
+def run_serving_series(args, pkg):
+    """North_star's serving target: daylight requests with hourly time series at 2305 patches + ground (the precision
+    configuration's sky, opaque scene: the serving form traces visibility bits) through the server, each batch's series
+    chunks of every request in it as one grouped split-BF16 tensor-core launch, against the plain FP32 form one request
+    per launch (trace, the ground reduce, kgb_series in its FP32 form) on the same GPU. Requests: seeded, sensors
+    log-uniform 1k..30k (contiguous ranges of the urban block), time ranges log-uniform 1 day .. 1 year, all submitted
+    at once (throughput); solves = sensors x series columns."""
+    import torch
+    torch.cuda.set_device(0)
+    kgb, lib = pkg.kgb, pkg.load()
+    mf = 4
+    e = pkg.engine()
+    Dsky, omega = pkg.workloads.patch_dirs(mf)
+    w = np.load(os.path.join(GOLDEN, "urban_sky", "weather.npy"))
+    yr = pkg.workloads.urban_year_sky(e, mf, w)
+    col = (w[0] + w[1]) > 1e-4
+    colOf = np.cumsum(col) - 1
+    sun = e.sun_noaa(np.stack([np.full(8760, 52.52), np.full(8760, 13.41), np.full(8760, 1.0), np.repeat(np.arange(1, 13), [24 * d for d in
+                                [31, 28, 31, 30, 31, 30, 31, 31, 30, 31, 30, 31]]),
+                               np.concatenate([np.repeat(np.arange(1, d + 1), 24) for d in [31, 28, 31, 30, 31, 30, 31, 31, 30, 31, 30, 31]]),
+                               np.tile(np.arange(24) + 0.5, 365), np.zeros(8760)], axis=1))
+    scene = pkg.workloads.urban_block()
+    P = len(Dsky)
+    rng = np.random.default_rng(args.series_seed)
+    reqs = []
+    for k in range(args.series_requests):
+        n = int(np.exp(rng.uniform(np.log(1000), np.log(30000))))
+        first = int(rng.integers(0, len(scene["P"]) - n))
+        days = float(np.exp(rng.uniform(0, np.log(365))))
+        h0 = int(rng.integers(0, 8760 - int(days * 24) + 1))
+        hrs = np.arange(h0, h0 + max(1, int(days * 24)))
+        hcols = hrs[col[hrs]]
+        if not len(hcols):
+            continue
+        cols = colOf[hcols]
+        ups = hrs[(sun[hrs, 2] > 0) & col[hrs]]
+        sunVec = sun[ups, 3:6].astype(np.float32)
+        D = np.concatenate([Dsky, -Dsky, sunVec]).astype(np.float32)
+        Wg = np.zeros(len(D), np.float32)
+        Wg[P:2 * P] = omega
+        Wr = np.zeros(len(D), np.float32)
+        Wr[:P] = omega * 0.1
+        Wr[2 * P:] = w[0][ups].astype(np.float32)
+        si = dict(nSky=P, row=np.arange(P, dtype=np.int32), wsky=omega, S=np.ascontiguousarray(yr["S"][:, cols]), g=np.ascontiguousarray(yr["g"][cols]),
+                  sun0=2 * P, sunStep=(colOf[ups] - cols[0]).astype(np.int32), sunVec=sunVec, sunW=w[0][ups].astype(np.float32))
+        reqs.append(dict(P=scene["P"][first:first + n], N=scene["N"][first:first + n], D=D, W=np.stack([Wg, Wr]), si=si))
+    solves = sum(len(r["P"]) * r["si"]["S"].shape[1] for r in reqs)
+    # the server: every request submitted at once
+    srv = kgb.Server(lib, 150e9)
+    sid = srv.add_scene(scene["v"], scene["tri"])
+    srv.autotune()
+    t0 = time.perf_counter()
+    tickets = [srv.submit_series(sid, r["P"], r["N"], r["D"], r["W"], [True, True], 0, **r["si"]) for r in reqs]
+    for t in tickets:
+        srv.wait(t, 600)
+    wall = time.perf_counter() - t0
+    st, tm = srv.stats(), srv.timing()
+    srv.close()
+    # the plain FP32 form: one request after another through the single-request entry points
+    e.build(scene["v"], scene["tri"])
+    e.set_series_form(1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for r in reqs:
+        e.set_scene(r["P"], r["N"], r["D"])
+        e.trace(0, len(r["P"]), lib.ray_flags(False, False))
+        G = e.reduce(len(r["P"]), r["W"][0], True)
+        e.reduce(len(r["P"]), r["W"][1], True)
+        e.series(len(r["P"]), G=G.astype(np.float32), **r["si"])
+    plain = time.perf_counter() - t0
+    e.set_series_form(0)
+    e.close()
+    return {"metric": "radiation solves/s (time series, serving)", "unit": "sensor-steps/s", "value": solves / wall,
+            "plain_fp32_one_request_per_launch": solves / plain, "speedup_vs_plain_fp32": plain / wall,
+            "p50_ms": 1e3 * st["p50_s"], "p99_ms": 1e3 * st["p99_s"], "wall_s": wall, "plain_s": plain,
+            "gpu": {"daylight_s": tm["day_gpu_s"], "queued_s": tm["queued_s"]}, "server": {k: st[k] for k in ("completed", "items", "chunk_sensors", "batch_rays")},
+            "config": {"workload": "%d daylight requests with hourly series on the urban block (%d triangles): 2305 patches + ground, sensors "
+                                   "log-uniform 1k..30k (%d in all), time ranges log-uniform 1 day..1 year (%d series columns in all), "
+                                   "submitted at once" % (len(reqs), len(scene["tri"]), sum(len(r["P"]) for r in reqs),
+                                                         sum(r["si"]["S"].shape[1] for r in reqs)),
+                       "solves": solves},
+            "dtype": "series: split-bf16 on tcgen05 (server) vs fp32 SIMT (plain form)"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -716,7 +801,9 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=20000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sensors", type=int, default=0, help="urban / precision / views: only the first N sensors (a small case for profiling)")
-    ap.add_argument("--config", default="urban", choices=["urban", "precision", "views", "serving"])
+    ap.add_argument("--config", default="urban", choices=["urban", "precision", "views", "serving", "serving_series"])
+    ap.add_argument("--series-requests", type=int, default=24)
+    ap.add_argument("--series-seed", type=int, default=12)
     ap.add_argument("--builder", type=int, default=1, choices=[0, 1], help="urban: 1 device LBVH with treelets (default), 0 host binned-SAH tree")
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--window", type=float, default=2.0)
@@ -731,6 +818,8 @@ def main():
         print(json.dumps(run_views(args, pkg)), flush=True)
     elif args.config == "serving":
         print(json.dumps(run_serving(args, pkg)), flush=True)
+    elif args.config == "serving_series":
+        print(json.dumps(run_serving_series(args, pkg)), flush=True)
     elif args.impl == "reference":
         run_reference(args, pkg)
     else:

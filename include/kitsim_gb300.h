@@ -263,6 +263,17 @@ typedef struct kgb_views_request {
   uint32_t isoDim;
   double* out;                 /* [nSensors x NA], gpu_reduce_view's columns */
 } kgb_views_request;
+/* A daylight request's hourly time series (the reference's --timeseries: gpu_series per chunk, src/run.cpp:672-687,
+ * src/gpu.cu:639-669), computed inside the server's daylight batches: in.* as for kgb_series (nSky, row, wsky, S, P, T,
+ * g, sun0, nSun, sunStep, sunVec, sunW; G and Sdc must be NULL: G is the request's quantity gQ, its sums as float, as
+ * run.cpp passes its ground reduce; the server has no reflected light). Every batch's series chunks, of any number of
+ * requests, run as ONE grouped split-BF16 tensor-core launch (at most 48 chunks), the rows of E bit-identical to
+ * kgb_series' tensor-core form on the same inputs. One sun direction per step (the tensor-core form's sun term). */
+typedef struct kgb_series_request {
+  kgb_series_in in;
+  uint32_t gQ;   /* the quantity of the request whose sums give G */
+  float* E;      /* [nSensors x T] out */
+} kgb_series_request;
 KGB_API kgb_server* kgb_server_create(uint64_t hbmBudgetBytes);
 KGB_API void kgb_server_destroy(kgb_server* s);
 /* a resident scene (8-wide BVH) for requests; *sceneId its index */
@@ -274,6 +285,9 @@ KGB_API int kgb_server_autotune(kgb_server* s);
 KGB_API int kgb_server_set_tuning(kgb_server* s, uint32_t chunkSensors, uint64_t batchRays, uint64_t viewRays);
 KGB_API int kgb_server_submit(kgb_server* s, const kgb_daylight_request* r, uint64_t* ticket);
 KGB_API int kgb_server_submit_views(kgb_server* s, const kgb_views_request* r, uint64_t* ticket);
+/* a daylight request that also gives its time series (its host arrays, the series' included, valid until it is waited
+ * for) */
+KGB_API int kgb_server_submit_series(kgb_server* s, const kgb_daylight_request* r, const kgb_series_request* q, uint64_t* ticket);
 /* 1 once the request completed (its out written), 0 on failure or timeout (kgb_last_error) */
 KGB_API int kgb_server_wait(kgb_server* s, uint64_t ticket, double timeoutSec);
 /* out[10]: completed requests, latency p50, p90, p99, max (s), rays, work items (daylight batches and views chunks), HBM

@@ -171,16 +171,22 @@ struct SeriesOperands {
   const int32_t* patchDirs;
   const float* wsky;
   const float* G;
+  const double* G64;   // when G is null: the ground sums as doubles, rounded to float here (a serving batch's reduce)
   const float* dc;
   const float* S;
   const float* g;
   const float* Sdc;
   bool rebuildS;
+  bool buildV = true;  // false: S^T only (a serving request's pieces, built once at its upload)
 };
 void build_series_operands(const SeriesTcPlan& p, const SeriesOperands& o, cudaStream_t st);
 const char* series_tc(const SeriesTcPlan& p, cudaStream_t st);   // null, or what failed
 // the rows of 128-sensor tiles mBase .. mBase + mCount - 1 only (E's rows mBase * 128 .. , the others untouched)
 const char* series_tc_rows(const SeriesTcPlan& p, uint32_t mBase, uint32_t mCount, cudaStream_t st);
+// n whole contractions (each its own operands, K and output) in one launch of the same kernel (at most
+// kMaxSeriesGroup); each output is the one series_tc would give it, bit for bit
+constexpr uint32_t kMaxSeriesGroup = 48;
+const char* series_tc_group(const SeriesTcPlan* plans, uint32_t n, cudaStream_t st);
 
 // What a reduce of the last trace reads, for the reduce entry points outside engine.cu (reduce_noalloc.cu).
 struct ReduceInputs {

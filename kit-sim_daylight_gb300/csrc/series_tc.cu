@@ -162,21 +162,41 @@ __device__ __forceinline__ unsigned long long sub2(unsigned long long a, unsigne
   return r;
 }
 
-struct SeriesTcArgs {
-  uint32_t nc, T, Kp, mTiles, nTiles;
-  uint32_t mBase;            // the launch's first row of tiles (a launch covers rows of tiles mBase .. mBase + mTiles - 1)
+// One contraction of a launch: the rows of tiles mBase .. mBase + mTiles - 1 of one chunk's E (a band of a chunk, or a
+// request's chunk in a serving batch), with its own operands, K extent and sun term.
+struct TcSeg {
+  CUtensorMap mapV;          // the three pieces of V stacked as rows [3 nc x Kp]
+  CUtensorMap mapS;          // the pieces of S^T stacked as [3 T x Kp]
   // sun term of the epilogue (the reference's k_series tail, gpu.cu:145-148): column t's sun direction, if any
   const int32_t* sunOfCol;   // [T] -> j or -1
   const float* sunVec;       // [nSun x 3]
   const float* sunW;         // [nSun]
-  uint32_t sun0;
-  const uint32_t* bits;      // visibility (bits, or bytes when non-null)
+  const uint32_t* bits;      // visibility (bits, or bytes when non-null), rows of nc sensors
   const uint8_t* bytes;
   const float* N;            // chunk normals
   float* E;                  // [nc x T]
+  uint32_t nc, T, Kp, sun0;
+  uint32_t mBase, mTiles, nTiles;
+  uint32_t tileBase;         // the launch's tiles tileBase .. tileBase + mTiles x nTiles - 1 are this contraction's
+};
+constexpr uint32_t kMaxTcSegs = kMaxSeriesGroup;   // contractions of one launch: their tensor maps travel as kernel parameters
+struct TcGroup {
+  TcSeg seg[kMaxTcSegs];
+  uint32_t nSegs, nTiles;
   uint32_t* status;
   uint64_t waitLimitNs;      // the pipeline's mbarrier waits give up past this (kWaitLimitNs)
 };
+static_assert(sizeof(TcGroup) <= 32000, "the group fits the 32 KB of kernel parameters");
+
+// the contraction that launch tile `tile` belongs to (tiles are numbered contraction after contraction)
+__device__ __forceinline__ uint32_t tc_seg_of(const TcGroup& g, uint32_t tile) {
+  uint32_t lo = 0, hi = g.nSegs - 1;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1) / 2;
+    if (g.seg[mid].tileBase <= tile) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
 
 // Tile order: bands of kBand step-tiles; within a band every row of tiles, steps fastest. The CTAs running at once share
 // a few V panels and the band's S panels (16 x 64 steps x K x 6 B, some 30 MB at K 4672), which stay in L2 for the
@@ -193,11 +213,12 @@ __device__ __forceinline__ float dotf_rn(const float* n, const float* d) {
   return __fadd_rn(__fadd_rn(__fmul_rn(n[0], d[0]), __fmul_rn(n[1], d[1])), __fmul_rn(n[2], d[2]));
 }
 
-// mapV: the three pieces of V stacked as rows [3 nc x Kp]; mapS: the pieces of S^T stacked as [3 T x Kp]. Piece p of
-// an operand tile at rows r0 is at rows r0 + p nc (p T); rows past a piece's end read the next piece's rows (or the
-// zero fill), which only reach accumulator rows and columns that are never stored.
-__global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant__ CUtensorMap mapV, const __grid_constant__ CUtensorMap mapS,
-                                                          SeriesTcArgs a) {
+// Per contraction, mapV holds the three pieces of V stacked as rows [3 nc x Kp] and mapS those of S^T as [3 T x Kp].
+// Piece p of an operand tile at rows r0 is at rows r0 + p nc (p T); rows past a piece's end read the next piece's rows
+// (or the zero fill), which only reach accumulator rows and columns that are never stored. Every role walks the same
+// tiles in the same order, each tile with its contraction's K blocks, so the pipeline's phases stay in step across
+// contractions of different K.
+__global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant__ TcGroup g) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
@@ -225,26 +246,27 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmemBase = *tmemSlot;
-  const uint32_t kBlocks = a.Kp / BK;
-  const uint32_t nTilesAll = a.mTiles * a.nTiles;
+  const uint32_t nTilesAll = g.nTiles;
 
   if (warp == 0) {
     if (lane == 0) {   // ---------------- TMA producer
       uint32_t stage = 0, phase = 0;
       uint32_t filled = 0, fillParity = 0;   // bit s: stage s received a fill; the phase parity of its last one
       for (uint32_t tile = blockIdx.x; tile < nTilesAll && !abortFlag; tile += gridDim.x) {
+        const TcSeg& a = g.seg[tc_seg_of(g, tile)];
         uint32_t tm, tn;
-        tile_coords(tile, a.mTiles, a.nTiles, tm, tn);
+        tile_coords(tile - a.tileBase, a.mTiles, a.nTiles, tm, tn);
         const int m0 = int(tm + a.mBase) * BM, n0 = int(tn) * BN;
+        const uint32_t kBlocks = a.Kp / BK;
         for (uint32_t kb = 0; kb < kBlocks; ++kb) {
-          if (!mbar_wait(&empty[stage], phase ^ 1, a.status, a.waitLimitNs)) { abortFlag = 1; break; }
+          if (!mbar_wait(&empty[stage], phase ^ 1, g.status, g.waitLimitNs)) { abortFlag = 1; break; }
           uint8_t* s = smem + stage * STAGE_BYTES;
           mbar_expect_tx(&full[stage], STAGE_BYTES);
           const int k0 = int(kb) * BK;
 #pragma unroll
           for (int p = 0; p < PIECES; ++p) {
-            tma_load_2d(s + p * V_TILE, &mapV, k0, m0 + p * int(a.nc), &full[stage]);
-            tma_load_2d(s + PIECES * V_TILE + p * S_TILE, &mapS, k0, n0 + p * int(a.T), &full[stage]);
+            tma_load_2d(s + p * V_TILE, &a.mapV, k0, m0 + p * int(a.nc), &full[stage]);
+            tma_load_2d(s + PIECES * V_TILE + p * S_TILE, &a.mapS, k0, n0 + p * int(a.T), &full[stage]);
           }
           filled |= 1u << stage;
           fillParity = (fillParity & ~(1u << stage)) | (phase << stage);
@@ -254,7 +276,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
       // A stage's fill is issued only after the previous one was consumed, so only the last fill of each stage can be
       // in flight here: wait until it has landed.
       for (uint32_t st = 0; st < uint32_t(STAGES); ++st)
-        if ((filled >> st) & 1u) mbar_wait(&full[st], (fillParity >> st) & 1u, a.status, kWaitLimitNs);
+        if ((filled >> st) & 1u) mbar_wait(&full[st], (fillParity >> st) & 1u, g.status, kWaitLimitNs);
     }
     __syncwarp();
   } else if (warp == 1) {
@@ -262,12 +284,13 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
       uint32_t stage = 0, phase = 0, chunk = 0;
       for (uint32_t tile = blockIdx.x; tile < nTilesAll && !abortFlag; tile += gridDim.x) {
         bool ok = true;
+        const uint32_t kBlocks = g.seg[tc_seg_of(g, tile)].Kp / BK;
         for (uint32_t kb = 0; kb < kBlocks; ++kb, ++chunk) {   // a chunk: one K block, its sums from zero in [H | C1 | C2]
           const uint32_t hbuf = chunk % NH;
-          if (!mbar_wait(&hEmpty[hbuf], ((chunk / NH) & 1) ^ 1, a.status, a.waitLimitNs)) { ok = false; break; }
+          if (!mbar_wait(&hEmpty[hbuf], ((chunk / NH) & 1) ^ 1, g.status, g.waitLimitNs)) { ok = false; break; }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t hT = tmemBase + hbuf * kChunkCols;
-          if (!mbar_wait(&full[stage], phase, a.status, a.waitLimitNs)) { ok = false; break; }
+          if (!mbar_wait(&full[stage], phase, g.status, g.waitLimitNs)) { ok = false; break; }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint8_t* s = smem + stage * STAGE_BYTES;
           const uint64_t v0 = smem_desc(s), v1 = smem_desc(s + V_TILE), v2 = smem_desc(s + 2 * V_TILE);
@@ -287,7 +310,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
       }
       // tcgen05.commit tracks every MMA this thread issued before it: once the drain barrier completes, none runs
       mma_commit(drain);
-      mbar_wait(drain, 0, a.status, kWaitLimitNs);
+      mbar_wait(drain, 0, g.status, kWaitLimitNs);
     }
     __syncwarp();
   } else {   // ---------------- epilogue: warps 2..5
@@ -295,6 +318,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
     const uint32_t laneBase = (q * 32u) << 16;
     uint32_t chunk = 0;
     for (uint32_t tile = blockIdx.x; tile < nTilesAll; tile += gridDim.x) {
+      const TcSeg& a = g.seg[tc_seg_of(g, tile)];
+      const uint32_t kBlocks = a.Kp / BK;
       // each chunk's H + (C1 + C2), added with Kahan compensation (acc - cmp is the running sum); columns 2p and 2p + 1
       // share the packed pair p of acc and cmp
       unsigned long long acc[BN / 2], cmp[BN / 2];
@@ -303,7 +328,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
       bool ok = true;
       for (uint32_t ch = 0; ch < kBlocks; ++ch, ++chunk) {
         const uint32_t hbuf = chunk % NH;
-        ok = __all_sync(~0u, mbar_wait(&hFull[hbuf], (chunk / NH) & 1, a.status, a.waitLimitNs));
+        ok = __all_sync(~0u, mbar_wait(&hFull[hbuf], (chunk / NH) & 1, g.status, g.waitLimitNs));
         if (!ok || abortFlag) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t hAt = tmemBase + laneBase + hbuf * kChunkCols;
@@ -325,7 +350,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
       }
       if (!ok || abortFlag) { abortFlag = 1; break; }
       uint32_t tm, tn;
-      tile_coords(tile, a.mTiles, a.nTiles, tm, tn);
+      tile_coords(tile - a.tileBase, a.mTiles, a.nTiles, tm, tn);
       const uint32_t m0 = (tm + a.mBase) * BM, n0 = tn * BN;
       const uint32_t row = m0 + q * 32 + lane;         // this thread's sensor
       float nrm[3] = {0.f, 0.f, 0.f};
@@ -391,6 +416,7 @@ struct VBuildArgs {
   const int32_t* patchDirs;
   const float* wsky;
   const float* G;
+  const double* G64;           // used when G is null
   const float* dc;             // [nBins x nc] or null
   __nv_bfloat16* v;            // [3 x nc x Kp]: hi, mid, lo
 };
@@ -422,7 +448,7 @@ __global__ void __launch_bounds__(256) k_build_v(VBuildArgs a) {
           else at = float((a.bits[size_t(d >> 5) * a.nc + i] >> (d & 31)) & 1u);
           if (at != 0.f) v = __fadd_rn(v, __fmul_rn(__fmul_rn(fmaxf(dotf_rn(n, a.D + 3 * d), 0.f), at), a.wsky[d]));
         }
-      } else if (k == a.P) v = a.G[i];
+      } else if (k == a.P) v = a.G ? a.G[i] : __double2float_rn(a.G64[i]);
       else if (a.dc && k < a.P + 1 + a.nBins) v = a.dc[size_t(k - a.P - 1) * a.nc + i];
     }
     tile[kk][lane] = v;
@@ -501,37 +527,70 @@ static bool make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t K
 
 const char* series_tc(const SeriesTcPlan& p, cudaStream_t st) { return series_tc_rows(p, 0, (p.nc + BM - 1) / BM, st); }
 
-const char* series_tc_rows(const SeriesTcPlan& p, uint32_t mBase, uint32_t mCount, cudaStream_t st) {
-  if (p.nc == 0 || p.T == 0 || mCount == 0) return nullptr;
+// a contraction's parameters (its tensor maps encoded here), tiles from tileBase on; null or what failed
+static const char* tc_seg(const SeriesTcPlan& p, uint32_t mBase, uint32_t mCount, uint32_t tileBase, TcSeg& a) {
   if (uint64_t(mBase) + mCount > (p.nc + BM - 1) / BM) return "series_tc: rows of tiles beyond the chunk";
-  if (p.Kp % BK) return "series_tc: K not padded to 64";
-  CUtensorMap mV, mS;
-  if (!make_map(&mV, p.v, uint64_t(PIECES) * p.nc, p.Kp, BM) || !make_map(&mS, p.s, uint64_t(PIECES) * p.T, p.Kp, BN))
-    return "series_tc: cuTensorMapEncodeTiled failed";
+  if (p.Kp % BK || !p.Kp) return "series_tc: K not padded to 64";
   if (uint64_t(PIECES) * p.nc + BM > 0x7fffffffull || uint64_t(PIECES) * p.T + BN > 0x7fffffffull) return "series_tc: chunk too large";
+  if (!make_map(&a.mapV, p.v, uint64_t(PIECES) * p.nc, p.Kp, BM) || !make_map(&a.mapS, p.s, uint64_t(PIECES) * p.T, p.Kp, BN))
+    return "series_tc: cuTensorMapEncodeTiled failed";
+  a.nc = p.nc; a.T = p.T; a.Kp = p.Kp;
+  a.mTiles = mCount; a.mBase = mBase; a.nTiles = (p.T + BN - 1) / BN; a.tileBase = tileBase;
+  a.sunOfCol = p.sunOfCol; a.sunVec = p.sunVec; a.sunW = p.sunW; a.sun0 = p.sun0;
+  a.bits = p.bits; a.bytes = p.bytes; a.N = p.N; a.E = p.E;
+  return nullptr;
+}
+
+static const char* tc_launch(TcGroup& g, int numSMs, cudaStream_t st) {
   static bool attr = false;
   if (!attr) {
     if (cudaFuncSetAttribute(k_series_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) != cudaSuccess)
       return "series_tc: cannot reserve shared memory";
     attr = true;
   }
-  SeriesTcArgs a{};
-  a.nc = p.nc; a.T = p.T; a.Kp = p.Kp;
-  a.mTiles = mCount; a.mBase = mBase; a.nTiles = (p.T + BN - 1) / BN;
-  a.sunOfCol = p.sunOfCol; a.sunVec = p.sunVec; a.sunW = p.sunW; a.sun0 = p.sun0;
-  a.bits = p.bits; a.bytes = p.bytes; a.N = p.N; a.E = p.E; a.status = p.status;
-  a.waitLimitNs = kWaitLimitNs;
-  const int grid = int(std::min<uint32_t>(uint32_t(p.numSMs), a.mTiles * a.nTiles));
-  k_series_tc<<<grid, THREADS, SMEM_BYTES, st>>>(mV, mS, a);
+  g.waitLimitNs = kWaitLimitNs;
+  const int grid = int(std::min<uint32_t>(uint32_t(numSMs), g.nTiles));
+  k_series_tc<<<grid, THREADS, SMEM_BYTES, st>>>(g);
   return nullptr;
+}
+
+const char* series_tc_rows(const SeriesTcPlan& p, uint32_t mBase, uint32_t mCount, cudaStream_t st) {
+  if (p.nc == 0 || p.T == 0 || mCount == 0) return nullptr;
+  thread_local TcGroup* tg = new TcGroup;   // 18 KB, off the stack; the launch copies it
+  TcGroup& G = *tg;
+  G.nSegs = 1;
+  if (const char* why = tc_seg(p, mBase, mCount, 0, G.seg[0])) return why;
+  G.nTiles = mCount * G.seg[0].nTiles;
+  G.status = p.status;
+  return tc_launch(G, p.numSMs, st);
+}
+
+const char* series_tc_group(const SeriesTcPlan* plans, uint32_t n, cudaStream_t st) {
+  if (!n) return nullptr;
+  if (n > kMaxTcSegs) return "series_tc: more contractions than one launch holds";
+  thread_local TcGroup* tg = new TcGroup;
+  TcGroup& G = *tg;
+  G.nSegs = 0;
+  G.nTiles = 0;
+  for (uint32_t k = 0; k < n; ++k) {
+    const SeriesTcPlan& p = plans[k];
+    if (p.nc == 0 || p.T == 0) continue;
+    const uint32_t mCount = (p.nc + BM - 1) / BM;
+    if (const char* why = tc_seg(p, 0, mCount, G.nTiles, G.seg[G.nSegs])) return why;
+    G.nTiles += mCount * G.seg[G.nSegs].nTiles;
+    ++G.nSegs;
+  }
+  if (!G.nSegs) return nullptr;
+  G.status = plans[0].status;
+  return tc_launch(G, plans[0].numSMs, st);
 }
 
 void build_series_operands(const SeriesTcPlan& p, const SeriesOperands& o, cudaStream_t st) {
   VBuildArgs v{};
   v.bits = p.bits; v.bytes = p.bytes; v.nc = p.nc; v.P = o.P; v.nBins = o.nBins; v.Kp = p.Kp; v.N = p.N; v.D = o.D;
-  v.patchFirst = o.patchFirst; v.patchDirs = o.patchDirs; v.wsky = o.wsky; v.G = o.G; v.dc = o.dc;
+  v.patchFirst = o.patchFirst; v.patchDirs = o.patchDirs; v.wsky = o.wsky; v.G = o.G; v.G64 = o.G64; v.dc = o.dc;
   v.v = static_cast<__nv_bfloat16*>(p.v);
-  k_build_v<<<dim3((p.nc + 31) / 32, p.Kp / 64), 256, 0, st>>>(v);
+  if (o.buildV && p.nc) k_build_v<<<dim3((p.nc + 31) / 32, p.Kp / 64), 256, 0, st>>>(v);
   if (o.rebuildS)
     k_build_st<<<dim3((p.T + 31) / 32, p.Kp / 32), 256, 0, st>>>(o.S, o.g, o.Sdc, o.P, o.nBins, p.T, p.Kp, static_cast<__nv_bfloat16*>(p.s));
 }

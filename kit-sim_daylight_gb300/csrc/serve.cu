@@ -19,6 +19,12 @@
 // results are bit-identical to the request run alone through the single-request entry points (same kernels, same
 // per-sensor arithmetic and summation order).
 //
+// A daylight request may also ask for its hourly time series (kgb_server_submit_series). Its S matrix is split into
+// bf16 pieces once, at upload; in each batch, right after the batch's graph, the series chunks of every request in it
+// get their V rows from the batch's visibility bits and ground sums, and all of them run as ONE grouped launch of the
+// tensor-core contraction (series_tc_group: a tile table across the chunks, each with its own tensor maps, K and output
+// rows), whose rows come down with the batch. A request's rows equal kgb_series' tensor-core form bit for bit.
+//
 // The autotuner times calibration batches on the first scene at start-up and keeps the chunk size and batch size
 // (rays per batch) for the daylight pipeline: the fastest, or a smaller batch within 5 % of it.
 #include "engine.h"
@@ -128,6 +134,8 @@ constexpr uint32_t kMaxViewChunk = 65536;       // sensors in one views chunk
 constexpr uint32_t kMaxNA = 3 * KGB_VIEW_CLASSES + 1 + 8 + 1 + 1;   // views columns
 constexpr double kAgeSeconds = 0.3;             // the priority's age offset
 constexpr double kOldSeconds = 1.2;             // past this wait a request goes first, in arrival order
+constexpr size_t kSeriesVBytes = size_t(256) << 20;   // per daylight slot: the series chunks' V pieces (bf16)
+constexpr size_t kSeriesEBytes = size_t(256) << 20;   // per daylight slot: their rows of E, on the device and pinned
 
 struct DScene {
   void* nodes = nullptr;
@@ -148,12 +156,17 @@ struct Request {
   uint64_t raysPerSensor = 0;
   void* dev = nullptr;        // P, N, D, ray table, W (daylight) | P, N, rowSin, wRow, label (views)
   uint64_t devBytes = 0;
+  // the time series of a daylight request (kgb_server_submit_series)
+  bool series = false;
+  kgb_series_request sq{};
+  uint32_t Kp = 0;            // its K (patches + ground), padded to 64
+  std::vector<int32_t> csr, sunOfCol;   // directions per patch (first [P + 1], then the directions); sun per column
   Clock::time_point tSubmit, tDone;
   bool done = false, failed = false;
   std::string err;
 };
 
-struct Part { Request* r; uint32_t i0, n; };
+struct Part { Request* r; uint32_t i0, n; size_t eOff = 0, vOff = 0; };   // its series rows (floats) and V pieces (bytes) in the slot's pools
 
 // a daylight batch slot: its pinned and device buffers, its graph and the nodes set per batch
 struct DaySlot {
@@ -172,6 +185,12 @@ struct DaySlot {
   cudaEvent_t ev[2] = {nullptr, nullptr};
   std::vector<Part> parts;
   uint64_t rays = 0;
+  // series: the chunks' V pieces and rows of E (device), the rows again (pinned), the series' status word (pinned)
+  void* dV = nullptr;
+  float* dE = nullptr;
+  float* hE = nullptr;
+  uint32_t* hSeriesStatus = nullptr;
+  bool anySeries = false;
 };
 // a views chunk slot: its status and columns come back into pinned memory
 struct ViewSlot {
@@ -257,9 +276,29 @@ ViewLayout view_layout(const kgb_views_request& v, uint32_t nTris) {
   L.total = up256(L.offLab + (v.label ? nTris : 0));
   return L;
 }
+// a series request's device arrays after its daylight ones: S^T in three bf16 pieces [3 x T x Kp], S [P x T] and g [T]
+// (the pieces' source), the directions per patch, wsky, the sun direction of each column, sunVec, sunW
+struct SeriesLayout { size_t offSt, offS, offG, offCsr, offWsky, offSunCol, offSunVec, offSunW, total; };
+SeriesLayout series_layout(const Request& r, size_t base) {
+  const kgb_series_in& in = r.sq.in;
+  const size_t T = size_t(in.T), P = size_t(in.P);
+  SeriesLayout L;
+  L.offSt = base;
+  L.offS = up256(L.offSt + 3 * T * r.Kp * 2);
+  L.offG = up256(L.offS + P * T * 4);
+  L.offCsr = up256(L.offG + T * 4);
+  L.offWsky = up256(L.offCsr + (P + 1 + in.nSky) * 4);
+  L.offSunCol = up256(L.offWsky + size_t(in.nSky) * 4);
+  L.offSunVec = up256(L.offSunCol + T * 4);
+  L.offSunW = up256(L.offSunVec + size_t(in.nSun) * 12);
+  L.total = up256(L.offSunW + size_t(in.nSun) * 4);
+  return L;
+}
 uint32_t views_NA(const kgb_views_request& r) { return 3 * r.nClass + 1 + r.nReach + (r.glazing ? 1 : 0) + (r.isoDim ? 1 : 0); }
 uint64_t request_bytes(const Server& s, const Request* r) {
-  return r->kind == 0 ? day_layout(r->d).total : view_layout(r->v, s.scenes[size_t(r->v.scene)].nTris).total;
+  if (r->kind == 1) return view_layout(r->v, s.scenes[size_t(r->v.scene)].nTris).total;
+  const size_t day = day_layout(r->d).total;
+  return r->series ? series_layout(*r, day).total : day;
 }
 
 // one slot's graph: table up, counter reset, trace, reduce, sums and status down
@@ -352,6 +391,26 @@ bool upload(Server& s, Request* r, std::string& err) {
          cuok(cudaMemcpyAsync(b + L.offD, d.D, size_t(d.nDir) * 12, cudaMemcpyHostToDevice, s.up), err, "upload") &&
          cuok(cudaMemcpyAsync(b + L.offW, r->w64.data(), r->w64.size() * 8, cudaMemcpyHostToDevice, s.up), err, "upload");
     if (ok) launch_ray_table(reinterpret_cast<const float*>(b + L.offD), d.nDir, b + L.offTab, s.up);
+    if (ok && r->series) {   // the series inputs, and S^T split into its bf16 pieces once for every batch of the request
+      const kgb_series_in& in = r->sq.in;
+      const size_t T = size_t(in.T), P = size_t(in.P);
+      const SeriesLayout S = series_layout(*r, L.total);
+      ok = cuok(cudaMemcpyAsync(b + S.offS, in.S, P * T * 4, cudaMemcpyHostToDevice, s.up), err, "upload") &&
+           cuok(cudaMemcpyAsync(b + S.offG, in.g, T * 4, cudaMemcpyHostToDevice, s.up), err, "upload") &&
+           cuok(cudaMemcpyAsync(b + S.offCsr, r->csr.data(), r->csr.size() * 4, cudaMemcpyHostToDevice, s.up), err, "upload") &&
+           cuok(cudaMemcpyAsync(b + S.offWsky, in.wsky, size_t(in.nSky) * 4, cudaMemcpyHostToDevice, s.up), err, "upload") &&
+           cuok(cudaMemcpyAsync(b + S.offSunCol, r->sunOfCol.data(), T * 4, cudaMemcpyHostToDevice, s.up), err, "upload") &&
+           (!in.nSun || (cuok(cudaMemcpyAsync(b + S.offSunVec, in.sunVec, size_t(in.nSun) * 12, cudaMemcpyHostToDevice, s.up), err, "upload") &&
+                         cuok(cudaMemcpyAsync(b + S.offSunW, in.sunW, size_t(in.nSun) * 4, cudaMemcpyHostToDevice, s.up), err, "upload")));
+      if (ok) {
+        SeriesTcPlan p{};
+        p.T = uint32_t(T); p.Kp = r->Kp; p.s = b + S.offSt;
+        SeriesOperands o{};
+        o.P = uint32_t(P); o.S = reinterpret_cast<const float*>(b + S.offS); o.g = reinterpret_cast<const float*>(b + S.offG);
+        o.rebuildS = true; o.buildV = false;
+        build_series_operands(p, o, s.up);
+      }
+    }
   } else {
     const kgb_views_request& v = r->v;
     const ViewLayout L = view_layout(v, s.scenes[size_t(v.scene)].nTris);
@@ -409,6 +468,47 @@ double priority(const Server& s, const Request* r, Clock::time_point now) {
   return rem / (age + kAgeSeconds);
 }
 
+// The batch's series, after its graph on the work stream: each series chunk's V pieces from the batch's visibility
+// bits and its ground sums (quantity gQ), then every chunk's contraction in one grouped launch, then their rows and the
+// series' status word down into pinned memory.
+bool launch_series(Server& s, DaySlot& d, std::string& err) {
+  std::vector<SeriesTcPlan> plans;
+  for (size_t j = 0; j < d.parts.size(); ++j) {
+    const Part& p = d.parts[j];
+    if (!p.r->series) continue;
+    const Seg& g = d.hSegs[j];
+    const kgb_series_in& in = p.r->sq.in;
+    const char* b = static_cast<const char*>(p.r->dev);
+    const SeriesLayout L = series_layout(*p.r, day_layout(p.r->d).total);
+    SeriesTcPlan pl{};
+    pl.nc = p.n; pl.T = uint32_t(in.T); pl.Kp = p.r->Kp; pl.sun0 = in.sun0; pl.numSMs = s.numSMs;
+    pl.v = static_cast<char*>(d.dV) + p.vOff;
+    pl.s = const_cast<char*>(b) + L.offSt;
+    pl.sunOfCol = reinterpret_cast<const int32_t*>(b + L.offSunCol);
+    pl.sunVec = reinterpret_cast<const float*>(b + L.offSunVec);
+    pl.sunW = reinterpret_cast<const float*>(b + L.offSunW);
+    pl.bits = d.dBits + g.bitsOff;
+    pl.N = g.N;
+    pl.E = d.dE + p.eOff;
+    pl.status = d.dCtl + 1;
+    SeriesOperands o{};
+    o.P = uint32_t(in.P); o.D = g.D;
+    o.patchFirst = reinterpret_cast<const int32_t*>(b + L.offCsr); o.patchDirs = o.patchFirst + in.P + 1;
+    o.wsky = reinterpret_cast<const float*>(b + L.offWsky);
+    o.G64 = d.dOut + g.outOff + size_t(p.r->sq.gQ) * p.n;
+    o.rebuildS = false;
+    build_series_operands(pl, o, s.st);
+    plans.push_back(pl);
+  }
+  if (!cuok(cudaGetLastError(), err, "series operands")) return false;
+  if (const char* why = series_tc_group(plans.data(), uint32_t(plans.size()), s.st)) { err = why; return false; }
+  size_t eEnd = 0;
+  for (const Part& p : d.parts) if (p.r->series) eEnd = p.eOff + size_t(p.n) * uint32_t(p.r->sq.in.T);
+  return cuok(cudaGetLastError(), err, "series launch") &&
+         cuok(cudaMemcpyAsync(d.hE, d.dE, eEnd * 4, cudaMemcpyDeviceToHost, s.st), err, "series rows") &&
+         cuok(cudaMemcpyAsync(d.hSeriesStatus, d.dCtl + 1, 4, cudaMemcpyDeviceToHost, s.st), err, "series status");
+}
+
 // a daylight batch of the given parts into slot k, launched on the work stream
 bool launch_day(Server& s, int k, const std::vector<Part>& parts, std::string& err) {
   DaySlot& d = s.day[k];
@@ -440,6 +540,23 @@ bool launch_day(Server& s, int k, const std::vector<Part>& parts, std::string& e
   }
   d.hHdr->nSegs = uint32_t(parts.size()); d.hHdr->nTasks = tasks; d.hHdr->nSens = sens;
   d.parts = parts;
+  // the series chunks' places in the slot's pools (the packer kept them within kSeriesVBytes / kSeriesEBytes)
+  d.anySeries = false;
+  size_t vUsed = 0, eUsed = 0;
+  uint32_t nSeries = 0;
+  for (Part& p : d.parts)
+    if (p.r->series) {
+      p.vOff = vUsed; p.eOff = eUsed;
+      vUsed += up256(size_t(3) * p.n * p.r->Kp * 2);
+      eUsed += (size_t(p.n) * uint32_t(p.r->sq.in.T) + 63) / 64 * 64;
+      ++nSeries;
+      d.anySeries = true;
+    }
+  if (vUsed > kSeriesVBytes || eUsed * 4 > kSeriesEBytes || nSeries > kMaxSeriesGroup) {
+    err = "internal: batch beyond its series pools";
+    d.parts.clear();
+    return false;
+  }
   void* aRed[] = {&d.dHdr, &d.dSegs, &d.dBits, &d.dOut};
   cudaKernelNodeParams kr{};
   kr.func = reinterpret_cast<void*>(k_reduce_batch); kr.gridDim = dim3((sens + 255) / 256); kr.blockDim = dim3(256); kr.kernelParams = aRed;
@@ -448,7 +565,7 @@ bool launch_day(Server& s, int k, const std::vector<Part>& parts, std::string& e
       cuok(cudaGraphExecKernelNodeSetParams(d.exec, d.nReduce, &kr), err, "batch reduce") &&
       cuok(cudaGraphExecMemcpyNodeSetParams1D(d.exec, d.nOut, d.hOut, d.dOut, sizeof(double) * out, cudaMemcpyDeviceToHost), err, "batch sums") &&
       order_after_uploads(s, err) && cuok(cudaEventRecord(d.ev[0], s.st), err, "batch") && cuok(cudaGraphLaunch(d.exec, s.st), err, "batch graph") &&
-      cuok(cudaEventRecord(d.ev[1], s.st), err, "batch");
+      (!d.anySeries || launch_series(s, d, err)) && cuok(cudaEventRecord(d.ev[1], s.st), err, "batch");
   if (!ok) d.parts.clear();
   return ok;
 }
@@ -549,17 +666,23 @@ bool launch_next(Server& s) {
   // daylight: chunks of the daylight candidates in priority order until the batch is full
   std::vector<Part> parts;
   uint64_t rays = 0;
-  size_t bits = 0, out = 0;
-  uint32_t sens = 0;
+  size_t bits = 0, out = 0, vUsed = 0, eUsed = 0;
+  uint32_t sens = 0, nSeries = 0;
   for (const auto& c : cand) {
     Request* r = c.second;
     if (r->kind != 0) continue;
+    if (r->series && nSeries >= kMaxSeriesGroup) continue;   // the grouped launch is full: other requests may still fit
     const size_t perSensor = (r->d.nDir + 31) / 32;
-    while (r->nextSensor < r->nSensors && parts.size() < kMaxSegs && rays < s.batchRays) {
-      // a chunk, cut to what is left of the batch's rays and of its pools
-      const uint64_t fit = std::min({uint64_t(s.chunkSensors), uint64_t(r->nSensors - r->nextSensor),
-                                     (s.batchRays - rays + r->d.nDir - 1) / r->d.nDir, uint64_t((s.bitsPoolWords - bits) / perSensor),
-                                     uint64_t((s.outPoolDoubles - out) / r->d.nQ), uint64_t(s.maxSensPerBatch - sens)});
+    while (r->nextSensor < r->nSensors && parts.size() < kMaxSegs && rays < s.batchRays && (!r->series || nSeries < kMaxSeriesGroup)) {
+      // a chunk, cut to what is left of the batch's rays and of its pools (a series chunk also to the series pools)
+      uint64_t fit = std::min({uint64_t(s.chunkSensors), uint64_t(r->nSensors - r->nextSensor),
+                               (s.batchRays - rays + r->d.nDir - 1) / r->d.nDir, uint64_t((s.bitsPoolWords - bits) / perSensor),
+                               uint64_t((s.outPoolDoubles - out) / r->d.nQ), uint64_t(s.maxSensPerBatch - sens)});
+      if (r->series) {
+        const size_t vRow = size_t(6) * r->Kp, eRow = size_t(4) * uint32_t(r->sq.in.T);
+        const size_t vLeft = kSeriesVBytes - vUsed > 256 ? kSeriesVBytes - vUsed - 256 : 0, eLeft = kSeriesEBytes - eUsed > 256 ? kSeriesEBytes - eUsed - 256 : 0;
+        fit = std::min<uint64_t>({fit, vLeft / vRow, eLeft / eRow});
+      }
       if (fit == 0) break;
       const uint32_t n = uint32_t(fit);
       const size_t words = perSensor * n;
@@ -569,11 +692,17 @@ bool launch_next(Server& s) {
       bits += words;
       out += size_t(r->d.nQ) * n;
       sens += n;
+      if (r->series) {   // as launch_day places them
+        vUsed += up256(size_t(3) * n * r->Kp * 2);
+        eUsed += ((size_t(n) * uint32_t(r->sq.in.T) + 63) / 64 * 64) * 4;
+        ++nSeries;
+      }
     }
     if (parts.size() >= kMaxSegs || rays >= s.batchRays) break;
     if (parts.empty()) {   // not one sensor of the top request fits an empty batch: it can never run
       r->nextSensor = r->nSensors;
-      account(s, r, 0, false, "daylight: one sensor's direction words exceed the batch pools (raise the batch rays)");
+      account(s, r, 0, false, r->series ? "daylight: one sensor's series row exceeds the batch's series pools" :
+                                          "daylight: one sensor's direction words exceed the batch pools (raise the batch rays)");
       return true;
     }
   }
@@ -604,12 +733,18 @@ void complete(Server& s, int kind, int k, cudaError_t q) {
   if (kind == 0) {
     DaySlot& d = s.day[k];
     if (ok && *d.hStatus) { ok = false; err = "batch: traversal stack overflow or visit limit"; }
+    if (ok && d.anySeries && (*d.hSeriesStatus & kStatusTimeout)) { ok = false; err = "batch: the series' tensor-core pipeline timed out waiting"; }
     for (size_t j = 0; j < d.parts.size(); ++j) {
       const Part& p = d.parts[j];
       const Seg& g = d.hSegs[j];
-      if (ok && !p.r->done)
+      if (ok && !p.r->done) {
         for (uint32_t qq = 0; qq < g.nQ; ++qq)
           std::memcpy(p.r->d.out + size_t(qq) * p.r->nSensors + p.i0, d.hOut + g.outOff + size_t(qq) * p.n, size_t(p.n) * 8);
+        if (p.r->series) {
+          const size_t T = size_t(p.r->sq.in.T);
+          std::memcpy(p.r->sq.E + size_t(p.i0) * T, d.hE + p.eOff, size_t(p.n) * T * 4);
+        }
+      }
       account(s, p.r, p.n, ok, err);
     }
     d.parts.clear();
@@ -774,6 +909,13 @@ KGB_API kgb_server* kgb_server_create(uint64_t hbmBudgetBytes) {
   if (!cuok(cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep), err, "memory pool") ||
       !cuok(cudaMemPoolSetAttribute(s->pool, cudaMemPoolReuseAllowInternalDependencies, &no), err, "memory pool"))
     return bad(err);
+  for (DaySlot& d : s->day) {   // the series pools
+    if (!cuok(cudaMalloc(&d.dV, kSeriesVBytes), err, "series pool") || !cuok(cudaMalloc(reinterpret_cast<void**>(&d.dE), kSeriesEBytes), err, "series pool") ||
+        !cuok(cudaMallocHost(reinterpret_cast<void**>(&d.hE), kSeriesEBytes), err, "series pool") ||
+        !cuok(cudaMallocHost(reinterpret_cast<void**>(&d.hSeriesStatus), 4), err, "pinned"))
+      return bad(err);
+    s->used += kSeriesVBytes + kSeriesEBytes;
+  }
   for (DaySlot& d : s->day)
     if (!cuok(cudaMallocHost(&d.hSegs, sizeof(Seg) * kMaxSegs), err, "pinned") || !cuok(cudaMallocHost(&d.hHdr, sizeof(BatchHdr)), err, "pinned") ||
         !cuok(cudaMallocHost(&d.hStatus, 4), err, "pinned") || !cuok(cudaMalloc(&d.dSegs, sizeof(Seg) * kMaxSegs), err, "segments") ||
@@ -818,6 +960,9 @@ KGB_API void kgb_server_destroy(kgb_server* h) {
     if (d.hHdr) cudaFreeHost(d.hHdr);
     if (d.hStatus) cudaFreeHost(d.hStatus);
     cudaFree(d.dSegs); cudaFree(d.dHdr); cudaFree(d.dCtl);
+    cudaFree(d.dV); cudaFree(d.dE);
+    if (d.hE) cudaFreeHost(d.hE);
+    if (d.hSeriesStatus) cudaFreeHost(d.hSeriesStatus);
     for (cudaEvent_t e : d.ev) if (e) cudaEventDestroy(e);
   }
   for (ViewSlot& v : s->view) {
@@ -904,6 +1049,57 @@ KGB_API int kgb_server_submit(kgb_server* h, const kgb_daylight_request* req, ui
   r->ticket = s->nextTicket++;
   if (!r->nSensors || !req->nDir) { std::fill(req->out, req->out + size_t(req->nQ) * req->nSensors, 0.0); finish(*s, r, true, ""); }
   else s->pending.push_back(r);
+  s->all[r->ticket] = r;
+  *ticket = r->ticket;
+  s->cv.notify_all();
+  return 1;
+}
+
+KGB_API int kgb_server_submit_series(kgb_server* h, const kgb_daylight_request* req, const kgb_series_request* q, uint64_t* ticket) {
+  Server* s = reinterpret_cast<Server*>(h);
+  const auto no = [](const char* m) { set_error(std::string("kgb_server_submit_series: ") + m); return 0; };
+  if (!q || !q->E) return no("no series or no E");
+  const kgb_series_in& in = q->in;
+  if (req->scene < 0 || size_t(req->scene) >= s->scenes.size()) return no("unknown scene");
+  if (req->nQ < 1 || req->nQ > kMaxQ) return no("1 to 8 quantities");
+  if (q->gQ >= req->nQ) return no("gQ is not one of the request's quantities");
+  if (in.G || in.Sdc) return no("G comes from quantity gQ and there is no reflected light: G and Sdc must be NULL");
+  if (in.P <= 0 || in.T <= 0 || !in.S || !in.g || (in.nSky && (!in.row || !in.wsky)) || (in.nSun && (!in.sunStep || !in.sunVec || !in.sunW)))
+    return no("missing series inputs");
+  if (in.nSky > req->nDir || uint64_t(in.sun0) + in.nSun > req->nDir) return no("directions beyond the request's direction table");
+  Request* r = new Request;
+  r->kind = 0;
+  r->d = *req;
+  r->series = true;
+  r->sq = *q;
+  r->Kp = uint32_t((uint64_t(in.P) + 1 + 63) / 64 * 64);
+  const size_t P = size_t(in.P), T = size_t(in.T);
+  r->csr.assign(P + 1 + in.nSky, 0);
+  for (uint32_t d = 0; d < in.nSky; ++d) {
+    if (in.row[d] < 0 || in.row[d] >= in.P) { delete r; return no("a sky direction's row is not a patch"); }
+    r->csr[size_t(in.row[d]) + 1]++;
+  }
+  for (size_t p = 0; p < P; ++p) r->csr[p + 1] += r->csr[p];
+  {
+    std::vector<int32_t> at(r->csr.begin(), r->csr.begin() + P);
+    for (uint32_t d = 0; d < in.nSky; ++d) r->csr[P + 1 + size_t(at[size_t(in.row[d])]++)] = int32_t(d);
+  }
+  r->sunOfCol.assign(T, -1);
+  for (uint32_t j = 0; j < in.nSun; ++j) {
+    if (in.sunStep[j] < 0 || size_t(in.sunStep[j]) >= T) { delete r; return no("a sun step is not a column"); }
+    if (r->sunOfCol[size_t(in.sunStep[j])] >= 0) { delete r; return no("two sun directions on one step (the tensor-core form's sun term takes one)"); }
+    r->sunOfCol[size_t(in.sunStep[j])] = int32_t(j);
+  }
+  r->nSensors = req->nSensors;
+  r->raysPerSensor = req->nDir;
+  r->tSubmit = Clock::now();
+  std::lock_guard<std::mutex> lk(s->m);
+  r->ticket = s->nextTicket++;
+  if (!r->nSensors || !req->nDir) {
+    std::fill(req->out, req->out + size_t(req->nQ) * req->nSensors, 0.0);
+    std::fill(q->E, q->E + size_t(req->nSensors) * T, 0.f);
+    finish(*s, r, true, "");
+  } else s->pending.push_back(r);
   s->all[r->ticket] = r;
   *ticket = r->ticket;
   s->cv.notify_all();

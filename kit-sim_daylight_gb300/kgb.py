@@ -60,6 +60,10 @@ class DaylightRequest(ctypes.Structure):
                 ("D", c_void_p), ("W", c_void_p), ("useCosMask", c_uint32), ("rayFlags", c_uint32), ("out", c_void_p)]
 
 
+class SeriesRequest(ctypes.Structure):
+    _fields_ = [("in", SeriesIn), ("gQ", c_uint32), ("E", c_void_p)]   # "in": the C field name
+
+
 class ViewsRequest(ctypes.Structure):
     _fields_ = [("scene", c_int32), ("nSensors", c_uint32), ("P", c_void_p), ("N", c_void_p), ("label", c_void_p), ("view", ViewIn),
                 ("rayFlags", c_uint32), ("wRow", c_void_p), ("nClass", c_uint32), ("farDist", c_double), ("reach", c_void_p),
@@ -113,6 +117,7 @@ SIGNATURES = [
     ("kgb_server_set_tuning", c_int, [c_void_p, c_uint32, c_uint64, c_uint64]),
     ("kgb_server_submit", c_int, [c_void_p, POINTER(DaylightRequest), POINTER(c_uint64)]),
     ("kgb_server_submit_views", c_int, [c_void_p, POINTER(ViewsRequest), POINTER(c_uint64)]),
+    ("kgb_server_submit_series", c_int, [c_void_p, POINTER(DaylightRequest), POINTER(SeriesRequest), POINTER(c_uint64)]),
     ("kgb_server_wait", c_int, [c_void_p, c_uint64, c_double]),
     ("kgb_server_stats", None, [c_void_p, POINTER(c_double)]),
     ("kgb_server_timing", None, [c_void_p, POINTER(c_double)]),
@@ -441,6 +446,29 @@ class Server:
         self._live[t.value] = (P, N, D, W, out, r)
         return t.value
 
+    def submit_series(self, scene, P, N, D, W, use_cos, gQ, nSky, row, wsky, S, g, sun0, sunStep, sunVec, sunW, flags=5):
+        """Daylight request with its time series: wait() gives (out [nQ x nSensors], E [nSensors x T]); G of the series is
+        quantity gQ's sums (as float), as the reference's run loop passes its ground reduce."""
+        P, N, D = _f32(P, (-1, 3)), _f32(N, (-1, 3)), _f32(D, (-1, 3))
+        W = _f32(W).reshape(len(use_cos), len(D))
+        out = np.zeros((len(use_cos), len(P)), np.float64)
+        mask = sum(1 << q for q, c in enumerate(use_cos) if c)
+        r = DaylightRequest(scene, len(P), len(D), len(use_cos), _p(P), _p(N), _p(D), _p(W), mask, flags, _p(out))
+        row = np.ascontiguousarray(row, dtype=np.int32)
+        wsky, S, g = _f32(wsky), _f32(S), _f32(g)
+        Pp, T = S.shape
+        sunStep = np.ascontiguousarray(sunStep, dtype=np.int32)
+        sunVec, sunW = _f32(sunVec, (-1, 3)), _f32(sunW)
+        E = np.zeros((len(P), T), np.float32)
+        si = SeriesIn(nSky, _typed(row, c_int32), _typed(wsky, c_float), _typed(S, c_float), Pp, T, _typed(g, c_float), None, sun0,
+                      len(sunStep), _typed(sunStep, c_int32), _typed(sunVec, c_float), _typed(sunW, c_float), None)
+        q = SeriesRequest(si, gQ, _p(E))
+        t = c_uint64(0)
+        if not self.d.kgb_server_submit_series(self.h, ctypes.byref(r), ctypes.byref(q), ctypes.byref(t)):
+            raise KgbError(self.lib.err())
+        self._live[t.value] = ("series", (P, N, D, W, row, wsky, S, g, sunStep, sunVec, sunW, r, q), out, E)
+        return t.value
+
     def submit_views(self, scene, P, N, nAz, nEl, az0, dAz, rowSin, wRow, nClass, farDist, reach=(), glazing=False, isoDim=0,
                      label=None, world=False, cull=False, jitter=True, back=False, vground=True, nS=1, groundZ=0.0, north=0.0, flags=1):
         P, N, rowSin = _f32(P, (-1, 3)), _f32(N, (-1, 3)), _f32(rowSin)
@@ -463,6 +491,8 @@ class Server:
         if not self.d.kgb_server_wait(self.h, ticket, timeout):
             raise KgbError(self.lib.err())
         keep = self._live.pop(ticket)
+        if keep[0] == "series":
+            return keep[2], keep[3]
         return keep[4] if len(keep) == 6 else keep[6]
 
     def stats(self):

@@ -1043,6 +1043,7 @@ KGB_API int kgb_server_autotune(kgb_server*) { return fail("not restated"); }
 KGB_API int kgb_server_set_tuning(kgb_server*, uint32_t, uint64_t, uint64_t) { return fail("not restated"); }
 KGB_API int kgb_server_submit(kgb_server*, const kgb_daylight_request*, uint64_t*) { return fail("not restated"); }
 KGB_API int kgb_server_submit_views(kgb_server*, const kgb_views_request*, uint64_t*) { return fail("not restated"); }
+KGB_API int kgb_server_submit_series(kgb_server*, const kgb_daylight_request*, const kgb_series_request*, uint64_t*) { return fail("not restated"); }
 KGB_API int kgb_server_wait(kgb_server*, uint64_t, double) { return fail("not restated"); }
 KGB_API void kgb_server_stats(kgb_server*, double* out) { for (int k = 0; k < 10; ++k) out[k] = 0; }
 KGB_API void kgb_server_timing(kgb_server*, double* out) { for (int k = 0; k < 5; ++k) out[k] = 0; }

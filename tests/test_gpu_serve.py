@@ -156,3 +156,100 @@ def test_chunks_cut_to_the_batch(engine_lib, kgb, pkg):
         assert srv.stats()["items"] >= n * len(D) // (1 << 22)
     finally:
         srv.close()
+
+
+def _series_inputs(rng, D_sky_n, P, T, nSun, sun0):
+    """Series inputs of one request: nSky sky directions over P patches, T steps, nSun suns on distinct steps."""
+    row = rng.integers(0, P, D_sky_n).astype(np.int32)
+    wsky = rng.uniform(0.005, 0.05, D_sky_n).astype(np.float32)
+    S = rng.uniform(0, 300, (P, T)).astype(np.float32)
+    g = rng.uniform(0, 60, T).astype(np.float32)
+    steps = np.sort(rng.choice(T, nSun, replace=False)).astype(np.int32)
+    return dict(nSky=D_sky_n, row=row, wsky=wsky, S=S, g=g, sun0=sun0, sunStep=steps, sunW=rng.uniform(0, 900, nSun).astype(np.float32))
+
+
+def _alone_series(kgb, lib, scene, P, N, D, W, use_cos, gQ, si):
+    """The request alone through the single-request entry points: trace, the quantities' reduces, the series with G =
+    quantity gQ's sums as float (the reference's run loop: gpu_reduce then gpu_series, src/run.cpp:672-687)."""
+    e = kgb.Engine(lib)
+    try:
+        e.build(scene["v"], scene["tri"])
+        e.set_scene(P, N, D)
+        e.trace(0, len(P), lib.ray_flags(False, False))
+        sums = np.stack([e.reduce(len(P), W[q], c) for q, c in enumerate(use_cos)])
+        E = e.series(len(P), G=sums[gQ].astype(np.float32), sunVec=D[si["sun0"]:si["sun0"] + len(si["sunStep"])], **si)
+        return sums, E
+    finally:
+        e.close()
+
+
+@pytest.mark.parametrize("budget_gb", [64, 0.4])
+def test_series_requests_equal_alone(engine_lib, kgb, pkg, budget_gb):
+    """Daylight requests with time series (145, 577 and 2305 patches, uneven steps and sensor counts) in a stream with
+    plain daylight and views requests: every request's sums and series rows equal the request run alone, bit for bit
+    (each batch's series chunks run as one grouped tensor-core launch); a small budget serialises admission."""
+    scenes = [pkg.workloads.random_city(s, n_boxes=40 + 10 * s) for s in (4, 5)]
+    srv = kgb.Server(engine_lib, budget_gb * 1e9)
+    try:
+        ids = [srv.add_scene(s["v"], s["tri"]) for s in scenes]
+        srv.set_tuning(chunk_sensors=1024, batch_rays=1 << 24)   # small chunks: a request's series spans several batches
+        rng = np.random.default_rng(8)
+        reqs = []
+        for k, (patches, T) in enumerate([(145, 300), (577, 700), (2305, 97), (145, 2000), (577, 64), (2305, 400), (145, 7)]):
+            sc = k % 2
+            s = scenes[sc]
+            n = int(rng.integers(100, min(len(s["P"]), 5000)))
+            first = int(rng.integers(0, len(s["P"]) - n))
+            P, N = s["P"][first:first + n], s["N"][first:first + n]
+            nSky = patches + int(rng.integers(0, 100))
+            nSun = int(rng.integers(0, min(T, 300) + 1))
+            D = pkg.workloads.hemisphere_dirs(nSky, nSun, 100 + k)
+            si = _series_inputs(rng, nSky, patches, T, nSun, 2 * nSky)
+            W = np.stack([np.concatenate([np.zeros(nSky), rng.uniform(0.001, 0.01, nSky), np.zeros(nSun)]),
+                          rng.uniform(0.0, 2.0, len(D))]).astype(np.float32)
+            use_cos = [True, bool(k % 2)]
+            t = srv.submit_series(ids[sc], P, N, D, W, use_cos, 0, sunVec=D[2 * nSky:], **si)
+            reqs.append((sc, P, N, D, W, use_cos, si, t))
+            if k == 2:   # plain requests and a views request in between
+                Dp = pkg.workloads.hemisphere_dirs(80, 40, 7)
+                plain = (sc, P[:700], N[:700], Dp, rng.uniform(0, 1, (2, len(Dp))).astype(np.float32), [True, False])
+                tp = srv.submit(ids[plain[0]], *plain[1:])
+                nAz, nEl, rowSin, wRow = _views_grid(120.0, 6.0)
+                tv = srv.submit_views(ids[0], scenes[0]["P"][:200], scenes[0]["N"][:200], nAz, nEl, -60.0, 120.0 / nAz, rowSin, wRow, 3, 500.0,
+                                      groundZ=float(scenes[0]["v"][:, 2].min()))
+        for sc, P, N, D, W, use_cos, si, t in reqs:
+            sums, E = srv.wait(t)
+            want_sums, want_E = _alone_series(kgb, engine_lib, scenes[sc], P, N, D, W, use_cos, 0, si)
+            assert np.array_equal(sums.view(np.uint64), want_sums.view(np.uint64))
+            assert np.array_equal(E.view(np.uint32), want_E.view(np.uint32)), "%d of %d series values differ (P %d, T %d)" % (
+                np.sum(E != want_E), E.size, si["S"].shape[0], si["S"].shape[1])
+            assert E.max() > 0
+        assert np.array_equal(srv.wait(tp), _alone_daylight(kgb, engine_lib, scenes[plain[0]], *plain[1:]))
+        srv.wait(tv)
+        assert srv.stats()["completed"] == len(reqs) + 2
+    finally:
+        srv.close()
+
+
+def test_series_request_refusals(engine_lib, kgb, pkg):
+    s = pkg.workloads.random_city(4, n_boxes=20)
+    srv = kgb.Server(engine_lib, 1e9)
+    try:
+        sid = srv.add_scene(s["v"], s["tri"])
+        rng = np.random.default_rng(1)
+        D = pkg.workloads.hemisphere_dirs(145, 10, 1)
+        si = _series_inputs(rng, 145, 145, 20, 10, 290)
+        W = np.ones((1, len(D)), np.float32)
+        with pytest.raises(kgb.KgbError, match="gQ is not one of the request's quantities"):
+            srv.submit_series(sid, s["P"][:10], s["N"][:10], D, W, [True], 1, sunVec=D[290:], **si)
+        bad = dict(si, sunStep=np.array([3, 3, 4, 5, 6, 7, 8, 9, 10, 11], np.int32))
+        with pytest.raises(kgb.KgbError, match="two sun directions on one step"):
+            srv.submit_series(sid, s["P"][:10], s["N"][:10], D, W, [True], 0, sunVec=D[290:], **bad)
+        bad = dict(si, row=np.full(145, 145, np.int32))
+        with pytest.raises(kgb.KgbError, match="row is not a patch"):
+            srv.submit_series(sid, s["P"][:10], s["N"][:10], D, W, [True], 0, sunVec=D[290:], **bad)
+        t = srv.submit_series(sid, s["P"][:0], s["N"][:0], D, W, [True], 0, sunVec=D[290:], **si)   # no sensors: empty results
+        out, E = srv.wait(t)
+        assert out.shape == (1, 0) and E.shape == (0, 20)
+    finally:
+        srv.close()
