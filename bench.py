@@ -712,7 +712,7 @@ def run_serving_series(args, pkg):
     configuration's sky, opaque scene: the serving form traces visibility bits) through the server, each batch's series
     chunks of every request in it as one grouped split-BF16 tensor-core launch, against the plain FP32 form one request
     per launch (trace, the ground reduce, kgb_series in its FP32 form) on the same GPU. Requests: seeded, sensors
-    log-uniform 1k..30k (contiguous ranges of the urban block), time ranges log-uniform 1 day .. 1 year, all submitted
+    log-uniform 1k..50k (contiguous ranges of the urban block), time ranges log-uniform 1 day .. 1 year, all submitted
     at once (throughput); solves = sensors x series columns."""
     import torch
     torch.cuda.set_device(0)
@@ -733,7 +733,7 @@ def run_serving_series(args, pkg):
     rng = np.random.default_rng(args.series_seed)
     reqs = []
     for k in range(args.series_requests):
-        n = int(np.exp(rng.uniform(np.log(1000), np.log(30000))))
+        n = int(np.exp(rng.uniform(np.log(1000), np.log(50000))))
         first = int(rng.integers(0, len(scene["P"]) - n))
         days = float(np.exp(rng.uniform(0, np.log(365))))
         h0 = int(rng.integers(0, 8760 - int(days * 24) + 1))
@@ -784,7 +784,7 @@ def run_serving_series(args, pkg):
             "p50_ms": 1e3 * st["p50_s"], "p99_ms": 1e3 * st["p99_s"], "wall_s": wall, "plain_s": plain,
             "gpu": {"daylight_s": tm["day_gpu_s"], "queued_s": tm["queued_s"]}, "server": {k: st[k] for k in ("completed", "items", "chunk_sensors", "batch_rays")},
             "config": {"workload": "%d daylight requests with hourly series on the urban block (%d triangles): 2305 patches + ground, sensors "
-                                   "log-uniform 1k..30k (%d in all), time ranges log-uniform 1 day..1 year (%d series columns in all), "
+                                   "log-uniform 1k..50k (%d in all), time ranges log-uniform 1 day..1 year (%d series columns in all), "
                                    "submitted at once" % (len(reqs), len(scene["tri"]), sum(len(r["P"]) for r in reqs),
                                                          sum(r["si"]["S"].shape[1] for r in reqs)),
                        "solves": solves},
@@ -802,7 +802,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sensors", type=int, default=0, help="urban / precision / views: only the first N sensors (a small case for profiling)")
     ap.add_argument("--config", default="urban", choices=["urban", "precision", "views", "serving", "serving_series"])
-    ap.add_argument("--series-requests", type=int, default=24)
+    ap.add_argument("--series-requests", type=int, default=64)
     ap.add_argument("--series-seed", type=int, default=12)
     ap.add_argument("--builder", type=int, default=1, choices=[0, 1], help="urban: 1 device LBVH with treelets (default), 0 host binned-SAH tree")
     ap.add_argument("--rate", type=float, default=200.0)

@@ -1058,7 +1058,7 @@ KGB_API int kgb_server_submit(kgb_server* h, const kgb_daylight_request* req, ui
 KGB_API int kgb_server_submit_series(kgb_server* h, const kgb_daylight_request* req, const kgb_series_request* q, uint64_t* ticket) {
   Server* s = reinterpret_cast<Server*>(h);
   const auto no = [](const char* m) { set_error(std::string("kgb_server_submit_series: ") + m); return 0; };
-  if (!q || !q->E) return no("no series or no E");
+  if (!q || (!q->E && req->nSensors)) return no("no series or no E");
   const kgb_series_in& in = q->in;
   if (req->scene < 0 || size_t(req->scene) >= s->scenes.size()) return no("unknown scene");
   if (req->nQ < 1 || req->nQ > kMaxQ) return no("1 to 8 quantities");
@@ -1097,7 +1097,7 @@ KGB_API int kgb_server_submit_series(kgb_server* h, const kgb_daylight_request* 
   r->ticket = s->nextTicket++;
   if (!r->nSensors || !req->nDir) {
     std::fill(req->out, req->out + size_t(req->nQ) * req->nSensors, 0.0);
-    std::fill(q->E, q->E + size_t(req->nSensors) * T, 0.f);
+    if (q->E) std::fill(q->E, q->E + size_t(req->nSensors) * T, 0.f);
     finish(*s, r, true, "");
   } else s->pending.push_back(r);
   s->all[r->ticket] = r;

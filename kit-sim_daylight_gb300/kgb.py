@@ -491,7 +491,7 @@ class Server:
         if not self.d.kgb_server_wait(self.h, ticket, timeout):
             raise KgbError(self.lib.err())
         keep = self._live.pop(ticket)
-        if keep[0] == "series":
+        if isinstance(keep[0], str):   # a series request: its sums and its rows of E
             return keep[2], keep[3]
         return keep[4] if len(keep) == 6 else keep[6]
 
