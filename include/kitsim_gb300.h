@@ -222,6 +222,19 @@ typedef struct kgb_sky_step {
  * row as gendaymtx_step writes it (ground first, then the patches; RGB). sun / sky / visible as its flags. */
 KGB_API int kgb_sky(kgb_engine* e, int32_t mf, const kgb_sky_step* steps, size_t T, double grefl, int32_t sun, int32_t sky,
                     int32_t visible, float* out);
+/* Ladybug mode's sky on the GPU (the reference's --mode ladybug, src/run.cpp:362-398 and 447-470: gendaymtx -A as
+ * ladybug runs it). steps [T x 4]: day of year (gendaymtx's jd), hour (decimal, the weather's clock), DNI, DHI (W/m2, as
+ * the steps hold them: truncated to integers here as ladybug's .wea prints them); lat, lon (degrees, east positive) and
+ * tz (hours east of UTC) of the weather, printed into the .wea as ladybug does (0.01 degree, the zone's integer
+ * meridian); grefl; durationHours (the steps' total hours). Per step the sun by Radiance's sun.c and the Perez sky twice
+ * (sun alone, sky alone), FP64 on the GPU; per patch the float sums over all steps in step order; their averages printed
+ * to three significant digits (%.3g) on the host. Writes lb [3 P + 1] doubles: per patch skyDirLB, then skyDifLB, then
+ * skyRad (their sum), then gndLB: the values run.cpp puts into its weight vectors (direct, diffuse, radiation; ground).
+ * acc [4 P + 6] floats, when non-null: the sums (red of the sun rows [P], the sky rows [3 P], the ground row of the sun
+ * rows [3] and of the sky rows [3]). S [P x Tup], g [Tup], when non-null: the series columns of the steps with
+ * DNI + DHI > 1e-4 (run.cpp:385-397). mf 1 or 2 (the reference's rule for ladybug mode). */
+KGB_API int kgb_sky_ladybug(kgb_engine* e, int32_t mf, const double* steps, size_t T, double lat, double lon, double tz, double grefl,
+                            double durationHours, double* lb, float* acc, float* S, float* g);
 /* NOAA solar positions of T steps on the GPU in FP64, restating sun_noaa (src/solar.cpp:66-105): in [T x 7] = lat, lon,
  * tz, month, day, hour (decimal), leap; out [T x 6] = altitude (deg, refracted), azimuth (deg), up, direction x y z. */
 KGB_API int kgb_sun_noaa(kgb_engine* e, const double* in, size_t T, double* out);

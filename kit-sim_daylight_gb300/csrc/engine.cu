@@ -758,6 +758,12 @@ KGB_API int kgb_sky(kgb_engine* e, int32_t mf, const kgb_sky_step* steps, size_t
   if (const char* why = sky_steps(mf, steps, T, grefl, sun, sky, visible, out, E(e)->st)) return fail(why);
   return 1;
 }
+KGB_API int kgb_sky_ladybug(kgb_engine* e, int32_t mf, const double* steps, size_t T, double lat, double lon, double tz, double grefl,
+                            double durationHours, double* lb, float* acc, float* S, float* g) {
+  if (!lb) return fail("kgb_sky_ladybug: no weights to write");
+  if (const char* why = sky_ladybug(mf, steps, T, lat, lon, tz, grefl, durationHours, lb, acc, S, g, E(e)->st)) return fail(why);
+  return 1;
+}
 KGB_API int kgb_sun_noaa(kgb_engine* e, const double* in, size_t T, double* out) {
   if (const char* why = sun_steps(in, T, out, E(e)->st)) return fail(why);
   return 1;

@@ -204,6 +204,9 @@ void engine_reduce_inputs(kgb_engine* e, ReduceInputs& in);
 // sky (sky.cu): Perez sky of T steps, NOAA sun positions; null or what failed
 const char* sky_steps(int mf, const kgb_sky_step* steps, size_t T, double grefl, int sun, int sky, int visible, float* out, cudaStream_t st);
 const char* sun_steps(const double* in, size_t T, double* out, cudaStream_t st);
+// ladybug mode's sky (kgb_sky_ladybug); null or what failed
+const char* sky_ladybug(int mf, const double* steps, size_t T, double lat, double lon, double tz, double grefl, double durationHours,
+                        double* lb, float* acc, float* S, float* g, cudaStream_t st);
 
 // host BVH builder (bvh_build.cpp): binned-SAH binary BVH, collapsed to the 8-wide float-plane layout of rt.cuh
 struct BvhOut {

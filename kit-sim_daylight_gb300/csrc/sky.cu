@@ -12,6 +12,9 @@
 #include "kgb_detmath.h"
 
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -279,6 +282,71 @@ __global__ void k_sun(SunArgs a) {
   o[3] = (float)v0; o[4] = (float)v1; o[5] = (float)sin(ar);
 }
 
+// ---------------------------------------------------------------------------------------------- ladybug mode
+// The reference's --mode ladybug emulates gendaymtx -A as ladybug runs it (src/run.cpp:362-398 per step, 447-470 at the
+// end): the sun by Radiance's sun.c at the site ladybug writes into its .wea (latitude and west longitude to 0.01
+// degree, the zone's integer meridian), each step's DNI and DHI truncated to integers, the sky of each step twice (the
+// sun alone, gendaymtx -d; the sky alone, -s), and per patch float sums over all steps in step order, averaged and
+// printed to three significant digits.
+
+// Radiance sun.c (rad5R4: sdec, stadj, salt, sazi), the reference's sun_radiance (src/sky.cpp:477-486), in FP64.
+__device__ __forceinline__ void sun_rad(double latDeg, double lonW, double meridW, int jd, double hour, double& alt, double& azi) {
+  const double lat = latDeg * (PI / 180.), lon = lonW * (PI / 180.), mer = meridW * (PI / 180.);
+  const double sd = 0.4093 * sin((2. * PI / 365.) * (jd - 81));
+  const double sta = 0.170 * sin((4. * PI / 373.) * (jd - 80)) - 0.129 * sin((2. * PI / 355.) * (jd - 8)) + (12. / PI) * (mer - lon);
+  const double st = hour + sta;
+  alt = asin(sin(lat) * sin(sd) - cos(lat) * cos(sd) * cos(st * (PI / 12.)));
+  azi = -atan2(cos(sd) * sin(st * (PI / 12.)), -cos(lat) * sin(sd) - sin(lat) * cos(sd) * cos(st * (PI / 12.))) + PI;
+}
+// per step: the sky step of the .wea (jd, the sun by sun.c, DNI and DHI truncated to integers)
+__global__ void k_lb_steps(const double* in, uint32_t T, double latW, double lonW, double meridW, kgb_sky_step* out) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  const double* p = in + 4 * size_t(t);
+  kgb_sky_step s{};
+  s.jd = int(p[0]);
+  sun_rad(latW, lonW, meridW, s.jd, p[1], s.alt, s.azi);
+  s.dni = double(int(p[2]));
+  s.dhi = double(int(p[3]));
+  out[t] = s;
+}
+// The float sums over the steps, in step order: accDir [P] (red of the sun rows), accDif [3 P], the ground row of the
+// sun rows [3], of the sky rows [3]. One thread per sum.
+__global__ void k_lb_acc(const float* dir, const float* dif, uint32_t T, uint32_t P, float* acc) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= 4 * P + 6) return;
+  const float* src;
+  uint32_t off;
+  if (k < P) { src = dir; off = 3 * (k + 1); }
+  else if (k < 4 * P) { src = dif; off = 3 + (k - P); }
+  else if (k < 4 * P + 3) { src = dir; off = k - 4 * P; }
+  else { src = dif; off = k - 4 * P - 3; }
+  const size_t row = 3 * size_t(P + 1);
+  float s = 0.f;
+  for (uint32_t t = 0; t < T; ++t) s = __fadd_rn(s, src[t * row + off]);
+  acc[k] = s;
+}
+// The series columns of the steps with DNI + DHI > 1e-4: S [p, col] = float(bright(sky row) + the sun row's red),
+// g [col] = float(grefl x sum_p L_p omega_p / P), the sum in patch order. One block per step.
+__global__ void k_lb_series(const float* dir, const float* dif, const int32_t* colOf, uint32_t T, uint32_t P, uint32_t Tup,
+                            const float* omega, double grefl, float* S, float* g) {
+  const uint32_t t = blockIdx.x;
+  const int32_t col = colOf[t];
+  if (col < 0) return;
+  const size_t row = 3 * size_t(P + 1) * t;
+  const auto L = [&](uint32_t p) {
+    const float* df = dif + row + 3 * (p + 1);
+    return __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(0.265074126, double(df[0])), __dmul_rn(0.670114631, double(df[1]))),
+                               __dmul_rn(0.064811243, double(df[2]))), double(dir[row + 3 * (p + 1)]));
+  };
+  for (uint32_t p = threadIdx.x; p < P; p += blockDim.x) S[size_t(p) * Tup + uint32_t(col)] = __double2float_rn(L(p));
+  if (threadIdx.x == 0) {
+    double mean = 0;
+    for (uint32_t p = 0; p < P; ++p) mean = __dadd_rn(mean, __dmul_rn(L(p), double(omega[p])));
+    g[col] = __double2float_rn(__ddiv_rn(__dmul_rn(grefl, mean), double(P)));
+  }
+}
+
 // make_patches (sky.cpp:240-270): Reinhart / Tregenza patch centres and solid angles, float as the reference's.
 void make_patches(int mf, std::vector<float>& alt, std::vector<float>& azi, std::vector<float>& omega) {
   static const int tnaz[7] = {30, 30, 24, 24, 18, 12, 6};
@@ -328,6 +396,87 @@ const char* sky_steps(int mf, const kgb_sky_step* hsteps, size_t T, double grefl
   cudaMemcpyAsync(hout, dout, outN * 4, cudaMemcpyDeviceToHost, st);
   cudaFreeAsync(d, st);
   if (cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess) return "kgb_sky: kernel failed";
+  return nullptr;
+}
+
+// ladybug mode: the steps' sky rows on the device (k_sky twice), the float sums, the series columns; the weights (the
+// averages printed to three significant digits, run.cpp:447-470) on the host from the downloaded sums, by the same
+// snprintf / strtod round trip as the reference's round_fmt.
+static double round_fmt(double x, const char* fmt) {
+  char buf[64];
+  std::snprintf(buf, sizeof buf, fmt, x);
+  return std::strtod(buf, nullptr);
+}
+const char* sky_ladybug(int mf, const double* hsteps, size_t T, double lat, double lon, double tz, double grefl, double durationHours,
+                        double* lb, float* hacc, float* hS, float* hg, cudaStream_t st) {
+  if (mf != 1 && mf != 2) return "kgb_sky_ladybug: ladybug mode supports sky density 1 or 2 (the reference's rule)";
+  if (!T) return nullptr;
+  std::vector<float> alt, azi, omega;
+  make_patches(mf, alt, azi, omega);
+  const uint32_t P = uint32_t(alt.size());
+  std::vector<double> costab(1025);
+  for (int i = 0; i <= 1024; i++) costab[i] = std::cos((PI / 2. / 1024) * i);
+  std::vector<int32_t> colOf(T, -1);
+  uint32_t Tup = 0;
+  for (size_t t = 0; t < T; ++t)
+    if (float(hsteps[4 * t + 2]) + float(hsteps[4 * t + 3]) > 1e-4) colOf[t] = int32_t(Tup++);   // the Step's float DNI + DHI
+  const size_t rowN = 3 * size_t(P + 1), nAcc = 4 * size_t(P) + 6;
+  const auto a256 = [](size_t x) { return (x + 255) & ~size_t(255); };
+  const size_t oSteps = 0, oSky = a256(oSteps + T * 4 * 8), oPatch = a256(oSky + T * sizeof(kgb_sky_step)), oCos = a256(oPatch + 3 * P * 4),
+               oCol = a256(oCos + 1025 * 8), oDir = a256(oCol + T * 4), oDif = a256(oDir + T * rowN * 4), oAcc = a256(oDif + T * rowN * 4),
+               oS = a256(oAcc + nAcc * 4), oG = a256(oS + size_t(P) * Tup * 4), total = a256(oG + size_t(Tup) * 4);
+  void* d = nullptr;
+  if (cudaMallocAsync(&d, total, st) != cudaSuccess) return "kgb_sky_ladybug: device memory";
+  char* b = static_cast<char*>(d);
+  double* dsteps = reinterpret_cast<double*>(b + oSteps);
+  kgb_sky_step* dsky = reinterpret_cast<kgb_sky_step*>(b + oSky);
+  float* dalt = reinterpret_cast<float*>(b + oPatch);
+  float* dazi = dalt + P;
+  float* dom = dazi + P;
+  double* dcos = reinterpret_cast<double*>(b + oCos);
+  int32_t* dcol = reinterpret_cast<int32_t*>(b + oCol);
+  float* ddir = reinterpret_cast<float*>(b + oDir);
+  float* ddif = reinterpret_cast<float*>(b + oDif);
+  float* dacc = reinterpret_cast<float*>(b + oAcc);
+  float* dS = reinterpret_cast<float*>(b + oS);
+  float* dg = reinterpret_cast<float*>(b + oG);
+  cudaMemcpyAsync(dsteps, hsteps, T * 4 * 8, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dalt, alt.data(), P * 4, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dazi, azi.data(), P * 4, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dom, omega.data(), P * 4, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dcos, costab.data(), 1025 * 8, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dcol, colOf.data(), T * 4, cudaMemcpyHostToDevice, st);
+  // the .wea's site: latitude and west longitude printed to 0.01 degree, the zone's meridian an integer of degrees west
+  const double latW = round_fmt(lat, "%.2f"), lonW = round_fmt(-lon, "%.2f"), meridW = static_cast<double>(static_cast<int>(-tz * 15.0));
+  k_lb_steps<<<uint32_t((T + 127) / 128), 128, 0, st>>>(dsteps, uint32_t(T), latW, lonW, meridW, dsky);
+  SkyArgs a{dsky, uint32_t(T), P, dalt, dazi, dom, dcos, grefl, 1, 0, 0, ddir};
+  k_sky<<<uint32_t(T), 128, 2 * P * sizeof(double), st>>>(a);   // -d: the sun alone
+  a.sun = 0; a.sky = 1; a.out = ddif;
+  k_sky<<<uint32_t(T), 128, 2 * P * sizeof(double), st>>>(a);   // -s: the sky alone
+  k_lb_acc<<<uint32_t((nAcc + 127) / 128), 128, 0, st>>>(ddir, ddif, uint32_t(T), P, dacc);
+  if (hS || hg) k_lb_series<<<uint32_t(T), 128, 0, st>>>(ddir, ddif, dcol, uint32_t(T), P, Tup, dom, grefl, dS, dg);
+  std::vector<float> acc(nAcc);
+  cudaMemcpyAsync(acc.data(), dacc, nAcc * 4, cudaMemcpyDeviceToHost, st);
+  if (hS) cudaMemcpyAsync(hS, dS, size_t(P) * Tup * 4, cudaMemcpyDeviceToHost, st);
+  if (hg) cudaMemcpyAsync(hg, dg, size_t(Tup) * 4, cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(d, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess) return "kgb_sky_ladybug: kernel failed";
+  if (hacc) std::memcpy(hacc, acc.data(), nAcc * 4);
+  // run.cpp:447-470: averages over all steps in float, printed %.3g; weights kWh/m2 per unit of radiance x solid angle
+  const float inv = static_cast<float>(1.0 / static_cast<double>(T));
+  double mean = 0;
+  for (uint32_t p = 0; p < P; ++p) {
+    const float avgDir = T > 1 ? acc[p] * inv : acc[p];
+    const float r = T > 1 ? acc[P + 3 * p] * inv : acc[P + 3 * p];
+    const float gch = T > 1 ? acc[P + 3 * p + 1] * inv : acc[P + 3 * p + 1];
+    const float bch = T > 1 ? acc[P + 3 * p + 2] * inv : acc[P + 3 * p + 2];
+    const double rd = round_fmt(avgDir, "%.3g"), rr = round_fmt(r, "%.3g"), rg = round_fmt(gch, "%.3g"), rb = round_fmt(bch, "%.3g");
+    lb[p] = rd * omega[p] * durationHours / 1000.0;
+    lb[P + p] = (0.265074126 * rr + 0.670114631 * rg + 0.064811243 * rb) * omega[p] * durationHours / 1000.0;
+    lb[2 * P + p] = lb[p] + lb[P + p];
+    mean += lb[2 * P + p];
+  }
+  lb[3 * P] = grefl * mean / static_cast<double>(P);
   return nullptr;
 }
 

@@ -123,6 +123,8 @@ SIGNATURES = [
     ("kgb_server_timing", None, [c_void_p, POINTER(c_double)]),
     ("kgb_sky", c_int, [_E, c_int32, c_void_p, c_size_t, c_double, c_int32, c_int32, c_int32, c_void_p]),
     ("kgb_sun_noaa", c_int, [_E, c_void_p, c_size_t, c_void_p]),
+    ("kgb_sky_ladybug", c_int, [_E, c_int32, c_void_p, c_size_t, c_double, c_double, c_double, c_double, c_double, c_void_p, c_void_p, c_void_p,
+                                c_void_p]),
     ("kgb_set_builder", c_int, [_E, c_int]),
     ("kgb_set_series_form", c_int, [_E, c_int]),
     ("kgb_trace_counters", c_int, [_E, c_size_t, c_size_t, c_uint32, POINTER(c_uint64)]),
@@ -247,6 +249,22 @@ class Engine:
         out = np.zeros((len(steps), P + 1, 3), np.float32)
         self._ok(self.d.kgb_sky(self.h, mf, st.ctypes.data_as(c_void_p), len(st), grefl, int(sun), int(sky), int(visible), _p(out)))
         return out
+
+    def sky_ladybug(self, mf, steps, lat, lon, tz, grefl=0.2, duration_hours=None, series=False):
+        """Ladybug mode's sky: steps [T x 4] (jd, hour, dni, dhi). Returns (lb [3P + 1] doubles, acc [4P + 6] floats) and,
+        with series, also (S [P x Tup], g [Tup]) of the steps with DNI + DHI > 1e-4."""
+        steps = np.ascontiguousarray(steps, np.float64).reshape(-1, 4)
+        T = len(steps)
+        P = 144 * mf * mf + 1
+        dur = float(T) if duration_hours is None else float(duration_hours)
+        lb = np.zeros(3 * P + 1, np.float64)
+        acc = np.zeros(4 * P + 6, np.float32)
+        Tup = int(np.sum(steps[:, 2].astype(np.float32) + steps[:, 3].astype(np.float32) > 1e-4))
+        S = np.zeros((P, Tup), np.float32) if series else None
+        g = np.zeros(Tup, np.float32) if series else None
+        self._ok(self.d.kgb_sky_ladybug(self.h, mf, _p(steps), T, lat, lon, tz, grefl, dur, _p(lb), _p(acc), _p(S) if series else None,
+                                        _p(g) if series else None))
+        return (lb, acc, S, g) if series else (lb, acc)
 
     def sun_noaa(self, rows):
         """rows: [T x 7] (lat, lon, tz, month, day, hour, leap). Returns [T x 6] (alt, azi, up, x, y, z)."""

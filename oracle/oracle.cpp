@@ -1050,6 +1050,9 @@ KGB_API void kgb_server_timing(kgb_server*, double* out) { for (int k = 0; k < 5
 KGB_API int kgb_sky(kgb_engine*, int32_t, const kgb_sky_step*, size_t, double, int32_t, int32_t, int32_t, float*) {
   return fail("kgb_sky: the sky's checker is the reference's own code (tests/golden/sky)");
 }
+KGB_API int kgb_sky_ladybug(kgb_engine*, int32_t, const double*, size_t, double, double, double, double, double, double*, float*, float*, float*) {
+  return fail("kgb_sky_ladybug: the sky is not restated here (the reference's own sky code is the checker: tests/golden/ladybug)");
+}
 KGB_API int kgb_sun_noaa(kgb_engine*, const double*, size_t, double*) {
   return fail("kgb_sun_noaa: the sun's checker is the reference's own code (tests/golden/sky)");
 }

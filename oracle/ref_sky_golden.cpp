@@ -9,7 +9,15 @@
 //                                      the binned sun alone, ground 0.2), on the reference's own host code, serial as in
 //                                      run.cpp:372-446. IN: N x 2 doubles (DNI, DHI) per hour of a non-leap year;
 //                                      OUT: 1 double, the seconds it took
+//   ref_sky_golden ladybug EPW OUT 0 MF GREFL
+//                                      ladybug mode's sky (the reference's run.cpp:362-398 and 447-470, restated here
+//                                      over the reference's own read_epw, make_steps, sun_radiance, gendaymtx_step and
+//                                      round_fmt) for the annual steps of the EPW. OUT: 7 doubles (T, P, Tup,
+//                                      durationHours, lat, lon, tz), steps [T x 4] doubles (jd, hour, DNI, DHI), the float
+//                                      accumulators [4 P + 6] (accDir, accDif, ground direct, ground diffuse), the weights
+//                                      [3 P + 1] doubles (skyDirLB, skyDifLB, skyRad, gndLB), S [P x Tup] and g [Tup] floats
 #include "internal.h"
+#include <cmath>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -18,7 +26,93 @@
 
 using namespace daylight;
 
+// run.cpp:23-27
+constexpr double kRf = 0.265074126, kGf = 0.670114631, kBf = 0.064811243;
+inline double bright(const float* rgb) { return kRf * rgb[0] + kGf * rgb[1] + kBf * rgb[2]; }
+
+static int ladybug(const char* epw, std::FILE* fo, int mf, double grefl) {
+  Weather w;
+  std::string err;
+  if (!read_epw(epw, w, err)) { std::fprintf(stderr, "%s\n", err.c_str()); return 5; }
+  Options opt;
+  opt.t0 = NAN;
+  opt.t1 = NAN;
+  std::vector<Step> steps;
+  if (!make_steps(opt, &w, steps, err, 0)) { std::fprintf(stderr, "%s\n", err.c_str()); return 6; }
+  const size_t T = steps.size();
+  const Patches pa = make_patches(mf);
+  const size_t Pz = size_t(pa.P);
+  double durationHours = 0;
+  for (const Step& st : steps) durationHours += st.dt;
+  const double lat = w.lat, lon = w.lon, tz = w.tz;
+  const double latW = round_fmt(lat, "%.2f"), lonWestW = round_fmt(-lon, "%.2f"), meridW = static_cast<double>(static_cast<int>(-w.tz * 15.0));
+  std::vector<int> colOf(T, -1);
+  int Tup = 0;
+  for (size_t t = 0; t < T; ++t) if (steps[t].dni + steps[t].dhi > 1e-4) colOf[t] = Tup++;
+  std::vector<float> S(Pz * size_t(Tup), 0.f), gS(size_t(Tup), 0.f), buf(3 * (Pz + 1)), buf2(3 * (Pz + 1));
+  std::vector<float> accDir(Pz, 0.f), accDif(3 * Pz, 0.f), gDif(3, 0.f), gDir(3, 0.f);
+  for (size_t t = 0; t < T; ++t) {
+    const Step& st = steps[t];
+    const int col = colOf[t];
+    double altS, aziS;
+    sun_radiance(latW, lonWestW, meridW, st.jd, st.hour, altS, aziS);
+    const double dniW = static_cast<double>(static_cast<int>(st.dni)), dhiW = static_cast<double>(static_cast<int>(st.dhi));
+    gendaymtx_step(pa, st.jd, altS, aziS, dniW, dhiW, grefl, true, false, false, buf.data());
+    gendaymtx_step(pa, st.jd, altS, aziS, dniW, dhiW, grefl, false, true, false, buf2.data());
+    for (int ch = 0; ch < 3; ++ch) { gDir[size_t(ch)] += buf[size_t(ch)]; gDif[size_t(ch)] += buf2[size_t(ch)]; }
+    double meanPatch = 0;
+    for (size_t p = 0; p < Pz; ++p) {
+      const float* dr = &buf[3 * (p + 1)];
+      const float* df = &buf2[3 * (p + 1)];
+      accDir[p] += dr[0];
+      for (int ch = 0; ch < 3; ++ch) accDif[3 * p + size_t(ch)] += df[ch];
+      if (col >= 0) {
+        const double Lp = bright(df) + dr[0];
+        S[p * size_t(Tup) + size_t(col)] = static_cast<float>(Lp);
+        meanPatch += Lp * pa.omega[p];
+      }
+    }
+    if (col >= 0) gS[size_t(col)] = static_cast<float>(grefl * meanPatch / static_cast<double>(pa.P));
+  }
+  const float inv = static_cast<float>(1.0 / static_cast<double>(T));
+  std::vector<double> lb(3 * Pz + 1, 0.0);
+  double mean = 0;
+  for (size_t p = 0; p < Pz; ++p) {
+    const float avgDir = T > 1 ? accDir[p] * inv : accDir[p];
+    const float r = T > 1 ? accDif[3 * p] * inv : accDif[3 * p];
+    const float gch = T > 1 ? accDif[3 * p + 1] * inv : accDif[3 * p + 1];
+    const float b = T > 1 ? accDif[3 * p + 2] * inv : accDif[3 * p + 2];
+    const double rd = round_fmt(avgDir, "%.3g"), rr = round_fmt(r, "%.3g"), rg = round_fmt(gch, "%.3g"), rb = round_fmt(b, "%.3g");
+    lb[p] = rd * pa.omega[p] * durationHours / 1000.0;
+    lb[Pz + p] = (kRf * rr + kGf * rg + kBf * rb) * pa.omega[p] * durationHours / 1000.0;
+    lb[2 * Pz + p] = lb[p] + lb[Pz + p];
+    mean += lb[2 * Pz + p];
+  }
+  lb[3 * Pz] = grefl * mean / static_cast<double>(pa.P);
+  const double head[7] = {double(T), double(Pz), double(Tup), durationHours, lat, lon, tz};
+  std::fwrite(head, 8, 7, fo);
+  for (const Step& st : steps) {
+    const double row[4] = {double(st.jd), st.hour, double(st.dni), double(st.dhi)};
+    std::fwrite(row, 8, 4, fo);
+  }
+  std::fwrite(accDir.data(), 4, Pz, fo);
+  std::fwrite(accDif.data(), 4, 3 * Pz, fo);
+  std::fwrite(gDir.data(), 4, 3, fo);
+  std::fwrite(gDif.data(), 4, 3, fo);
+  std::fwrite(lb.data(), 8, lb.size(), fo);
+  std::fwrite(S.data(), 4, S.size(), fo);
+  std::fwrite(gS.data(), 4, gS.size(), fo);
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc >= 7 && !std::strcmp(argv[1], "ladybug")) {
+    std::FILE* fo = std::fopen(argv[3], "wb");
+    if (!fo) return 3;
+    const int rc = ladybug(argv[2], fo, std::atoi(argv[5]), std::atof(argv[6]));
+    std::fclose(fo);
+    return rc;
+  }
   if (argc < 5) return 2;
   const size_t n = std::strtoul(argv[4], nullptr, 10);
   std::FILE* fi = std::fopen(argv[2], "rb");

@@ -9,7 +9,8 @@ written with its inputs and results to tests/golden/<case>/. The tests replay th
 It also extracts the reference's published outputs for tests/box.obj from its docs (docs/daylight.md, docs/views.md:
 the example blocks) into published.json, and checks the recorded runs against them.
 
-usage: python tests/golden/make_golden.py [--ref REFERENCE_CHECKOUT]  (default: $KITSIM_REFERENCE, else ../reference beside the repo)
+usage: python tests/golden/make_golden.py [--ref REFERENCE_CHECKOUT] [--only urban_ladybug,ladybug,...]
+       (the reference: $KITSIM_REFERENCE, else ../reference beside the repo)
 """
 import argparse
 import ctypes
@@ -46,8 +47,12 @@ CASES = {
     # and the per-quantity weights under the synthetic urban weather, from a one-quad run (they do not depend on the
     # geometry); the bench traces the full block with them
     "urban_sky": (DL_DAYLIGHT, ["--epw", "@TMP@/urban.epw", "--sky-density", "2", "--quantity", "radiation,irradiance,illuminance,sunhours"]),
+    # ladybug mode on the same weather year (gendaymtx -A as ladybug runs it: .wea-rounded site and irradiance, float
+    # accumulation, %.3g): its weights pin the ladybug goldens below (tests/golden/ladybug)
+    "urban_ladybug": (DL_DAYLIGHT, ["--epw", "@TMP@/urban.epw", "--mode", "ladybug", "--sky-density", "2", "--quantity", "radiation,direct,diffuse"]),
 }
-MESH = {"urban_sky": "quad"}   # cases on one 1 m quad instead of tests/box.obj
+MESH = {"urban_sky": "quad", "urban_ladybug": "quad"}   # cases on one 1 m quad instead of tests/box.obj
+LADYBUG_COLS = 256   # series columns of the ladybug goldens kept (the first ones)
 
 
 def urban_weather(ref, tmp):
@@ -131,7 +136,7 @@ def run_case(name, ref):
     tmp = os.path.join(out, "_tmp")
     os.makedirs(tmp, exist_ok=True)
     argv = [a.replace("@TMP@", tmp) for a in argv]
-    if name == "urban_sky":
+    if name in ("urban_sky", "urban_ladybug"):
         urban_weather(ref, tmp)
     L, run = _lib(ref)
     res = run(L, tool, argv, MESH.get(name, "box"))
@@ -219,24 +224,73 @@ def sky_goldens(ref):
     print("sky: %d sun rows, %d sky cases" % (n, len(cases)))
 
 
+def record(name, ref):
+    """One case's run of the reference's dl_run with the boundary recorder on, into tests/golden/<name>/."""
+    d = os.path.join(HERE, name)
+    shutil.rmtree(d, ignore_errors=True)
+    os.makedirs(d)
+    env = dict(os.environ, KGB_RECORD=d, KGB_ORACLE_THREADS="8")
+    subprocess.check_call([sys.executable, __file__, "--ref", ref, "--case", name], env=env)
+    n = sum(1 for _ in open(os.path.join(d, "calls.jsonl")))
+    print("%s: %d calls recorded" % (name, n))
+
+
+def ladybug_goldens(ref):
+    """Ladybug mode's sky on the urban weather year at sky densities 1 and 2, from the reference's own functions
+    (oracle/ref_sky_golden.cpp, mode ladybug): the steps, the float accumulators, the weights, and the first
+    LADYBUG_COLS series columns. tests/golden/ladybug/mf<k>.npz"""
+    d = os.path.join(HERE, "ladybug")
+    shutil.rmtree(d, ignore_errors=True)
+    os.makedirs(d)
+    tmp = os.path.join(d, "_tmp")
+    os.makedirs(tmp)
+    urban_weather(ref, tmp)
+    exe = os.path.join(REPO, "oracle", "_ref", "ref_sky_golden")
+    for mf in (1, 2):
+        raw = os.path.join(tmp, "lb.bin")
+        subprocess.check_call([exe, "ladybug", os.path.join(tmp, "urban.epw"), raw, "0", str(mf), "0.2"])
+        b = open(raw, "rb").read()
+        head = np.frombuffer(b, np.float64, 7)
+        T, P, Tup = int(head[0]), int(head[1]), int(head[2])
+        at = 56
+        steps = np.frombuffer(b, np.float64, 4 * T, at).reshape(T, 4); at += 32 * T
+        acc = np.frombuffer(b, np.float32, 4 * P + 6, at); at += 4 * (4 * P + 6)
+        lb = np.frombuffer(b, np.float64, 3 * P + 1, at); at += 8 * (3 * P + 1)
+        S = np.frombuffer(b, np.float32, P * Tup, at).reshape(P, Tup); at += 4 * P * Tup
+        g = np.frombuffer(b, np.float32, Tup, at)
+        np.savez_compressed(os.path.join(d, "mf%d.npz" % mf), head=head, steps=steps, acc=acc, lb=lb, S=np.ascontiguousarray(S[:, :LADYBUG_COLS]),
+                            g=g[:LADYBUG_COLS].copy(), grefl=0.2)
+        print("ladybug mf %d: %d steps, %d patches, %d series columns" % (mf, T, P, Tup))
+    shutil.rmtree(tmp, ignore_errors=True)
+    for f in ("weather.npy", "cloud_factor.npy"):   # the urban_sky case keeps the weather year
+        if os.path.exists(os.path.join(d, f)):
+            os.remove(os.path.join(d, f))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("KITSIM_REFERENCE") or os.path.join(os.path.dirname(REPO), "reference"))
     ap.add_argument("--case")
+    ap.add_argument("--only", help="comma-separated parts to regenerate: recorded case names, sky, ladybug")
     a = ap.parse_args()
     if a.case:
         run_case(a.case, a.ref)
         return
+    if a.only:
+        subprocess.check_call(["make", "-s", "-j8", "-C", os.path.join(REPO, "oracle"), "ref", "REF=" + a.ref])
+        for part in a.only.split(","):
+            if part == "sky":
+                sky_goldens(a.ref)
+            elif part == "ladybug":
+                ladybug_goldens(a.ref)
+            else:
+                record(part, a.ref)
+        return
     subprocess.check_call(["make", "-s", "-j8", "-C", os.path.join(REPO, "oracle"), "ref", "REF=" + a.ref])
     for name in CASES:
-        d = os.path.join(HERE, name)
-        shutil.rmtree(d, ignore_errors=True)
-        os.makedirs(d)
-        env = dict(os.environ, KGB_RECORD=d, KGB_ORACLE_THREADS="8")
-        subprocess.check_call([sys.executable, __file__, "--ref", a.ref, "--case", name], env=env)
-        n = sum(1 for _ in open(os.path.join(d, "calls.jsonl")))
-        print("%s: %d calls recorded" % (name, n))
+        record(name, a.ref)
     sky_goldens(a.ref)
+    ladybug_goldens(a.ref)
     pub = published(a.ref)
     with open(os.path.join(HERE, "published.json"), "w") as f:
         json.dump(pub, f, indent=1)
