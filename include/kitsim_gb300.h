@@ -210,6 +210,25 @@ KGB_API uint32_t kgb_bounce_flags(int cullBackfaces);
  * out[5] = 1 when the last trace wrote bytes. */
 KGB_API void kgb_dims(const kgb_engine* e, uint64_t out[6]);
 
+/* --- scene preparation (the reference's host code beside its GPU contract, here on the GPU) ------------------------ */
+/* replaces triangulate_into (src/mesh.cpp:137-168; scene_acquire calls it per mesh): one mesh's faces as triangles.
+ * points [nPoints x 3] doubles, counts [nFaces] corners per face, indices [sum of counts], faceSlot [nFaces] the face's
+ * optics slot (NULL: 0), c [3] the centre the scene is recentred on. Writes v [nPoints x 3] floats (each point minus c),
+ * tri [capacity x 3] (vertex indices + base) and slot [capacity] (slotBase + the face's slot; NULL: none), capacity =
+ * sum over faces of max(0, corners - 2); triangles in face order: a triangle as given, a quad as 0-1-2 and 0-2-3, five or
+ * more corners by ear clipping on the face's Newell plane (include/kgb_earcut.h, mapbox earcut's algorithm, at most
+ * corners - 2 of them). *made: the triangles written; *skipped: the faces that gave none (fewer than 3 corners, no
+ * area, or no ear). */
+KGB_API int kgb_triangulate(kgb_engine* e, const double* points, size_t nPoints, const int32_t* counts, size_t nFaces, const int32_t* indices,
+                            const uint32_t* faceSlot, const double* c, uint32_t base, uint32_t slotBase, float* v, uint32_t* tri, uint32_t* slot,
+                            size_t* made, int32_t* skipped);
+/* replaces thin_solid (src/mesh.cpp:275-304) for every slot of a mesh at once: flags[s] (s < nSlots) = KGB_SLOT_THIN,
+ * with KGB_SLOT_TWIN (no volume: twice the volume over the area under 1e-5 m) or KGB_SLOT_INWARD (negative volume), when
+ * slot s's faces weld (0.01 mm grid, recentred on c) into a closed surface (every directed edge matched by its reverse)
+ * with twice the volume over the area under 0.1 m; else 0. */
+KGB_API int kgb_thin_solids(kgb_engine* e, const double* points, size_t nPoints, const int32_t* counts, size_t nFaces, const int32_t* indices,
+                            const uint32_t* faceSlot, uint32_t nSlots, const double* c, uint32_t* flags);
+
 /* --- sky (no C ABI counterpart in the reference: it builds its sky on the host) ---------------------------------- */
 /* One time step of the sky model, the inputs of the reference's gendaymtx_step (src/sky.cpp:297): day of year (as
  * gendaymtx computes it), sun altitude and azimuth (radians, azimuth clockwise from north), DNI and DHI (W/m2). */

@@ -758,6 +758,18 @@ KGB_API int kgb_sky(kgb_engine* e, int32_t mf, const kgb_sky_step* steps, size_t
   if (const char* why = sky_steps(mf, steps, T, grefl, sun, sky, visible, out, E(e)->st)) return fail(why);
   return 1;
 }
+KGB_API int kgb_triangulate(kgb_engine* e, const double* points, size_t nPoints, const int32_t* counts, size_t nFaces, const int32_t* indices,
+                            const uint32_t* faceSlot, const double* c, uint32_t base, uint32_t slotBase, float* v, uint32_t* tri, uint32_t* slot,
+                            size_t* made, int32_t* skipped) {
+  const std::string why = triangulate_mesh(points, nPoints, counts, nFaces, indices, faceSlot, c, base, slotBase, v, tri, slot, made, skipped, E(e)->st);
+  return why.empty() ? 1 : fail("kgb_triangulate: " + why);
+}
+KGB_API int kgb_thin_solids(kgb_engine* e, const double* points, size_t nPoints, const int32_t* counts, size_t nFaces, const int32_t* indices,
+                            const uint32_t* faceSlot, uint32_t nSlots, const double* c, uint32_t* flags) {
+  const std::string why = thin_solids(points, nPoints, counts, nFaces, indices, faceSlot, nSlots, c, flags, E(e)->st);
+  return why.empty() ? 1 : fail("kgb_thin_solids: " + why);
+}
+
 KGB_API int kgb_sky_ladybug(kgb_engine* e, int32_t mf, const double* steps, size_t T, double lat, double lon, double tz, double grefl,
                             double durationHours, double* lb, float* acc, float* S, float* g) {
   if (!lb) return fail("kgb_sky_ladybug: no weights to write");

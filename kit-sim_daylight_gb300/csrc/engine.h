@@ -204,6 +204,12 @@ void engine_reduce_inputs(kgb_engine* e, ReduceInputs& in);
 // sky (sky.cu): Perez sky of T steps, NOAA sun positions; null or what failed
 const char* sky_steps(int mf, const kgb_sky_step* steps, size_t T, double grefl, int sun, int sky, int visible, float* out, cudaStream_t st);
 const char* sun_steps(const double* in, size_t T, double* out, cudaStream_t st);
+// the scene's preparation on the GPU (mesh.cu): "" or what failed
+std::string triangulate_mesh(const double* points, size_t nPoints, const int32_t* counts, size_t nFaces, const int32_t* indices, const uint32_t* faceSlot,
+                             const double* c, uint32_t base, uint32_t slotBase, float* v, uint32_t* tri, uint32_t* slot, size_t* made, int32_t* skipped,
+                             cudaStream_t st);
+std::string thin_solids(const double* points, size_t nPoints, const int32_t* counts, size_t nFaces, const int32_t* indices, const uint32_t* faceSlot,
+                        uint32_t nSlots, const double* c, uint32_t* flags, cudaStream_t st);
 // ladybug mode's sky (kgb_sky_ladybug); null or what failed
 const char* sky_ladybug(int mf, const double* steps, size_t T, double lat, double lon, double tz, double grefl, double durationHours,
                         double* lb, float* acc, float* S, float* g, cudaStream_t st);

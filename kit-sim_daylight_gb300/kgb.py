@@ -123,6 +123,9 @@ SIGNATURES = [
     ("kgb_server_timing", None, [c_void_p, POINTER(c_double)]),
     ("kgb_sky", c_int, [_E, c_int32, c_void_p, c_size_t, c_double, c_int32, c_int32, c_int32, c_void_p]),
     ("kgb_sun_noaa", c_int, [_E, c_void_p, c_size_t, c_void_p]),
+    ("kgb_triangulate", c_int, [_E, c_void_p, c_size_t, c_void_p, c_size_t, c_void_p, c_void_p, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p,
+                                c_void_p, POINTER(c_size_t), POINTER(c_int32)]),
+    ("kgb_thin_solids", c_int, [_E, c_void_p, c_size_t, c_void_p, c_size_t, c_void_p, c_void_p, c_uint32, c_void_p, c_void_p]),
     ("kgb_sky_ladybug", c_int, [_E, c_int32, c_void_p, c_size_t, c_double, c_double, c_double, c_double, c_double, c_void_p, c_void_p, c_void_p,
                                 c_void_p]),
     ("kgb_set_builder", c_int, [_E, c_int]),
@@ -249,6 +252,35 @@ class Engine:
         out = np.zeros((len(steps), P + 1, 3), np.float32)
         self._ok(self.d.kgb_sky(self.h, mf, st.ctypes.data_as(c_void_p), len(st), grefl, int(sun), int(sky), int(visible), _p(out)))
         return out
+
+    def triangulate(self, points, counts, indices, face_slot=None, c=(0.0, 0.0, 0.0), base=0, slot_base=0):
+        """One mesh's faces as triangles (the reference's triangulate_into): (v [nPoints x 3] float32, tri [made x 3],
+        slot [made], skipped faces)."""
+        points = np.ascontiguousarray(points, np.float64).reshape(-1, 3)
+        counts = np.ascontiguousarray(counts, np.int32)
+        indices = np.ascontiguousarray(indices, np.int32)
+        fs = None if face_slot is None else np.ascontiguousarray(face_slot, np.uint32)
+        cap = int(np.maximum(counts.astype(np.int64) - 2, 0).sum())
+        v = np.zeros((len(points), 3), np.float32)
+        tri = np.zeros((max(cap, 1), 3), np.uint32)
+        slot = np.zeros(max(cap, 1), np.uint32)
+        cc = np.ascontiguousarray(c, np.float64)
+        made, skipped = c_size_t(0), c_int32(0)
+        self._ok(self.d.kgb_triangulate(self.h, _p(points), len(points), _p(counts), len(counts), _p(indices), _p(fs), _p(cc), base, slot_base,
+                                        _p(v), _p(tri), _p(slot), ctypes.byref(made), ctypes.byref(skipped)))
+        return v, tri[:made.value], slot[:made.value], skipped.value
+
+    def thin_solids(self, points, counts, indices, face_slot=None, n_slots=1, c=(0.0, 0.0, 0.0)):
+        """Per slot: KGB_SLOT_THIN (| TWIN or INWARD) when its faces form a closed thin solid, else 0 (the reference's
+        thin_solid for every slot)."""
+        points = np.ascontiguousarray(points, np.float64).reshape(-1, 3)
+        counts = np.ascontiguousarray(counts, np.int32)
+        indices = np.ascontiguousarray(indices, np.int32)
+        fs = None if face_slot is None else np.ascontiguousarray(face_slot, np.uint32)
+        flags = np.zeros(n_slots, np.uint32)
+        cc = np.ascontiguousarray(c, np.float64)
+        self._ok(self.d.kgb_thin_solids(self.h, _p(points), len(points), _p(counts), len(counts), _p(indices), _p(fs), n_slots, _p(cc), _p(flags)))
+        return flags
 
     def sky_ladybug(self, mf, steps, lat, lon, tz, grefl=0.2, duration_hours=None, series=False):
         """Ladybug mode's sky: steps [T x 4] (jd, hour, dni, dhi). Returns (lb [3P + 1] doubles, acc [4P + 6] floats) and,

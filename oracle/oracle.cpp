@@ -1050,6 +1050,13 @@ KGB_API void kgb_server_timing(kgb_server*, double* out) { for (int k = 0; k < 5
 KGB_API int kgb_sky(kgb_engine*, int32_t, const kgb_sky_step*, size_t, double, int32_t, int32_t, int32_t, float*) {
   return fail("kgb_sky: the sky's checker is the reference's own code (tests/golden/sky)");
 }
+KGB_API int kgb_triangulate(kgb_engine*, const double*, size_t, const int32_t*, size_t, const int32_t*, const uint32_t*, const double*, uint32_t, uint32_t,
+                            float*, uint32_t*, uint32_t*, size_t*, int32_t*) {
+  return fail("kgb_triangulate: not restated here (the reference's own mesh code is the checker: tests/golden/mesh)");
+}
+KGB_API int kgb_thin_solids(kgb_engine*, const double*, size_t, const int32_t*, size_t, const int32_t*, const uint32_t*, uint32_t, const double*, uint32_t*) {
+  return fail("kgb_thin_solids: not restated here (the reference's own mesh code is the checker: tests/golden/mesh)");
+}
 KGB_API int kgb_sky_ladybug(kgb_engine*, int32_t, const double*, size_t, double, double, double, double, double, double*, float*, float*, float*) {
   return fail("kgb_sky_ladybug: the sky is not restated here (the reference's own sky code is the checker: tests/golden/ladybug)");
 }

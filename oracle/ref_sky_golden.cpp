@@ -16,6 +16,11 @@
 //                                      durationHours, lat, lon, tz), steps [T x 4] doubles (jd, hour, DNI, DHI), the float
 //                                      accumulators [4 P + 6] (accDir, accDif, ground direct, ground diffuse), the weights
 //                                      [3 P + 1] doubles (skyDirLB, skyDifLB, skyRad, gndLB), S [P x Tup] and g [Tup] floats
+//   ref_sky_golden mesh IN OUT 0       the reference's triangulate_into and thin_solid (src/mesh.cpp) on one mesh.
+//                                      IN: u64 nPoints, nFaces, nIdx; 3 doubles c; points [nPoints x 3] doubles; counts
+//                                      [nFaces] i32; indices [nIdx] i32; slots [nFaces] u16. OUT: u64 made, i64 skipped,
+//                                      u64 nSlots; v [nPoints x 3] f32; tri [made x 3] u32; slot [made] u32 (slot base
+//                                      0, vertex base 0); thin_solid of each slot [nSlots] u32
 #include "internal.h"
 #include <cmath>
 #include <chrono>
@@ -105,7 +110,46 @@ static int ladybug(const char* epw, std::FILE* fo, int mf, double grefl) {
   return 0;
 }
 
+static int mesh(std::FILE* fi, std::FILE* fo) {
+  uint64_t head[3];
+  double c[3];
+  if (std::fread(head, 8, 3, fi) != 3 || std::fread(c, 8, 3, fi) != 3) return 4;
+  SimulationMesh m;
+  m.points.resize(3 * head[0]);
+  m.counts.resize(head[1]);
+  m.indices.resize(head[2]);
+  m.slot.resize(head[1]);
+  if (std::fread(m.points.data(), 8, m.points.size(), fi) != m.points.size() || std::fread(m.counts.data(), 4, m.counts.size(), fi) != m.counts.size() ||
+      std::fread(m.indices.data(), 4, m.indices.size(), fi) != m.indices.size() || std::fread(m.slot.data(), 2, m.slot.size(), fi) != m.slot.size())
+    return 4;
+  const size_t cap = tri_cap(m);
+  std::vector<float3> v(m.numPoints());
+  std::vector<uint3> tri(cap);
+  std::vector<uint32_t> slots(cap);
+  int skipped = 0;
+  const size_t made = triangulate_into(m, c, v.data(), tri.data(), slots.data(), 0, 0, skipped);
+  const uint64_t nSlots = m.slot.empty() ? 1 : uint64_t(slot_count(m));
+  std::vector<uint32_t> thin(nSlots);
+  for (uint64_t s = 0; s < nSlots; ++s) thin[s] = thin_solid(m, unsigned(s), c);
+  const uint64_t out[3] = {uint64_t(made), uint64_t(int64_t(skipped)), nSlots};
+  std::fwrite(out, 8, 3, fo);
+  std::fwrite(v.data(), 4, 3 * v.size(), fo);
+  std::fwrite(tri.data(), 4, 3 * made, fo);
+  std::fwrite(slots.data(), 4, made, fo);
+  std::fwrite(thin.data(), 4, thin.size(), fo);
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc >= 4 && !std::strcmp(argv[1], "mesh")) {
+    std::FILE* fi = std::fopen(argv[2], "rb");
+    std::FILE* fo = std::fopen(argv[3], "wb");
+    if (!fi || !fo) return 3;
+    const int rc = mesh(fi, fo);
+    std::fclose(fi);
+    std::fclose(fo);
+    return rc;
+  }
   if (argc >= 7 && !std::strcmp(argv[1], "ladybug")) {
     std::FILE* fo = std::fopen(argv[3], "wb");
     if (!fo) return 3;

@@ -9,7 +9,7 @@ written with its inputs and results to tests/golden/<case>/. The tests replay th
 It also extracts the reference's published outputs for tests/box.obj from its docs (docs/daylight.md, docs/views.md:
 the example blocks) into published.json, and checks the recorded runs against them.
 
-usage: python tests/golden/make_golden.py [--ref REFERENCE_CHECKOUT] [--only urban_ladybug,ladybug,...]
+usage: python tests/golden/make_golden.py [--ref REFERENCE_CHECKOUT] [--only urban_ladybug,ladybug,mesh,...]
        (the reference: $KITSIM_REFERENCE, else ../reference beside the repo)
 """
 import argparse
@@ -267,6 +267,110 @@ def ladybug_goldens(ref):
             os.remove(os.path.join(d, f))
 
 
+def golden_meshes(rng):
+    """Seeded meshes for the triangulation and thin-solid goldens: (name, points, counts, indices, slots, centre)."""
+    out = []
+    # n-gons: star-shaped (concave) rings of 5..60 corners on tilted planes, convex rings, rings with duplicate and
+    # collinear corners, a self-touching ring, degenerate faces; mixed with triangles, quads and faces of 0..2 corners
+    pts, counts, idx, slots = [], [], [], []
+    def add(ring, slot):
+        base = len(pts)
+        pts.extend(ring)
+        counts.append(len(ring))
+        idx.extend(range(base, base + len(ring)))
+        slots.append(slot)
+    for k in range(220):
+        kind = rng.integers(0, 7)
+        n = int(rng.integers(5, 61))
+        ang = np.sort(rng.uniform(0, 2 * np.pi, n))
+        rad = rng.uniform(0.3, 1.0, n) if kind in (0, 1) else np.ones(n)
+        ring2 = np.stack([np.cos(ang) * rad, np.sin(ang) * rad], 1) * rng.uniform(0.5, 300)
+        if kind == 2:   # duplicate and collinear corners
+            ring2 = np.concatenate([ring2, ring2[:3]])[: n + 3]
+            ring2[2] = ring2[1]
+            ring2 = np.insert(ring2, 4, (ring2[3] + ring2[4]) / 2, axis=0)
+        if kind == 3:   # clockwise
+            ring2 = ring2[::-1]
+        ax = rng.normal(size=3); ax /= np.linalg.norm(ax)
+        u = np.cross(ax, [0.3, 0.5, 0.8]); u /= np.linalg.norm(u)
+        w = np.cross(ax, u)
+        o = rng.uniform(-2000, 2000, 3)
+        ring = o + ring2[:, :1] * u + ring2[:, 1:2] * w
+        if kind == 4:   # slightly warped
+            ring = ring + ax * rng.normal(0, 1e-3, (len(ring), 1))
+        if kind == 5:   # collinear: no area
+            ring = o + np.linspace(0, 1, n)[:, None] * u
+        if kind == 6:   # a bow tie (self-touching)
+            ring = o + np.array([[0, 0], [2, 2], [2, 0], [1, 1.0001], [0, 2], [-1, 1]])[:, :1] * u + np.array([[0, 0], [2, 2], [2, 0], [1, 1.0001], [0, 2], [-1, 1]])[:, 1:2] * w
+        add([tuple(p) for p in ring], int(rng.integers(0, 4)))
+        if k % 5 == 0:
+            add([tuple(o + [0, 0, 0]), tuple(o + [1, 0, 0]), tuple(o + [0, 1, 0])], 1)
+            add([tuple(o + [0, 0, 1]), tuple(o + [1, 0, 1]), tuple(o + [1, 1, 1]), tuple(o + [0, 1, 1])], 2)
+        if k % 37 == 0:
+            add([], 0)
+            add([tuple(o)], 0)
+            add([tuple(o), tuple(o + 1)], 3)
+    out.append(("ngons", np.array(pts, np.float64), np.array(counts, np.int32), np.array(idx, np.int32), np.array(slots, np.uint16),
+                np.array([12.5, -7.25, 3.0])))
+    # thin solids (check_mesh.cpp:278-309's shapes): a 20 x 20 x 0.01 m pane box (slot 0), the same box flipped (slot 1),
+    # an open box (slot 2), a 3 m cube (slot 3), a double-faced sheet (slot 4), two touching thin boxes (slot 5)
+    def box(x0, y0, z0, x1, y1, z1, flip=False):
+        c = [(x0, y0, z0), (x1, y0, z0), (x1, y1, z0), (x0, y1, z0), (x0, y0, z1), (x1, y0, z1), (x1, y1, z1), (x0, y1, z1)]
+        f = [[0, 3, 2, 1], [4, 5, 6, 7], [0, 1, 5, 4], [1, 2, 6, 5], [2, 3, 7, 6], [3, 0, 4, 7]]
+        if flip:
+            f = [q[::-1] for q in f]
+        return c, f
+    pts, counts, idx, slots = [], [], [], []
+    def add_box(c, faces, slot, drop=0):
+        base = len(pts)
+        pts.extend(c)
+        for q in faces[: len(faces) - drop]:
+            counts.append(4)
+            idx.extend(base + i for i in q)
+            slots.append(slot)
+    add_box(*box(0, 0, 1, 20, 20, 1.01), 0)
+    add_box(*box(30, 0, 1, 50, 20, 1.01, flip=True), 1)
+    add_box(*box(60, 0, 1, 80, 20, 1.01), 2, drop=1)
+    add_box(*box(-1.5, -1.5, 1, 1.5, 1.5, 4), 3)
+    sheet = [(0, 0, 10), (2, 0, 10), (2, 2, 10), (0, 2, 10)]
+    base = len(pts)
+    pts.extend(sheet)
+    for q in ([0, 1, 2, 3], [3, 2, 1, 0]):
+        counts.append(4); idx.extend(base + i for i in q); slots.append(4)
+    add_box(*box(100, 0, 0, 101, 1, 0.01), 5)
+    add_box(*box(101, 0, 0, 102, 1, 0.01), 5)
+    out.append(("solids", np.array(pts, np.float64), np.array(counts, np.int32), np.array(idx, np.int32), np.array(slots, np.uint16),
+                np.array([1e5, -3e5, 50.0])))
+    return out
+
+
+def mesh_goldens(ref):
+    """The reference's own triangulate_into and thin_solid (oracle/ref_sky_golden.cpp, mode mesh) on seeded meshes: the
+    n-gons through the engine's restatement of earcut (the reference's earcut stand-in here). tests/golden/mesh/<name>.npz"""
+    d = os.path.join(HERE, "mesh")
+    shutil.rmtree(d, ignore_errors=True)
+    os.makedirs(d)
+    exe = os.path.join(REPO, "oracle", "_ref", "ref_sky_golden")
+    for name, P, C, I, S, c in golden_meshes(np.random.default_rng(31)):
+        raw_in, raw_out = os.path.join(d, "in.bin"), os.path.join(d, "out.bin")
+        with open(raw_in, "wb") as f:
+            f.write(np.array([len(P), len(C), len(I)], np.uint64).tobytes() + c.astype(np.float64).tobytes() + P.tobytes() + C.tobytes() +
+                    I.tobytes() + S.tobytes())
+        subprocess.check_call([exe, "mesh", raw_in, raw_out, "0"])
+        b = open(raw_out, "rb").read()
+        made, skipped, nSlots = [int(x) for x in np.frombuffer(b, np.int64, 3)]
+        at = 24
+        v = np.frombuffer(b, np.float32, 3 * len(P), at).reshape(-1, 3); at += 12 * len(P)
+        tri = np.frombuffer(b, np.uint32, 3 * made, at).reshape(-1, 3); at += 12 * made
+        slot = np.frombuffer(b, np.uint32, made, at); at += 4 * made
+        thin = np.frombuffer(b, np.uint32, nSlots, at)
+        np.savez_compressed(os.path.join(d, name + ".npz"), points=P, counts=C, indices=I, slots=S, c=c, v=v, tri=tri, slot=slot, skipped=skipped,
+                            thin=thin)
+        os.remove(raw_in)
+        os.remove(raw_out)
+        print("mesh %s: %d faces, %d triangles, %d skipped, thin %s" % (name, len(C), made, skipped, thin.tolist()))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("KITSIM_REFERENCE") or os.path.join(os.path.dirname(REPO), "reference"))
@@ -283,6 +387,8 @@ def main():
                 sky_goldens(a.ref)
             elif part == "ladybug":
                 ladybug_goldens(a.ref)
+            elif part == "mesh":
+                mesh_goldens(a.ref)
             else:
                 record(part, a.ref)
         return
@@ -291,6 +397,7 @@ def main():
         record(name, a.ref)
     sky_goldens(a.ref)
     ladybug_goldens(a.ref)
+    mesh_goldens(a.ref)
     pub = published(a.ref)
     with open(os.path.join(HERE, "published.json"), "w") as f:
         json.dump(pub, f, indent=1)
