@@ -132,11 +132,16 @@ def profiled(key):
     return None
 
 
+def oracle_lib(pkg):
+    """The oracle (the checker, and the CPU legs' restatement), built from oracle/ if needed."""
+    subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle"), "all"])
+    return pkg.kgb.Lib(os.path.join(REPO, "oracle", "_build", "liboracle.so"))
+
+
 def cpu_baseline(pkg, scene, D, Ws, sample, seed=0):
     """The oracle (the CPU restatement) on the host's cores: trace + the four reduces of a seeded sensor sample."""
     sys.path.insert(0, os.path.join(REPO, "tests"))
-    subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle"), "all"])
-    lib = pkg.kgb.Lib(os.path.join(REPO, "oracle", "_build", "liboracle.so"))
+    lib = oracle_lib(pkg)
     o = pkg.kgb.Engine(lib)
     o.build(scene["v"], scene["tri"])
     pick = np.sort(np.random.default_rng(seed).choice(len(scene["P"]), sample, replace=False))
@@ -331,7 +336,8 @@ def run_ours(args, pkg):
     e.close()
     if rank == 0 and world == 1 and not args.no_extras and not args.sensors:
         # the other measured configurations, after the timed region: each keeps its own metric and config
-        for key, fn in (("precision", run_precision), ("views", run_views), ("serving", run_serving), ("serving_series", run_serving_series)):
+        for key, fn in (("precision", run_precision), ("views", run_views), ("serving", run_serving), ("serving_series", run_serving_series),
+                        ("ingest", run_ingest)):
             t0 = time.perf_counter()
             try:
                 line[key] = fn(args, pkg)
@@ -791,6 +797,74 @@ def run_serving_series(args, pkg):
             "dtype": "series: split-bf16 on tcgen05 (server) vs fp32 SIMT (plain form)"}
 
 
+# ---------------------------------------------------------------------------------------------- .dmesh ingest
+def dmesh_grid(n):
+    """The reference's ingest benchmark mesh (validate/ingest.py: an n x n quad grid, (n + 1)^2 points), as a .dmesh
+    image with a slot per face."""
+    xs, ys = np.meshgrid(np.arange(n + 1, dtype=np.float64), np.arange(n + 1, dtype=np.float64), indexing="ij")
+    P = np.stack([xs.ravel(), ys.ravel(), 0.01 * np.sin(xs.ravel()) * np.cos(ys.ravel())], 1)
+    q = np.arange(n * (n + 1)).reshape(n, n + 1)[:, :n].ravel()
+    I = np.stack([q, q + n + 1, q + n + 2, q + 1], 1).astype(np.int32).ravel()
+    C = np.full(n * n, 4, np.int32)
+    S = (np.arange(n * n) % 3).astype(np.uint16)
+    head = b"DLM1" + np.array([1], np.uint32).tobytes() + np.array([len(P), len(C), len(I)], np.uint64).tobytes()
+    return head + P.tobytes() + C.tobytes() + I.tobytes() + S.tobytes()
+
+
+def run_ingest(args, pkg):
+    """A 1000 x 1000 quad grid (2M triangles) as a .dmesh file in the page cache: read to the device and checked there
+    (kgb_mesh_file), then the scene built from it on the device (kgb_build_meshes: triangulation + BVH); beside it the
+    oracle's restatement of the reference's read_dmesh (whole file into host memory, arrays copied out, checked) on
+    one host core. Wall-clock seconds, median of the repeats."""
+    import tempfile
+    img = dmesh_grid(1000)
+    d = tempfile.mkdtemp(prefix="kgb_ingest_")
+    path = os.path.join(d, "grid.dmesh")
+    with open(path, "wb") as f:
+        f.write(img)
+    with open(path, "rb") as f:   # in the page cache, as a file just written or read before
+        f.read()
+    reps = max(3, args.steps)
+    e = pkg.engine()
+    try:
+        for _ in range(2):
+            e.mesh_free(e.mesh_file(path).id)
+        t_read, t_mem, t_build = [], [], []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            info = e.mesh_file(path)
+            t_read.append(time.perf_counter() - t0)
+            t0 = time.perf_counter()
+            made, skipped = e.build_meshes([info.id], [(info.lo[a] + info.hi[a]) / 2 for a in range(3)])
+            t_build.append(time.perf_counter() - t0)
+            e.mesh_free(info.id)
+            t0 = time.perf_counter()
+            e.mesh_free(e.mesh_read(img, "grid").id)
+            t_mem.append(time.perf_counter() - t0)
+        tris = int(made.sum())
+    finally:
+        e.close()
+    o = pkg.kgb.Engine(oracle_lib(pkg))
+    try:
+        t_cpu = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            o.mesh_free(o.mesh_file(path).id)
+            t_cpu.append(time.perf_counter() - t0)
+    finally:
+        o.close()
+    os.remove(path)
+    os.rmdir(d)
+    med = lambda x: float(np.median(x))
+    return {"metric": "s per .dmesh read", "unit": "s", "higher_is_better": False, "value": med(t_read),
+            "config": {"workload": "1000 x 1000 quad grid: 1,002,001 points, 1,000,000 quads with slots, %d bytes, page cache warm" % len(img),
+                       "repeats": reps},
+            "from_memory_s": med(t_mem), "build_scene_s": med(t_build), "triangles": tris, "skipped": skipped,
+            "cpu_baseline": {"value": med(t_cpu), "unit": "s", "cores": 1, "kind": "port",
+                             "sample": "the oracle's restatement of read_dmesh (src/mesh.cpp:480-489) on the same file"},
+            "read_gb_per_s": len(img) / med(t_read) / 1e9}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -801,7 +875,7 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=20000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sensors", type=int, default=0, help="urban / precision / views: only the first N sensors (a small case for profiling)")
-    ap.add_argument("--config", default="urban", choices=["urban", "precision", "views", "serving", "serving_series"])
+    ap.add_argument("--config", default="urban", choices=["urban", "precision", "views", "serving", "serving_series", "ingest"])
     ap.add_argument("--series-requests", type=int, default=64)
     ap.add_argument("--series-seed", type=int, default=12)
     ap.add_argument("--builder", type=int, default=1, choices=[0, 1], help="urban: 1 device LBVH with treelets (default), 0 host binned-SAH tree")
@@ -820,6 +894,8 @@ def main():
         print(json.dumps(run_serving(args, pkg)), flush=True)
     elif args.config == "serving_series":
         print(json.dumps(run_serving_series(args, pkg)), flush=True)
+    elif args.config == "ingest":
+        print(json.dumps(run_ingest(args, pkg)), flush=True)
     elif args.impl == "reference":
         run_reference(args, pkg)
     else:

@@ -229,6 +229,49 @@ KGB_API int kgb_triangulate(kgb_engine* e, const double* points, size_t nPoints,
 KGB_API int kgb_thin_solids(kgb_engine* e, const double* points, size_t nPoints, const int32_t* counts, size_t nFaces, const int32_t* indices,
                             const uint32_t* faceSlot, uint32_t nSlots, const double* c, uint32_t* flags);
 
+/* --- meshes read straight to the device (the reference reads them into host vectors) ------------------------------- */
+/* A .dmesh image (the reference's format, src/daylight.h:129-136: "DLM1", u32 flags (bit 0: a slot block), u64 nPoints,
+ * nFaces, nIndices; then float64 xyz points, int32 counts, int32 0-based indices, and with bit 0 one uint16 slot per
+ * face; little-endian, no padding) held by the engine on the device after the reference's checks. */
+typedef struct kgb_mesh_info {
+  uint32_t id;          /* the mesh's handle in this engine; KGB_NO_MESH when the image holds no faces (nothing is kept:
+                           the reference drops an empty mesh, src/mesh.cpp:472) */
+  uint32_t slots;       /* slot_count (src/mesh.cpp:170): 1 + the largest face slot, 1 without a slot block */
+  uint64_t nPoints, nFaces, nIndices;
+  uint32_t hasSlots;    /* the image had the slot block */
+  uint32_t maxCorners;  /* the largest face's corner count */
+  uint64_t triCap;      /* tri_cap (src/mesh.cpp:120-124): the sum over faces of corners - 2 */
+  double lo[3], hi[3];  /* the points' bounds, fmin / fmax per axis as bbox_centre takes them (src/mesh.cpp:107-118);
+                           +inf / -inf without points */
+} kgb_mesh_info;
+#define KGB_NO_MESH 0xffffffffu
+/* replaces read_dmesh(data, size, name, ...) (src/mesh.cpp:476-478 over parse_dmesh, 450-474): one image in host
+ * memory. The 32-byte header is checked on the host; the arrays are copied to the device (straight from page-locked
+ * memory, else through pinned slices) and checked there by the reference's rules (mesh_ok, src/mesh.cpp:436-445: faces
+ * of 3 or more corners, the counts summing to nIndices, every index within the points). A failure gives the reference's
+ * message, `name` first ("NAME: truncated", "NAME: vertex index out of range", ...). The engine keeps the arrays, with
+ * each face's first index, until kgb_mesh_free or kgb_destroy. Points, faces and indices beyond 2^32 - 1 are refused. */
+KGB_API int kgb_mesh_read(kgb_engine* e, const void* data, size_t size, const char* name, kgb_mesh_info* info);
+/* replaces read_dmesh(path, ...) (src/mesh.cpp:480-489): the file read in 32 MiB slices into two pinned buffers, each
+ * slice copied to the device while the next one is read; the checks and messages as kgb_mesh_read's, with the path as
+ * the name ("cannot open PATH", "PATH: truncated", ...). */
+KGB_API int kgb_mesh_file(kgb_engine* e, const char* path, kgb_mesh_info* info);
+/* A kept mesh's arrays back to the host (each pointer may be NULL; slot only when the image had the slot block). */
+KGB_API int kgb_mesh_download(kgb_engine* e, uint32_t id, double* points, int32_t* counts, int32_t* indices, uint16_t* slot);
+KGB_API int kgb_mesh_free(kgb_engine* e, uint32_t id);
+/* kgb_thin_solids on a kept mesh: flags [info.slots], its faces' slots as the image gives them. */
+KGB_API int kgb_mesh_thin_solids(kgb_engine* e, uint32_t id, const double* c, uint32_t* flags);
+/* replaces the scene assembly of scene_acquire (src/run.cpp:98-150) and its gpu_build, for kept meshes: no array of the
+ * scene passes through the host. Meshes ids[0 .. nMeshes) in the run's order; blocks[k] (NULL: all) whether mesh k
+ * blocks rays. As run.cpp lays it out: the points of the blocking meshes one after the other, recentred on c (the
+ * caller's bbox_centre over the infos' lo / hi); slot bases over every mesh, each mesh taking its info.slots; the
+ * triangles of the blocking meshes in mesh order, each mesh's faces triangulated as kgb_triangulate does, with its
+ * vertex base and slot base. The scene is then built as kgb_build builds it from those arrays (slots / nSlots /
+ * perSlot as there). made [nMeshes] (may be NULL): each mesh's triangles (0 for one that does not block); *skipped
+ * (may be NULL): the faces that gave none. */
+KGB_API int kgb_build_meshes(kgb_engine* e, const uint32_t* ids, size_t nMeshes, const uint8_t* blocks, const double* c, const kgb_slot* slots,
+                             size_t nSlots, int perSlot, uint64_t* made, int32_t* skipped);
+
 /* --- sky (no C ABI counterpart in the reference: it builds its sky on the host) ---------------------------------- */
 /* One time step of the sky model, the inputs of the reference's gendaymtx_step (src/sky.cpp:297): day of year (as
  * gendaymtx computes it), sun altitude and azimuth (radians, azimuth clockwise from north), DNI and DHI (W/m2). */

@@ -464,10 +464,10 @@ std::string build_bvh8_gpu(const float* v, size_t nv, const uint32_t* tri, size_
   const size_t tiles = (nt + 255) / 256;
   KGB_TRY(cudaMalloc(&dv.p, nv * 12));
   KGB_TRY(cudaMalloc(&dtri.p, nt * 12));
-  KGB_TRY(cudaMemcpyAsync(dv.p, v, nv * 12, cudaMemcpyHostToDevice, st));
-  KGB_TRY(cudaMemcpyAsync(dtri.p, tri, nt * 12, cudaMemcpyHostToDevice, st));
-  if (slot) { KGB_TRY(cudaMalloc(&dslot.p, nt * 4)); KGB_TRY(cudaMemcpyAsync(dslot.p, slot, nt * 4, cudaMemcpyHostToDevice, st)); }
-  if (translucent) { KGB_TRY(cudaMalloc(&dtr.p, nt)); KGB_TRY(cudaMemcpyAsync(dtr.p, translucent, nt, cudaMemcpyHostToDevice, st)); }
+  KGB_TRY(cudaMemcpyAsync(dv.p, v, nv * 12, cudaMemcpyDefault, st));
+  KGB_TRY(cudaMemcpyAsync(dtri.p, tri, nt * 12, cudaMemcpyDefault, st));
+  if (slot) { KGB_TRY(cudaMalloc(&dslot.p, nt * 4)); KGB_TRY(cudaMemcpyAsync(dslot.p, slot, nt * 4, cudaMemcpyDefault, st)); }
+  if (translucent) { KGB_TRY(cudaMalloc(&dtr.p, nt)); KGB_TRY(cudaMemcpyAsync(dtr.p, translucent, nt, cudaMemcpyDefault, st)); }
   // 1. eps
   KGB_TRY(cudaMalloc(&maxabs.p, 4));
   KGB_TRY(cudaMemsetAsync(maxabs.p, 0, 4, st));

@@ -9,6 +9,13 @@
 #include "engine.h"
 #include "rt.cuh"
 
+#include <thrust/device_ptr.h>
+#include <thrust/execution_policy.h>
+#include <thrust/functional.h>
+#include <thrust/reduce.h>
+
+#include <fcntl.h>
+#include <sys/stat.h>
 #include <unistd.h>
 
 #include <algorithm>
@@ -17,6 +24,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -299,6 +307,7 @@ struct Engine {
   int builder = 1;            // 1 device LBVH with treelet restructuring (default), 0 host binned SAH (kgb_set_builder)
   uint32_t nodeLimit = 0;     // kgb_set_limits: the walks see only this many of the BVH's nodes (0: all)
   uint64_t bounceLimitNs = kBounceLimitNs;   // kgb_set_limits: a bounce step kernel's time limit
+  std::vector<DevMesh*> meshes;               // meshes read to the device, by id (null: freed)
 };
 
 namespace {
@@ -358,6 +367,160 @@ float elapsed(Engine& g) {
   return ms;
 }
 
+// ---------------------------------------------------------------------------------------------------- .dmesh ingest
+// The .dmesh header (the reference's parse_dmesh, src/mesh.cpp:451): magic, flags (bit 0: the slot block), counts.
+struct DmeshHeader { char magic[4]; uint32_t flags; uint64_t nPoints, nFaces, nIndices; };
+static_assert(sizeof(DmeshHeader) == 32, "the .dmesh header is 32 bytes");
+
+// parse_dmesh's header checks (src/mesh.cpp:456-461) for an image of `size` bytes, in its order and words (without
+// the label); payload: the arrays' bytes after the header
+std::string dmesh_header(const DmeshHeader& h, uint64_t size, uint64_t& payload) {
+  if (std::memcmp(h.magic, "DLM1", 4)) return "not a .dmesh file (magic DLM1)";
+  if (h.flags & ~1u) return "unsupported header flags " + std::to_string(h.flags) + " (only bit 0, the slot block, is defined)";
+  if (!(h.nPoints <= size / 24 && h.nFaces <= size / 4 && h.nIndices <= size / 4 && 32 + 24 * h.nPoints + 4 * h.nFaces + 4 * h.nIndices <= size))
+    return "truncated";
+  const uint64_t nSlots = (h.flags & 1) ? h.nFaces : 0;
+  if (32 + 24 * h.nPoints + 4 * h.nFaces + 4 * h.nIndices + 2 * nSlots > size) return "truncated slot block";
+  payload = 24 * h.nPoints + 4 * h.nFaces + 4 * h.nIndices + 2 * nSlots;
+  return "";
+}
+// The device allocation of a checked header: the payload's arrays in the image's order, then the face offsets.
+int mesh_alloc(const DmeshHeader& h, uint64_t payload, const std::string& label, std::unique_ptr<DevMesh>& out) {
+  if (h.nPoints > 0xffffffffull || h.nFaces > 0xffffffffull || h.nIndices > 0xffffffffull)
+    return fail(label + ": more than 2^32 - 1 points, faces or indices (the engine's limit)");
+  std::unique_ptr<DevMesh> m(new DevMesh);
+  const uint64_t offAt = (payload + 255) / 256 * 256;
+  m->bytes = std::max<uint64_t>(256, offAt + 8 * h.nFaces);
+  if (cudaMalloc(&m->buf, m->bytes) != cudaSuccess) {
+    m->buf = nullptr;
+    cudaGetLastError();
+    return fail(label + ": out of device memory (" + std::to_string(m->bytes) + " bytes for the mesh)");
+  }
+  char* b = static_cast<char*>(m->buf);
+  MeshView& v = m->view;
+  v.pts = reinterpret_cast<const double*>(b);
+  v.counts = reinterpret_cast<const int32_t*>(b + 24 * h.nPoints);
+  v.idx = reinterpret_cast<const int32_t*>(b + 24 * h.nPoints + 4 * h.nFaces);
+  v.slot16 = (h.flags & 1) ? reinterpret_cast<const uint16_t*>(b + 24 * h.nPoints + 4 * h.nFaces + 4 * h.nIndices) : nullptr;
+  v.slot32 = nullptr;
+  v.idxOff = reinterpret_cast<const uint64_t*>(b + offAt);
+  v.nPoints = h.nPoints; v.nFaces = h.nFaces; v.nIdx = h.nIndices;
+  out = std::move(m);
+  return 1;
+}
+// The copied image's checks on the device; then the mesh is kept (an id) or, without faces, dropped.
+int mesh_keep(Engine& g, std::unique_ptr<DevMesh> m, const std::string& label, kgb_mesh_info* info) {
+  const std::string why = mesh_check(*m, g.st);
+  if (!why.empty()) {
+    cudaStreamSynchronize(g.st);
+    return fail(label + ": " + why);
+  }
+  m->info.id = KGB_NO_MESH;
+  if (m->view.nFaces) {
+    size_t id = 0;
+    while (id < g.meshes.size() && g.meshes[id]) ++id;
+    if (id >= KGB_NO_MESH) return fail(label + ": too many meshes held");
+    if (id == g.meshes.size()) g.meshes.push_back(nullptr);
+    m->info.id = uint32_t(id);
+    *info = m->info;
+    g.meshes[id] = m.release();
+    return 1;
+  }
+  *info = m->info;
+  return 1;
+}
+// `bytes` of a file from byte `off` to device memory: the file read in staging slices (several threads per slice), each
+// slice's copy queued while the next is read. A short read is the reference's "truncated".
+int read_to_device(Engine& g, int fd, uint64_t off, uint64_t bytes, void* dst, const std::string& label) {
+  Staging& s = g.staging;
+  for (int k = 0; k < 2; ++k) {
+    if (!s.h[k]) CU(cudaMallocHost(&s.h[k], Staging::kSlice));
+    if (!s.ev[k]) CU(cudaEventCreateWithFlags(&s.ev[k], cudaEventDisableTiming));
+  }
+  const size_t n = (bytes + Staging::kSlice - 1) / Staging::kSlice;
+  for (size_t k = 0; k < n; ++k) {
+    const int b = int(k & 1);
+    const size_t len = std::min<uint64_t>(Staging::kSlice, bytes - k * Staging::kSlice);
+    CU(cudaEventSynchronize(s.ev[b]));   // the slice's previous copy has left it
+    constexpr size_t kPart = size_t(8) << 20;
+    const int parts = int(std::max<size_t>(1, std::min<size_t>(4, len / kPart)));
+    const size_t per = (len + parts - 1) / parts;
+    std::vector<int> ok(parts, 1);
+    const auto part = [&](int q) {
+      char* h = static_cast<char*>(s.h[b]);
+      const size_t a0 = size_t(q) * per, a1 = std::min(len, a0 + per);
+      for (size_t a = a0; a < a1;) {
+        const ssize_t r = pread(fd, h + a, a1 - a, off_t(off + k * Staging::kSlice + a));
+        if (r < 0 && errno == EINTR) continue;
+        if (r <= 0) { ok[q] = 0; return; }
+        a += size_t(r);
+      }
+    };
+    if (parts == 1) part(0);
+    else {
+      std::vector<std::thread> th;
+      for (int q = 0; q < parts; ++q) th.emplace_back(part, q);
+      for (auto& t : th) t.join();
+    }
+    for (int q = 0; q < parts; ++q)
+      if (!ok[q]) {
+        cudaStreamSynchronize(g.st);
+        return fail(label + ": truncated");
+      }
+    CU(cudaMemcpyAsync(static_cast<char*>(dst) + k * Staging::kSlice, s.h[b], len, cudaMemcpyHostToDevice, g.st));
+    CU(cudaEventRecord(s.ev[b], g.st));
+  }
+  return 1;
+}
+DevMesh* find_mesh(Engine& g, uint32_t id) { return id < g.meshes.size() ? g.meshes[id] : nullptr; }
+
+// The scene's records from checked arrays (kgb_build's host arrays, or kgb_build_meshes's device arrays when onDevice):
+// the device builder reads either; the host builder gets device arrays copied back first.
+int build_scene(Engine& g, const float* v, size_t nv, const uint32_t* tri, size_t nt, const uint32_t* slot, const uint8_t* translucent, bool onDevice) {
+  CU(cudaEventRecord(g.ev[0], g.st));
+  SceneObj& s = *g.sc;
+  if (g.builder == 1) {   // on the device
+    void* nodes = nullptr;
+    void* tris = nullptr;
+    uint32_t nNodes = 0;
+    uint64_t temp = 0;
+    const std::string why = build_bvh8_gpu(v, nv, tri, nt, slot, translucent, g.st, &nodes, &tris, &nNodes, &temp);
+    s.nodes.p = nodes; s.nodes.cap = std::max<size_t>(1, nt) * kNodeBytes;
+    s.tris.p = tris; s.tris.cap = nt * 48;
+    if (!why.empty()) return fail("gpu_build: " + why);
+    s.nNodes = nNodes;
+    s.bytes = uint64_t(nNodes) * kNodeBytes + uint64_t(nt) * 48;
+    g.stats.buildTempBytes = temp;
+  } else {   // on the host (binned SAH)
+    std::vector<float> hv;
+    std::vector<uint32_t> htri, hslot;
+    std::vector<uint8_t> htr;
+    if (onDevice) {
+      hv.resize(3 * nv); htri.resize(3 * nt);
+      if (nv) CU(cudaMemcpyAsync(hv.data(), v, nv * 12, cudaMemcpyDeviceToHost, g.st));
+      CU(cudaMemcpyAsync(htri.data(), tri, nt * 12, cudaMemcpyDeviceToHost, g.st));
+      if (slot) { hslot.resize(nt); CU(cudaMemcpyAsync(hslot.data(), slot, nt * 4, cudaMemcpyDeviceToHost, g.st)); }
+      if (translucent) { htr.resize(nt); CU(cudaMemcpyAsync(htr.data(), translucent, nt, cudaMemcpyDeviceToHost, g.st)); }
+      CU(cudaStreamSynchronize(g.st));
+      v = hv.data(); tri = htri.data(); slot = slot ? hslot.data() : nullptr; translucent = translucent ? htr.data() : nullptr;
+    }
+    BvhOut b;
+    build_bvh8(v, nv, tri, nt, slot, translucent, b);
+    if (!upload(s.nodes, b.nodes.data(), b.nodes.size() * 4, g.st) || !upload(s.tris, b.tris.data(), b.tris.size() * 4, g.st)) return 0;
+    s.nNodes = b.nNodes;
+    s.bytes = b.nodes.size() * 4 + b.tris.size() * 4;
+    g.stats.buildTempBytes = uint64_t(nt) * 64;
+  }
+  if (s.nNodes >= kMaxNodes) return fail("gpu_build: 2^24 nodes or more (the node records' child index has 24 bits)");
+  s.nTris = uint32_t(nt);
+  CU(cudaEventRecord(g.ev[1], g.st));
+  CU(cudaStreamSynchronize(g.st));
+  g.stats.buildMs += elapsed(g);
+  g.stats.gasBytes = s.bytes;
+  g.stats.buildOutputBytes = s.bytes;
+  return 1;
+}
+
 }  // namespace
 
 int set_error(const std::string& message) { return fail(message); }
@@ -404,6 +567,7 @@ KGB_API void kgb_destroy(kgb_engine* e) {
   Engine* g = E(e);
   if (g->st) cudaStreamSynchronize(g->st);
   delete g->sc;
+  for (DevMesh* m : g->meshes) delete m;
   for (Buf* b : {&g->slots, &g->P, &g->N, &g->D, &g->rayTab, &g->vis, &g->dc, &g->contrib, &g->viewCls, &g->viewDist, &g->rowSin, &g->label, &g->scratch, &g->out, &g->ctl,
                  &g->vop, &g->sop, &g->csr, &g->sunCol, &g->rows, &g->border, &g->slotLog, &g->bq}) b->free();
   g->staging.free();
@@ -438,42 +602,12 @@ KGB_API int kgb_build(kgb_engine* e, const float* v, size_t nv, const uint32_t* 
   if (slotted && !slot) return fail("gpu_build: per-slot records need a slot per triangle");
   if (nt > (size_t(1) << 31)) return fail("gpu_build: more than 2^31 triangles");
   for (size_t k = 0; k < 3 * nt; ++k) if (tri[k] >= nv) return fail("gpu_build: a triangle's vertex index exceeds the vertices");
-  CU(cudaEventRecord(g.ev[0], g.st));
   std::vector<uint8_t> translucent;
   if (slotted) {
     translucent.resize(nt);
     for (size_t k = 0; k < nt; ++k) translucent[k] = slots[slot[k]].tau > 0 ? 1 : 0;
   }
-  SceneObj& s = *g.sc;
-  if (g.builder == 1) {   // on the device
-    void* nodes = nullptr;
-    void* tris = nullptr;
-    uint32_t nNodes = 0;
-    uint64_t temp = 0;
-    const std::string why = build_bvh8_gpu(v, nv, tri, nt, slotted ? slot : nullptr, slotted ? translucent.data() : nullptr, g.st, &nodes, &tris,
-                                           &nNodes, &temp);
-    s.nodes.p = nodes; s.nodes.cap = std::max<size_t>(1, nt) * kNodeBytes;
-    s.tris.p = tris; s.tris.cap = nt * 48;
-    if (!why.empty()) return fail("gpu_build: " + why);
-    s.nNodes = nNodes;
-    s.bytes = uint64_t(nNodes) * kNodeBytes + uint64_t(nt) * 48;
-    g.stats.buildTempBytes = temp;
-  } else {   // on the host (binned SAH)
-    BvhOut b;
-    build_bvh8(v, nv, tri, nt, slotted ? slot : nullptr, slotted ? translucent.data() : nullptr, b);
-    if (!upload(s.nodes, b.nodes.data(), b.nodes.size() * 4, g.st) || !upload(s.tris, b.tris.data(), b.tris.size() * 4, g.st)) return 0;
-    s.nNodes = b.nNodes;
-    s.bytes = b.nodes.size() * 4 + b.tris.size() * 4;
-    g.stats.buildTempBytes = uint64_t(nt) * 64;
-  }
-  if (s.nNodes >= kMaxNodes) return fail("gpu_build: 2^24 nodes or more (the node records' child index has 24 bits)");
-  s.nTris = uint32_t(nt);
-  CU(cudaEventRecord(g.ev[1], g.st));
-  CU(cudaStreamSynchronize(g.st));
-  g.stats.buildMs += elapsed(g);
-  g.stats.gasBytes = s.bytes;
-  g.stats.buildOutputBytes = s.bytes;
-  return 1;
+  return build_scene(g, v, nv, tri, nt, slotted ? slot : nullptr, slotted ? translucent.data() : nullptr, false);
 }
 
 KGB_API void kgb_trim(kgb_engine* e, int sensors) {
@@ -768,6 +902,137 @@ KGB_API int kgb_thin_solids(kgb_engine* e, const double* points, size_t nPoints,
                             const uint32_t* faceSlot, uint32_t nSlots, const double* c, uint32_t* flags) {
   const std::string why = thin_solids(points, nPoints, counts, nFaces, indices, faceSlot, nSlots, c, flags, E(e)->st);
   return why.empty() ? 1 : fail("kgb_thin_solids: " + why);
+}
+
+KGB_API int kgb_mesh_read(kgb_engine* e, const void* data, size_t size, const char* name, kgb_mesh_info* info) {
+  Engine& g = *E(e);
+  const std::string label = name ? name : "";
+  if (!info) return fail("kgb_mesh_read: no info to write");
+  if (size && !data) return fail("kgb_mesh_read: no image");
+  DmeshHeader h{};
+  if (size < sizeof h) return fail(label + ": truncated");
+  std::memcpy(&h, data, sizeof h);
+  uint64_t payload = 0;
+  const std::string why = dmesh_header(h, size, payload);
+  if (!why.empty()) return fail(label + ": " + why);
+  std::unique_ptr<DevMesh> m;
+  if (!mesh_alloc(h, payload, label, m)) return 0;
+  if (payload && !upload_large(g.staging, m->buf, static_cast<const char*>(data) + sizeof h, payload, g.st)) {
+    cudaStreamSynchronize(g.st);
+    return 0;
+  }
+  return mesh_keep(g, std::move(m), label, info);
+}
+
+KGB_API int kgb_mesh_file(kgb_engine* e, const char* path, kgb_mesh_info* info) {
+  Engine& g = *E(e);
+  const std::string p = path ? path : "";
+  if (!info) return fail("kgb_mesh_file: no info to write");
+  const int fd = open(p.c_str(), O_RDONLY | O_CLOEXEC);
+  if (fd < 0) return fail("cannot open " + p);
+  struct Closer { int fd; ~Closer() { close(fd); } } closer{fd};
+  struct stat sb{};
+  if (fstat(fd, &sb) != 0 || !S_ISREG(sb.st_mode)) return fail("cannot open " + p);
+  const uint64_t size = uint64_t(sb.st_size);
+  DmeshHeader h{};
+  if (size < sizeof h || pread(fd, &h, sizeof h, 0) != ssize_t(sizeof h)) return fail(p + ": truncated");
+  uint64_t payload = 0;
+  const std::string why = dmesh_header(h, size, payload);
+  if (!why.empty()) return fail(p + ": " + why);
+  std::unique_ptr<DevMesh> m;
+  if (!mesh_alloc(h, payload, p, m)) return 0;
+  if (payload && !read_to_device(g, fd, sizeof h, payload, m->buf, p)) return 0;
+  return mesh_keep(g, std::move(m), p, info);
+}
+
+KGB_API int kgb_mesh_download(kgb_engine* e, uint32_t id, double* points, int32_t* counts, int32_t* indices, uint16_t* slot) {
+  Engine& g = *E(e);
+  const DevMesh* m = find_mesh(g, id);
+  if (!m) return fail("kgb_mesh_download: no mesh " + std::to_string(id));
+  const MeshView& v = m->view;
+  if (points && v.nPoints) CU(cudaMemcpyAsync(points, v.pts, v.nPoints * 24, cudaMemcpyDeviceToHost, g.st));
+  if (counts && v.nFaces) CU(cudaMemcpyAsync(counts, v.counts, v.nFaces * 4, cudaMemcpyDeviceToHost, g.st));
+  if (indices && v.nIdx) CU(cudaMemcpyAsync(indices, v.idx, v.nIdx * 4, cudaMemcpyDeviceToHost, g.st));
+  if (slot && v.slot16 && v.nFaces) CU(cudaMemcpyAsync(slot, v.slot16, v.nFaces * 2, cudaMemcpyDeviceToHost, g.st));
+  CU(cudaStreamSynchronize(g.st));
+  return 1;
+}
+
+KGB_API int kgb_mesh_free(kgb_engine* e, uint32_t id) {
+  Engine& g = *E(e);
+  DevMesh* m = find_mesh(g, id);
+  if (!m) return fail("kgb_mesh_free: no mesh " + std::to_string(id));
+  CU(cudaStreamSynchronize(g.st));
+  delete m;
+  g.meshes[id] = nullptr;
+  return 1;
+}
+
+KGB_API int kgb_mesh_thin_solids(kgb_engine* e, uint32_t id, const double* c, uint32_t* flags) {
+  Engine& g = *E(e);
+  const DevMesh* m = find_mesh(g, id);
+  if (!m) return fail("kgb_mesh_thin_solids: no mesh " + std::to_string(id));
+  const std::string why = thin_solids_view(m->view, m->info.slots, c, flags, g.st);
+  return why.empty() ? 1 : fail("kgb_mesh_thin_solids: " + why);
+}
+
+KGB_API int kgb_build_meshes(kgb_engine* e, const uint32_t* ids, size_t nMeshes, const uint8_t* blocks, const double* c, const kgb_slot* slots,
+                             size_t nSlots, int perSlot, uint64_t* made, int32_t* skipped) {
+  Engine& g = *E(e);
+  delete g.sc;
+  g.sc = new SceneObj;
+  g.stats.gasBytes = 0;
+  if (skipped) *skipped = 0;
+  std::vector<const DevMesh*> ms(nMeshes);
+  // run.cpp:101-106's ranges: points and at most tri_cap triangles of each blocking mesh, slots of every mesh
+  std::vector<uint64_t> vBase(nMeshes + 1, 0), tBase(nMeshes + 1, 0), sBase(nMeshes + 1, 0);
+  for (size_t k = 0; k < nMeshes; ++k) {
+    ms[k] = find_mesh(g, ids[k]);
+    if (!ms[k]) return fail("kgb_build_meshes: no mesh " + std::to_string(ids[k]));
+    const bool b = !blocks || blocks[k];
+    vBase[k + 1] = vBase[k] + (b ? ms[k]->info.nPoints : 0);
+    tBase[k + 1] = tBase[k] + (b ? ms[k]->info.triCap : 0);
+    sBase[k + 1] = sBase[k] + ms[k]->info.slots;
+    if (made) made[k] = 0;
+  }
+  const uint64_t nPts = vBase.back(), nCap = tBase.back();
+  if (nPts > 0xffffffffull || sBase.back() > 0xffffffffull) return fail("kgb_build_meshes: more than 2^32 - 1 points or slots");
+  bool anyTau = false;
+  for (size_t s = 0; s < nSlots; ++s) anyTau = anyTau || slots[s].tau > 0;
+  const bool slotted = perSlot || anyTau;
+  Buf dv, dtri, dslot, dtr, dslots;
+  if (!grow(dv, nPts * 12) || !grow(dtri, nCap * 12) || (slotted && !grow(dslot, nCap * 4))) return 0;
+  uint64_t at = 0;
+  int32_t skip = 0;
+  for (size_t k = 0; k < nMeshes; ++k) {
+    if (blocks && !blocks[k]) continue;
+    uint64_t mk = 0;
+    int32_t sk = 0;
+    const std::string why = triangulate_view(ms[k]->view, c, uint32_t(vBase[k]), uint32_t(sBase[k]), static_cast<float*>(dv.p) + 3 * vBase[k],
+                                             static_cast<uint32_t*>(dtri.p) + 3 * at, slotted ? static_cast<uint32_t*>(dslot.p) + at : nullptr, &mk, &sk,
+                                             g.st);
+    if (!why.empty()) return fail("kgb_build_meshes: " + why);
+    if (made) made[k] = mk;
+    at += mk;
+    skip += sk;
+  }
+  if (skipped) *skipped = skip;
+  const size_t nt = size_t(at);
+  if (!nt) return 1;   // empty scene: every ray misses
+  if (nt > (size_t(1) << 31)) return fail("gpu_build: more than 2^31 triangles");
+  if (slotted) {
+    uint32_t top = 0;
+    thrust::device_ptr<const uint32_t> sl(static_cast<const uint32_t*>(dslot.p));
+    top = thrust::reduce(thrust::cuda::par.on(g.st), sl, sl + nt, 0u, thrust::maximum<uint32_t>());
+    if (top >= nSlots) return fail("gpu_build: a triangle's slot has no Slot");
+    if (!upload(dslots, slots, nSlots * sizeof(kgb_slot), g.st) || !grow(dtr, nt)) return 0;
+    launch_translucent(static_cast<const uint32_t*>(dslot.p), nt, static_cast<const kgb_slot*>(dslots.p), static_cast<uint8_t*>(dtr.p), g.st);
+    CU(cudaGetLastError());
+  }
+  const int ok = build_scene(g, static_cast<const float*>(dv.p), size_t(nPts), static_cast<const uint32_t*>(dtri.p), nt,
+                             slotted ? static_cast<const uint32_t*>(dslot.p) : nullptr, slotted ? static_cast<const uint8_t*>(dtr.p) : nullptr, true);
+  for (Buf* b : {&dv, &dtri, &dslot, &dtr, &dslots}) b->free();
+  return ok;
 }
 
 KGB_API int kgb_sky_ladybug(kgb_engine* e, int32_t mf, const double* steps, size_t T, double lat, double lon, double tz, double grefl,

@@ -204,6 +204,40 @@ void engine_reduce_inputs(kgb_engine* e, ReduceInputs& in);
 // sky (sky.cu): Perez sky of T steps, NOAA sun positions; null or what failed
 const char* sky_steps(int mf, const kgb_sky_step* steps, size_t T, double grefl, int sun, int sky, int visible, float* out, cudaStream_t st);
 const char* sun_steps(const double* in, size_t T, double* out, cudaStream_t st);
+// A mesh's arrays on the device, as the .dmesh format lays them out, and each face's first index.
+struct MeshView {
+  const double* pts;         // [nPoints x 3]
+  const int32_t* counts;     // [nFaces]
+  const int32_t* idx;        // [nIdx]
+  const uint64_t* idxOff;    // [nFaces]
+  const uint16_t* slot16;    // [nFaces] the faces' slots as the image holds them, or null
+  const uint32_t* slot32;    // [nFaces] the same as a caller's 32-bit array, or null (neither: slot 0)
+  uint64_t nPoints, nFaces, nIdx;
+};
+// A mesh the engine keeps (kgb_mesh_read / kgb_mesh_file): one allocation holding points, counts, indices and slots in
+// the image's order (the image's payload copied as it is), then the face offsets at a 256-byte boundary.
+struct DevMesh {
+  void* buf = nullptr;
+  size_t bytes = 0;
+  MeshView view{};
+  kgb_mesh_info info{};
+  DevMesh() = default;
+  DevMesh(const DevMesh&) = delete;
+  DevMesh& operator=(const DevMesh&) = delete;
+  ~DevMesh() { if (buf) cudaFree(buf); }
+};
+// mesh.cu: the reference's array checks on a copied image (mesh_ok), then the face offsets, bounds, largest face,
+// largest slot and tri_cap into m.info; "" or the rule that failed, as the reference words it (without the label)
+std::string mesh_check(DevMesh& m, cudaStream_t st);
+// mesh.cu: the faces of a mesh on the device as triangles into device arrays: v [nPoints x 3] (recentred on c), tri at
+// most tri_cap triangles (vertex indices + base), slot (slotBase + the face's slot) or null; *made and *skipped as
+// kgb_triangulate's. "" or what failed.
+std::string triangulate_view(const MeshView& m, const double* c, uint32_t base, uint32_t slotBase, float* v, uint32_t* tri, uint32_t* slot,
+                             uint64_t* made, int32_t* skipped, cudaStream_t st);
+// mesh.cu: kgb_thin_solids over a mesh on the device; flags in host memory [nSlots] (every face's slot below nSlots)
+std::string thin_solids_view(const MeshView& m, uint32_t nSlots, const double* c, uint32_t* flags, cudaStream_t st);
+// mesh.cu: translucent[k] = slots[slot[k]].tau > 0 for device arrays (slots [nSlots] in device memory)
+void launch_translucent(const uint32_t* slot, size_t nt, const kgb_slot* slots, uint8_t* translucent, cudaStream_t st);
 // the scene's preparation on the GPU (mesh.cu): "" or what failed
 std::string triangulate_mesh(const double* points, size_t nPoints, const int32_t* counts, size_t nFaces, const int32_t* indices, const uint32_t* faceSlot,
                              const double* c, uint32_t base, uint32_t slotBase, float* v, uint32_t* tri, uint32_t* slot, size_t* made, int32_t* skipped,
@@ -221,7 +255,8 @@ struct BvhOut {
   uint32_t nNodes = 0;
 };
 void build_bvh8(const float* v, size_t nv, const uint32_t* tri, size_t nt, const uint32_t* slot, const uint8_t* translucent, BvhOut& out);
-// device builder (bvh_gpu.cu): the same records, built on the GPU from a Morton-ordered radix tree; "" or what failed
+// device builder (bvh_gpu.cu): the same records, built on the GPU from a Morton-ordered radix tree; the input arrays
+// in host or device memory (copied by kind cudaMemcpyDefault); "" or what failed
 std::string build_bvh8_gpu(const float* v, size_t nv, const uint32_t* tri, size_t nt, const uint32_t* slot, const uint8_t* translucent,
                            cudaStream_t st, void** nodesOut, void** trisOut, uint32_t* nNodesOut, uint64_t* tempBytes);
 

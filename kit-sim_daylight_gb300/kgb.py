@@ -70,6 +70,17 @@ class ViewsRequest(ctypes.Structure):
                 ("nReach", c_uint32), ("glazing", c_int32), ("isoDim", c_uint32), ("out", c_void_p)]
 
 
+class MeshInfo(ctypes.Structure):
+    _fields_ = [("id", c_uint32), ("slots", c_uint32), ("nPoints", c_uint64), ("nFaces", c_uint64), ("nIndices", c_uint64),
+                ("hasSlots", c_uint32), ("maxCorners", c_uint32), ("triCap", c_uint64), ("lo", c_double * 3), ("hi", c_double * 3)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["lo"], d["hi"] = list(self.lo), list(self.hi)
+        return d
+
+
+NO_MESH = 0xFFFFFFFF
 RAY_DISABLE_ANYHIT, RAY_TERMINATE_ON_FIRST_HIT, RAY_CULL_BACK_FACING = 1, 4, 16
 SLOT_GLASS, SLOT_THIN, SLOT_INWARD, SLOT_TWIN = 1, 2, 4, 8
 LABEL_PASS, MAX_PANES, VIEW_GLAZED = 255, 16, 0x80
@@ -132,6 +143,12 @@ SIGNATURES = [
     ("kgb_set_series_form", c_int, [_E, c_int]),
     ("kgb_trace_counters", c_int, [_E, c_size_t, c_size_t, c_uint32, POINTER(c_uint64)]),
     ("kgb_set_limits", c_int, [_E, c_uint32, c_uint64]),
+    ("kgb_mesh_read", c_int, [_E, c_void_p, c_size_t, c_char_p, POINTER(MeshInfo)]),
+    ("kgb_mesh_file", c_int, [_E, c_char_p, POINTER(MeshInfo)]),
+    ("kgb_mesh_download", c_int, [_E, c_uint32, c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("kgb_mesh_free", c_int, [_E, c_uint32]),
+    ("kgb_mesh_thin_solids", c_int, [_E, c_uint32, c_void_p, c_void_p]),
+    ("kgb_build_meshes", c_int, [_E, c_void_p, c_size_t, c_void_p, c_void_p, c_void_p, c_size_t, c_int, c_void_p, POINTER(c_int32)]),
 ]
 
 
@@ -281,6 +298,51 @@ class Engine:
         cc = np.ascontiguousarray(c, np.float64)
         self._ok(self.d.kgb_thin_solids(self.h, _p(points), len(points), _p(counts), len(counts), _p(indices), _p(fs), n_slots, _p(cc), _p(flags)))
         return flags
+
+    # --- meshes read to the device
+    def mesh_read(self, image, name="mesh"):
+        """A .dmesh image (bytes) read to the device (the reference's read_dmesh of memory): its MeshInfo (id NO_MESH
+        for an image without faces)."""
+        buf = np.frombuffer(bytes(image), np.uint8) if not isinstance(image, np.ndarray) else np.ascontiguousarray(image, np.uint8)
+        info = MeshInfo()
+        self._ok(self.d.kgb_mesh_read(self.h, _p(buf), buf.size, name.encode(), ctypes.byref(info)))
+        return info
+
+    def mesh_file(self, path):
+        """A .dmesh file read to the device (the reference's read_dmesh of a path): its MeshInfo."""
+        info = MeshInfo()
+        self._ok(self.d.kgb_mesh_file(self.h, str(path).encode(), ctypes.byref(info)))
+        return info
+
+    def mesh_download(self, info):
+        """A kept mesh's arrays: (points [nPoints x 3], counts, indices, slot or None)."""
+        P = np.zeros((info.nPoints, 3), np.float64)
+        C = np.zeros(info.nFaces, np.int32)
+        I = np.zeros(info.nIndices, np.int32)
+        S = np.zeros(info.nFaces, np.uint16) if info.hasSlots else None
+        self._ok(self.d.kgb_mesh_download(self.h, info.id, _p(P), _p(C), _p(I), _p(S)))
+        return P, C, I, S
+
+    def mesh_free(self, mesh_id):
+        self._ok(self.d.kgb_mesh_free(self.h, mesh_id))
+
+    def mesh_thin_solids(self, info, c=(0.0, 0.0, 0.0)):
+        flags = np.zeros(info.slots, np.uint32)
+        cc = np.ascontiguousarray(c, np.float64)
+        self._ok(self.d.kgb_mesh_thin_solids(self.h, info.id, _p(cc), _p(flags)))
+        return flags
+
+    def build_meshes(self, ids, c, blocks=None, slots=None, per_slot=False):
+        """The scene from kept meshes (the reference's scene assembly + gpu_build): (made per mesh, skipped faces)."""
+        ids = np.ascontiguousarray(ids, np.uint32)
+        bl = None if blocks is None else np.ascontiguousarray(blocks, np.uint8)
+        sl = slots_array(slots if slots is not None else [Slot(0.2, 0, 0, 0)])
+        cc = np.ascontiguousarray(c, np.float64)
+        made = np.zeros(len(ids), np.uint64)
+        skipped = c_int32(0)
+        self._ok(self.d.kgb_build_meshes(self.h, _p(ids), len(ids), _p(bl), _p(cc), ctypes.cast(sl, c_void_p), len(sl), int(per_slot), _p(made),
+                                         ctypes.byref(skipped)))
+        return made, skipped.value
 
     def sky_ladybug(self, mf, steps, lat, lon, tz, grefl=0.2, duration_hours=None, series=False):
         """Ladybug mode's sky: steps [T x 4] (jd, hour, dni, dhi). Returns (lb [3P + 1] doubles, acc [4P + 6] floats) and,

@@ -28,10 +28,12 @@
 #include <chrono>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <limits>
+#include <memory>
 #include <string>
 #include <thread>
 #include <vector>
@@ -333,7 +335,77 @@ struct Engine {
   kgb_view_in view{}; std::vector<float> rowSin;
   std::vector<uint8_t> label;
   kgb_stats stats{};
+  std::vector<std::unique_ptr<struct HostMesh>> meshes;   // kgb_mesh_read / kgb_mesh_file, by id
 };
+
+// ---------------------------------------------------------------------------------------------------- .dmesh
+// The reference's .dmesh reader restated on the host (parse_dmesh, src/mesh.cpp:450-474, with mesh_ok at 436-445 and
+// the file variant at 480-489): the header's checks in its order and words, the arrays copied out, then the array
+// rules. The engine's kgb_mesh_* do the same with the arrays on the device; tests/golden/dmesh holds the reference's
+// own answers on the same images.
+struct HostMesh {
+  std::vector<double> points;
+  std::vector<int32_t> counts, indices;
+  std::vector<uint16_t> slot;
+  kgb_mesh_info info{};
+};
+
+int dmesh_parse(Engine& g, const char* data, size_t size, const std::string& label, kgb_mesh_info* info) {
+  struct Header { char magic[4]; uint32_t flags; uint64_t nPoints, nFaces, nIndices; };
+  static_assert(sizeof(Header) == 32, "the .dmesh header is 32 bytes");
+  Header h{};
+  if (size < sizeof h) return fail(label + ": truncated");
+  std::memcpy(&h, data, sizeof h);
+  if (std::memcmp(h.magic, "DLM1", 4)) return fail(label + ": not a .dmesh file (magic DLM1)");
+  if (h.flags & ~1u) return fail(label + ": unsupported header flags " + std::to_string(h.flags) + " (only bit 0, the slot block, is defined)");
+  if (!(h.nPoints <= size / 24 && h.nFaces <= size / 4 && h.nIndices <= size / 4 && 32 + 24 * h.nPoints + 4 * h.nFaces + 4 * h.nIndices <= size))
+    return fail(label + ": truncated");
+  const uint64_t nSlots = (h.flags & 1) ? h.nFaces : 0;
+  if (32 + 24 * h.nPoints + 4 * h.nFaces + 4 * h.nIndices + 2 * nSlots > size) return fail(label + ": truncated slot block");
+  std::unique_ptr<HostMesh> m(new HostMesh);
+  m->points.resize(3 * h.nPoints); m->counts.resize(h.nFaces); m->indices.resize(h.nIndices); m->slot.resize(nSlots);
+  const char* p = data + sizeof h;
+  if (h.nPoints) std::memcpy(m->points.data(), p, 24 * h.nPoints);
+  p += 24 * h.nPoints;
+  if (h.nFaces) std::memcpy(m->counts.data(), p, 4 * h.nFaces);
+  p += 4 * h.nFaces;
+  if (h.nIndices) std::memcpy(m->indices.data(), p, 4 * h.nIndices);
+  p += 4 * h.nIndices;
+  if (nSlots) std::memcpy(m->slot.data(), p, 2 * nSlots);
+  // mesh_ok
+  uint64_t sum = 0;
+  uint32_t maxCorners = 0;
+  for (int32_t c : m->counts) {
+    if (c < 3) return fail(label + ": face with fewer than 3 vertices");
+    sum += uint64_t(c);
+    maxCorners = std::max(maxCorners, uint32_t(c));
+  }
+  if (sum != m->indices.size()) return fail(label + ": sum(counts) != n_indices");
+  for (int32_t i : m->indices) if (i < 0 || uint64_t(i) >= h.nPoints) return fail(label + ": vertex index out of range");
+  kgb_mesh_info& in = m->info;
+  in.id = KGB_NO_MESH;
+  in.nPoints = h.nPoints; in.nFaces = h.nFaces; in.nIndices = h.nIndices;
+  in.hasSlots = nSlots ? 1u : 0u;
+  uint32_t top = 0;
+  for (uint16_t s : m->slot) top = std::max<uint32_t>(top, s);
+  in.slots = (h.flags & 1) ? top + 1 : 1u;   // slot_count (src/mesh.cpp:170)
+  in.maxCorners = maxCorners;
+  in.triCap = sum - 2 * h.nFaces;
+  for (int a = 0; a < 3; ++a) { in.lo[a] = INFINITY; in.hi[a] = -INFINITY; }
+  for (size_t i = 0; i < m->points.size(); ++i) {   // bbox_centre's per-mesh box (src/mesh.cpp:110-112)
+    in.lo[i % 3] = std::fmin(in.lo[i % 3], m->points[i]);
+    in.hi[i % 3] = std::fmax(in.hi[i % 3], m->points[i]);
+  }
+  if (h.nFaces) {   // an empty mesh is dropped (src/mesh.cpp:472)
+    in.id = uint32_t(g.meshes.size());
+    *info = in;
+    g.meshes.push_back(std::move(m));
+    return 1;
+  }
+  *info = in;
+  return 1;
+}
+HostMesh* host_mesh(Engine& g, uint32_t id) { return id < g.meshes.size() ? g.meshes[id].get() : nullptr; }
 
 unsigned n_threads() {
   if (const char* e = std::getenv("KGB_ORACLE_THREADS")) { const int k = std::atoi(e); if (k > 0) return unsigned(k); }
@@ -1056,6 +1128,46 @@ KGB_API int kgb_triangulate(kgb_engine*, const double*, size_t, const int32_t*, 
 }
 KGB_API int kgb_thin_solids(kgb_engine*, const double*, size_t, const int32_t*, size_t, const int32_t*, const uint32_t*, uint32_t, const double*, uint32_t*) {
   return fail("kgb_thin_solids: not restated here (the reference's own mesh code is the checker: tests/golden/mesh)");
+}
+KGB_API int kgb_mesh_read(kgb_engine* e, const void* data, size_t size, const char* name, kgb_mesh_info* info) {
+  if (!info) return fail("kgb_mesh_read: no info to write");
+  if (size && !data) return fail("kgb_mesh_read: no image");
+  return dmesh_parse(*reinterpret_cast<Engine*>(e), static_cast<const char*>(data), size, name ? name : "", info);
+}
+KGB_API int kgb_mesh_file(kgb_engine* e, const char* path, kgb_mesh_info* info) {   // read_dmesh(path): the whole file, then the image's parse
+  const std::string p = path ? path : "";
+  if (!info) return fail("kgb_mesh_file: no info to write");
+  std::FILE* f = std::fopen(p.c_str(), "rb");
+  if (!f) return fail("cannot open " + p);
+  std::fseek(f, 0, SEEK_END);
+  const long n = std::ftell(f);
+  std::vector<char> buf(n > 0 ? size_t(n) : 0);
+  std::rewind(f);
+  const bool ok = n >= 0 && std::fread(buf.data(), 1, buf.size(), f) == buf.size();
+  std::fclose(f);
+  if (!ok) return fail(p + ": truncated");
+  return dmesh_parse(*reinterpret_cast<Engine*>(e), buf.data(), buf.size(), p, info);
+}
+KGB_API int kgb_mesh_download(kgb_engine* e, uint32_t id, double* points, int32_t* counts, int32_t* indices, uint16_t* slot) {
+  const HostMesh* m = host_mesh(*reinterpret_cast<Engine*>(e), id);
+  if (!m) return fail("kgb_mesh_download: no mesh " + std::to_string(id));
+  if (points) std::copy(m->points.begin(), m->points.end(), points);
+  if (counts) std::copy(m->counts.begin(), m->counts.end(), counts);
+  if (indices) std::copy(m->indices.begin(), m->indices.end(), indices);
+  if (slot) std::copy(m->slot.begin(), m->slot.end(), slot);
+  return 1;
+}
+KGB_API int kgb_mesh_free(kgb_engine* e, uint32_t id) {
+  Engine& g = *reinterpret_cast<Engine*>(e);
+  if (!host_mesh(g, id)) return fail("kgb_mesh_free: no mesh " + std::to_string(id));
+  g.meshes[id].reset();
+  return 1;
+}
+KGB_API int kgb_mesh_thin_solids(kgb_engine*, uint32_t, const double*, uint32_t*) {
+  return fail("kgb_mesh_thin_solids: not restated here (the reference's own mesh code is the checker: tests/golden/mesh)");
+}
+KGB_API int kgb_build_meshes(kgb_engine*, const uint32_t*, size_t, const uint8_t*, const double*, const kgb_slot*, size_t, int, uint64_t*, int32_t*) {
+  return fail("kgb_build_meshes: not restated here (the scene's checker is kgb_build on the triangulated arrays)");
 }
 KGB_API int kgb_sky_ladybug(kgb_engine*, int32_t, const double*, size_t, double, double, double, double, double, double*, float*, float*, float*) {
   return fail("kgb_sky_ladybug: the sky is not restated here (the reference's own sky code is the checker: tests/golden/ladybug)");

@@ -21,6 +21,10 @@
 //                                      [nFaces] i32; indices [nIdx] i32; slots [nFaces] u16. OUT: u64 made, i64 skipped,
 //                                      u64 nSlots; v [nPoints x 3] f32; tri [made x 3] u32; slot [made] u32 (slot base
 //                                      0, vertex base 0); thin_solid of each slot [nSlots] u32
+//   ref_sky_golden dmesh IN OUT 0      the reference's read_dmesh (src/mesh.cpp:476-478) on one image named "case".
+//                                      IN: the image's bytes. OUT: u64 ok, u64 meshes read, u64 message length, the
+//                                      message; per mesh read u64 nPoints, nFaces, nIndices, nSlots and its arrays
+//                                      (points f64, counts i32, indices i32, slots u16)
 #include "internal.h"
 #include <cmath>
 #include <chrono>
@@ -140,7 +144,37 @@ static int mesh(std::FILE* fi, std::FILE* fo) {
   return 0;
 }
 
+static int dmesh(std::FILE* fi, std::FILE* fo) {
+  std::vector<char> img;
+  char buf[65536];
+  for (size_t n; (n = std::fread(buf, 1, sizeof buf, fi)) > 0;) img.insert(img.end(), buf, buf + n);
+  std::vector<SimulationMesh> out;
+  std::string err;
+  const bool ok = read_dmesh(img.data(), img.size(), "case", out, err);
+  const uint64_t head[3] = {uint64_t(ok), uint64_t(out.size()), uint64_t(err.size())};
+  std::fwrite(head, 8, 3, fo);
+  std::fwrite(err.data(), 1, err.size(), fo);
+  for (const SimulationMesh& m : out) {
+    const uint64_t n[4] = {uint64_t(m.numPoints()), uint64_t(m.counts.size()), uint64_t(m.indices.size()), uint64_t(m.slot.size())};
+    std::fwrite(n, 8, 4, fo);
+    std::fwrite(m.points.data(), 8, m.points.size(), fo);
+    std::fwrite(m.counts.data(), 4, m.counts.size(), fo);
+    std::fwrite(m.indices.data(), 4, m.indices.size(), fo);
+    std::fwrite(m.slot.data(), 2, m.slot.size(), fo);
+  }
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc >= 4 && !std::strcmp(argv[1], "dmesh")) {
+    std::FILE* fi = std::fopen(argv[2], "rb");
+    std::FILE* fo = std::fopen(argv[3], "wb");
+    if (!fi || !fo) return 3;
+    const int rc = dmesh(fi, fo);
+    std::fclose(fi);
+    std::fclose(fo);
+    return rc;
+  }
   if (argc >= 4 && !std::strcmp(argv[1], "mesh")) {
     std::FILE* fi = std::fopen(argv[2], "rb");
     std::FILE* fo = std::fopen(argv[3], "wb");

@@ -371,11 +371,94 @@ def mesh_goldens(ref):
         print("mesh %s: %d faces, %d triangles, %d skipped, thin %s" % (name, len(C), made, skipped, thin.tolist()))
 
 
+def dmesh_image(points, counts, indices, slots=None, flags=None, magic=b"DLM1", n=None):
+    """A .dmesh image (the reference's layout, src/daylight.h:129-136); n overrides the header's three counts."""
+    P = np.ascontiguousarray(points, np.float64).reshape(-1, 3)
+    C = np.ascontiguousarray(counts, np.int32)
+    I = np.ascontiguousarray(indices, np.int32)
+    fl = (1 if slots is not None else 0) if flags is None else flags
+    nP, nF, nI = n if n is not None else (len(P), len(C), len(I))
+    head = magic + np.array([fl], np.uint32).tobytes() + np.array([nP, nF, nI], np.uint64).tobytes()
+    body = P.tobytes() + C.tobytes() + I.tobytes() + (np.ascontiguousarray(slots, np.uint16).tobytes() if slots is not None else b"")
+    return head + body
+
+
+def dmesh_cases(rng):
+    """Seeded images for the reader's rules: valid meshes (with and without the slot block, trailing bytes, an empty
+    mesh), and one image per failure of the header and of the arrays, some failing two rules at once (the first in the
+    reference's order must be reported)."""
+    P = rng.uniform(-50, 80, (40, 3)).round(3)
+    C = np.array([3, 4, 5, 3, 6, 4, 3, 7], np.int32)
+    I = rng.integers(0, 40, int(C.sum())).astype(np.int32)
+    S = rng.integers(0, 5, len(C)).astype(np.uint16)
+    good = dmesh_image(P, C, I, S)
+    cases = [("slots", good), ("no_slots", dmesh_image(P, C, I)), ("trailing_bytes", good + b"\x07" * 13),
+             ("empty", dmesh_image(P[:3], [], [])), ("empty_with_indices", dmesh_image(P[:3], [], [0, 1, 2])),
+             ("short_header", good[:20]), ("nothing", b""), ("bad_magic", dmesh_image(P, C, I, magic=b"DLM2")),
+             ("bad_flags", dmesh_image(P, C, I, flags=2)), ("bad_flags_high", dmesh_image(P, C, I, S, flags=0x80000001)),
+             ("truncated_arrays", dmesh_image(P, C, I)[:-10]), ("truncated_slot_block", good[:-1]),
+             ("huge_points", dmesh_image(P, C, I, n=(1 << 62, len(C), len(I)))),
+             ("sum_overflow", dmesh_image(P, C, I, n=(len(P), (1 << 61), len(I))))]
+    c2 = C.copy(); c2[3] = 2
+    cases.append(("face_of_two", dmesh_image(P, c2, I[:-1])))
+    c3 = C.copy(); c3[1] = -4
+    cases.append(("negative_count", dmesh_image(P, c3, I)))
+    cases.append(("sum_mismatch", dmesh_image(P, C, np.concatenate([I, [0]]))))
+    i2 = I.copy(); i2[7] = 40
+    cases.append(("index_past_points", dmesh_image(P, C, i2)))
+    i3 = I.copy(); i3[0] = -1
+    cases.append(("negative_index", dmesh_image(P, C, i3, S)))
+    cases.append(("face_of_two_and_bad_index", dmesh_image(P, c2, i2[:-1])))
+    cases.append(("sum_mismatch_and_bad_index", dmesh_image(P, C, np.concatenate([i2, [0]]))))
+    # a grid of quads with a slot per face (the ingest benchmark's mesh, small)
+    g = 24
+    xs, ys = np.meshgrid(np.arange(g + 1, dtype=np.float64), np.arange(g + 1, dtype=np.float64), indexing="ij")
+    gp = np.stack([xs.ravel() * 1.5 + 1e5, ys.ravel() * 1.5 - 3e5, np.sin(xs.ravel()) * 0.1], 1)
+    q = np.arange(g * (g + 1)).reshape(g, g + 1)[:, :g].ravel()
+    gi = np.stack([q, q + g + 1, q + g + 2, q + 1], 1).astype(np.int32).ravel()
+    cases.append(("quad_grid", dmesh_image(gp, np.full(g * g, 4, np.int32), gi, (np.arange(g * g) % 3).astype(np.uint16))))
+    return cases
+
+
+def dmesh_goldens(ref):
+    """The reference's own read_dmesh (oracle/ref_sky_golden.cpp, mode dmesh) on seeded images:
+    tests/golden/dmesh/cases.npz holds each image and the reference's answer (ok, message, the arrays it read)."""
+    d = os.path.join(HERE, "dmesh")
+    shutil.rmtree(d, ignore_errors=True)
+    os.makedirs(d)
+    exe = os.path.join(REPO, "oracle", "_ref", "ref_sky_golden")
+    out = {}
+    names = []
+    for name, img in dmesh_cases(np.random.default_rng(41)):
+        raw_in, raw_out = os.path.join(d, "in.bin"), os.path.join(d, "out.bin")
+        open(raw_in, "wb").write(img)
+        subprocess.check_call([exe, "dmesh", raw_in, raw_out, "0"])
+        b = open(raw_out, "rb").read()
+        ok, nm, ln = [int(x) for x in np.frombuffer(b, np.uint64, 3)]
+        msg = b[24:24 + ln].decode()
+        at = 24 + ln
+        out[name + "/image"] = np.frombuffer(img, np.uint8)
+        out[name + "/answer"] = np.array([ok, nm], np.int64)
+        out[name + "/message"] = np.frombuffer(msg.encode(), np.uint8)
+        for k in range(nm):
+            nP, nF, nI, nS = [int(x) for x in np.frombuffer(b, np.uint64, 4, at)]
+            at += 32
+            for key, dt, cnt in (("points", np.float64, 3 * nP), ("counts", np.int32, nF), ("indices", np.int32, nI), ("slot", np.uint16, nS)):
+                out[name + "/" + key] = np.frombuffer(b, dt, cnt, at).copy()
+                at += np.dtype(dt).itemsize * cnt
+        names.append(name)
+        os.remove(raw_in)
+        os.remove(raw_out)
+        print("dmesh %s: %s" % (name, "ok, %d mesh" % nm if ok else msg))
+    out["names"] = np.frombuffer("\n".join(names).encode(), np.uint8)
+    np.savez_compressed(os.path.join(d, "cases.npz"), **out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("KITSIM_REFERENCE") or os.path.join(os.path.dirname(REPO), "reference"))
     ap.add_argument("--case")
-    ap.add_argument("--only", help="comma-separated parts to regenerate: recorded case names, sky, ladybug")
+    ap.add_argument("--only", help="comma-separated parts to regenerate: recorded case names, sky, ladybug, mesh, dmesh")
     a = ap.parse_args()
     if a.case:
         run_case(a.case, a.ref)
@@ -389,6 +472,8 @@ def main():
                 ladybug_goldens(a.ref)
             elif part == "mesh":
                 mesh_goldens(a.ref)
+            elif part == "dmesh":
+                dmesh_goldens(a.ref)
             else:
                 record(part, a.ref)
         return
@@ -398,6 +483,7 @@ def main():
     sky_goldens(a.ref)
     ladybug_goldens(a.ref)
     mesh_goldens(a.ref)
+    dmesh_goldens(a.ref)
     pub = published(a.ref)
     with open(os.path.join(HERE, "published.json"), "w") as f:
         json.dump(pub, f, indent=1)

@@ -14,6 +14,7 @@ STRUCTS = {   # C struct -> the binding's class
     "kgb_slot": "Slot", "kgb_scene": "SceneHandle", "kgb_stats": "Stats", "kgb_series_in": "SeriesIn",
     "kgb_sky_step": "SkyStep", "kgb_bounce_in": "BounceIn", "kgb_view_in": "ViewIn",
     "kgb_daylight_request": "DaylightRequest", "kgb_views_request": "ViewsRequest", "kgb_series_request": "SeriesRequest",
+    "kgb_mesh_info": "MeshInfo",
 }
 
 
