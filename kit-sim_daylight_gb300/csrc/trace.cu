@@ -336,9 +336,11 @@ __device__ __forceinline__ void enqueue(bool go, const PathState& st, PathState*
   if (go) q[base + __popc(m & ((1u << lane) - 1u))] = st;
 }
 
+// One mask for the sum and its leader: two reads of __activemask() may see different sets of converged lanes.
 __device__ __forceinline__ void add_segments(const BounceArgs& a, uint32_t segments) {
-  const uint32_t sum = __reduce_add_sync(__activemask(), segments);
-  if ((threadIdx.x & 31) == __ffs(__activemask()) - 1) atomicAdd(reinterpret_cast<unsigned long long*>(a.status + 1), (unsigned long long)sum);
+  const uint32_t m = __activemask();
+  const uint32_t sum = __reduce_add_sync(m, segments);
+  if ((threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(reinterpret_cast<unsigned long long*>(a.status + 1), (unsigned long long)sum);
 }
 
 // Paths as a wavefront: k_bounce_paths traces every path's first segment, one thread a path; with a.order, sensor
