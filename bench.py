@@ -120,11 +120,12 @@ def measured_peak(key):
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}[key], "fallback"
 
 
-def profiled(key):
-    """A figure of the committed ncu summary of k_bits on the urban block (profiles/k_bits_urban.md: lines `key: value`),
-    or None: traffic_per_full_trace_bytes (DRAM read + write of one trace), inst_per_full_trace (warp instructions of
-    one trace), thread_inst_per_full_trace (the same counted per active thread)."""
-    p = os.path.join(REPO, "profiles", "k_bits_urban.md")
+def profiled(key, summary="k_bits_urban.md"):
+    """A figure of a committed ncu summary (profiles/<summary>: lines `key: value`), or None. k_bits_urban.md (k_bits on
+    the urban block): traffic_per_full_trace_bytes (DRAM read + write of one trace), inst_per_full_trace (warp
+    instructions of one trace), thread_inst_per_full_trace (the same counted per active thread). k_view_views.md
+    (k_view on the views city): inst_per_fov120_trace, thread_inst_per_fov120_trace (the whole city at fov 120)."""
+    p = os.path.join(REPO, "profiles", summary)
     if os.path.exists(p):
         for line in open(p):
             if line.startswith(key + ":"):
@@ -541,16 +542,20 @@ def run_views(args, pkg):
         e.view(0, min(nc, 4096), flags, nAz, nEl, 0.0 if world else -fov / 2, dAz, rowSin, **kw)   # warm-up
         torch.cuda.synchronize()
         best = None
-        for _ in range(max(1, args.steps)):
-            t0 = time.perf_counter()
-            e.view(0, nc, flags, nAz, nEl, 0.0 if world else -fov / 2, dAz, rowSin, **kw)
-            t1 = time.perf_counter()
-            out = e.reduce_view(nc, wRow, 6, 1000.0, reach=reach, glazing=False, isoDim=iso)
-            t2 = time.perf_counter()
-            if best is None or t1 - t0 < best[0]:
-                best = (t1 - t0, t2 - t1)
+        with Clocks(0) as clk:
+            for _ in range(max(1, args.steps)):
+                st0 = e.stats()
+                t0 = time.perf_counter()
+                e.view(0, nc, flags, nAz, nEl, 0.0 if world else -fov / 2, dAz, rowSin, **kw)
+                t1 = time.perf_counter()
+                st1 = e.stats()
+                out = e.reduce_view(nc, wRow, 6, 1000.0, reach=reach, glazing=False, isoDim=iso)
+                t2 = time.perf_counter()
+                if best is None or t1 - t0 < best[0]:
+                    best = (t1 - t0, t2 - t1, (st1["traceMs"] - st0["traceMs"]) / 1e3, st1["launches"] - st0["launches"])
         K = nAz * nEl
-        res[name] = {"rays": nc * K, "trace_s": best[0], "reduce_s": best[1], "mrays_s": nc * K / best[0] / 1e6,
+        res[name] = {"rays": nc * K, "trace_s": best[0], "reduce_s": best[1], "mrays_s": nc * K / best[0] / 1e6, "kernel_s": best[2],
+                     "launches": int(best[3]), "clocks": clk.summary(),
                      "shares_sum_check": float(np.abs(out[:, 0] + out[:, 3] + out[:, 6] + out[:, 9] + out[:, 12] + out[:, 15] + out[:, 18] - 1).max())}
         if world:   # the per-ray rows (gpu_download_view: classes + distances, [nc x K]), transposed on the device, into
             # buffers already written (the reference's caller resizes its vectors first, gpu.cu:730-731)
@@ -587,7 +592,22 @@ def run_views(args, pkg):
         t1 = time.perf_counter()
         best = t1 - t0 if best is None else min(best, t1 - t0)
     host_tree = {"build_s": host_build_s, "fov120_mrays_s": nc * nAz * nEl / best / 1e6, "gas_bytes": e.stats()["gasBytes"]}
-    line = {"metric": "Mrays/s (closest hit)", "unit": "Mrays/s", "value": res["fov120"]["mrays_s"],
+    # k_view's ceiling is instruction issue, as k_bits': the warp instructions of a whole-city fov 120 trace (ncu,
+    # profiles/k_view_views.md) over its kernels' CUDA-event time, against 4 issue slots per SM per cycle
+    inst = profiled("inst_per_fov120_trace", "k_view_views.md") if not args.sensors else None
+    tinst = profiled("thread_inst_per_fov120_trace", "k_view_views.md") if not args.sensors else None
+    sm_mhz = res["fov120"]["clocks"]["sm_mhz"] or 2070.0
+    num_sms = torch.cuda.get_device_properties(0).multi_processor_count
+    issue_peak = 4.0 * num_sms * sm_mhz * 1e6
+    kern_s = res["fov120"]["kernel_s"]
+    roof = {"bound": "issue", "kernel": "k_view", "achieved": inst / kern_s if inst else None, "peak": issue_peak, "unit": "warp-inst/s",
+            "frac": inst / kern_s / issue_peak if inst else None,
+            "peak_kind": "4 issue slots per SM per cycle x %d SMs at the sampled median SM clock (%.0f MHz)" % (num_sms, sm_mhz),
+            "lanes_active_of_32": tinst / inst if (inst and tinst) else None, "kernel_s": kern_s,
+            "note": "closest-hit walk: its 2 M-triangle tree stays in L2 and most loads hit L1 (DRAM nearly idle), so instruction "
+                    "issue bounds it; achieved = warp instructions of the fov 120 trace of the whole city (ncu, "
+                    "profiles/k_view_views.md) / its kernels' CUDA-event time"}
+    line = {"metric": "Mrays/s (closest hit)", "unit": "Mrays/s", "value": res["fov120"]["mrays_s"], "roofline": roof,
             "config": {"workload": "views city: %d facade sensors, %d triangles, 3 target groups; fov 120 / 2 deg (3600 rays), fov 360 / 2 deg "
                                    "(10800 rays, isovist volume, reach 6/20/50), jitter on" % (nc, len(city["tri"]))},
             "fov120": res["fov120"], "fov360": res["fov360"], "bvh_build_s": build_s, "bvh": "device LBVH + treelet restructuring",
