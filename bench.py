@@ -662,6 +662,8 @@ def run_serving(args, pkg):
     srv = kgb.Server(lib, 150e9)
     ids = [srv.add_scene(s["v"], s["tri"]) for s in scenes]
     srv.autotune()
+    if args.old_seconds:
+        srv.set_priority(args.old_seconds)
     reqs = serving_requests(pkg, scenes, args.rate, args.window)
     grids = {fov: pkg.workloads.views_grid(fov, 2.0) for fov in (120.0, 360.0)}
     t0 = time.perf_counter()
@@ -900,6 +902,7 @@ def main():
     ap.add_argument("--series-seed", type=int, default=12)
     ap.add_argument("--builder", type=int, default=1, choices=[0, 1], help="urban: 1 device LBVH with treelets (default), 0 host binned-SAH tree")
     ap.add_argument("--rate", type=float, default=200.0)
+    ap.add_argument("--old-seconds", type=float, default=0.0, help="serving: the scheduler's wait past which requests go in arrival order")
     ap.add_argument("--window", type=float, default=2.0)
     ap.add_argument("--full-fp32", action="store_true")
     ap.add_argument("--accuracy-sensors", type=int, default=1024, help="precision: sensors of the FP64 accuracy check")

@@ -358,6 +358,9 @@ KGB_API int kgb_server_autotune(kgb_server* s);
 /* sets by hand what the autotuner picks (call while idle; 0 keeps a value): sensors per daylight chunk (32..2^20), rays
  * per daylight batch (2^16..2^32) and rays per views chunk (2^16..2^31, default 2^27) */
 KGB_API int kgb_server_set_tuning(kgb_server* s, uint32_t chunkSensors, uint64_t batchRays, uint64_t viewRays);
+/* the scheduler's priority: a request that has waited more than oldSeconds goes first, in arrival order; the others by
+ * their remaining work divided by (their age + ageSeconds). Defaults 1.0 s and 0.3 s; takes effect at the next pick. */
+KGB_API int kgb_server_set_priority(kgb_server* s, double oldSeconds, double ageSeconds);
 KGB_API int kgb_server_submit(kgb_server* s, const kgb_daylight_request* r, uint64_t* ticket);
 KGB_API int kgb_server_submit_views(kgb_server* s, const kgb_views_request* r, uint64_t* ticket);
 /* a daylight request that also gives its time series (its host arrays, the series' included, valid until it is waited

@@ -10,7 +10,7 @@
 //    CUDA graph built once per slot and replayed per batch, its copy sizes and the reduce's grid set per batch;
 //  - a views chunk: the view kernels (k_view, k_view_reduce, k_iso) on a range of one request's sensors, sized by rays.
 // The scheduler picks the next item by a priority over every request with sensors not yet issued: a request that has
-// waited more than 1.2 s goes first, in arrival order; the others by their remaining work (rays times a running
+// waited more than 1.0 s goes first, in arrival order; the others by their remaining work (rays times a running
 // estimate of seconds per ray of its kind, measured from the items' own GPU time) divided by their age plus 0.3 s.
 // Short requests overtake long ones, which keeps the p50 near one item's time, and no request waits behind younger
 // ones for long, which keeps the p99 at arrival order's. A daylight batch is packed in that order, a chunk at a time.
@@ -153,8 +153,8 @@ constexpr int kSlots = 2;                       // work items of each kind that 
 constexpr size_t kDepth = 2;                    // work items queued on the work stream at once
 constexpr uint32_t kMaxViewChunk = 65536;       // sensors in one views chunk
 constexpr uint32_t kMaxNA = 3 * KGB_VIEW_CLASSES + 1 + 8 + 1 + 1;   // views columns
-constexpr double kAgeSeconds = 0.3;             // the priority's age offset
-constexpr double kOldSeconds = 1.2;             // past this wait a request goes first, in arrival order
+constexpr double kAgeSeconds = 0.3;             // the priority's age offset (default; kgb_server_set_priority)
+constexpr double kOldSeconds = 1.0;             // past this wait a request goes first, in arrival order (default)
 constexpr size_t kSeriesVBytes = size_t(256) << 20;   // per daylight slot: the series chunks' V pieces (bf16)
 constexpr size_t kSeriesEBytes = size_t(256) << 20;   // per daylight slot: their rows of E, on the device and pinned
 
@@ -237,6 +237,7 @@ struct Server {
   uint32_t chunkSensors = 8192;
   uint64_t batchRays = uint64_t(1) << 28;
   uint64_t viewRays = uint64_t(1) << 27;
+  double oldSeconds = kOldSeconds, ageSeconds = kAgeSeconds;   // the scheduler's priority (kgb_server_set_priority)
   // batch pools (fixed for the graphs)
   size_t bitsPoolWords = 0, outPoolDoubles = 0;
   uint32_t maxSensPerBatch = 0;
@@ -484,9 +485,9 @@ bool order_after_uploads(Server& s, std::string& err) {
 
 double priority(const Server& s, const Request* r, Clock::time_point now) {
   const double age = std::chrono::duration<double>(now - r->tSubmit).count();
-  if (age > kOldSeconds) return -1e9 - age;   // the oldest first, before every younger request
+  if (age > s.oldSeconds) return -1e9 - age;   // the oldest first, before every younger request
   const double rem = double(r->nSensors - r->nextSensor) * double(r->raysPerSensor) * s.cost[r->kind];
-  return rem / (age + kAgeSeconds);
+  return rem / (age + s.ageSeconds);
 }
 
 // The batch's series, after its graph on the work stream: each series chunk's V pieces from the batch's visibility
@@ -1053,6 +1054,18 @@ KGB_API int kgb_server_set_tuning(kgb_server* h, uint32_t chunkSensors, uint64_t
   if (viewRays) s->viewRays = viewRays;
   std::string err;
   if (!make_pools(*s, err) || !cuok(cudaStreamSynchronize(s->st), err, "tuning")) { set_error(err); return 0; }
+  return 1;
+}
+
+KGB_API int kgb_server_set_priority(kgb_server* h, double oldSeconds, double ageSeconds) {
+  Server* s = reinterpret_cast<Server*>(h);
+  if (!(oldSeconds > 0 && oldSeconds < 1e6 && ageSeconds > 0 && ageSeconds < 1e6)) {
+    set_error("kgb_server_set_priority: both times in (0, 1e6) seconds");
+    return 0;
+  }
+  std::unique_lock<std::mutex> lk(s->m);
+  s->oldSeconds = oldSeconds;
+  s->ageSeconds = ageSeconds;
   return 1;
 }
 

@@ -126,6 +126,7 @@ SIGNATURES = [
     ("kgb_server_add_scene", c_int, [c_void_p, c_void_p, c_size_t, c_void_p, c_size_t, POINTER(c_int32)]),
     ("kgb_server_autotune", c_int, [c_void_p]),
     ("kgb_server_set_tuning", c_int, [c_void_p, c_uint32, c_uint64, c_uint64]),
+    ("kgb_server_set_priority", c_int, [c_void_p, c_double, c_double]),
     ("kgb_server_submit", c_int, [c_void_p, POINTER(DaylightRequest), POINTER(c_uint64)]),
     ("kgb_server_submit_views", c_int, [c_void_p, POINTER(ViewsRequest), POINTER(c_uint64)]),
     ("kgb_server_submit_series", c_int, [c_void_p, POINTER(DaylightRequest), POINTER(SeriesRequest), POINTER(c_uint64)]),
@@ -543,6 +544,12 @@ class Server:
     def set_tuning(self, chunk_sensors=0, batch_rays=0, view_rays=0):
         """Chunk sensors, daylight batch rays and views chunk rays by hand (0 keeps a value)."""
         if not self.d.kgb_server_set_tuning(self.h, int(chunk_sensors), int(batch_rays), int(view_rays)):
+            raise KgbError(self.lib.err())
+
+    def set_priority(self, old_seconds=1.0, age_seconds=0.3):
+        """The scheduler's priority: requests older than old_seconds first, in arrival order; the others by remaining
+        work / (age + age_seconds)."""
+        if not self.d.kgb_server_set_priority(self.h, float(old_seconds), float(age_seconds)):
             raise KgbError(self.lib.err())
 
     def submit(self, scene, P, N, D, W, use_cos, flags=5):
