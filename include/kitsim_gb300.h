@@ -394,9 +394,15 @@ KGB_API int kgb_set_builder(kgb_engine* e, int which);
  * nodeLimit nodes, and so at most nodeLimit + 8 node visits per query; a query that needs more gives up and the call
  * fails ("traversal gave up ...", the message of a walk past its visit cap; 0: every node, the cap then the node count
  * + 8, at most 2^20). bounceLimitNs: how long one bounce step kernel may run before it ends its remaining paths and
- * kgb_bounce fails ("... passed its ... limit ..."; 0: the default, 10 s; larger values are clamped to it). The engine
- * stays usable after such a failure. */
-KGB_API int kgb_set_limits(kgb_engine* e, uint32_t nodeLimit, uint64_t bounceLimitNs);
+ * kgb_bounce fails ("... passed its ... limit ..."; 0: the default, 10 s; larger values are clamped to it).
+ * seriesWaitNs: how long a wait of the tensor-core series pipeline (its producer, MMA issuer and epilogue on their
+ * mbarriers) may last before the kernel records a timeout, finishes the copies and MMAs it issued, frees its TMEM and
+ * ends, and kgb_series fails ("... timed out waiting ..."; 0: the default, 4 s; larger values are clamped to it).
+ * flags: KGB_LIMIT_WITHHOLD_FILLS makes the series pipeline's producer issue no shared-memory fills, so that its waits
+ * run out for certain (a barrier nothing completes): the test of that path. The engine stays usable after any of
+ * these failures. */
+#define KGB_LIMIT_WITHHOLD_FILLS 1u
+KGB_API int kgb_set_limits(kgb_engine* e, uint32_t nodeLimit, uint64_t bounceLimitNs, uint64_t seriesWaitNs, uint32_t flags);
 /* Instrumentation for the traversal roofline: traces sensors [i0, i0+nc) exactly as kgb_trace does (same bits / bytes
  * left on the device) with counting kernels, out[0] = BVH nodes visited, out[1] = triangles tested, out[2] = rays
  * traced past the hemisphere cull, out[3] = BVH bytes (nodes + triangle records). */

@@ -307,6 +307,8 @@ struct Engine {
   int builder = 1;            // 1 device LBVH with treelet restructuring (default), 0 host binned SAH (kgb_set_builder)
   uint32_t nodeLimit = 0;     // kgb_set_limits: the walks see only this many of the BVH's nodes (0: all)
   uint64_t bounceLimitNs = kBounceLimitNs;   // kgb_set_limits: a bounce step kernel's time limit
+  uint64_t seriesWaitNs = 0;                  // kgb_set_limits: the series pipeline's wait limit (0: its default)
+  bool withholdFills = false;                 // kgb_set_limits: KGB_LIMIT_WITHHOLD_FILLS
   std::vector<DevMesh*> meshes;               // meshes read to the device, by id (null: freed)
 };
 
@@ -827,6 +829,7 @@ static int series_impl(Engine& g, size_t nc, const kgb_series_in* in, const Sink
     p.v = g.vop.p; p.s = g.sop.p;
     p.sunOfCol = static_cast<const int32_t*>(g.sunCol.p); p.sunVec = a.sunVec; p.sunW = a.sunW;
     p.bits = a.bits; p.bytes = a.bytes; p.N = a.N; p.E = a.E; p.status = static_cast<uint32_t*>(g.ctl.p) + 1;
+    p.waitLimitNs = g.seriesWaitNs; p.withholdFills = g.withholdFills;
     SeriesOperands o{};
     o.P = P; o.nBins = nBins; o.D = a.D; o.patchFirst = dFirst; o.patchDirs = dDirs; o.wsky = a.wsky; o.G = a.G; o.dc = a.dc;
     o.S = a.S; o.g = a.g; o.Sdc = a.Sdc; o.rebuildS = true;
@@ -1052,10 +1055,13 @@ KGB_API int kgb_set_builder(kgb_engine* e, int which) {
   return 1;
 }
 
-KGB_API int kgb_set_limits(kgb_engine* e, uint32_t nodeLimit, uint64_t bounceLimitNs) {
+KGB_API int kgb_set_limits(kgb_engine* e, uint32_t nodeLimit, uint64_t bounceLimitNs, uint64_t seriesWaitNs, uint32_t flags) {
   Engine& g = *E(e);
+  if (flags & ~KGB_LIMIT_WITHHOLD_FILLS) return fail("kgb_set_limits: unknown flags");
   g.nodeLimit = nodeLimit;
   g.bounceLimitNs = bounceLimitNs ? std::min(bounceLimitNs, kBounceLimitNs) : kBounceLimitNs;
+  g.seriesWaitNs = seriesWaitNs;
+  g.withholdFills = (flags & KGB_LIMIT_WITHHOLD_FILLS) != 0;
   return 1;
 }
 

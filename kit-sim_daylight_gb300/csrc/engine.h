@@ -163,6 +163,8 @@ struct SeriesTcPlan {
   const float* N;          // the chunk's normals
   float* E;                // [nc x T]
   uint32_t* status;
+  uint64_t waitLimitNs = 0;   // the pipeline's waits give up past this (0: the default, 4 s)
+  bool withholdFills = false; // the producer issues no fills (kgb_set_limits' test of the bounded waits)
 };
 struct SeriesOperands {
   uint32_t P, nBins;

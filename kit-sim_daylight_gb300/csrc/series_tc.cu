@@ -184,7 +184,8 @@ struct TcGroup {
   TcSeg seg[kMaxTcSegs];
   uint32_t nSegs, nTiles;
   uint32_t* status;
-  uint64_t waitLimitNs;      // the pipeline's mbarrier waits give up past this (kWaitLimitNs)
+  uint64_t waitLimitNs;      // the pipeline's mbarrier waits give up past this (kWaitLimitNs, or lower)
+  uint32_t withholdFills;    // 1: the producer issues no fills, so that the waits run out (a test of the bounded waits)
 };
 static_assert(sizeof(TcGroup) <= 32000, "the group fits the 32 KB of kernel parameters");
 
@@ -260,6 +261,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
         const uint32_t kBlocks = a.Kp / BK;
         for (uint32_t kb = 0; kb < kBlocks; ++kb) {
           if (!mbar_wait(&empty[stage], phase ^ 1, g.status, g.waitLimitNs)) { abortFlag = 1; break; }
+          if (g.withholdFills) {   // nothing completes full[stage]: the MMA issuer's wait on it runs out
+            if (++stage == STAGES) { stage = 0; phase ^= 1; }
+            continue;
+          }
           uint8_t* s = smem + stage * STAGE_BYTES;
           mbar_expect_tx(&full[stage], STAGE_BYTES);
           const int k0 = int(kb) * BK;
@@ -541,14 +546,15 @@ static const char* tc_seg(const SeriesTcPlan& p, uint32_t mBase, uint32_t mCount
   return nullptr;
 }
 
-static const char* tc_launch(TcGroup& g, int numSMs, cudaStream_t st) {
+static const char* tc_launch(TcGroup& g, int numSMs, uint64_t waitLimitNs, bool withholdFills, cudaStream_t st) {
   static bool attr = false;
   if (!attr) {
     if (cudaFuncSetAttribute(k_series_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) != cudaSuccess)
       return "series_tc: cannot reserve shared memory";
     attr = true;
   }
-  g.waitLimitNs = kWaitLimitNs;
+  g.waitLimitNs = waitLimitNs ? std::min(waitLimitNs, kWaitLimitNs) : kWaitLimitNs;
+  g.withholdFills = withholdFills ? 1u : 0u;
   const int grid = int(std::min<uint32_t>(uint32_t(numSMs), g.nTiles));
   k_series_tc<<<grid, THREADS, SMEM_BYTES, st>>>(g);
   return nullptr;
@@ -562,7 +568,7 @@ const char* series_tc_rows(const SeriesTcPlan& p, uint32_t mBase, uint32_t mCoun
   if (const char* why = tc_seg(p, mBase, mCount, 0, G.seg[0])) return why;
   G.nTiles = mCount * G.seg[0].nTiles;
   G.status = p.status;
-  return tc_launch(G, p.numSMs, st);
+  return tc_launch(G, p.numSMs, p.waitLimitNs, p.withholdFills, st);
 }
 
 const char* series_tc_group(const SeriesTcPlan* plans, uint32_t n, cudaStream_t st) {
@@ -582,7 +588,7 @@ const char* series_tc_group(const SeriesTcPlan* plans, uint32_t n, cudaStream_t 
   }
   if (!G.nSegs) return nullptr;
   G.status = plans[0].status;
-  return tc_launch(G, plans[0].numSMs, st);
+  return tc_launch(G, plans[0].numSMs, plans[0].waitLimitNs, plans[0].withholdFills, st);
 }
 
 void build_series_operands(const SeriesTcPlan& p, const SeriesOperands& o, cudaStream_t st) {

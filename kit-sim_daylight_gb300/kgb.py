@@ -81,6 +81,7 @@ class MeshInfo(ctypes.Structure):
 
 
 NO_MESH = 0xFFFFFFFF
+LIMIT_WITHHOLD_FILLS = 1
 RAY_DISABLE_ANYHIT, RAY_TERMINATE_ON_FIRST_HIT, RAY_CULL_BACK_FACING = 1, 4, 16
 SLOT_GLASS, SLOT_THIN, SLOT_INWARD, SLOT_TWIN = 1, 2, 4, 8
 LABEL_PASS, MAX_PANES, VIEW_GLAZED = 255, 16, 0x80
@@ -143,7 +144,7 @@ SIGNATURES = [
     ("kgb_set_builder", c_int, [_E, c_int]),
     ("kgb_set_series_form", c_int, [_E, c_int]),
     ("kgb_trace_counters", c_int, [_E, c_size_t, c_size_t, c_uint32, POINTER(c_uint64)]),
-    ("kgb_set_limits", c_int, [_E, c_uint32, c_uint64]),
+    ("kgb_set_limits", c_int, [_E, c_uint32, c_uint64, c_uint64, c_uint32]),
     ("kgb_mesh_read", c_int, [_E, c_void_p, c_size_t, c_char_p, POINTER(MeshInfo)]),
     ("kgb_mesh_file", c_int, [_E, c_char_p, POINTER(MeshInfo)]),
     ("kgb_mesh_download", c_int, [_E, c_uint32, c_void_p, c_void_p, c_void_p, c_void_p]),
@@ -376,10 +377,11 @@ class Engine:
         """0: split-BF16 on the tensor cores (default); 1: the plain FP32 form."""
         self._ok(self.d.kgb_set_series_form(self.h, form))
 
-    def set_limits(self, node_limit=0, bounce_limit_ns=0):
-        """Lowers the traversal's node limit (the walks see only the BVH's first node_limit nodes) and the bounce step's
-        time limit; 0 restores a default."""
-        self._ok(self.d.kgb_set_limits(self.h, int(node_limit), int(bounce_limit_ns)))
+    def set_limits(self, node_limit=0, bounce_limit_ns=0, series_wait_ns=0, withhold_fills=False):
+        """Lowers the traversal's node limit (the walks see only the BVH's first node_limit nodes), the bounce step's
+        time limit and the series pipeline's wait limit; 0 restores a default. withhold_fills: the series pipeline's
+        producer issues no fills, so that its waits run out (the test of that path)."""
+        self._ok(self.d.kgb_set_limits(self.h, int(node_limit), int(bounce_limit_ns), int(series_wait_ns), LIMIT_WITHHOLD_FILLS if withhold_fills else 0))
 
     def trace_counters(self, i0, nc, flags):
         """The instrumented trace: dict(nodes, tris, rays, bvh_bytes) for the roofline (results as trace())."""

@@ -1180,7 +1180,7 @@ KGB_API int kgb_sun_noaa(kgb_engine*, const double*, size_t, double*) {
 KGB_API int kgb_set_builder(kgb_engine*, int which) { return which == 0 || which == 1 ? 1 : fail("kgb_set_builder: 0 or 1"); }
 // The engine's bounded-execution limits guard its device walks; the oracle's host recursion needs none, so there is
 // nothing to lower here.
-KGB_API int kgb_set_limits(kgb_engine*, uint32_t, uint64_t) { return 1; }
+KGB_API int kgb_set_limits(kgb_engine*, uint32_t, uint64_t, uint64_t, uint32_t) { return 1; }
 KGB_API int kgb_set_series_form(kgb_engine*, int form) { return form == 0 || form == 1 ? 1 : fail("kgb_set_series_form: 0 or 1"); }
 KGB_API int kgb_trace_counters(kgb_engine*, size_t, size_t, uint32_t, uint64_t out[4]) {
   out[0] = out[1] = out[2] = out[3] = 0;

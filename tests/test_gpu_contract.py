@@ -4,6 +4,8 @@ launches), the build-memory estimate (check_gpu.cpp:124-127), resident scenes pa
 (check_gpu.cpp:692-728, run()'s sceneKey and residentScenes on top of gpu_detach / gpu_attach / gpu_free), cancel
 between sub-launches of gpu_bounce and gpu_view (gpu.cu:554, 594; check_gpu.cpp:730-734), the per-run stats
 (check_gpu.cpp:790-797), and the engine's bounded-execution limits driven to their error returns."""
+import time
+
 import numpy as np
 import pytest
 
@@ -302,3 +304,31 @@ def test_per_run_stats(eng, engine_lib, pkg):
     assert st1["rays"] - st0["rays"] == nc * len(D)
     assert st1["paths"] - st0["paths"] == nc * 32
     assert st1["launches"] > st0["launches"] and st1["bounceLaunches"] > st0["bounceLaunches"]
+
+
+def test_series_pipeline_wait_limit(eng, engine_lib, pkg, kgb):
+    """The tensor-core series pipeline's bounded waits: with the producer withholding its fills (a barrier nothing
+    completes) and a 1 ms wait limit, the MMA issuer's and the epilogue's waits run out; the kernel finishes what it
+    issued, frees its TMEM and ends, and kgb_series fails with the timeout message. With the limits restored the same
+    engine gives the series it gave before, bit for bit."""
+    s = pkg.workloads.random_city(45, n_boxes=40)
+    nc, P, T, nSun = 1024, 145, 200, 60
+    D = pkg.workloads.hemisphere_dirs(P, nSun, 45)
+    eng.build(s["v"], s["tri"])
+    eng.set_scene(s["P"][:nc], s["N"][:nc], D)
+    eng.trace(0, nc, engine_lib.ray_flags(False, False))
+    rng = np.random.default_rng(45)
+    args = dict(nSky=P, row=np.arange(P), wsky=np.full(P, 2 * np.pi / P, np.float32), S=rng.uniform(0, 300, (P, T)).astype(np.float32),
+                g=rng.uniform(0, 50, T).astype(np.float32), G=rng.uniform(0.1, 1.0, nc).astype(np.float32), sun0=2 * P,
+                sunStep=np.sort(rng.choice(T, nSun, replace=False)), sunVec=D[2 * P:2 * P + nSun], sunW=rng.uniform(100, 900, nSun).astype(np.float32))
+    E0 = eng.series(nc, **args)
+    eng.set_limits(series_wait_ns=1_000_000, withhold_fills=True)
+    t0 = time.perf_counter()
+    with pytest.raises(kgb.KgbError, match="timed out waiting"):
+        eng.series(nc, **args)
+    assert time.perf_counter() - t0 < 3.0   # the waits gave up at their 1 ms limit, not the default 4 s
+    eng.set_limits()
+    E1 = eng.series(nc, **args)
+    assert np.array_equal(E0.view(np.uint32), E1.view(np.uint32))
+    eng.trace(0, nc, engine_lib.ray_flags(False, False))   # the engine's other kernels still run
+
