@@ -685,6 +685,7 @@ def run_serving(args, pkg):
     wall = time.perf_counter() - t0
     st = srv.stats()
     tm = srv.timing()
+    tuning = srv.tuning()
     srv.close()
     sensors = sum(len(r["P"]) for r in reqs)
     # the plain form: one request per launch, FIFO, through the single-request entry points (scenes parked and attached)
@@ -728,7 +729,7 @@ def run_serving(args, pkg):
             "config": {"workload": "serving: Poisson %.0f req/s for %.1f s (%d requests: %d daylight, %d views), 4 resident scenes of %s triangles, "
                                    "150 GB HBM budget" % (args.rate, args.window, len(reqs), sum(r["kind"] == "daylight" for r in reqs),
                                                          sum(r["kind"] == "views" for r in reqs), "/".join("%.1fM" % (len(s["tri"]) / 1e6) for s in scenes))},
-            "server": {k: st[k] for k in ("completed", "items", "rays", "chunk_sensors", "batch_rays")}, "wall_s": wall,
+            "server": dict({k: st[k] for k in ("completed", "items", "rays")}, **tuning), "wall_s": wall,
             "gpu": {"daylight_s": tm["day_gpu_s"], "daylight_mrays_s": tm["day_rays"] / max(tm["day_gpu_s"], 1e-9) / 1e6, "views_s": tm["views_gpu_s"],
                     "views_mrays_s": tm["views_rays"] / max(tm["views_gpu_s"], 1e-9) / 1e6, "queued_s": tm["queued_s"]}}
     return line

@@ -361,6 +361,9 @@ KGB_API int kgb_server_set_tuning(kgb_server* s, uint32_t chunkSensors, uint64_t
 /* the scheduler's priority: a request that has waited more than oldSeconds goes first, in arrival order; the others by
  * their remaining work divided by (their age + ageSeconds). Defaults 1.0 s and 0.3 s; takes effect at the next pick. */
 KGB_API int kgb_server_set_priority(kgb_server* s, double oldSeconds, double ageSeconds);
+/* out[3]: the tuning in use (autotuned or set by hand): sensors per daylight chunk, rays per daylight batch, rays per
+ * views chunk */
+KGB_API void kgb_server_tuning(kgb_server* s, uint64_t* out);
 KGB_API int kgb_server_submit(kgb_server* s, const kgb_daylight_request* r, uint64_t* ticket);
 KGB_API int kgb_server_submit_views(kgb_server* s, const kgb_views_request* r, uint64_t* ticket);
 /* a daylight request that also gives its time series (its host arrays, the series' included, valid until it is waited

@@ -827,9 +827,78 @@ bool run_batch_now(Server& s, const std::vector<Part>& parts, double& sec, std::
   return true;
 }
 
+// a views request's chunks one after another in slot 0 at the server's views chunk size; its rays per second
+bool run_views_now(Server& s, Request& r, double& rate, std::string& err) {
+  const auto t0 = Clock::now();
+  uint64_t rays = 0;
+  for (uint32_t i0 = 0; i0 < r.nSensors;) {
+    r.nextSensor = i0;
+    const uint32_t n = views_chunk(s, &r);
+    if (uint64_t(n) * r.raysPerSensor > s.viewCap) { err = "calibration views chunk beyond the scratch"; return false; }
+    if (!launch_views(s, 0, Part{&r, i0, n}, err)) return false;
+    if (!cuok(cudaEventSynchronize(s.view[0].ev[1]), err, "calibration views chunk")) return false;
+    if (*s.view[0].hStatus) { err = "calibration views chunk: traversal stack overflow"; return false; }
+    rays += uint64_t(n) * r.raysPerSensor;
+    i0 += n;
+  }
+  rate = double(rays) / std::chrono::duration<double>(Clock::now() - t0).count();
+  return true;
+}
+
+// the views chunk size: one synthetic fov 120 request (2-degree cells, 40,960 sensors: 147 M rays, the size of the
+// larger views requests) from the same sensors, run whole at each candidate size; the size with the most rays per
+// second, or a smaller one within 1 % of it. (Picking the smallest within 5 % on a 16 k-sensor request chose 2^26 rays,
+// and the serving config's views then ran 5 % slower than at 2^27.)
+bool tune_views(Server& s, const std::vector<float>& P, const std::vector<float>& N, uint32_t nSens, std::string& err) {
+  const uint32_t nAz = 60, nEl = 60;   // 3600 rays a sensor
+  std::vector<float> rowSin(2 * nEl);
+  std::vector<double> wRow(nEl);
+  for (uint32_t j = 0; j < nEl; ++j) {
+    const double lo = (-60.0 + 2.0 * j) * KGB_PI_D / 180, hi = (-58.0 + 2.0 * j) * KGB_PI_D / 180;
+    rowSin[2 * j] = float(std::sin(lo)); rowSin[2 * j + 1] = float(std::sin(hi));
+    wRow[j] = std::sin(hi) - std::sin(lo);
+  }
+  std::vector<double> out(size_t(nSens) * (3 * 1 + 1));
+  struct Trial { uint64_t rays; double rate; };
+  std::vector<Trial> trials;
+  const uint64_t keep = s.viewRays;
+  for (uint64_t vr : {uint64_t(1) << 25, uint64_t(1) << 26, uint64_t(1) << 27, uint64_t(1) << 28}) {
+    s.viewRays = vr;
+    if (!make_pools(s, err)) return false;
+    Request r;
+    r.kind = 1;
+    r.v = kgb_views_request{};
+    r.v.scene = 0; r.v.nSensors = nSens; r.v.P = P.data(); r.v.N = N.data(); r.v.label = nullptr;
+    r.v.view.nAz = nAz; r.v.view.nEl = nEl; r.v.view.az0 = -60.f; r.v.view.dAz = 2.f; r.v.view.rowSin = rowSin.data();
+    r.v.view.jitter = 1; r.v.view.vground = 1; r.v.view.nS = 1; r.v.view.groundZ = -1e4f;
+    r.v.rayFlags = KGB_RAY_DISABLE_ANYHIT; r.v.wRow = wRow.data(); r.v.nClass = 1; r.v.farDist = 1000.0; r.v.out = out.data();
+    r.rowSin = rowSin; r.wRow = wRow;
+    r.nSensors = nSens;
+    r.raysPerSensor = uint64_t(nAz) * nEl;
+    r.devBytes = request_bytes(s, &r);
+    if (!upload(s, &r, err)) return false;
+    cudaEventRecord(s.upDone, s.up);
+    double best = 0;
+    for (int rep = 0; rep < 2; ++rep) {   // the first run warms the caches
+      double rate = 0;
+      if (!run_views_now(s, r, rate, err)) { cudaFreeAsync(r.dev, s.st); return false; }
+      best = std::max(best, rate);
+    }
+    cudaFreeAsync(r.dev, s.st);
+    trials.push_back(Trial{vr, best});
+  }
+  double top = 0;
+  for (const Trial& t : trials) top = std::max(top, t.rate);
+  s.viewRays = keep;
+  for (const Trial& t : trials)
+    if (t.rate >= 0.99 * top) { s.viewRays = t.rays; break; }   // the candidates run smallest first
+  return true;
+}
+
 // the autotuner: calibration batches of one synthetic request on scene 0 (its first sensors against a fixed
 // direction table); keeps the chunk size and batch size with the most rays per second, or the smallest batch within
-// 5 % of that rate (a smaller batch is a shorter wait for requests that arrive while it runs)
+// 5 % of that rate (a smaller batch is a shorter wait for requests that arrive while it runs); then the views chunk
+// size the same way (tune_views)
 bool autotune(Server& s, std::string& err) {
   const DScene& sc = s.scenes[0];
   if (!sc.nNodes) return true;
@@ -892,6 +961,7 @@ bool autotune(Server& s, std::string& err) {
     if (t.rate >= 0.95 * top && (!have || t.rays < pick.rays || (t.rays == pick.rays && t.rate > pick.rate))) { pick = t; have = true; }
   s.chunkSensors = pick.chunk;
   s.batchRays = pick.rays;
+  if (!tune_views(s, P, N, 40960, err)) return false;
   s.rays = 0;
   s.items = 0;
   s.gpuSec[0] = s.gpuSec[1] = s.kindRays[0] = s.kindRays[1] = s.queuedSec = 0;
@@ -1055,6 +1125,14 @@ KGB_API int kgb_server_set_tuning(kgb_server* h, uint32_t chunkSensors, uint64_t
   std::string err;
   if (!make_pools(*s, err) || !cuok(cudaStreamSynchronize(s->st), err, "tuning")) { set_error(err); return 0; }
   return 1;
+}
+
+KGB_API void kgb_server_tuning(kgb_server* h, uint64_t* out) {
+  Server* s = reinterpret_cast<Server*>(h);
+  std::unique_lock<std::mutex> lk(s->m);
+  out[0] = s->chunkSensors;
+  out[1] = s->batchRays;
+  out[2] = s->viewRays;
 }
 
 KGB_API int kgb_server_set_priority(kgb_server* h, double oldSeconds, double ageSeconds) {

@@ -128,6 +128,7 @@ SIGNATURES = [
     ("kgb_server_autotune", c_int, [c_void_p]),
     ("kgb_server_set_tuning", c_int, [c_void_p, c_uint32, c_uint64, c_uint64]),
     ("kgb_server_set_priority", c_int, [c_void_p, c_double, c_double]),
+    ("kgb_server_tuning", None, [c_void_p, POINTER(c_uint64)]),
     ("kgb_server_submit", c_int, [c_void_p, POINTER(DaylightRequest), POINTER(c_uint64)]),
     ("kgb_server_submit_views", c_int, [c_void_p, POINTER(ViewsRequest), POINTER(c_uint64)]),
     ("kgb_server_submit_series", c_int, [c_void_p, POINTER(DaylightRequest), POINTER(SeriesRequest), POINTER(c_uint64)]),
@@ -547,6 +548,12 @@ class Server:
         """Chunk sensors, daylight batch rays and views chunk rays by hand (0 keeps a value)."""
         if not self.d.kgb_server_set_tuning(self.h, int(chunk_sensors), int(batch_rays), int(view_rays)):
             raise KgbError(self.lib.err())
+
+    def tuning(self):
+        """The tuning in use: chunk sensors, daylight batch rays, views chunk rays."""
+        out = (c_uint64 * 3)()
+        self.d.kgb_server_tuning(self.h, out)
+        return {"chunk_sensors": int(out[0]), "batch_rays": int(out[1]), "view_rays": int(out[2])}
 
     def set_priority(self, old_seconds=1.0, age_seconds=0.3):
         """The scheduler's priority: requests older than old_seconds first, in arrival order; the others by remaining

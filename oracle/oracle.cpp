@@ -1114,6 +1114,7 @@ KGB_API int kgb_server_add_scene(kgb_server*, const float*, size_t, const uint32
 KGB_API int kgb_server_autotune(kgb_server*) { return fail("not restated"); }
 KGB_API int kgb_server_set_tuning(kgb_server*, uint32_t, uint64_t, uint64_t) { return fail("not restated"); }
 KGB_API int kgb_server_set_priority(kgb_server*, double, double) { return fail("not restated"); }
+KGB_API void kgb_server_tuning(kgb_server*, uint64_t* out) { out[0] = out[1] = out[2] = 0; }
 KGB_API int kgb_server_submit(kgb_server*, const kgb_daylight_request*, uint64_t*) { return fail("not restated"); }
 KGB_API int kgb_server_submit_views(kgb_server*, const kgb_views_request*, uint64_t*) { return fail("not restated"); }
 KGB_API int kgb_server_submit_series(kgb_server*, const kgb_daylight_request*, const kgb_series_request*, uint64_t*) { return fail("not restated"); }
