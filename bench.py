@@ -492,6 +492,9 @@ def run_precision(args, pkg):
     paths = nc_all * M
     line = {"metric": "radiation solves/s", "unit": "sensor-steps/s",
             "value": nc_all * T / tt["tc"], "fp32_value": n_fp32 * T / tt["fp32"], "speedup_vs_fp32": (nc_all * T / tt["tc"]) / (n_fp32 * T / tt["fp32"]),
+            # the plain FP32 form is the reference's k_series restated (a thread per sensor, one product a term): its own
+            # rate, 2 K flop an output, beside the GPU's FP32 rate, so the speed-up reads as over that form
+            "fp32_form_tflops": n_fp32 * T * 2.0 * Kp / tt["fp32"] / 1e12,
             "config": {"workload": "precision: urban block, %d sensors, %d patches + ground, %d directions, %d series columns (non-night hours), "
                                    "20%% glass tau 0.64 (byte mode), 1 bounce x %d paths (%d reflected-light bins in K), chunks of %d sensors"
                                    % (nc_all, P, len(D), T, M, P + 1, chunk)},
