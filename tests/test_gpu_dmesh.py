@@ -151,3 +151,35 @@ def test_scene_from_kept_meshes(engine_lib, oracle, kgb, pkg, per_slot):
     finally:
         e.close()
         o.close()
+
+
+def test_scene_from_kept_meshes_refusals(engine_lib, kgb):
+    """kgb_build_meshes refuses an unknown mesh and a slot beyond the table (gpu_build's own message), builds an empty
+    scene from meshes that do not block (every ray misses), and kgb_mesh_thin_solids refuses an unknown mesh."""
+    P, C, I, _ = quad_grid(4, 0.0, 0.0, 1.0, seed=1)
+    S = (np.arange(16) % 3).astype(np.uint16)
+    e = kgb.Engine(engine_lib)
+    try:
+        info = e.mesh_read(image(P, C, I, S), "grid")
+        with pytest.raises(kgb.KgbError, match="no mesh 77"):
+            e.build_meshes([info.id, 77], (2.0, 2.0, 0.0))
+        with pytest.raises(kgb.KgbError, match="a triangle's slot has no Slot"):
+            e.build_meshes([info.id], (2.0, 2.0, 0.0), slots=[(0.2, 0.0, 0.0, 0)], per_slot=True)   # slots 0..2 in the mesh
+        made, skipped = e.build_meshes([info.id], (2.0, 2.0, 0.0), blocks=[0])
+        assert made.tolist() == [0] and skipped == 0
+        Ps = np.array([[0.5, 0.5, 5.0]], np.float32)
+        e.set_scene(Ps, np.array([[0, 0, -1]], np.float32), np.array([[0, 0, -1]], np.float32))
+        e.trace(0, 1, engine_lib.ray_flags(False, False))
+        assert e.download_bits(1)[0, 0] & 1   # nothing blocks: the ray down to the grid sees through
+        made, _ = e.build_meshes([info.id], (2.0, 2.0, 0.0), slots=[(0.2, 0.0, 0.0, 0)] * 3, per_slot=True)
+        assert made.tolist() == [32]
+        e.trace(0, 1, engine_lib.ray_flags(False, False))
+        assert not e.download_bits(1)[0, 0] & 1   # the grid blocks it now
+        with pytest.raises(kgb.KgbError, match="no mesh"):
+            e.mesh_thin_solids(kgb.MeshInfo(id=999, slots=1))
+        e.mesh_free(info.id)
+        with pytest.raises(kgb.KgbError, match="no mesh"):
+            e.build_meshes([info.id], (0.0, 0.0, 0.0))
+    finally:
+        e.close()
+
