@@ -578,6 +578,39 @@ def run_views(args, pkg):
             del back_c, back_d
             res[name]["download_rows"] = {"bytes": nc * K * 5, "s": dl_s, "gb_s": nc * K * 5 / dl_s / 1e9, "host_transpose_s": t2 - t1}
             del cls, dist
+    # many sensor meshes: 40 meshes of sizes log-uniform 500..50k (seeded), each a contiguous run of the city's facade
+    # sensors from a seeded start, their sensors one after another in the engine's sensor array. Fov 120: one
+    # kgb_view + kgb_reduce_view per mesh, against all meshes packed into one call (what the reference's views run does:
+    # every mesh's sensors in one array, chunked by memory); the same sums either way
+    rng = np.random.default_rng(4)
+    sizes = [int(np.exp(rng.uniform(np.log(500), np.log(50_000)))) for _ in range(40)]
+    firsts = [int(rng.integers(0, nc - n + 1)) for n in sizes]
+    Pm = np.concatenate([city["P"][a:a + n] for a, n in zip(firsts, sizes)])
+    Nm = np.concatenate([city["N"][a:a + n] for a, n in zip(firsts, sizes)])
+    ncm = len(Pm)
+    e.set_scene(Pm, Nm, np.zeros((0, 3), np.float32))
+    nAz, nEl, dAz, rowSin, wRow = pkg.workloads.views_grid(120.0, 2.0)
+    kw = dict(world=False, cull=False, jitter=True, vground=True, groundZ=city["groundZ"])
+    starts = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(int)
+    per_mesh, packed = [], []
+    for rep in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sums_m = []
+        for a, n in zip(starts, sizes):
+            e.view(int(a), n, flags, nAz, nEl, -60.0, dAz, rowSin, **kw)
+            sums_m.append(e.reduce_view(n, wRow, 6, 1000.0))
+        per_mesh.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        e.view(0, ncm, flags, nAz, nEl, -60.0, dAz, rowSin, **kw)
+        sums_p = e.reduce_view(ncm, wRow, 6, 1000.0)
+        packed.append(time.perf_counter() - t0)
+    same = bool(np.array_equal(np.concatenate(sums_m).view(np.uint64), sums_p.view(np.uint64)))
+    meshes = {"meshes": len(sizes), "sensors": ncm, "smallest": int(min(sizes)), "largest": int(max(sizes)),
+              "per_mesh_s": min(per_mesh), "packed_s": min(packed), "per_mesh_mrays_s": ncm * nAz * nEl / min(per_mesh) / 1e6,
+              "packed_mrays_s": ncm * nAz * nEl / min(packed) / 1e6, "speedup": min(per_mesh) / min(packed), "sums_identical": same,
+              "what": "fov 120 view + reduce_view of 40 sensor meshes: one call per mesh against one call for all (wall time, sums in host memory)"}
+    e.set_scene(city["P"], city["N"], np.zeros((0, 3), np.float32))
     # the host binned-SAH builder on the same city: build time, and the fov 120 trace on its tree (same results)
     e.set_builder(0)
     t0 = time.perf_counter()
@@ -613,7 +646,7 @@ def run_views(args, pkg):
     line = {"metric": "Mrays/s (closest hit)", "unit": "Mrays/s", "value": res["fov120"]["mrays_s"], "roofline": roof,
             "config": {"workload": "views city: %d facade sensors, %d triangles, 3 target groups; fov 120 / 2 deg (3600 rays), fov 360 / 2 deg "
                                    "(10800 rays, isovist volume, reach 6/20/50), jitter on" % (nc, len(city["tri"]))},
-            "fov120": res["fov120"], "fov360": res["fov360"], "bvh_build_s": build_s, "bvh": "device LBVH + treelet restructuring",
+            "fov120": res["fov120"], "fov360": res["fov360"], "meshes": meshes, "bvh_build_s": build_s, "bvh": "device LBVH + treelet restructuring",
             "host_sah_tree": host_tree}
     e.close()
     return line
