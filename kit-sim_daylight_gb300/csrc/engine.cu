@@ -1004,6 +1004,10 @@ KGB_API int kgb_build_meshes(kgb_engine* e, const uint32_t* ids, size_t nMeshes,
   for (size_t s = 0; s < nSlots; ++s) anyTau = anyTau || slots[s].tau > 0;
   const bool slotted = perSlot || anyTau;
   Buf dv, dtri, dslot, dtr, dslots;
+  struct Release {   // the assembly's arrays go on every return (the scene keeps its own records)
+    Buf* b[5];
+    ~Release() { for (Buf* x : b) x->free(); }
+  } release{{&dv, &dtri, &dslot, &dtr, &dslots}};
   if (!grow(dv, nPts * 12) || !grow(dtri, nCap * 12) || (slotted && !grow(dslot, nCap * 4))) return 0;
   uint64_t at = 0;
   int32_t skip = 0;
@@ -1032,10 +1036,8 @@ KGB_API int kgb_build_meshes(kgb_engine* e, const uint32_t* ids, size_t nMeshes,
     launch_translucent(static_cast<const uint32_t*>(dslot.p), nt, static_cast<const kgb_slot*>(dslots.p), static_cast<uint8_t*>(dtr.p), g.st);
     CU(cudaGetLastError());
   }
-  const int ok = build_scene(g, static_cast<const float*>(dv.p), size_t(nPts), static_cast<const uint32_t*>(dtri.p), nt,
-                             slotted ? static_cast<const uint32_t*>(dslot.p) : nullptr, slotted ? static_cast<const uint8_t*>(dtr.p) : nullptr, true);
-  for (Buf* b : {&dv, &dtri, &dslot, &dtr, &dslots}) b->free();
-  return ok;
+  return build_scene(g, static_cast<const float*>(dv.p), size_t(nPts), static_cast<const uint32_t*>(dtri.p), nt,
+                     slotted ? static_cast<const uint32_t*>(dslot.p) : nullptr, slotted ? static_cast<const uint8_t*>(dtr.p) : nullptr, true);
 }
 
 KGB_API int kgb_sky_ladybug(kgb_engine* e, int32_t mf, const double* steps, size_t T, double lat, double lon, double tz, double grefl,
