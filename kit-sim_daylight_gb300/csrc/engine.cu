@@ -294,6 +294,7 @@ struct Engine {
   Buf label;
   size_t nLabel = 0;
   Buf scratch, out;
+  Buf w64;           // a reduce's weights as doubles
   Buf ctl;   // [0] task counter, [1] status, [2..7] three u64 counters of the instrumented kernels
   bool ownStream = true;
   int seriesForm = 0;         // 0 split-BF16 tensor cores, 1 plain FP32
@@ -571,7 +572,7 @@ KGB_API void kgb_destroy(kgb_engine* e) {
   delete g->sc;
   for (DevMesh* m : g->meshes) delete m;
   for (Buf* b : {&g->slots, &g->P, &g->N, &g->D, &g->rayTab, &g->vis, &g->dc, &g->contrib, &g->viewCls, &g->viewDist, &g->rowSin, &g->label, &g->scratch, &g->out, &g->ctl,
-                 &g->vop, &g->sop, &g->csr, &g->sunCol, &g->rows, &g->border, &g->slotLog, &g->bq}) b->free();
+                 &g->vop, &g->sop, &g->csr, &g->sunCol, &g->rows, &g->border, &g->slotLog, &g->bq, &g->w64}) b->free();
   g->staging.free();
   for (cudaEvent_t ev : g->ev) if (ev) cudaEventDestroy(ev);
   for (cudaEvent_t ev : g->bandEv) if (ev) cudaEventDestroy(ev);
@@ -615,7 +616,7 @@ KGB_API int kgb_build(kgb_engine* e, const float* v, size_t nv, const uint32_t* 
 KGB_API void kgb_trim(kgb_engine* e, int sensors) {
   Engine& g = *E(e);
   cudaStreamSynchronize(g.st);
-  g.vis.free(); g.dc.free(); g.contrib.free(); g.scratch.free(); g.out.free(); g.viewCls.free(); g.viewDist.free();
+  g.vis.free(); g.dc.free(); g.contrib.free(); g.scratch.free(); g.out.free(); g.w64.free(); g.viewCls.free(); g.viewDist.free();
   g.vop.free(); g.sop.free(); g.csr.free(); g.sunCol.free();
   g.viewN = 0;
   if (sensors) { g.P.free(); g.N.free(); g.label.free(); g.nLabel = 0; g.nSensors = 0; }
@@ -750,12 +751,13 @@ KGB_API int kgb_reduce(kgb_engine* e, size_t nc, const float* W, int useCos, dou
   Engine& g = *E(e);
   if (nc == 0) return 1;
   if (nc != g.visN) return fail("gpu_reduce: no trace of this chunk");
-  if (!upload(g.scratch, W, g.nDir * 4, g.st) || !grow(g.out, nc * 8)) return 0;
+  if (!upload(g.scratch, W, g.nDir * 4, g.st) || !grow(g.out, nc * 8) || !grow(g.w64, g.nDir * 8)) return 0;
   const float* N = static_cast<const float*>(g.N.p) + 3 * g.i0;
+  double* w64 = static_cast<double*>(g.w64.p);
   if (g.bytes) launch_reduce_bytes(static_cast<const uint8_t*>(g.vis.p), uint32_t(nc), uint32_t(g.nDir), N, static_cast<const float*>(g.D.p),
-                                   static_cast<const float*>(g.scratch.p), useCos, static_cast<double*>(g.out.p), g.st);
+                                   static_cast<const float*>(g.scratch.p), useCos, static_cast<double*>(g.out.p), g.st, w64);
   else launch_reduce_bits(static_cast<const uint32_t*>(g.vis.p), uint32_t(nc), uint32_t(g.nWords), uint32_t(g.nDir), N, static_cast<const float*>(g.D.p),
-                          static_cast<const float*>(g.scratch.p), useCos, static_cast<double*>(g.out.p), g.st);
+                          static_cast<const float*>(g.scratch.p), useCos, static_cast<double*>(g.out.p), g.st, w64);
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(out, g.out.p, nc * 8, cudaMemcpyDeviceToHost, g.st));
   CU(cudaStreamSynchronize(g.st));

@@ -107,10 +107,12 @@ size_t bounce_state_bytes();   // one queued path
 int bounce_step_blocks_per_sm();
 
 // reductions (reduce.cu)
+// w64: a device array of nDir doubles for the weights (the fast form), or null (the weights staged per block in
+// shared memory: for callers with no room for the array)
 void launch_reduce_bits(const uint32_t* bits, uint32_t nc, uint32_t nWords, uint32_t nDir, const float* N, const float* D, const float* W,
-                        int useCos, double* out, cudaStream_t st);
+                        int useCos, double* out, cudaStream_t st, double* w64 = nullptr);
 void launch_reduce_bytes(const uint8_t* bytes, uint32_t nc, uint32_t nDir, const float* N, const float* D, const float* W, int useCos,
-                         double* out, cudaStream_t st);
+                         double* out, cudaStream_t st, double* w64 = nullptr);
 void launch_reduce_dc(const float* dc, uint32_t nc, uint32_t nBins, const float* W, double* out, cudaStream_t st);
 struct ViewReduceArgs {
   const uint8_t* cls;

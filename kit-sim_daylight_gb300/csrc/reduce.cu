@@ -15,7 +15,8 @@ __device__ __forceinline__ float dotf(F3 a, F3 b) { return (a.x * b.x + a.y * b.
 
 // GB300's FP64 pipe is narrow (a few lanes per clock per SM), so each term of a sum costs one FP64 instruction:
 //  - the float factor x > 0 becomes a double exactly by integer operations (widen, rt.cuh);
-//  - the weights are read as doubles, converted once per block into shared memory;
+//  - the weights are read as doubles: converted once per call into a device array (or, where the caller has no room
+//    for one, once per block into shared memory);
 //  - the product of two floats is exact in double, so fma(x, w, acc) equals acc + x * w rounded once, as the
 //    reference's separate multiply and add;
 //  - a zero factor adds +0, which leaves the sum as it is: it is skipped.
@@ -231,15 +232,76 @@ static bool reduce_smem_ready() {
   }();
   return ok;
 }
+// The weights as doubles in global memory (read through L1), one thread per sensor in blocks of 128: no shared memory
+// per block, so the SMs hold as many blocks as their registers allow and take new ones as blocks end. The shared-memory
+// form below (a block's copy of every weight, 45 KB at 5610 directions) kept four or five 256-thread blocks an SM, about
+// one wave for the urban block, and the blocks of heavy sensors (roofs see most directions) held their SMs while the
+// others idled: the urban step's four reduces took 8.85 ms that way, 4.93 ms this way (sums bit-identical; blocks of
+// 64 and 256 threads: 5.23 and 5.76 ms). Widening the float weights in the kernel instead of converting them once
+// took 9.95 ms.
+constexpr uint32_t kReduceBlock = 128;
+__global__ void k_weights64(const float* __restrict__ W, uint32_t n, double* __restrict__ W64) {
+  const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d < n) W64[d] = (double)W[d];
+}
+__global__ void __launch_bounds__(kReduceBlock) k_reduce_bits_w64(const uint32_t* __restrict__ bits, uint32_t nc, uint32_t nWords,
+                                                                  const float* __restrict__ N, const float* __restrict__ D,
+                                                                  const double* __restrict__ W64, int useCos, double* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  const F3 n = ld3(N + 3 * size_t(i));
+  double acc = 0;
+  for (uint32_t w = 0; w < nWords; ++w) {
+    uint32_t m = bits[size_t(w) * nc + i];
+    while (m) {
+      const uint32_t d = w * 32 + (__ffs(m) - 1);
+      m &= m - 1;
+      const float c = useCos ? fmaxf(dotf(n, ld3(D + 3 * d)), 0.f) : 1.f;
+      if (c != 0.f) acc = __fma_rn(widen(c), __ldg(W64 + d), acc);
+    }
+  }
+  out[i] = acc;
+}
+__global__ void __launch_bounds__(kReduceBlock) k_reduce_bytes_w64(const uint8_t* __restrict__ bytes, uint32_t nc, uint32_t nDir,
+                                                                   const float* __restrict__ N, const float* __restrict__ D,
+                                                                   const double* __restrict__ W64, int useCos, double* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  const F3 n = ld3(N + 3 * size_t(i));
+  double acc = 0;
+  constexpr uint32_t G = 16;   // 16 directions' bytes in flight before any is used, then added in direction order
+  for (uint32_t d0 = 0; d0 < nDir; d0 += G) {
+    uint32_t bb[G];
+#pragma unroll
+    for (uint32_t k = 0; k < G; ++k) bb[k] = d0 + k < nDir ? uint32_t(__ldg(bytes + size_t(d0 + k) * nc + i)) : 0u;
+#pragma unroll
+    for (uint32_t k = 0; k < G; ++k) {
+      if (!bb[k]) continue;
+      const uint32_t d = d0 + k;
+      const float at = float(bb[k]) / 255.f;
+      const float c = useCos ? fmaxf(dotf(n, ld3(D + 3 * d)), 0.f) : 1.f;
+      const float x = c * at;
+      if (x != 0.f) acc = __fma_rn(widen(x), __ldg(W64 + d), acc);
+    }
+  }
+  out[i] = acc;
+}
+
 void launch_reduce_bits(const uint32_t* bits, uint32_t nc, uint32_t nWords, uint32_t nDir, const float* N, const float* D, const float* W,
-                        int useCos, double* out, cudaStream_t st) {
-  if (nDir <= kReduceSmemDirs && reduce_smem_ready())
+                        int useCos, double* out, cudaStream_t st, double* w64) {
+  if (w64) {
+    k_weights64<<<(nDir + 255) / 256, 256, 0, st>>>(W, nDir, w64);
+    k_reduce_bits_w64<<<(nc + kReduceBlock - 1) / kReduceBlock, kReduceBlock, 0, st>>>(bits, nc, nWords, N, D, w64, useCos, out);
+  } else if (nDir <= kReduceSmemDirs && reduce_smem_ready())
     k_reduce_bits<true><<<(nc + 255) / 256, 256, nDir * sizeof(double), st>>>(bits, nc, nWords, nDir, N, D, W, useCos, out);
   else k_reduce_bits<false><<<(nc + 255) / 256, 256, 0, st>>>(bits, nc, nWords, nDir, N, D, W, useCos, out);
 }
 void launch_reduce_bytes(const uint8_t* bytes, uint32_t nc, uint32_t nDir, const float* N, const float* D, const float* W, int useCos,
-                         double* out, cudaStream_t st) {
-  if (nDir <= kReduceSmemDirs && reduce_smem_ready())
+                         double* out, cudaStream_t st, double* w64) {
+  if (w64) {
+    k_weights64<<<(nDir + 255) / 256, 256, 0, st>>>(W, nDir, w64);
+    k_reduce_bytes_w64<<<(nc + kReduceBlock - 1) / kReduceBlock, kReduceBlock, 0, st>>>(bytes, nc, nDir, N, D, w64, useCos, out);
+  } else if (nDir <= kReduceSmemDirs && reduce_smem_ready())
     k_reduce_bytes<true><<<(nc + 255) / 256, 256, nDir * sizeof(double), st>>>(bytes, nc, nDir, N, D, W, useCos, out);
   else k_reduce_bytes<false><<<(nc + 255) / 256, 256, 0, st>>>(bytes, nc, nDir, N, D, W, useCos, out);
 }
