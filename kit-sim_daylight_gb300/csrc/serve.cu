@@ -126,7 +126,8 @@ __device__ __forceinline__ void reduce_chunk_sensor(const Seg& g, uint32_t i, co
   for (uint32_t q = 0; q < NQ; ++q) outPool[g.outOff + size_t(q) * g.n + i] = acc[q];
 }
 static_assert(kMaxQ == 8, "k_reduce_batch dispatches 1..8 quantities");
-__global__ void __launch_bounds__(256) k_reduce_batch(const BatchHdr* hdr, const Seg* segs, const uint32_t* bitsPool, double* outPool) {
+constexpr uint32_t kReduceBatchBlock = 128;   // as the single-request reduce: small blocks keep the SMs busy to the end
+__global__ void __launch_bounds__(kReduceBatchBlock) k_reduce_batch(const BatchHdr* hdr, const Seg* segs, const uint32_t* bitsPool, double* outPool) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= hdr->nSens) return;
   const Seg& g = segs[find_seg(segs, hdr->nSegs, t, true)];
@@ -336,7 +337,7 @@ bool build_graph(Server& s, DaySlot& d, std::string& err) {
   cudaKernelNodeParams kb{};
   kb.func = reinterpret_cast<void*>(k_bits_batch); kb.gridDim = dim3(unsigned(s.gridBits)); kb.blockDim = dim3(256); kb.kernelParams = aBits;
   cudaKernelNodeParams kr{};
-  kr.func = reinterpret_cast<void*>(k_reduce_batch); kr.gridDim = dim3((s.maxSensPerBatch + 255) / 256); kr.blockDim = dim3(256);
+  kr.func = reinterpret_cast<void*>(k_reduce_batch); kr.gridDim = dim3((s.maxSensPerBatch + kReduceBatchBlock - 1) / kReduceBatchBlock); kr.blockDim = dim3(kReduceBatchBlock);
   kr.kernelParams = aRed;
   cudaMemsetParams ms{};
   ms.dst = d.dCtl; ms.value = 0; ms.elementSize = 4; ms.width = 2; ms.height = 1;
@@ -581,7 +582,7 @@ bool launch_day(Server& s, int k, const std::vector<Part>& parts, std::string& e
   }
   void* aRed[] = {&d.dHdr, &d.dSegs, &d.dBits, &d.dOut};
   cudaKernelNodeParams kr{};
-  kr.func = reinterpret_cast<void*>(k_reduce_batch); kr.gridDim = dim3((sens + 255) / 256); kr.blockDim = dim3(256); kr.kernelParams = aRed;
+  kr.func = reinterpret_cast<void*>(k_reduce_batch); kr.gridDim = dim3((sens + kReduceBatchBlock - 1) / kReduceBatchBlock); kr.blockDim = dim3(kReduceBatchBlock); kr.kernelParams = aRed;
   const bool ok =
       cuok(cudaGraphExecMemcpyNodeSetParams1D(d.exec, d.nSegs, d.dSegs, d.hSegs, sizeof(Seg) * parts.size(), cudaMemcpyHostToDevice), err, "batch table") &&
       cuok(cudaGraphExecKernelNodeSetParams(d.exec, d.nReduce, &kr), err, "batch reduce") &&
