@@ -773,7 +773,7 @@ def run_serving(args, pkg):
 
 # ---------------------------------------------------------------------------------------------- serving: time series
 def run_serving_series(args, pkg):
-    """North_star's serving target: daylight requests with hourly time series at 2305 patches + ground (the precision
+    """The serving form of the time series: daylight requests with hourly time series at 2305 patches + ground (the precision
     configuration's sky, opaque scene: the serving form traces visibility bits) through the server, each batch's series
     chunks of every request in it as one grouped split-BF16 tensor-core launch, against the plain FP32 form one request
     per launch (trace, the ground reduce, kgb_series in its FP32 form) on the same GPU. Requests: seeded, sensors

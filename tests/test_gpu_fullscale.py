@@ -20,7 +20,7 @@ import replay
 pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-# the series against FP64 (the benchmark spec: within 1e-6 relative, stated per output column)
+# the series against FP64 (the criterion: within 1e-6 relative, stated per output column)
 COLUMN_TOL = 1e-6          # per column: max_i |E - E64| / max_i |E64|
 ELEMENT_TOL = 1e-6         # per output: |E - E64| / E64 over outputs above ELEMENT_FLOOR x their column's maximum
 ELEMENT_P99_TOL = 5e-7

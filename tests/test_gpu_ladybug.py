@@ -5,7 +5,7 @@ The steps' sun (Radiance sun.c) and Perez skies run in FP64 on the GPU, whose el
 C library's in the last ulp; the float sums over the year then agree to about 1e-7, and the weights printed to three
 significant digits agree exactly unless a sum lies within that of a printing boundary. The stated bounds: every sum
 within SUM_TOL relative, every weight equal or one printed step off (a %.3g rounding flip), and the radiation an open
-horizontal sensor sums from the weights within RAD_TOL relative (the benchmark spec: ladybug radiation within 1e-6)."""
+horizontal sensor sums from the weights within RAD_TOL relative (the criterion: ladybug radiation within 1e-6 relative)."""
 import os
 
 import numpy as np

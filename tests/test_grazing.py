@@ -8,7 +8,7 @@ hit (|cos| < 0.05, the reference's own exclusion, validate/README.md:189), a sig
 reference excludes rays within 1e-6 of a sign test and hits within 1 mm of the downward ray's end), or, in views, a tie
 of two hits within 1e-5 of each other's distance, or a float distance off by more than the reference's distance check
 (1e-5 t + 1e-4 m). The tests require no ray outside these classes, and view distances within DIST_REL of the double
-walk's (the benchmark spec: within 1e-5 relative)."""
+walk's (the criterion: within 1e-5 relative)."""
 import ctypes
 
 import numpy as np
