@@ -1,5 +1,5 @@
 #!/usr/bin/env python3
-"""Benchmark of the ray-cast-and-accumulate hot path on GB300: the urban block (config 2 of the measured set).
+"""Benchmark of the ray-cast-and-accumulate hot path on GB300: the urban block (200k sensor faces, 403k triangles, 5610 directions).
 
 Workload (one step): the seeded 20 x 20 urban block (199,976 sensor faces, 403,152 triangles, resident BVH) traced
 against 5610 directions (577 Reinhart sky patches, their ground mirror, 4456 sun-up hours of the synthetic urban
@@ -351,9 +351,9 @@ def run_ours(args, pkg):
         torch.distributed.destroy_process_group()
 
 
-# ---------------------------------------------------------------------------------------------- config 3: precision
+# ---------------------------------------------------------------------------------------------- precision: 2305-patch series
 def run_precision(args, pkg):
-    """Config 3: the urban block at 2305 patches, 20 % glass (byte mode), one diffuse bounce of 1024 paths per sensor,
+    """The precision configuration: the urban block at 2305 patches, 20 % glass (byte mode), one diffuse bounce of 1024 paths per sensor,
     and the hourly series of the non-night hours with reflected light, chunk by chunk as the reference's run() does
     (run.cpp:623-688: trace, bounce, ground reduce, series). The split-BF16 tensor-core series is timed against the
     plain FP32 form on the same inputs, and its error per output column is measured against the oracle's FP64
@@ -519,7 +519,7 @@ def run_precision(args, pkg):
     return line
 
 
-# ---------------------------------------------------------------------------------------------- config 4: views
+# ---------------------------------------------------------------------------------------------- views: the 2 M-triangle city
 def run_views(args, pkg):
     import torch
     torch.cuda.set_device(0)
@@ -652,7 +652,7 @@ def run_views(args, pkg):
     return line
 
 
-# ---------------------------------------------------------------------------------------------- config 5: serving
+# ---------------------------------------------------------------------------------------------- serving: a mixed request stream
 def serving_requests(pkg, scenes, rate, window, seed=5):
     """A seeded Poisson stream: 70 % daylight (sensors log-uniform 100..200k, sky density 145 / 577 / 2305 patches, time
     range log-uniform 1 h .. 1 year -> its sun-up hours as sun directions, radiation + sun hours), 30 % views (fov 120

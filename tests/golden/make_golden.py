@@ -27,7 +27,7 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 DL_DAYLIGHT, DL_VIEWS = 0, 1
 
 CASES = {
-    # config 1: box.obj, a clear-sky year in Berlin, Tregenza sky (docs/daylight.md:133-149 publishes radiation + sunhours)
+    # the box scene: box.obj, a clear-sky year in Berlin, Tregenza sky (docs/daylight.md:133-149 publishes radiation + sunhours)
     "box_clearsky": (DL_DAYLIGHT, ["--clear-sky", "--lat", "52.52", "--lon", "13.41", "--quantity", "radiation,direct,diffuse,sunhours"]),
     # sun hours of 21 June in 10-minute steps (docs/daylight.md:163-179)
     "box_sunhours_day": (DL_DAYLIGHT, ["--quantity", "sunhours", "--lat", "52.52", "--lon", "13.41", "--tz", "1", "--from", "06-21T00:00",
@@ -43,7 +43,7 @@ CASES = {
     # views all around at 4 degree cells: isovist volume, reach 6/20/50, the box as a target group, jitter on
     "box_views360": (DL_VIEWS, ["--fov", "360", "--cell", "4", "--reach", "en17037", "--target", "box=landmark", "--distance",
                                 "isovist,mean,min,group"]),
-    # the urban block's sky (config 2): the direction table (577 Reinhart patches, their ground mirror, the sun-up hours)
+    # the urban block's sky: the direction table (577 Reinhart patches, their ground mirror, the sun-up hours)
     # and the per-quantity weights under the synthetic urban weather, from a one-quad run (they do not depend on the
     # geometry); the bench traces the full block with them
     "urban_sky": (DL_DAYLIGHT, ["--epw", "@TMP@/urban.epw", "--sky-density", "2", "--quantity", "radiation,irradiance,illuminance,sunhours"]),

@@ -75,7 +75,7 @@ def check(s):
 
 
 def test_urban_block_bits_against_double(oracle, kgb, pkg):
-    """Config 2: the urban block with the reference's direction table (577 patches, ground, 4456 sun hours)."""
+    """The urban block with the reference's direction table (577 patches, ground, 4456 sun hours)."""
     import replay
     s = pkg.workloads.urban_block()
     D, _ = replay.urban_sky()
@@ -98,7 +98,7 @@ def views_city(pkg):
 
 
 def test_views_city_against_double(oracle, kgb, pkg, views_city):
-    """Config 4: the 2 M-triangle views city (rotated boxes, gable roofs, km-long ground quads), fov 120 and fov 360 at
+    """The 2 M-triangle views city (rotated boxes, gable roofs, km-long ground quads), fov 120 and fov 360 at
     2 degree cells with jitter, and the visibility bits of a hemisphere of directions on its facades."""
     c = views_city
     o = kgb.Engine(oracle)
