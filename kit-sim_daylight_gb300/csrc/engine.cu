@@ -900,11 +900,13 @@ KGB_API int kgb_sky(kgb_engine* e, int32_t mf, const kgb_sky_step* steps, size_t
 KGB_API int kgb_triangulate(kgb_engine* e, const double* points, size_t nPoints, const int32_t* counts, size_t nFaces, const int32_t* indices,
                             const uint32_t* faceSlot, const double* c, uint32_t base, uint32_t slotBase, float* v, uint32_t* tri, uint32_t* slot,
                             size_t* made, int32_t* skipped) {
+  if (!c || !made || !skipped || (nPoints && !v)) return fail("kgb_triangulate: the centre, v, made and skipped are required");
   const std::string why = triangulate_mesh(points, nPoints, counts, nFaces, indices, faceSlot, c, base, slotBase, v, tri, slot, made, skipped, E(e)->st);
   return why.empty() ? 1 : fail("kgb_triangulate: " + why);
 }
 KGB_API int kgb_thin_solids(kgb_engine* e, const double* points, size_t nPoints, const int32_t* counts, size_t nFaces, const int32_t* indices,
                             const uint32_t* faceSlot, uint32_t nSlots, const double* c, uint32_t* flags) {
+  if (!c || (nSlots && !flags)) return fail("kgb_thin_solids: the centre and the flags are required");
   const std::string why = thin_solids(points, nPoints, counts, nFaces, indices, faceSlot, nSlots, c, flags, E(e)->st);
   return why.empty() ? 1 : fail("kgb_thin_solids: " + why);
 }
@@ -977,6 +979,7 @@ KGB_API int kgb_mesh_thin_solids(kgb_engine* e, uint32_t id, const double* c, ui
   Engine& g = *E(e);
   const DevMesh* m = find_mesh(g, id);
   if (!m) return fail("kgb_mesh_thin_solids: no mesh " + std::to_string(id));
+  if (!c || !flags) return fail("kgb_mesh_thin_solids: the centre and the flags are required");
   const std::string why = thin_solids_view(m->view, m->info.slots, c, flags, g.st);
   return why.empty() ? 1 : fail("kgb_mesh_thin_solids: " + why);
 }
@@ -984,6 +987,7 @@ KGB_API int kgb_mesh_thin_solids(kgb_engine* e, uint32_t id, const double* c, ui
 KGB_API int kgb_build_meshes(kgb_engine* e, const uint32_t* ids, size_t nMeshes, const uint8_t* blocks, const double* c, const kgb_slot* slots,
                              size_t nSlots, int perSlot, uint64_t* made, int32_t* skipped) {
   Engine& g = *E(e);
+  if (!c || (nMeshes && !ids) || !slots || !nSlots) return fail("kgb_build_meshes: the centre, the ids and a slot table are required");
   delete g.sc;
   g.sc = new SceneObj;
   g.stats.gasBytes = 0;
