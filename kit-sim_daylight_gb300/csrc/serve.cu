@@ -886,6 +886,7 @@ bool tune_views(Server& s, const std::vector<float>& P, const std::vector<float>
       best = std::max(best, rate);
     }
     cudaFreeAsync(r.dev, s.st);
+    s.view[0].part = Part{nullptr, 0, 0};   // the calibration request is gone; nothing refers to it
     trials.push_back(Trial{vr, best});
   }
   double top = 0;
