@@ -400,6 +400,7 @@ def run_precision(args, pkg):
         f_ref.write(b"\0" * 128)
         fd_dir = os.open(os.path.join(tmpdir, "direct.npy"), os.O_CREAT | os.O_RDWR | os.O_TRUNC, 0o644)
     st0 = e.stats()
+    tc_calls = 0   # tensor-core series calls (the timed ones, their repeats and the file-writing ones)
     t_all = time.perf_counter()
     for i0 in range(0, nc_all, chunk):
         nc = min(chunk, nc_all - i0)
@@ -421,6 +422,7 @@ def run_precision(args, pkg):
             for _ in range(2 if key == "tc" else 1):
                 t0 = time.perf_counter()
                 E = e.series(nc, G=G, out=Ebuf[:nc], **sargs)
+                tc_calls += 1 if key == "tc" else 0
                 dt = time.perf_counter() - t0
                 if best is not None:
                     tt["tc_repeat"] += max(dt, best)   # the pipeline's wall time counts one call
@@ -433,6 +435,7 @@ def run_precision(args, pkg):
                 d1 = time.perf_counter() - t1
                 t1 = time.perf_counter()
                 e.series_file(nc, fd_dir, 128 + i0 * T * 4, G=G, **sargs)
+                tc_calls += 1
                 d2 = time.perf_counter() - t1
                 tt["fwrite"] += d1
                 tt["direct"] += d2
@@ -519,7 +522,8 @@ def run_precision(args, pkg):
             "trace_mrays_s": nc_all * len(D) / tt["trace"] / 1e6, "bounce_mpaths_s": paths / tt["bounce"] / 1e6, "sky_build_s": yr["sky_s"],
             "trace_s": tt["trace"], "bounce_s": tt["bounce"], "series_tc_s": tt["tc"], "series_fp32_s_timed": tt["fp32"],
             "device_s": {"trace": (st1["traceMs"] - st0["traceMs"]) / 1000, "bounce": (st1["bounceMs"] - st0["bounceMs"]) / 1000,
-                         "series_tc": series_ms / 1000, "bounce_launches": int(st1["bounceLaunches"] - st0["bounceLaunches"])},
+                         "series_tc": series_ms / 1000, "series_tc_calls": tc_calls, "series_tc_per_pass": series_ms / 1000 / max(tc_calls, 1) * ((nc_all + chunk - 1) // chunk),
+                         "bounce_launches": int(st1["bounceLaunches"] - st0["bounceLaunches"])},
             "pipeline_s": pipeline_s - (tt["fp32"] if not args.full_fp32 else 0.0),
             "pipeline_solves_s": nc_all * T / (pipeline_s - (tt["fp32"] if not args.full_fp32 else 0.0)),
             "E_bytes": nc_all * T * 4, "series_file": series_file, "note": "series times include the E download to host memory (pageable, one buffer reused across chunks), as the reference's gpu_series"}
