@@ -367,6 +367,15 @@ def run_precision(args, pkg):
     Dsky, omega = pkg.workloads.patch_dirs(mf)
     P = len(Dsky)
     yr = pkg.workloads.urban_year_sky(e, mf, np.load(os.path.join(GOLDEN, "urban_sky", "weather.npy")))
+    # ladybug mode's sky of the same weather year on the device (sky density 2; the steps as the reference makes them,
+    # tests/golden/ladybug): the faster of two calls
+    lbg = np.load(os.path.join(GOLDEN, "ladybug", "mf2.npz"))
+    _, _, _, lb_hours, lb_lat, lb_lon, lb_tz = lbg["head"]
+    lb_s = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        e.sky_ladybug(2, lbg["steps"], lb_lat, lb_lon, lb_tz, float(lbg["grefl"]), lb_hours, series=True)
+        lb_s.append(time.perf_counter() - t0)
     D = np.concatenate([Dsky, -Dsky, yr["sunVec"]]).astype(np.float32)
     nSky, sun0 = P, 2 * P
     scene = pkg.workloads.urban_block(glass_share=0.2)
@@ -520,6 +529,7 @@ def run_precision(args, pkg):
             "fp32_column_error_vs_fp64": {"max": float(ce32.max()), "median": float(np.median(ce32))},
             "fp32_element_error_vs_fp64": elemerr(fp32_first),
             "trace_mrays_s": nc_all * len(D) / tt["trace"] / 1e6, "bounce_mpaths_s": paths / tt["bounce"] / 1e6, "sky_build_s": yr["sky_s"],
+            "ladybug_sky_s": min(lb_s), "ladybug_sky": "mf 2 (577 patches), %d steps: sun.c, the Perez sky twice a step, the float sums and the %%.3g weights, with the series columns" % len(lbg["steps"]),
             "trace_s": tt["trace"], "bounce_s": tt["bounce"], "series_tc_s": tt["tc"], "series_fp32_s_timed": tt["fp32"],
             "device_s": {"trace": (st1["traceMs"] - st0["traceMs"]) / 1000, "bounce": (st1["bounceMs"] - st0["bounceMs"]) / 1000,
                          "series_tc": series_ms / 1000, "series_tc_calls": tc_calls, "series_tc_per_pass": series_ms / 1000 / max(tc_calls, 1) * ((nc_all + chunk - 1) // chunk),
