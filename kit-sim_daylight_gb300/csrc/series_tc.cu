@@ -15,8 +15,9 @@
 //    64 of K (a chunk) accumulates from zero in TMEM (4 K steps), and the epilogue adds the chunk's sum into FP32
 //    registers with Kahan compensation (chains of 8 K steps doubled the column error, 4e-7 to 7e-7 of the column's
 //    maximum);
-//  - the sun term (one direction per step, exact in the reference's float arithmetic) is added in the epilogue, where
-//    each output is finished in registers and stored with 16-byte row stores.
+//  - the sun term (one direction per step, exact in the reference's float arithmetic) is added by k_series_sun, which
+//    runs after the contraction on the same stream: E[i, t] = E[i, t] + term, the same float operations in the same
+//    order as the reference's k_series tail.
 //
 // The six products take three MMAs per K step: the three S pieces are consecutive tiles in shared memory, so one B
 // operand of N 192 is [S hi | S mid | S lo], and a chunk's accumulator [H | C1 | C2] (3 x 64 columns) receives
@@ -40,8 +41,11 @@
 //               hands the finished chunk to the epilogue
 //   warps 2-5   epilogue, one per TMEM lane quarter (warp w reads lanes 32 (w % 4) ..), a thread per output row: per
 //               chunk, tcgen05.ld of H, C1, C2 (one wait), H + (C1 + C2) added into the row's 64 Kahan-compensated FP32
-//               sums (32 packed pairs each of sum and compensation); per tile, the sun term and the row of E stored 16
-//               bytes at a time
+//               sums (32 packed pairs each of sum and compensation); per tile, the row of E stored 16 bytes at a time
+// With two chunk accumulators the MMA issuer waits for the epilogue whenever the epilogue's tile-end work outlasts two
+// chunks of MMAs. The sun term at the tile's end (per column its sun direction, then the sensor's visibility of it: two
+// dependent global loads behind a branch, 64 times) did: it took a 29,609-sensor chunk from 5.1 to 8.8 ms at 1.95 GHz.
+// k_series_sun adds it in a pass of its own over E (about 0.05 ms a band of 7424 sensors).
 // The 64-column tile keeps the Kahan sums in registers: six warps per CTA leave a scheduler at most two warps, so a
 // thread may hold up to 255 registers (the register file is split between the SM's four schedulers).
 // Every wait on an mbarrier is bounded: past the limit the kernel records kStatusTimeout and leaves its loops. Before the
@@ -178,11 +182,12 @@ struct TcSeg {
   uint32_t nc, T, Kp, sun0;
   uint32_t mBase, mTiles, nTiles;
   uint32_t tileBase;         // the launch's tiles tileBase .. tileBase + mTiles x nTiles - 1 are this contraction's
+  uint32_t sunBase;          // k_series_sun's blocks sunBase .. sunBase + (row blocks x column blocks) - 1, likewise
 };
 constexpr uint32_t kMaxTcSegs = kMaxSeriesGroup;   // contractions of one launch: their tensor maps travel as kernel parameters
 struct TcGroup {
   TcSeg seg[kMaxTcSegs];
-  uint32_t nSegs, nTiles;
+  uint32_t nSegs, nTiles, nSunBlocks;
   uint32_t* status;
   uint64_t waitLimitNs;      // the pipeline's mbarrier waits give up past this (kWaitLimitNs, or lower)
   uint32_t withholdFills;    // 1: the producer issues no fills, so that the waits run out (a test of the bounded waits)
@@ -361,35 +366,17 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
       tile_coords(tile - a.tileBase, a.mTiles, a.nTiles, tm, tn);
       const uint32_t m0 = (tm + a.mBase) * BM, n0 = tn * BN;
       const uint32_t row = m0 + q * 32 + lane;         // this thread's sensor
-      float nrm[3] = {0.f, 0.f, 0.f};
-      if (row < a.nc) { nrm[0] = a.N[3 * row]; nrm[1] = a.N[3 * row + 1]; nrm[2] = a.N[3 * row + 2]; }
       float* Erow = a.E + size_t(row) * a.T;
       const bool vec = (a.T & 3u) == 0;                  // 16-byte row stores when rows are 16-byte aligned
+      if (row < a.nc) {
 #pragma unroll
-      for (int g = 0; g < BN / 16; ++g) {
-        float v[16];
+        for (int g = 0; g < BN / 16; ++g) {
+          float v[16];
 #pragma unroll
-        for (int c = 0; c < 16; c += 2) {
-          const unsigned long long d = sub2(acc[(g * 16 + c) / 2], cmp[(g * 16 + c) / 2]);
-          v[c] = __uint_as_float(uint32_t(d)); v[c + 1] = __uint_as_float(uint32_t(d >> 32));
-        }
-#pragma unroll
-        for (int c = 0; c < 16; ++c) {
-          float x = v[c];
-          const uint32_t t = n0 + g * 16 + c;
-          if (t < a.T && row < a.nc) {
-            const int j = __ldg(a.sunOfCol + t);
-            if (j >= 0) {
-              const uint32_t d = a.sun0 + uint32_t(j);
-              float at;
-              if (a.bytes) { const uint32_t b = a.bytes[size_t(d) * a.nc + row]; at = b ? float(b) / 255.f : 0.f; }
-              else at = float((a.bits[size_t(d >> 5) * a.nc + row] >> (d & 31)) & 1u);
-              if (at != 0.f) x = __fadd_rn(x, __fmul_rn(__fmul_rn(fmaxf(dotf_rn(nrm, a.sunVec + 3 * j), 0.f), at), a.sunW[j]));
-            }
+          for (int c = 0; c < 16; c += 2) {
+            const unsigned long long d = sub2(acc[(g * 16 + c) / 2], cmp[(g * 16 + c) / 2]);
+            v[c] = __uint_as_float(uint32_t(d)); v[c + 1] = __uint_as_float(uint32_t(d >> 32));
           }
-          v[c] = x;
-        }
-        if (row < a.nc) {
           const uint32_t t0 = n0 + g * 16;
           if (vec && t0 + 16 <= a.T) {
 #pragma unroll
@@ -407,6 +394,59 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
   if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmemBase), "r"(TMEM_COLS));
+  }
+}
+
+// The sun term of the reference's k_series tail (gpu.cu:145-148), added to E after the contraction: for column t with a
+// sun direction j (sunOfCol), E[i, t] + max(0, N_i . sun_j) at(i, sun0 + j) w_j when the sensor's visibility at of it
+// is not zero, in float with the reference's operation order. A block covers 32 sensors x 64 columns: the terms are
+// computed with lanes over sensors (the visibility reads coalesce) and added with lanes over columns (the E reads and
+// writes coalesce), through shared memory.
+constexpr uint32_t kSunRows = 32, kSunCols = 64;
+constexpr uint32_t kNoTerm = 0xffffffffu;   // no sun term (a NaN pattern the term's arithmetic does not produce on the GPU)
+__device__ __forceinline__ uint32_t sun_seg_of(const TcGroup& g, uint32_t block) {
+  uint32_t lo = 0, hi = g.nSegs - 1;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1) / 2;
+    if (g.seg[mid].sunBase <= block) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+__global__ void __launch_bounds__(256) k_series_sun(const __grid_constant__ TcGroup g) {
+  __shared__ uint32_t term[kSunCols][kSunRows + 1];
+  __shared__ int32_t jOf[kSunCols];
+  const TcSeg& a = g.seg[sun_seg_of(g, blockIdx.x)];
+  const uint32_t colBlocks = (a.T + kSunCols - 1) / kSunCols, local = blockIdx.x - a.sunBase;
+  const uint32_t r0 = a.mBase * BM + (local / colBlocks) * kSunRows, t0 = (local % colBlocks) * kSunCols;
+  const uint32_t rowEnd = min(a.nc, (a.mBase + a.mTiles) * BM);
+  if (threadIdx.x < kSunCols) jOf[threadIdx.x] = t0 + threadIdx.x < a.T ? __ldg(a.sunOfCol + t0 + threadIdx.x) : -1;
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t row = r0 + lane;
+  float nrm[3] = {0.f, 0.f, 0.f};
+  if (row < rowEnd) { nrm[0] = a.N[3 * row]; nrm[1] = a.N[3 * row + 1]; nrm[2] = a.N[3 * row + 2]; }
+  for (uint32_t c = warp; c < kSunCols; c += 8) {
+    const int j = jOf[c];
+    uint32_t u = kNoTerm;
+    if (j >= 0 && row < rowEnd) {
+      const uint32_t d = a.sun0 + uint32_t(j);
+      float at;
+      if (a.bytes) { const uint32_t b = a.bytes[size_t(d) * a.nc + row]; at = b ? float(b) / 255.f : 0.f; }
+      else at = float((a.bits[size_t(d >> 5) * a.nc + row] >> (d & 31)) & 1u);
+      if (at != 0.f) u = __float_as_uint(__fmul_rn(__fmul_rn(fmaxf(dotf_rn(nrm, a.sunVec + 3 * j), 0.f), at), a.sunW[j]));
+    }
+    term[c][lane] = u;
+  }
+  __syncthreads();
+  for (uint32_t r = warp; r < kSunRows; r += 8) {
+    const uint32_t i = r0 + r;
+    if (i >= rowEnd) break;
+    float* Erow = a.E + size_t(i) * a.T;
+#pragma unroll
+    for (uint32_t h = 0; h < kSunCols / 32; ++h) {
+      const uint32_t c = h * 32 + lane, u = term[c][r];
+      if (u != kNoTerm) Erow[t0 + c] = __fadd_rn(Erow[t0 + c], __uint_as_float(u));
+    }
   }
 }
 
@@ -536,7 +576,8 @@ static bool make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t K
 const char* series_tc(const SeriesTcPlan& p, cudaStream_t st) { return series_tc_rows(p, 0, (p.nc + BM - 1) / BM, st); }
 
 // a contraction's parameters (its tensor maps encoded here), tiles from tileBase on; null or what failed
-static const char* tc_seg(const SeriesTcPlan& p, uint32_t mBase, uint32_t mCount, uint32_t tileBase, TcSeg& a) {
+static const char* tc_seg(const SeriesTcPlan& p, uint32_t mBase, uint32_t mCount, uint32_t tileBase, uint32_t sunBase, TcSeg& a,
+                          uint32_t& sunBlocks) {
   if (uint64_t(mBase) + mCount > (p.nc + BM - 1) / BM) return "series_tc: rows of tiles beyond the chunk";
   if (p.Kp % BK || !p.Kp) return "series_tc: K not padded to 64";
   if (uint64_t(PIECES) * p.nc + BM > 0x7fffffffull || uint64_t(PIECES) * p.T + BN > 0x7fffffffull) return "series_tc: chunk too large";
@@ -544,6 +585,9 @@ static const char* tc_seg(const SeriesTcPlan& p, uint32_t mBase, uint32_t mCount
     return "series_tc: cuTensorMapEncodeTiled failed";
   a.nc = p.nc; a.T = p.T; a.Kp = p.Kp;
   a.mTiles = mCount; a.mBase = mBase; a.nTiles = (p.T + BN - 1) / BN; a.tileBase = tileBase;
+  const uint32_t rows = std::min<uint32_t>(p.nc, (mBase + mCount) * BM) - mBase * BM;
+  a.sunBase = sunBase;
+  sunBlocks = ((rows + kSunRows - 1) / kSunRows) * ((p.T + kSunCols - 1) / kSunCols);
   a.sunOfCol = p.sunOfCol; a.sunVec = p.sunVec; a.sunW = p.sunW; a.sun0 = p.sun0;
   a.bits = p.bits; a.bytes = p.bytes; a.N = p.N; a.E = p.E;
   return nullptr;
@@ -560,6 +604,7 @@ static const char* tc_launch(TcGroup& g, int numSMs, uint64_t waitLimitNs, bool 
   g.withholdFills = withholdFills ? 1u : 0u;
   const int grid = int(std::min<uint32_t>(uint32_t(numSMs), g.nTiles));
   k_series_tc<<<grid, THREADS, SMEM_BYTES, st>>>(g);
+  if (g.nSunBlocks) k_series_sun<<<g.nSunBlocks, 256, 0, st>>>(g);
   return nullptr;
 }
 
@@ -568,7 +613,7 @@ const char* series_tc_rows(const SeriesTcPlan& p, uint32_t mBase, uint32_t mCoun
   thread_local TcGroup* tg = new TcGroup;   // 18 KB, off the stack; the launch copies it
   TcGroup& G = *tg;
   G.nSegs = 1;
-  if (const char* why = tc_seg(p, mBase, mCount, 0, G.seg[0])) return why;
+  if (const char* why = tc_seg(p, mBase, mCount, 0, 0, G.seg[0], G.nSunBlocks)) return why;
   G.nTiles = mCount * G.seg[0].nTiles;
   G.status = p.status;
   return tc_launch(G, p.numSMs, p.waitLimitNs, p.withholdFills, st);
@@ -581,12 +626,15 @@ const char* series_tc_group(const SeriesTcPlan* plans, uint32_t n, cudaStream_t 
   TcGroup& G = *tg;
   G.nSegs = 0;
   G.nTiles = 0;
+  G.nSunBlocks = 0;
   for (uint32_t k = 0; k < n; ++k) {
     const SeriesTcPlan& p = plans[k];
     if (p.nc == 0 || p.T == 0) continue;
     const uint32_t mCount = (p.nc + BM - 1) / BM;
-    if (const char* why = tc_seg(p, 0, mCount, G.nTiles, G.seg[G.nSegs])) return why;
+    uint32_t sunBlocks = 0;
+    if (const char* why = tc_seg(p, 0, mCount, G.nTiles, G.nSunBlocks, G.seg[G.nSegs], sunBlocks)) return why;
     G.nTiles += mCount * G.seg[G.nSegs].nTiles;
+    G.nSunBlocks += sunBlocks;
     ++G.nSegs;
   }
   if (!G.nSegs) return nullptr;
