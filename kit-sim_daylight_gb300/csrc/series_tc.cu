@@ -39,15 +39,15 @@
 //   warp 1      MMA issuer (one thread): 12 tcgen05.mma per stage (M 128, K 16; N 192, 128, 64) into the chunk's
 //               accumulator [H | C1 | C2] (two of them, at TMEM columns 0 and 256); tcgen05.commit frees the stage and
 //               hands the finished chunk to the epilogue
-//   warps 2-5   epilogue, one per TMEM lane quarter (warp w reads lanes 32 (w % 4) ..), a thread per output row: per
-//               chunk, tcgen05.ld of H, C1, C2 (one wait), H + (C1 + C2) added into the row's 64 Kahan-compensated FP32
-//               sums (32 packed pairs each of sum and compensation); per tile, the row of E stored 16 bytes at a time
+//   warps 2-9   epilogue, two per TMEM lane quarter (warp w reads lanes 32 (w % 4) ..) with 32 of the tile's 64 columns
+//               each, a thread per output row: per chunk, tcgen05.ld of H, C1, C2 (one wait per 16 columns),
+//               H + (C1 + C2) added into the row's 32 Kahan-compensated FP32 sums (16 packed pairs each of sum and
+//               compensation); per tile, those columns of the row of E stored 16 bytes at a time
 // With two chunk accumulators the MMA issuer waits for the epilogue whenever the epilogue's tile-end work outlasts two
 // chunks of MMAs. The sun term at the tile's end (per column its sun direction, then the sensor's visibility of it: two
 // dependent global loads behind a branch, 64 times) did: it took a 29,609-sensor chunk from 5.1 to 8.8 ms at 1.95 GHz.
 // k_series_sun adds it in a pass of its own over E (about 0.05 ms a band of 7424 sensors).
-// The 64-column tile keeps the Kahan sums in registers: six warps per CTA leave a scheduler at most two warps, so a
-// thread may hold up to 255 registers (the register file is split between the SM's four schedulers).
+// The Kahan sums stay in registers: ten warps per CTA (one CTA per SM) leave each thread up to 204 registers.
 // Every wait on an mbarrier is bounded: past the limit the kernel records kStatusTimeout and leaves its loops. Before the
 // CTA releases its TMEM and exits, the producer waits for the last fill it issued into each stage (so no bulk copy still
 // writes shared memory) and the MMA issuer commits to a drain barrier and waits for it (so no MMA still runs); both
@@ -68,7 +68,8 @@ constexpr uint32_t NH = 2;                           // chunk accumulators [H | 
 constexpr int V_TILE = BM * BK * 2;                  // 16 KB: one bf16 V tile (128 rows x 128 B)
 constexpr int S_TILE = BN * BK * 2;                  // 8 KB: one bf16 S^T tile (64 rows x 128 B)
 constexpr int STAGE_BYTES = PIECES * (V_TILE + S_TILE); // V hi mid lo, S hi mid lo
-constexpr int EPI_WARPS = 4;                        // one per TMEM lane quarter, the tile's 64 columns each
+constexpr int EPI_WARPS = 8;                        // two per TMEM lane quarter, 32 of the tile's 64 columns each
+constexpr int EPI_COLS = BN * 4 / EPI_WARPS;        // the columns of one epilogue warp
 constexpr int THREADS = 32 * (2 + EPI_WARPS);
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /* align */ + 256 /* barriers */;
 static_assert((2 * STAGES + 2 * NH + 1) * 8 + 4 <= 256, "the barriers and the TMEM slot fit their 256 bytes");
@@ -326,8 +327,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
       mbar_wait(drain, 0, g.status, kWaitLimitNs);
     }
     __syncwarp();
-  } else {   // ---------------- epilogue: warps 2..5
+  } else {   // ---------------- epilogue: warps 2..9
     const uint32_t q = warp & 3;                       // the TMEM lane quarter this warp may read
+    const uint32_t c0 = (warp - 2) / 4 * EPI_COLS;     // and its columns of the tile
     const uint32_t laneBase = (q * 32u) << 16;
     uint32_t chunk = 0;
     for (uint32_t tile = blockIdx.x; tile < nTilesAll; tile += gridDim.x) {
@@ -335,18 +337,18 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
       const uint32_t kBlocks = a.Kp / BK;
       // each chunk's H + (C1 + C2), added with Kahan compensation (acc - cmp is the running sum); columns 2p and 2p + 1
       // share the packed pair p of acc and cmp
-      unsigned long long acc[BN / 2], cmp[BN / 2];
+      unsigned long long acc[EPI_COLS / 2], cmp[EPI_COLS / 2];
 #pragma unroll
-      for (int c = 0; c < BN / 2; ++c) { acc[c] = 0ull; cmp[c] = 0ull; }
+      for (int c = 0; c < EPI_COLS / 2; ++c) { acc[c] = 0ull; cmp[c] = 0ull; }
       bool ok = true;
       for (uint32_t ch = 0; ch < kBlocks; ++ch, ++chunk) {
         const uint32_t hbuf = chunk % NH;
         ok = __all_sync(~0u, mbar_wait(&hFull[hbuf], (chunk / NH) & 1, g.status, g.waitLimitNs));
         if (!ok || abortFlag) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t hAt = tmemBase + laneBase + hbuf * kChunkCols;
+        const uint32_t hAt = tmemBase + laneBase + hbuf * kChunkCols + c0;
 #pragma unroll
-        for (int g = 0; g < BN / 16; ++g) {
+        for (int g = 0; g < EPI_COLS / 16; ++g) {
           uint32_t v[16], c1[16], c2[16];
           tmem_ld16x3(hAt + g * 16, hAt + BN + g * 16, hAt + 2 * BN + g * 16, v, c1, c2);
 #pragma unroll
@@ -370,14 +372,14 @@ __global__ void __launch_bounds__(THREADS, 1) k_series_tc(const __grid_constant_
       const bool vec = (a.T & 3u) == 0;                  // 16-byte row stores when rows are 16-byte aligned
       if (row < a.nc) {
 #pragma unroll
-        for (int g = 0; g < BN / 16; ++g) {
+        for (int g = 0; g < EPI_COLS / 16; ++g) {
           float v[16];
 #pragma unroll
           for (int c = 0; c < 16; c += 2) {
             const unsigned long long d = sub2(acc[(g * 16 + c) / 2], cmp[(g * 16 + c) / 2]);
             v[c] = __uint_as_float(uint32_t(d)); v[c + 1] = __uint_as_float(uint32_t(d >> 32));
           }
-          const uint32_t t0 = n0 + g * 16;
+          const uint32_t t0 = n0 + c0 + g * 16;
           if (vec && t0 + 16 <= a.T) {
 #pragma unroll
             for (int c = 0; c < 16; c += 4) *reinterpret_cast<float4*>(Erow + t0 + c) = make_float4(v[c], v[c + 1], v[c + 2], v[c + 3]);
