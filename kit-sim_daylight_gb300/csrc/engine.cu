@@ -279,6 +279,9 @@ struct Engine {
   uint32_t nSlots = 0;
   Buf P, N, D, rayTab;   // rayTab: 48 bytes per direction (the direction-only part of each ray)
   size_t nSensors = 0, nDir = 0, nWords = 0;
+  Buf order;                          // the sensors grouped by normal orientation (TraceArgs::order), on the device
+  std::vector<uint32_t> orderHost;    // and here, to find a call's runs
+  uint32_t classStart[7] = {};        // class c's sensors are orderHost[classStart[c] .. classStart[c + 1])
   Buf vis;
   bool bytes = false;
   size_t i0 = 0, visN = 0;
@@ -619,7 +622,10 @@ KGB_API void kgb_trim(kgb_engine* e, int sensors) {
   g.vis.free(); g.dc.free(); g.contrib.free(); g.scratch.free(); g.out.free(); g.w64.free(); g.viewCls.free(); g.viewDist.free();
   g.vop.free(); g.sop.free(); g.csr.free(); g.sunCol.free();
   g.viewN = 0;
-  if (sensors) { g.P.free(); g.N.free(); g.label.free(); g.nLabel = 0; g.nSensors = 0; }
+  if (sensors) {
+    g.P.free(); g.N.free(); g.label.free(); g.order.free(); g.nLabel = 0; g.nSensors = 0;
+    std::vector<uint32_t>().swap(g.orderHost);
+  }
 }
 
 KGB_API int kgb_set_slots(kgb_engine* e, const kgb_slot* slots, size_t n) {
@@ -659,11 +665,35 @@ KGB_API uint64_t kgb_free_bytes(void) {
   return cudaMemGetInfo(&f, &t) == cudaSuccess ? f : 0;
 }
 
+// The tracing order of the visibility kernels: the sensors stably partitioned by the dominant axis of their normal and its
+// sign. A warp traces one direction for 32 consecutive sensors of that order, so a warp whose sensors straddle two faces
+// of different orientation (whose lanes on the face turned away from the direction idle) becomes one straddling two
+// faces of the same orientation. Urban block, the reference's direction table: trace 60.9 to 58.1 ms. The results of
+// every sensor do not depend on the order.
+static uint32_t orientation_class(const float* n) {
+  const float ax = std::fabs(n[0]), ay = std::fabs(n[1]), az = std::fabs(n[2]);
+  const int k = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
+  return 2u * uint32_t(k) + (n[k] > 0.f ? 1u : 0u);
+}
+static bool sensor_order(Engine& g, const float* N, size_t nSensors) {
+  std::vector<uint32_t> cls(nSensors);
+  uint32_t count[6] = {};
+  for (size_t i = 0; i < nSensors; ++i) count[cls[i] = orientation_class(N + 3 * i)]++;
+  g.classStart[0] = 0;
+  for (int c = 0; c < 6; ++c) g.classStart[c + 1] = g.classStart[c] + count[c];
+  uint32_t at[6];
+  for (int c = 0; c < 6; ++c) at[c] = g.classStart[c];
+  g.orderHost.resize(nSensors);
+  for (size_t i = 0; i < nSensors; ++i) g.orderHost[at[cls[i]]++] = uint32_t(i);
+  return upload(g.order, g.orderHost.data(), nSensors * 4, g.st);
+}
+
 KGB_API int kgb_set_scene(kgb_engine* e, const float* P, const float* N, size_t nSensors, const float* D, size_t nDir) {
   Engine& g = *E(e);
+  if (nSensors > 0xffffffffull) return fail("gpu_set_scene: more sensors than 32-bit indices hold");
   g.nSensors = nSensors; g.nDir = nDir; g.nWords = (nDir + 31) / 32;
   if (!upload(g.P, P, nSensors * 12, g.st) || !upload(g.N, N, nSensors * 12, g.st) || !upload(g.D, D, nDir * 12, g.st) ||
-      !grow(g.rayTab, nDir * 48)) return 0;
+      !grow(g.rayTab, nDir * 48) || !sensor_order(g, N, nSensors)) return 0;
   launch_ray_table(static_cast<const float*>(g.D.p), uint32_t(nDir), g.rayTab.p, g.st);
   CU(cudaGetLastError());
   CU(cudaStreamSynchronize(g.st));
@@ -704,8 +734,22 @@ static int trace_impl(Engine& g, size_t i0, size_t nc, uint32_t rayFlags, uint64
   a.slots = static_cast<const kgb_slot*>(g.slots.p); a.nSlots = g.nSlots; a.slotLog = static_cast<const float2*>(g.slotLog.p);
   a.counter = static_cast<uint32_t*>(g.ctl.p); a.status = static_cast<uint32_t*>(g.ctl.p) + 1;
   a.rayTab = static_cast<const RayDir*>(g.rayTab.p);
+  if (g.orderHost.size() == g.nSensors) {   // the call's range in tracing order: per class, its run of the order
+    a.order = static_cast<const uint32_t*>(g.order.p);
+    a.callI0 = uint32_t(i0);
+    uint32_t end = 0;
+    for (int c = 0; c < 6; ++c) {
+      const uint32_t* b = g.orderHost.data() + g.classStart[c];
+      const uint32_t* x = g.orderHost.data() + g.classStart[c + 1];
+      const uint32_t lo = uint32_t(std::lower_bound(b, x, uint32_t(i0)) - g.orderHost.data());
+      const uint32_t hi = uint32_t(std::lower_bound(b, x, uint32_t(i0 + nc)) - g.orderHost.data());
+      a.pieceG[c] = lo - end;   // modulo 2^32: pieceG[c] + p = lo + (p - end) for the run's positions p
+      end += hi - lo;
+      a.pieceEnd[c] = end;
+    }
+  }
   while (done < nc) {
-    a.first = uint32_t(i0 + done); a.n = uint32_t(n); a.out0 = uint32_t(done);
+    a.first = uint32_t(i0 + done); a.n = uint32_t(n); a.out0 = uint32_t(done); a.p0 = uint32_t(done);
     if (!reset_ctl(g)) return 0;
     const size_t tasks = (n + 31) / 32 * g.nWords;   // warp tasks: 32 sensors x one 32-direction word
     const int grid = int(std::min<size_t>(size_t(any ? g.gridBytes : g.gridBits), (tasks + 7) / 8));

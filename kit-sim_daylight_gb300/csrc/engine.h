@@ -44,6 +44,14 @@ struct TraceArgs {
   uint32_t* status;
   const RayDir* rayTab;   // the directions' precomputed ray parts (k_bits), or null
   const float2* slotLog;  // [nSlots]: ln tn per slot as a float pair (k_slot_logs)
+  // Tracing order. Null: sensors first .. first + n - 1, output columns out0 .. out0 + n - 1. Otherwise the call's sensors
+  // grouped by normal orientation: order lists every sensor of the scene, stably partitioned into six classes (the
+  // dominant axis of the normal and its sign); the call's range is, per class, a contiguous run of it. Position p of the
+  // call (p0 + i for lane position i of this launch) is sensor order[pieceG[c] + p] for the class c whose run holds it
+  // (pieceEnd[c - 1] <= p < pieceEnd[c]), written to output column sensor - callI0.
+  const uint32_t* order;
+  uint32_t p0, callI0;
+  uint32_t pieceG[6], pieceEnd[6];
 };
 
 struct ViewArgs {

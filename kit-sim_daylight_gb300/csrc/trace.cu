@@ -12,6 +12,20 @@
 
 namespace kgb {
 
+// The sensor (scene index) at lane position i of a launch and its output column (see TraceArgs::order).
+__device__ __forceinline__ void task_sensor(const TraceArgs& a, uint32_t i, uint32_t& gi, uint32_t& col) {
+  if (!a.order) { gi = a.first + i; col = a.out0 + i; return; }
+  const uint32_t p = a.p0 + i;
+  uint32_t g = a.pieceG[0];   // the runs' ends do not decrease: the last one passed names the run
+  if (p >= a.pieceEnd[0]) g = a.pieceG[1];
+  if (p >= a.pieceEnd[1]) g = a.pieceG[2];
+  if (p >= a.pieceEnd[2]) g = a.pieceG[3];
+  if (p >= a.pieceEnd[3]) g = a.pieceG[4];
+  if (p >= a.pieceEnd[4]) g = a.pieceG[5];
+  gi = a.order[g + p];
+  col = gi - a.callI0;
+}
+
 __device__ __forceinline__ uint32_t next_task(uint32_t* counter) {
   uint32_t t = 0;
   if ((threadIdx.x & 31) == 0) t = atomicAdd(counter, 1u);
@@ -33,10 +47,11 @@ __global__ void __launch_bounds__(256) k_bits(TraceArgs a) {
   for (uint32_t task = next_task(a.counter); task < nTasks; task = next_task(a.counter)) {
     const uint32_t b = task / a.nWords, w = task % a.nWords, i = b * 32 + lane;
     if (i >= a.n) continue;
-    const uint32_t gi = a.first + i;
+    uint32_t gi, col;
+    task_sensor(a, i, gi, col);
     const F3 n = ld3(a.N + 3 * gi), o = offset_ray(ld3(a.P + 3 * gi), n);
     const uint32_t word = trace_word<COUNT>(s, n, o, a.D, a.rayTab, a.nDir, w, cull, overflow, ctr, rays);
-    a.bits[size_t(w) * a.stride + a.out0 + i] = word;
+    a.bits[size_t(w) * a.stride + col] = word;
   }
   if (overflow) atomicOr(a.status, (overflow & 1u ? kStatusStackOverflow : 0u) | (overflow & 2u ? kStatusVisitLimit : 0u));
   if (COUNT) {
@@ -131,12 +146,13 @@ __global__ void __launch_bounds__(256, 3) k_bytes(TraceArgs a) {   // 3 blocks a
   for (uint32_t task = next_task(a.counter); task < nTasks; task = next_task(a.counter)) {
     const uint32_t b = task / a.nWords, w = task % a.nWords, i = b * 32 + lane;
     if (i >= a.n) continue;
-    const uint32_t gi = a.first + i;
+    uint32_t gi, col;
+    task_sensor(a, i, gi, col);
     const F3 n = ld3(a.N + 3 * gi), o = offset_ray(ld3(a.P + 3 * gi), n);
     for (uint32_t k = 0; k < 32; ++k) {
       const uint32_t d = w * 32 + k;
       if (d >= a.nDir) break;
-      a.bytes[size_t(d) * a.stride + a.out0 + i] = trace_byte(s, a, o, n, d, ld3(a.D + 3 * d), cull, overflow);
+      a.bytes[size_t(d) * a.stride + col] = trace_byte(s, a, o, n, d, ld3(a.D + 3 * d), cull, overflow);
     }
   }
   if (overflow) atomicOr(a.status, (overflow & 1u ? kStatusStackOverflow : 0u) | (overflow & 2u ? kStatusVisitLimit : 0u));
