@@ -282,6 +282,7 @@ struct Engine {
   Buf order;                          // the sensors grouped by normal orientation (TraceArgs::order), on the device
   std::vector<uint32_t> orderHost;    // and here, to find a call's runs
   uint32_t classStart[7] = {};        // class c's sensors are orderHost[classStart[c] .. classStart[c + 1])
+  Buf cls, clsFlags;                  // the classes the order was built from (a byte per sensor); the class kernel's flags
   Buf vis;
   bool bytes = false;
   size_t i0 = 0, visN = 0;
@@ -623,7 +624,7 @@ KGB_API void kgb_trim(kgb_engine* e, int sensors) {
   g.vop.free(); g.sop.free(); g.csr.free(); g.sunCol.free();
   g.viewN = 0;
   if (sensors) {
-    g.P.free(); g.N.free(); g.label.free(); g.order.free(); g.nLabel = 0; g.nSensors = 0;
+    g.P.free(); g.N.free(); g.label.free(); g.order.free(); g.cls.free(); g.nLabel = 0; g.nSensors = 0;
     std::vector<uint32_t>().swap(g.orderHost);
   }
 }
@@ -669,18 +670,26 @@ KGB_API uint64_t kgb_free_bytes(void) {
 // sign. A warp traces one direction for 32 consecutive sensors of that order, so a warp whose sensors straddle two faces
 // of different orientation (whose lanes on the face turned away from the direction idle) becomes one straddling two
 // faces of the same orientation. Urban block, the reference's direction table: trace 60.9 to 58.1 ms. The results of
-// every sensor do not depend on the order.
-static uint32_t orientation_class(const float* n) {
-  const float ax = std::fabs(n[0]), ay = std::fabs(n[1]), az = std::fabs(n[2]);
-  const int k = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
-  return 2u * uint32_t(k) + (n[k] > 0.f ? 1u : 0u);
-}
-static bool sensor_order(Engine& g, const float* N, size_t nSensors) {
-  std::vector<uint32_t> cls(nSensors);
-  uint32_t count[6] = {};
-  for (size_t i = 0; i < nSensors; ++i) count[cls[i] = orientation_class(N + 3 * i)]++;
+// every sensor do not depend on the order: any partition of the sensors into six runs, each in index order, traces the
+// same rays, so the order is rebuilt only when the classes of the sensors just uploaded differ from those it was built
+// from (a kernel compares them on the device; a caller that sends the same sensors every step pays for that kernel).
+static bool sensor_order(Engine& g, size_t nSensors) {
+  const bool fresh = g.orderHost.size() != nSensors || !g.order.p;
+  if (!grow(g.cls, nSensors) || !grow(g.clsFlags, 7 * 4)) return false;
+  if (fresh && nSensors) CU(cudaMemsetAsync(g.cls.p, 0xff, nSensors, g.st));   // no class yet: every sensor differs
+  CU(cudaMemsetAsync(g.clsFlags.p, 0, 7 * 4, g.st));
+  launch_sensor_classes(static_cast<const float*>(g.N.p), uint32_t(nSensors), static_cast<uint8_t*>(g.cls.p),
+                        static_cast<uint32_t*>(g.clsFlags.p), g.st);
+  CU(cudaGetLastError());
+  uint32_t f[7];
+  CU(cudaMemcpyAsync(f, g.clsFlags.p, sizeof f, cudaMemcpyDeviceToHost, g.st));
+  CU(cudaStreamSynchronize(g.st));
+  if (!f[0] && !fresh) return true;
+  std::vector<uint8_t> cls(nSensors);
+  if (nSensors) CU(cudaMemcpy(cls.data(), g.cls.p, nSensors, cudaMemcpyDeviceToHost));
   g.classStart[0] = 0;
-  for (int c = 0; c < 6; ++c) g.classStart[c + 1] = g.classStart[c] + count[c];
+  for (int c = 0; c < 6; ++c) g.classStart[c + 1] = g.classStart[c] + f[1 + c];
+  if (g.classStart[6] != nSensors) return fail("gpu_set_scene: the sensors' classes do not add up");
   uint32_t at[6];
   for (int c = 0; c < 6; ++c) at[c] = g.classStart[c];
   g.orderHost.resize(nSensors);
@@ -693,9 +702,10 @@ KGB_API int kgb_set_scene(kgb_engine* e, const float* P, const float* N, size_t 
   if (nSensors > 0xffffffffull) return fail("gpu_set_scene: more sensors than 32-bit indices hold");
   g.nSensors = nSensors; g.nDir = nDir; g.nWords = (nDir + 31) / 32;
   if (!upload(g.P, P, nSensors * 12, g.st) || !upload(g.N, N, nSensors * 12, g.st) || !upload(g.D, D, nDir * 12, g.st) ||
-      !grow(g.rayTab, nDir * 48) || !sensor_order(g, N, nSensors)) return 0;
+      !grow(g.rayTab, nDir * 48)) return 0;
   launch_ray_table(static_cast<const float*>(g.D.p), uint32_t(nDir), g.rayTab.p, g.st);
   CU(cudaGetLastError());
+  if (!sensor_order(g, nSensors)) return 0;
   CU(cudaStreamSynchronize(g.st));
   return 1;
 }

@@ -101,6 +101,9 @@ struct BounceArgs {
 };
 
 void launch_ray_table(const float* D, uint32_t nDir, void* tab, cudaStream_t st);   // 48 bytes per direction
+// The sensors' orientation classes (TraceArgs::order) against the classes in cls: cls updated, flags[0] = 1 where one
+// differs, flags[1 + c] += the sensors of class c (flags zeroed by the caller).
+void launch_sensor_classes(const float* N, uint32_t n, uint8_t* cls, uint32_t* flags, cudaStream_t st);
 void launch_slot_logs(const kgb_slot* slots, uint32_t n, float2* out, cudaStream_t st);   // ln tn per slot, a float pair
 // rows.cu: out[i K + d] = in[d ld + i] for d < K, i < m, elements of 1 or 4 bytes; false if the grid cannot hold K
 bool launch_rows(const void* in, size_t ld, void* out, size_t esize, uint32_t K, uint32_t m, cudaStream_t st);

@@ -455,6 +455,27 @@ __global__ void __launch_bounds__(256) k_ray_table(const float* D, uint32_t nDir
   const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
   if (d < nDir) tab[d] = ray_dir_of(ld3(D + 3 * d));
 }
+// A sensor's orientation class: twice the dominant axis of its normal (x 0, y 1, z 2), plus one when that component is
+// positive.
+__global__ void k_sensor_classes(const float* N, uint32_t n, uint8_t* cls, uint32_t* flags) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t c = 6;   // no sensor
+  if (i < n) {
+    const float x = N[3 * i], y = N[3 * i + 1], z = N[3 * i + 2];
+    const float ax = fabsf(x), ay = fabsf(y), az = fabsf(z);
+    const uint32_t k = (ax >= ay && ax >= az) ? 0u : (ay >= az ? 1u : 2u);
+    c = 2u * k + ((k == 0 ? x : k == 1 ? y : z) > 0.f ? 1u : 0u);
+    if (cls[i] != c) { cls[i] = uint8_t(c); atomicOr(flags, 1u); }
+  }
+  for (uint32_t k = 0; k < 6; ++k) {   // counts, one atomic per warp and class
+    const uint32_t m = __ballot_sync(~0u, c == k);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(flags + 1 + k, uint32_t(__popc(m)));
+  }
+}
+void launch_sensor_classes(const float* N, uint32_t n, uint8_t* cls, uint32_t* flags, cudaStream_t st) {
+  if (n) k_sensor_classes<<<(n + 255) / 256, 256, 0, st>>>(N, n, cls, flags);
+}
+
 void launch_ray_table(const float* D, uint32_t nDir, void* tab, cudaStream_t st) {
   if (nDir) k_ray_table<<<(nDir + 255) / 256, 256, 0, st>>>(D, nDir, static_cast<RayDir*>(tab));
 }
