@@ -145,7 +145,10 @@ KGB_API kgb_scene kgb_detach(kgb_engine* e);
 KGB_API void kgb_attach(kgb_engine* e, kgb_scene s);
 KGB_API void kgb_free_scene(kgb_scene* s);
 KGB_API uint64_t kgb_free_bytes(void);
-/* replaces gpu_set_scene (src/internal.h:146): resident sensors (recentred, offset applied) and directions */
+/* replaces gpu_set_scene (src/internal.h:146): resident sensors (recentred, offset applied) and directions. The
+ * visibility traces take a call's sensors grouped by the orientation of their normals (each sensor's result, and where
+ * it is written, do not change); that order is rebuilt here when the sensors' orientation classes differ from those it
+ * was built from (checked on the device), so resending the same sensors costs one small kernel. */
 KGB_API int kgb_set_scene(kgb_engine* e, const float* P, const float* N, size_t nSensors, const float* D, size_t nDir);
 /* replaces gpu_set_labels (src/internal.h:197): class per triangle in build order; n == 0: none */
 KGB_API int kgb_set_labels(kgb_engine* e, const uint8_t* label, size_t n);
