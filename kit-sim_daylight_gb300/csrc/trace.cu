@@ -6,7 +6,9 @@
 //           reflected-light paths binned by sky patch (replaces __raygen__bounce, trace_dev.cu:260-311), as a wavefront
 //           of segments: first segments, then steps over a compacted queue of the paths that go on
 // The visibility kernels are persistent: each warp takes tasks of 32 consecutive sensors x one 32-direction word
-// from a global counter, so a warp traces one direction for 32 neighbouring sensors at a time (coherent rays).
+// from a global counter, so a warp traces one direction for 32 neighbouring sensors at a time (coherent rays). k_bits
+// and k_bytes take a call's sensors in the engine's tracing order (grouped by the orientation of their normals:
+// TraceArgs::order), so that a warp's sensors face the same way more often; each result goes to its sensor's column.
 #include "engine.h"
 #include "rt.cuh"
 
