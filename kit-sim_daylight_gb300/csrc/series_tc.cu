@@ -211,6 +211,8 @@ __device__ __forceinline__ uint32_t tc_seg_of(const TcGroup& g, uint32_t tile) {
 // Measured on a precision chunk (29,609 sensors x 4456 steps, K 4672; kernel time of the chunk, DRAM read of one of its
 // four launches): bands of 4 / 8 / 16 / 32 / all step-tiles 8.71 / 8.67 / 8.60 / 8.84 / 9.23 ms, 2.33 GB at 8, 1.55 GB
 // at 16, 1.92 GB at 32. The MMA issue bounds the kernel (DRAM at about a tenth of its rate), and 16 reads the least.
+// On the kernel with its sun term in a pass of its own (six launches a chunk): 8 / 12 / 16 / 24 / 32 gave 5.325 / 5.320 /
+// 5.318 / 5.317 / 5.327 ms, the same within the noise.
 constexpr uint32_t kBand = 16;
 __device__ __forceinline__ void tile_coords(uint32_t tile, uint32_t mTiles, uint32_t nTiles, uint32_t& m, uint32_t& n) {
   const uint32_t perBand = mTiles * kBand, band = tile / perBand, idx = tile - band * perBand;
