@@ -689,7 +689,10 @@ static bool sensor_order(Engine& g, size_t nSensors) {
   CU(cudaStreamSynchronize(g.st));
   if (!f[0] && !fresh) return true;
   std::vector<uint8_t> cls(nSensors);
-  if (nSensors) CU(cudaMemcpy(cls.data(), g.cls.p, nSensors, cudaMemcpyDeviceToHost));
+  if (nSensors) {
+    CU(cudaMemcpyAsync(cls.data(), g.cls.p, nSensors, cudaMemcpyDeviceToHost, g.st));
+    CU(cudaStreamSynchronize(g.st));
+  }
   g.classStart[0] = 0;
   for (int c = 0; c < 6; ++c) g.classStart[c + 1] = g.classStart[c] + f[1 + c];
   if (g.classStart[6] != nSensors) return fail("gpu_set_scene: the sensors' classes do not add up");
