@@ -162,7 +162,7 @@ struct SeriesArgs {
 };
 void launch_series_fp32(const SeriesArgs& a, cudaStream_t st);
 
-// time series on the tensor cores (series_tc.cu): split-BF16 operands, tcgen05 MMA, sun term in the epilogue
+// time series on the tensor cores (series_tc.cu): split-BF16 operands, tcgen05 MMA, then the sun term in a pass over E
 struct SeriesTcPlan {
   uint32_t nc, T, Kp, sun0;
   int numSMs;

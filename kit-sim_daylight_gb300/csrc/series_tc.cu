@@ -209,7 +209,7 @@ __device__ __forceinline__ uint32_t tc_seg_of(const TcGroup& g, uint32_t tile) {
 // a few V panels and the band's S panels (16 x 64 steps x K x 6 B, some 30 MB at K 4672), which stay in L2 for the
 // band; S is read from DRAM about once and V once per band (a steps-fastest order over all steps re-read S per row).
 // Measured on a precision chunk (29,609 sensors x 4456 steps, K 4672; kernel time of the chunk, DRAM read of one of its
-// four launches): bands of 4 / 8 / 16 / 32 / all step-tiles 8.71 / 8.67 / 8.60 / 8.84 / 9.23 ms, 2.33 GB at 8, 1.55 GB
+// four launches, on the earlier kernel that added the sun term itself): bands of 4 / 8 / 16 / 32 / all step-tiles 8.71 / 8.67 / 8.60 / 8.84 / 9.23 ms, 2.33 GB at 8, 1.55 GB
 // at 16, 1.92 GB at 32. The MMA issue bounds the kernel (DRAM at about a tenth of its rate), and 16 reads the least.
 // On the kernel with its sun term in a pass of its own (six launches a chunk): 8 / 12 / 16 / 24 / 32 gave 5.325 / 5.320 /
 // 5.318 / 5.317 / 5.327 ms, the same within the noise.
