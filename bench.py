@@ -518,7 +518,7 @@ def run_precision(args, pkg):
             "config": {"workload": "precision: urban block, %d sensors, %d patches + ground, %d directions, %d series columns (non-night hours), "
                                    "20%% glass tau 0.64 (byte mode), 1 bounce x %d paths (%d reflected-light bins in K), chunks of %d sensors"
                                    % (nc_all, P, len(D), T, M, P + 1, chunk)},
-            "dtype": "split-bf16 (3 pieces, 6 products) on tcgen05, fp32 accumulate in chains of 64 of K, added per 128 of K with Kahan compensation; sun term fp32",
+            "dtype": "split-bf16 (3 pieces, 6 products) on tcgen05, fp32 accumulate in chains of 64 of K, each chain added into fp32 sums with Kahan compensation; sun term fp32",
             "roofline": {"bound": "tensor", "kernel": "k_series_tc", "achieved": series_flop / (series_ms / 1000) / 1e12 if series_ms else None,
                          "peak": tc_peak[0], "unit": "TFLOP/s", "peak_kind": tc_peak[1] + " bf16 sustained",
                          "frac": series_flop / (series_ms / 1000) / 1e12 / tc_peak[0] if series_ms else None, "traffic": None,
